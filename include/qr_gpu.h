@@ -1,0 +1,192 @@
+/*
+ * qr_gpu.h: C ABI of the GB300 QuadRay render backend.
+ *
+ * This is the boundary between the host engine (rt_Platform / rt_Scene, which
+ * keeps the reference API of VectorChief/QuadRay-engine core/engine/engine.h
+ * and flattens the object tree) and the sm_103a CUDA tracer.  It replaces the
+ * reference's backend entry points, which take pre-broadcast SIMD structs:
+ *
+ *   rt_Platform::render0(rt_SIMD_INFOX*)   core/tracer/tracer.cpp:8454
+ *                                          (declared core/engine/engine.h:129)
+ *   rt_Platform::update0(rt_SIMD_SURFACE*) core/tracer/tracer.cpp:8115
+ *                                          (declared core/engine/engine.h:128)
+ *   rt_Platform::switch0(...)              core/tracer/tracer.cpp:8180
+ *
+ * Everything here is plain C: fixed-layout structs, integers, pointers and
+ * sizes.  Every entry point returns a status (QR_OK = 0); nothing throws.
+ *
+ * Flattened scene ("qr_scene_desc"): one record per surface or transform
+ * node (qr_srf, the fields the reference keeps in rt_SIMD_SURFACE,
+ * core/tracer/tracer.h:1024-1183), one per material (rt_SIMD_MATERIAL,
+ * tracer.h:1193-1292) and light (rt_SIMD_LIGHT, tracer.h:968-1014), and flat
+ * element arrays for the linked lists the reference walks (rt_ELEM,
+ * tracer.h:132-146): the camera's surface list, per-surface clipper lists,
+ * per-side light lists with their shadow lists, and per-side lists for
+ * reflected/refracted rays.
+ */
+#ifndef QR_GPU_H
+#define QR_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define QR_OK               0
+#define QR_ERR_ARG          1   /* invalid argument / size */
+#define QR_ERR_OOM          2   /* device or host allocation failed */
+#define QR_ERR_CUDA         3   /* CUDA runtime error (message in last_error) */
+#define QR_ERR_TIMEOUT      4   /* bounded device wait expired */
+#define QR_ERR_STATE        5   /* call out of order (e.g. render w/o scene) */
+#define QR_ERR_NOSCENE      6   /* unknown scene id */
+#define QR_ERR_LIMIT        7   /* request exceeds a compiled-in limit */
+
+/* ---- material / context property bits (tracer.h:66-77) ----------------- */
+#define QR_PROP_LIGHT       0x00000010
+#define QR_PROP_METAL       0x00000020
+#define QR_PROP_GAMMA       0x00000040
+#define QR_PROP_FRESNEL     0x00000080
+#define QR_PROP_NORMAL      0x00000100
+#define QR_PROP_OPAQUE      0x00000200
+#define QR_PROP_TRANSP      0x00000400
+#define QR_PROP_TEXTURE     0x00000800
+#define QR_PROP_REFLECT     0x00001000
+#define QR_PROP_REFRACT     0x00002000
+#define QR_PROP_DIFFUSE     0x00004000
+#define QR_PROP_SPECULAR    0x00008000
+
+/* ---- element kinds in flattened lists ------------------------------------ */
+#define QR_ELM_SURFACE      0   /* ref = surface index */
+#define QR_ELM_TRNODE       1   /* ref = node index, last = index (in the same
+                                   list) of the node's last surface element */
+#define QR_ELM_ACC_ENTER    2   /* clip lists: boolean accumulator enter */
+#define QR_ELM_ACC_LEAVE    3   /* clip lists: boolean accumulator leave */
+
+typedef struct qr_elem
+{
+    int32_t kind;       /* QR_ELM_* */
+    int32_t ref;        /* surface / node index */
+    int32_t last;       /* trnode: list index of its last element */
+    int32_t rel;        /* clip lists: -1 minus inner, +1 minus outer */
+} qr_elem;
+
+/* light list element: a light and the surfaces that can shadow it */
+typedef struct qr_lelem
+{
+    int32_t light;      /* light index */
+    int32_t shd_off;    /* shadow list: offset into qr_scene_desc.elems */
+    int32_t shd_num;    /* shadow list length */
+    int32_t pad;
+} qr_lelem;
+
+/*
+ * Surface or transform-node record, 256 bytes, 16-byte aligned.
+ * Axis mapping: local axis I/J/K of the surface is stored in world (or
+ * transform-node) axis amap[0..2] with sign asgn[0..2] (1 = negated);
+ * amap[3] is the transform class (0 none, 1 scaling only, 2 rotation,
+ * 3 rotation + scaling) and asgn[3] is 1 when the surface's coordinates come
+ * from a transform node (the IJK fields of the reference context).
+ */
+typedef struct qr_srf
+{
+    float   pos[3];     int32_t tag;        /* RT_TAG_* of format.h */
+    float   tci[3];     int32_t solver;     /* 1 plane 2 quadric 3 two-plane */
+    float   tcj[3];     int32_t nrmk;       /* normal kind (update0 srf_t[1]) */
+    float   tck[3];     int32_t clpk;       /* clipper kind (srf_t[2]) */
+    float   sci[4];                         /* x,y,z,w quadric coefficients */
+    float   scj[3];     int32_t conic;      /* apex adjust: 0 no, 1 cone, 2 hc */
+    float   bmin[3];    int32_t mint;       /* axis clip min, bit k = active */
+    float   bmax[3];    int32_t maxt;       /* axis clip max, bit k = active */
+    int32_t amap[4];
+    int32_t asgn[4];
+    int32_t mat[2];                         /* outer/inner material index */
+    int32_t props[2];                       /* outer/inner material props */
+    int32_t trnode;                         /* transform node index or -1 */
+    int32_t clip_off, clip_num;             /* clipper list in elems */
+    int32_t is_node;                        /* 1 for transform-node records */
+    int32_t lgt_off[2], lgt_num[2];         /* per-side light lists, lelems */
+    int32_t sec_off[2], sec_num[2];         /* per-side lists for secondary
+                                               rays, in elems */
+    int32_t id;                             /* generation index (hit IDs) */
+    int32_t pad[7];
+} qr_srf;
+
+typedef struct qr_mat
+{
+    float   l_dff, l_spc;   int32_t l_pow;  int32_t props;
+    float   c_rfl, c_trn, c_rfr, rfr_2;
+    float   c_rcp, ext_2;   float col_e[2];         /* col_e: reserved */
+    float   xscal, yscal, xoffs, yoffs;             /* texture transform */
+    int32_t xmask, ymask, yshft, tex_off;           /* texel offset in texels */
+    int32_t tmap[2];    int32_t pad0[2];            /* UV -> XY mapping */
+    float   emit[4];                                /* PT emission r,g,b,src */
+} qr_mat;
+
+typedef struct qr_light
+{
+    float   pos[3];     float t_max;
+    float   col[3];     float l_src;
+    float   a_qdr, a_lnr, a_cnt, a_rng;
+} qr_light;
+
+/* flattened scene (host memory, copied to the device by qr_scene_upload) */
+typedef struct qr_scene_desc
+{
+    int32_t         nsrf;       const qr_srf   *srf;
+    int32_t         nmat;       const qr_mat   *mat;
+    int32_t         nlgt;       const qr_light *lgt;
+    int32_t         nelem;      const qr_elem  *elems;
+    int32_t         nlelem;     const qr_lelem *lelems;
+    int32_t         ntex;       const uint32_t *texels;
+    int32_t         cam_off, cam_num;   /* camera's surface list in elems */
+} qr_scene_desc;
+
+/* per-frame camera and mode parameters (rt_SIMD_CAMERA, tracer.h:869-958,
+ * and the per-thread setup of rt_Scene::render_slice, engine.cpp:3514) */
+typedef struct qr_frame_params
+{
+    float   org[3];     float t_min;        /* camera position, near clip */
+    float   dir[3];     float t_max;        /* ray to pixel (0,0) centre */
+    float   hor[3];     float pad0;         /* per-pixel horizontal step */
+    float   ver[3];     float pad1;         /* per-pixel vertical step */
+    float   amb[3];     float l_amb;        /* accumulated ambient colour */
+    int32_t x_res, y_res, x_row;            /* frame size, row stride (px) */
+    int32_t fsaa;                           /* 0 none, 1 2x, 2 4x */
+    int32_t depth;                          /* secondary-ray depth */
+    int32_t ctx_props;                      /* QR_PROP_GAMMA when gamma on */
+    int32_t pt_on;                          /* path-tracer samples (0 off) */
+    int32_t frame_idx;                      /* PT frame counter */
+    uint64_t seed;                          /* PT seed */
+    float   pts_c;  float pad2;             /* PT samples so far */
+} qr_frame_params;
+
+typedef struct qr_ctx qr_ctx;
+
+/* library / device context */
+int qr_ctx_create(int device, qr_ctx **out);
+int qr_ctx_destroy(qr_ctx *ctx);
+const char *qr_last_error(qr_ctx *ctx);
+
+/* scenes are kept resident on the device; returns a scene id */
+int qr_scene_upload(qr_ctx *ctx, const qr_scene_desc *desc, int *scene_id);
+/* replace the scene's records in place (same list structure, new fields) */
+int qr_scene_update(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc);
+int qr_scene_release(qr_ctx *ctx, int scene_id);
+
+/* render one frame into a device frame buffer (uint32 XRGB, x_row stride),
+ * asynchronously on `stream` (a cudaStream_t, 0 = default stream) */
+int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                     uint32_t *dev_frame, void *stream);
+/* render one frame into host memory: copies in, renders, copies out, syncs */
+int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                   uint32_t *host_frame);
+int qr_sync(qr_ctx *ctx, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QR_GPU_H */

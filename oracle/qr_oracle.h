@@ -1,0 +1,24 @@
+/*
+ * qr_oracle.h: CPU restatement of the QuadRay Whitted render path.
+ * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline).
+ */
+#ifndef QR_ORACLE_H
+#define QR_ORACLE_H
+
+#include <stdint.h>
+#include "qr_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* render rows [y0, y1) of the frame into frame[y * x_row + x] (XRGB);
+ * nrays (optional) receives the number of traced segments */
+int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
+                     uint32_t *frame, int y0, int y1, uint64_t *nrays);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QR_ORACLE_H */

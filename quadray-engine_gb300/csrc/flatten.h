@@ -1,0 +1,165 @@
+/*
+ * flatten.h: host-side object tree and its flattening into qr_scene_desc.
+ *
+ * Restates the reference engine's per-frame update phases
+ * (core/engine/object.cpp and core/engine/engine.cpp) for the render path:
+ *   phase 0.5  hierarchical transforms and transform-node selection
+ *              (rt_Object::update_matrix, object.cpp:221-389;
+ *               rt_Array::update_object, object.cpp:1753-1781)
+ *   phase 1    per-object backend fields: inverse transforms, axis mapping,
+ *              quadric coefficients, lights, camera
+ *              (object.cpp:826-857, 1786-1850, 2497-2528, 2920-3936, 649-667)
+ *   phase 2    custom clipper lists and clip boxes
+ *              (engine.cpp:1850-1979 sclip; object.cpp:2533-2870 minmax)
+ *   lists      camera surface list, light/shadow lists, secondary-ray lists
+ *              (engine.cpp:1145-2782), brute force: no culling, same order
+ *   phase 3    solver/normal/clipper kinds (rt_Platform::update0,
+ *              core/tracer/tracer.cpp:8115-8149)
+ *   camera     ray basis and ambient (rt_Scene::render, engine.cpp:3078-3318;
+ *              render_slice, engine.cpp:3514-3672)
+ * All float arithmetic is written in the reference's operation order and must
+ * be compiled with -ffp-contract=off so results are bit-identical on x86-64
+ * and AArch64.
+ */
+#ifndef QR_FLATTEN_H
+#define QR_FLATTEN_H
+
+#include <vector>
+#include "format.h"
+#include "qr_gpu.h"
+
+namespace qr
+{
+
+struct Node;
+
+/* material as seen by the backend (rt_Material, object.cpp:4038-4180) */
+struct Material
+{
+    rt_MATERIAL *mat;
+    rt_SIDE     *sd;
+    int          props;
+    int          map[2];
+    float        scl[2];
+    qr_mat       m;         /* backend record */
+    rt_ui32     *texels;    /* resolved texel pointer */
+    int          x_dim, y_dim;
+};
+
+struct Node
+{
+    int          kind;      /* 0 array, 1 surface, 2 camera, 3 light */
+    int          tag;
+    rt_OBJECT   *obj;
+    rt_TRANSFORM3D *trm;
+    Node        *parent;
+    Node        *trnode;
+    float        mtx[4][4];
+    float        inv[4][4];
+    float        scm[4][4];     /* arrays: scalers for sub-objects */
+    float      (*pmtx)[4];      /* matrix handed down by the parent */
+    int          map[4];
+    int          sgn[4];
+    float        scl[4];
+    int          obj_changed, obj_has_trm, mtx_has_trm;
+    std::vector<Node*> children;
+
+    /* surfaces */
+    rt_SURFACE  *srf;
+    int          outer, inner;  /* material indices */
+    float        sci[4], scj[4];/* shape (before the 0.5 scj scale) */
+    float        bmin[4], bmax[4], cmin[4], cmax[4];
+    /* relations template: (data, object or NULL for accum markers) in the
+     * order the backend evaluates them */
+    struct Rel { int data; Node *obj; };
+    std::vector<Rel> rel;
+    int          index;         /* flat record index */
+    int          gen;           /* creation order among surfaces */
+
+    /* lights */
+    float        lcol[3];       /* colour * source intensity */
+    float        hdr[4];        /* light / camera colour */
+    /* arrays: accumulated light colour for emitters */
+    float        acc[4];
+
+    /* camera */
+    float        pov;
+
+    qr_srf       rec;           /* backend record */
+
+    Node() : kind(0), tag(0), obj(0), trm(0), parent(0), trnode(0), pmtx(0),
+             obj_changed(0), obj_has_trm(0), mtx_has_trm(0), srf(0),
+             outer(-1), inner(-1), index(-1), gen(-1), pov(1.0f) {}
+};
+
+/*
+ * Scene tree built once from the scene structs; update(time) recomputes all
+ * backend fields for a frame and refreshes the flat arrays.
+ */
+class Flat
+{
+public:
+    Flat(rt_SCENE *scn, int opts, int x_res, int y_res, int fsaa);
+    ~Flat();
+
+    /* run the update phases for `time` and rebuild the flat arrays */
+    void update(rt_time time);
+    /* ambient/camera parameters for the current camera */
+    void frame_params(qr_frame_params *fp) const;
+    /* descriptor pointing into this object's arrays */
+    void desc(qr_scene_desc *d) const;
+
+    int  opts;
+    int  x_res, y_res, fsaa;
+    int  depth;
+    int  cam_idx;
+    float factor, aspect;
+
+    std::vector<Node*>  nodes;      /* all nodes, creation order */
+    std::vector<Node*>  surfaces;   /* creation order */
+    std::vector<Node*>  arrays;     /* creation order */
+    std::vector<Node*>  lights;     /* creation order */
+    std::vector<Node*>  cameras;    /* creation order */
+    std::vector<Material> mats;
+
+    std::vector<qr_srf>   srf;
+    std::vector<qr_mat>   mat;
+    std::vector<qr_light> lgt;
+    std::vector<qr_elem>  elems;
+    std::vector<qr_lelem> lelems;
+    std::vector<rt_ui32>  texels;
+    int cam_off, cam_num;
+
+    Node *root;
+    rt_OBJECT rootobj;
+
+private:
+    Node *build(Node *parent, rt_OBJECT *obj);
+    int   material(rt_SIDE *sd, rt_MATERIAL *mt);
+    void  relations(Node *arr);
+    void  add_relation(Node *n, const std::vector<Node::Rel> &lst);
+
+    void  update_object(Node *n, rt_time time, int flags, Node *trnode,
+                        float (*mtx)[4]);
+    void  update_status(Node *n, rt_time time, int flags, Node *trnode);
+    void  update_matrix(Node *n, float (*mtx)[4]);
+    void  fields_node(Node *n);
+    void  fields_surface(Node *n);
+    void  fields_array(Node *n);
+    void  bounds(Node *n);
+    void  recalc_minmax(Node *n, float *smin, float *smax, float *bmin,
+                        float *bmax, float *cmin, float *cmax);
+    void  adjust_minmax(Node *n, const float *smin, const float *smax,
+                        float *bmin, float *bmax, float *cmin, float *cmax);
+    void  invert_minmax(Node *n, const float *smin, const float *smax,
+                        float *dmin, float *dmax);
+    void  direct_minmax(Node *n, const float *smin, const float *smax,
+                        float *dmin, float *dmax);
+    void  emit_records();
+    void  emit_lists();
+    int   emit_surface_list(const std::vector<Node*> &order);
+};
+
+} /* namespace qr */
+
+#endif /* QR_FLATTEN_H */

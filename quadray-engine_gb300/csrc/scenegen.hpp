@@ -1,0 +1,392 @@
+/*
+ * scenegen.hpp: seeded synthetic scenes in the QuadRay scene-struct format.
+ *
+ * The reference publishes no scene set for its render benchmarks, so the
+ * workloads are generated from a seed: random quadrics, planes, clippers,
+ * lights and materials written into the scene structs of format.h.  The
+ * generator only uses the struct API, so the same source builds against the
+ * reference's core/engine/format.h (to render golden frames with the
+ * reference engine) and against this package's format.h (to render the same
+ * scene on the GPU).  Random numbers come from SplitMix64 and are turned into
+ * floats with plain double arithmetic, so a seed gives bit-identical scenes
+ * on x86-64 and AArch64 when built with -ffp-contract=off.
+ *
+ * Workloads (sizes are the caller's choice):
+ *   QR_SCN_PLAIN   one ground plane z=0 plus N quadrics (sphere, cylinder,
+ *                  cone, paraboloid, 1-sheet hyperboloid), each with its own
+ *                  random rotation, 2 point lights, plain materials, shadows
+ *   QR_SCN_ANIM    N quadrics under a 3-level array hierarchy with animated
+ *                  rotations, 1-2 plane clippers per quadric, boolean-minus
+ *                  pairs, 4 lights, 25% transparent (refractive) materials,
+ *                  mirror/metal materials, Fresnel on
+ *   QR_SCN_PT      a closed box of 5 planes with N quadrics inside, 60%
+ *                  Lambertian / 25% mirror / 15% dielectric, a LIGHT-material
+ *                  emitter with a light cluster, for the path tracer
+ * Flag QR_GEN_IDS replaces every material with a LIGHT material whose colour
+ * encodes (surface index, side), so the rendered frame is a hit-ID buffer.
+ */
+#ifndef QR_SCENEGEN_HPP
+#define QR_SCENEGEN_HPP
+
+#include <stdint.h>
+#include <math.h>
+#include <string.h>
+#include <vector>
+#include <deque>
+
+/* the reference's format.h defines RT_FORMAT_H; use it when already seen */
+#if !defined(RT_FORMAT_H) && !defined(QR_FORMAT_H)
+#include "format.h"
+#endif
+
+#define QR_SCN_PLAIN    1
+#define QR_SCN_ANIM     2
+#define QR_SCN_PT       3
+
+#define QR_GEN_IDS      (1 << 0)   /* hit-ID materials */
+#define QR_GEN_NOSPEC   (1 << 1)   /* debug: no specular */
+#define QR_GEN_ONELIGHT (1 << 2)   /* debug: a single light */
+
+namespace qr_gen
+{
+
+/* SplitMix64 (Steele, Lea, Flood 2014) */
+struct Rng
+{
+    uint64_t s;
+    explicit Rng(uint64_t seed) : s(seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull) {}
+    uint64_t next()
+    {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double u01() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+    float uf(double lo, double hi) { double t = u01(); return (float)(lo + (hi - lo) * t); }
+    int ui(int lo, int hi) /* inclusive */
+    {
+        return lo + (int)(next() % (uint64_t)(hi - lo + 1));
+    }
+};
+
+static inline rt_ui32 pack_rgb(float r, float g, float b)
+{
+    rt_ui32 cr = (rt_ui32)(r * 255.0f + 0.5f), cg = (rt_ui32)(g * 255.0f + 0.5f),
+            cb = (rt_ui32)(b * 255.0f + 0.5f);
+    if (cr > 255) cr = 255;
+    if (cg > 255) cg = 255;
+    if (cb > 255) cb = 255;
+    return (cr << 16) | (cg << 8) | cb;
+}
+
+/* animator for QR_SCN_ANIM: rotation speed (deg/frame) is taken from the
+ * object's scale slot W (encoded in the transform's unused precision via the
+ * per-object table below); frames are 16 ms apart */
+struct AnimEntry { rt_TRANSFORM3D *trm; float base[3]; float rate[3]; };
+
+static std::vector<AnimEntry> &anim_table()
+{
+    static std::vector<AnimEntry> t;
+    return t;
+}
+
+static void anim_rotate(rt_time time, rt_time last_time, rt_TRANSFORM3D *trm,
+                        rt_pntr pobj)
+{
+    (void)last_time; (void)pobj;
+    std::vector<AnimEntry> &t = anim_table();
+    for (size_t i = 0; i < t.size(); i++)
+    {
+        if (t[i].trm != trm) continue;
+        double f = (double)time / 16.0;   /* frame index at 16 ms per frame */
+        for (int k = 0; k < 3; k++)
+        {
+            double a = (double)t[i].base[k] + (double)t[i].rate[k] * f;
+            a = fmod(a, 360.0);
+            if (a >= 180.0) a -= 360.0;
+            trm->rot[k] = (float)a;
+        }
+        return;
+    }
+}
+
+/*
+ * Scene storage: every struct lives in a deque so pointers stay valid while
+ * the scene is built.  The scene is usable as long as the holder lives.
+ */
+struct Scene
+{
+    rt_SCENE scn;
+    std::deque<rt_OBJECT>   objs;       /* individual objects (copied) */
+    std::deque<std::vector<rt_OBJECT> > arrays;
+    std::deque<std::vector<rt_RELATION> > rels;
+    std::deque<rt_MATERIAL> mats;
+    std::deque<rt_CAMERA>   cams;
+    std::deque<rt_LIGHT>    lgts;
+    std::deque<rt_PLANE>    planes;
+    std::deque<rt_CYLINDER> cyls;
+    std::deque<rt_SPHERE>   sphs;
+    std::deque<rt_CONE>     cones;
+    std::deque<rt_PARABOLOID> pars;
+    std::deque<rt_HYPERBOLOID> hyps;
+    std::deque<rt_PARACYLINDER> pcyls;
+    std::deque<rt_HYPERCYLINDER> hcyls;
+    std::deque<rt_HYPERPARABOLOID> hpars;
+    int nsurf;          /* surfaces generated, in generation order */
+    int flags;
+
+    Scene() : nsurf(0), flags(0) { memset(&scn, 0, sizeof(scn)); }
+
+    rt_MATERIAL *material(int tag, rt_ui32 col, float dff, float spc, float pw,
+                          float rfl, float trn, float rfr, float ext)
+    {
+        rt_MATERIAL m;
+        memset(&m, 0, sizeof(m));
+        m.tag = tag;
+        m.tex.tag = RT_TEX_PCOLOR;
+        m.tex.col.val = col;
+        m.lgt[0] = dff; m.lgt[1] = spc; m.lgt[2] = pw; m.lgt[3] = 0.0f;
+        m.prp[0] = rfl; m.prp[1] = trn; m.prp[2] = rfr; m.prp[3] = ext;
+        mats.push_back(m);
+        return &mats.back();
+    }
+
+    /* hit-ID material: colour = (surface index + 1) * 2 + side */
+    rt_MATERIAL *id_material(int sidx, int side)
+    {
+        rt_ui32 id = (rt_ui32)((sidx + 1) * 2 + side) & 0xFFFFFF;
+        return material(RT_MAT_LIGHT, id, 1.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f, 0.0f);
+    }
+
+    void side(rt_SIDE *sd, rt_MATERIAL *m)
+    {
+        sd->scl[0] = 1.0f; sd->scl[1] = 1.0f; sd->rot = 0.0f;
+        sd->pos[0] = 0.0f; sd->pos[1] = 0.0f; sd->pmat = m;
+    }
+
+    void srf_init(rt_SURFACE *s, rt_MATERIAL *mo, rt_MATERIAL *mi)
+    {
+        for (int k = 0; k < 3; k++) { s->min[k] = -RT_INF; s->max[k] = +RT_INF; }
+        if (flags & QR_GEN_IDS)
+        {
+            mo = id_material(nsurf, 0);
+            mi = id_material(nsurf, 1);
+        }
+        side(&s->side_outer, mo);
+        side(&s->side_inner, mi);
+        nsurf++;
+    }
+
+    static void trm_set(rt_TRANSFORM3D *t, float sx, float sy, float sz,
+                        float rx, float ry, float rz, float px, float py, float pz)
+    {
+        t->scl[0] = sx; t->scl[1] = sy; t->scl[2] = sz;
+        t->rot[0] = rx; t->rot[1] = ry; t->rot[2] = rz;
+        t->pos[0] = px; t->pos[1] = py; t->pos[2] = pz;
+    }
+
+    static rt_OBJECT obj(int tag, void *p, int num)
+    {
+        rt_OBJECT o;
+        memset(&o, 0, sizeof(o));
+        trm_set(&o.trm, 1, 1, 1, 0, 0, 0, 0, 0, 0);
+        o.obj.tag = tag;
+        o.obj.pobj = p;
+        o.obj.obj_num = num;
+        return o;
+    }
+
+    rt_OBJECT camera(float px, float py, float pz, float rx, float ry, float rz,
+                     float pov, rt_ui32 amb_col, float amb_lum)
+    {
+        rt_CAMERA c;
+        memset(&c, 0, sizeof(c));
+        c.tag = RT_CAM_PLAIN;
+        c.col.val = amb_col;
+        c.lum[0] = amb_lum;
+        c.vpt[0] = pov;
+        cams.push_back(c);
+        rt_OBJECT o = obj(RT_TAG_CAMERA, &cams.back(), 1);
+        trm_set(&o.trm, 1, 1, 1, rx, ry, rz, px, py, pz);
+        return o;
+    }
+
+    rt_OBJECT light(float px, float py, float pz, rt_ui32 col, float lamb,
+                    float lsrc, float a_cnt, float a_lnr, float a_qdr)
+    {
+        rt_LIGHT l;
+        memset(&l, 0, sizeof(l));
+        l.tag = RT_LGT_PLAIN;
+        l.col.val = col;
+        l.lum[0] = lamb; l.lum[1] = lsrc;
+        l.atn[0] = 0.0f; l.atn[1] = a_cnt; l.atn[2] = a_lnr; l.atn[3] = a_qdr;
+        lgts.push_back(l);
+        rt_OBJECT o = obj(RT_TAG_LIGHT, &lgts.back(), 1);
+        o.trm.pos[0] = px; o.trm.pos[1] = py; o.trm.pos[2] = pz;
+        return o;
+    }
+
+    rt_OBJECT array(const std::vector<rt_OBJECT> &v,
+                    const std::vector<rt_RELATION> *rel = RT_NULL)
+    {
+        arrays.push_back(v);
+        rt_OBJECT o = obj(RT_TAG_ARRAY, arrays.back().data(), (int)v.size());
+        if (rel != RT_NULL && !rel->empty())
+        {
+            rels.push_back(*rel);
+            o.obj.prel = rels.back().data();
+            o.obj.rel_num = (int)rel->size();
+        }
+        return o;
+    }
+
+    rt_OBJECT plane(rt_MATERIAL *mo, rt_MATERIAL *mi)
+    {
+        rt_PLANE p; memset(&p, 0, sizeof(p));
+        srf_init(&p.srf, mo, mi);
+        planes.push_back(p);
+        return obj(RT_TAG_PLANE, &planes.back(), 1);
+    }
+
+    /* quadric of a given tag with shape parameters a, b and K-extent */
+    rt_OBJECT quadric(int tag, float a, float b, float kmin, float kmax,
+                      rt_MATERIAL *mo, rt_MATERIAL *mi)
+    {
+        rt_SURFACE *s = RT_NULL;
+        void *p = RT_NULL;
+        switch (tag)
+        {
+        case RT_TAG_CYLINDER:
+        { rt_CYLINDER q; memset(&q, 0, sizeof(q)); q.rad = a; cyls.push_back(q);
+          s = &cyls.back().srf; p = &cyls.back(); } break;
+        case RT_TAG_SPHERE:
+        { rt_SPHERE q; memset(&q, 0, sizeof(q)); q.rad = a; sphs.push_back(q);
+          s = &sphs.back().srf; p = &sphs.back(); } break;
+        case RT_TAG_CONE:
+        { rt_CONE q; memset(&q, 0, sizeof(q)); q.rat = a; cones.push_back(q);
+          s = &cones.back().srf; p = &cones.back(); } break;
+        case RT_TAG_PARABOLOID:
+        { rt_PARABOLOID q; memset(&q, 0, sizeof(q)); q.par = a; pars.push_back(q);
+          s = &pars.back().srf; p = &pars.back(); } break;
+        case RT_TAG_HYPERBOLOID:
+        { rt_HYPERBOLOID q; memset(&q, 0, sizeof(q)); q.rat = a; q.hyp = b;
+          hyps.push_back(q); s = &hyps.back().srf; p = &hyps.back(); } break;
+        case RT_TAG_PARACYLINDER:
+        { rt_PARACYLINDER q; memset(&q, 0, sizeof(q)); q.par = a;
+          pcyls.push_back(q); s = &pcyls.back().srf; p = &pcyls.back(); } break;
+        case RT_TAG_HYPERCYLINDER:
+        { rt_HYPERCYLINDER q; memset(&q, 0, sizeof(q)); q.rat = a; q.hyp = b;
+          hcyls.push_back(q); s = &hcyls.back().srf; p = &hcyls.back(); } break;
+        case RT_TAG_HYPERPARABOLOID:
+        { rt_HYPERPARABOLOID q; memset(&q, 0, sizeof(q)); q.pr1 = a; q.pr2 = b;
+          hpars.push_back(q); s = &hpars.back().srf; p = &hpars.back(); } break;
+        default: return obj(RT_TAG_ARRAY, RT_NULL, 0);
+        }
+        srf_init(s, mo, mi);
+        s->min[RT_K] = kmin;
+        s->max[RT_K] = kmax;
+        return obj(tag, p, 1);
+    }
+};
+
+static const int plain_tags[5] =
+{
+    RT_TAG_SPHERE, RT_TAG_CYLINDER, RT_TAG_CONE, RT_TAG_PARABOLOID,
+    RT_TAG_HYPERBOLOID
+};
+
+/* random quadric of one of the five plain kinds, radii/scales U[0.5,2] */
+static rt_OBJECT random_quadric(Scene &sc, Rng &r, rt_MATERIAL *mo,
+                                rt_MATERIAL *mi, int *ptag)
+{
+    int tag = plain_tags[r.ui(0, 4)];
+    float a = r.uf(0.5, 2.0), b = 0.0f, kmin = -RT_INF, kmax = +RT_INF;
+    switch (tag)
+    {
+    case RT_TAG_SPHERE: break;
+    case RT_TAG_CYLINDER:
+        kmax = r.uf(0.5, 2.0); kmin = -kmax; break;
+    case RT_TAG_CONE:
+        a = r.uf(0.3, 1.0); kmax = r.uf(0.5, 2.0); kmin = -kmax; break;
+    case RT_TAG_PARABOLOID:
+        kmax = r.uf(0.5, 2.0); break;
+    case RT_TAG_HYPERBOLOID:
+        a = r.uf(0.3, 1.0); b = r.uf(0.25, 1.5);
+        kmax = r.uf(0.5, 2.0); kmin = -kmax; break;
+    }
+    *ptag = tag;
+    return sc.quadric(tag, a, b, kmin, kmax, mo, mi);
+}
+
+static rt_MATERIAL *random_plain(Scene &sc, Rng &r)
+{
+    rt_ui32 col = pack_rgb(r.uf(0.2, 1.0), r.uf(0.2, 1.0), r.uf(0.2, 1.0));
+    float dff = r.uf(0.2, 0.9);
+    float spc = r.uf(0.1, 0.6);
+    float pw  = (float)r.ui(8, 64);
+    if (sc.flags & QR_GEN_NOSPEC) spc = 0.0f;
+    return sc.material(RT_MAT_PLAIN, col, dff, spc, pw, 0.0f, 0.0f, 1.0f, 0.0f);
+}
+
+/* camera at (0,-25,8) looking at the origin: rotation about X only,
+ * hor = +X, nrm = direction to the origin */
+static rt_OBJECT look_camera(Scene &sc, float px, float py, float pz,
+                             float fov_deg)
+{
+    double dy = -py, dz = -pz;
+    double ang = atan2(-dy, dz) * 180.0 / RT_PI;  /* nrm = (0,-sin,cos) */
+    float pov = (float)(0.5 / tan(0.5 * fov_deg * RT_PI / 180.0));
+    return sc.camera(px, py, pz, (float)ang, 0.0f, 0.0f, pov, 0xFFFFFF, 0.1f);
+}
+
+/* QR_SCN_PLAIN: ground plane + nq quadrics + 2 lights */
+static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
+{
+    Rng r(seed);
+    std::vector<rt_OBJECT> root;
+    root.push_back(look_camera(sc, 0.0f, -25.0f, 8.0f, 60.0f));
+    for (int i = 0; i < nl; i++)
+    {
+        float px = r.uf(-15, 15), py = r.uf(-15, 15), pz = r.uf(8, 15);
+        rt_ui32 col = pack_rgb(r.uf(0.3, 1.0), r.uf(0.3, 1.0), r.uf(0.3, 1.0));
+        if ((sc.flags & QR_GEN_ONELIGHT) && i > 0) continue;
+        root.push_back(sc.light(px, py, pz, col, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f));
+    }
+    rt_MATERIAL *gm = sc.material(RT_MAT_PLAIN, 0xB0B0A8, 0.8f,
+                                  (sc.flags & QR_GEN_NOSPEC) ? 0.0f : 0.2f, 16.0f,
+                                  0.0f, 0.0f, 1.0f, 0.0f);
+    root.push_back(sc.plane(gm, gm));
+    for (int i = 0; i < nq; i++)
+    {
+        rt_MATERIAL *m = random_plain(sc, r);
+        int tag;
+        rt_OBJECT q = random_quadric(sc, r, m, m, &tag);
+        float px = r.uf(-10, 10), py = r.uf(-10, 10), pz = r.uf(0.5, 5);
+        float rx = r.uf(-180, 180), ry = r.uf(-180, 180), rz = r.uf(-180, 180);
+        Scene::trm_set(&q.trm, 1, 1, 1, rx, ry, rz, px, py, pz);
+        root.push_back(q);
+    }
+    rt_OBJECT ro = sc.array(root);
+    sc.scn.root = ro.obj;
+    sc.scn.opts = 0;
+    sc.scn.lock = RT_NULL;
+}
+
+static Scene *build(int kind, uint64_t seed, int nq, int flags)
+{
+    Scene *sc = new Scene();
+    sc->flags = flags;
+    switch (kind)
+    {
+    case QR_SCN_PLAIN:
+    default:
+        build_plain(*sc, seed, nq > 0 ? nq : 16, 2);
+        break;
+    }
+    return sc;
+}
+
+} /* namespace qr_gen */
+
+#endif /* QR_SCENEGEN_HPP */
