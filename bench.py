@@ -1,0 +1,306 @@
+"""Benchmark of the GB300 QuadRay render path (rays/s, frames/s, latency).
+
+A step renders one frame of the workload.  ``value`` is rays/s with the scene
+resident in HBM and the frame written to device memory (CUDA events on the
+launching stream, L2 flushed between steps).  ``e2e`` is the same metric
+through the engine API (rt_Scene::render) with a host frame buffer: host
+update phases, scene upload, render and frame download inside the timed
+region.  Rays are traced segments (primary + shadow + reflected/refracted),
+counted in an instrumented launch of the same frame.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload plain|anim]
+"""
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+# algorithmic FP32 operations per unit of work (div / sqrt count 1, FMA 2;
+# this build issues no FMAs): per solver test, transform, clip evaluation,
+# shaded hit, light evaluation, refraction and reflection
+FLOPS = {
+    "test_plane": 3, "test_quadric": 40, "test_twoplane": 28, "xform": 33,
+    "clip_root": 12, "clip_custom": 15, "shade": 30, "light": 55,
+    "refract": 40, "reflect": 25,
+}
+STAT_NAMES = ["ray_primary", "ray_shadow", "ray_secondary", "test_plane",
+              "test_quadric", "test_twoplane", "xform", "clip_root",
+              "clip_custom", "shade", "light", "refract", "reflect"]
+
+WORKLOADS = {
+    # 800x480, 1 spp, 1 ground plane + 16 quadrics, 2 lights, shadows
+    "plain": dict(kind=1, seed=1, nq=16, w=800, h=480, fsaa=0, depth=10, anim=False),
+}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(qr, wl, seconds=12.0):
+    """The CPU restatement of the reference tracer on the host cores, on a
+    bounded band of rows of the same frame; returns rays/s and the setup."""
+    import build as oracle_build
+    O = oracle_build.load_oracle()
+    g = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)
+    f = qr.Flat(g, wl["w"], wl["h"], wl["fsaa"])
+    desc, params = f.update(0, wl["depth"])
+    cores = os.cpu_count() or 1
+    out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+    rows_done = [0]
+    rays = [0]
+    lock = threading.Lock()
+    t_end = time.perf_counter() + seconds
+
+    def worker(k):
+        y = k
+        while time.perf_counter() < t_end:
+            yy = y % params.y_res
+            nr = ctypes.c_uint64()
+            O.qr_oracle_render(ctypes.addressof(desc), ctypes.addressof(params),
+                               out.ctypes.data, yy, yy + 1, ctypes.byref(nr))
+            with lock:
+                rows_done[0] += 1
+                rays[0] += nr.value
+            y += cores
+
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=worker, args=(k,)) for k in range(cores)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    dt = time.perf_counter() - t0
+    return {"value": rays[0] / dt, "unit": "rays/s", "cores": cores, "kind": "port",
+            "sample": "%d rows of the %dx%d frame (%.1f s, %d threads)" % (
+                rows_done[0], wl["w"], wl["h"], dt, cores)}
+
+
+def run_reference(args, wl):
+    qr = importlib.import_module("quadray-engine_gb300")
+    vals = []
+    cb = None
+    for _ in range(args.warmup):
+        cpu_baseline(qr, wl, seconds=1.0)
+    for _ in range(args.steps):
+        cb = cpu_baseline(qr, wl, seconds=max(2.0, 20.0 / max(1, args.steps)))
+        vals.append(cb["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": "rays_per_s", "value": v, "unit": "rays/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, **{k: wl[k] for k in ("w", "h", "fsaa", "nq", "seed")}},
+            "cpu_baseline": {"value": v, "unit": "rays/s", "cores": cb["cores"],
+                             "kind": cb["kind"], "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plain", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    wl = WORKLOADS[args.workload]
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, wl)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    qr = importlib.import_module("quadray-engine_gb300")
+    gen = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)
+    flat = qr.Flat(gen, wl["w"], wl["h"], wl["fsaa"])
+    desc, params = flat.update(0, wl["depth"])
+    ctx = qr.Context(local)
+    sid = ctx.upload(desc)
+
+    # instrumented launch: rays and work counters of one frame
+    counts = (ctypes.c_uint64 * 13)()
+    host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+    rc = qr.lib().qr_render_stats(ctx.h, sid, ctypes.byref(params),
+                                  host.ctypes.data_as(ctypes.c_void_p), counts)
+    assert rc == 0, ctx.error()
+    stats = dict(zip(STAT_NAMES, [int(c) for c in counts]))
+    rays = stats["ray_primary"] + stats["ray_shadow"] + stats["ray_secondary"]
+    flops = sum(stats[k] * v for k, v in FLOPS.items())
+
+    frame = torch.empty((params.y_res, params.x_row), dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    for _ in range(args.warmup):
+        ctx.render_device(sid, params, frame.data_ptr(), sp)
+    torch.cuda.synchronize()
+
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        ctx.render_device(sid, params, frame.data_ptr(), sp)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(ms) / 1000.0
+    if dist is not None:
+        tt = torch.tensor([t_total], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+        dist.barrier()
+    value = rays * args.steps * world / t_total
+    fps = args.steps * world / t_total
+
+    # end to end through the engine API with a host frame buffer
+    eng = qr.Engine(qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0), wl["w"], wl["h"],
+                    fsaa=wl["fsaa"], depth=wl["depth"])
+    hbuf = np.zeros((wl["h"], wl["w"]), dtype=np.uint32)
+    for i in range(args.warmup):
+        eng.render(0, hbuf)
+    lat = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        eng.render(0, hbuf)
+        lat.append(time.perf_counter() - t0)
+    e2e_t = sum(lat)
+    h2d = (desc.nsrf * 256 + desc.nmat * 96 + desc.nlgt * 48 + desc.nelem * 16 +
+           desc.nlelem * 16 + desc.ntex * 4)
+    d2h = wl["w"] * wl["h"] * 4
+    eng.close()
+
+    pk, pk_kind = peaks()
+    sm_mhz = pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12   # TFLOP/s, FMA = 2
+    achieved = flops * args.steps / t_total / 1e12
+    line = {
+        "metric": "rays_per_s", "value": value, "unit": "rays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * t_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "width": wl["w"], "height": wl["h"],
+                   "fsaa": wl["fsaa"], "quadrics": wl["nq"], "seed": wl["seed"],
+                   "depth": wl["depth"], "rays_per_frame": rays,
+                   "l2": "256 MiB buffer written between timed steps",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "frames_per_s": fps,
+        "frame_ms_p50": float(np.percentile(ms, 50)),
+        "frame_ms_p99": float(np.percentile(ms, 99)),
+        "e2e": {"value": rays * args.steps / e2e_t, "unit": "rays/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "frame_ms_p50": 1000.0 * float(np.percentile(lat, 50)),
+                "frame_ms_p99": 1000.0 * float(np.percentile(lat, 99))},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x max clock)",
+                     "flops_per_frame": flops},
+        "work": stats,
+        "gpu_launches": args.steps,
+        "clocks": ck,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(qr, wl)
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

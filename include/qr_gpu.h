@@ -185,6 +185,28 @@ int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                    uint32_t *host_frame);
 int qr_sync(qr_ctx *ctx, void *stream);
 
+/* instrumented render: counts the work of one frame (traced segments by
+ * kind, solver tests, clip evaluations, shaded hits, light evaluations) into
+ * counts[QR_STAT_*]; the frame is rendered into host_frame as usual.  Used to
+ * derive rays/s and the algorithmic FLOPs of the roofline; the counters are
+ * never compiled into timed launches */
+#define QR_STAT_RAY_PRIMARY     0
+#define QR_STAT_RAY_SHADOW      1
+#define QR_STAT_RAY_SECONDARY   2
+#define QR_STAT_TEST_PLANE      3
+#define QR_STAT_TEST_QUADRIC    4
+#define QR_STAT_TEST_TWOPLANE   5
+#define QR_STAT_XFORM           6
+#define QR_STAT_CLIP_ROOT       7
+#define QR_STAT_CLIP_CUSTOM     8
+#define QR_STAT_SHADE           9
+#define QR_STAT_LIGHT           10
+#define QR_STAT_REFRACT         11
+#define QR_STAT_REFLECT         12
+#define QR_STAT_COUNT           13
+int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                    uint32_t *host_frame, uint64_t *counts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,51 @@
+"""Build the test oracle (TEST INFRASTRUCTURE ONLY).
+
+``build_oracle()`` compiles the CPU restatement ``qr_oracle.c`` into
+``oracle/_build/libqr_oracle.so`` (plain C, ``-ffp-contract=off``, no
+fast-math).  ``build_ref()`` compiles the reference engine's own renderer
+from its sources with ``oracle/Makefile`` into ``oracle/_ref/`` when the
+reference tree is available (the golden-fixture generator uses it).
+
+``load_oracle()`` returns a ctypes handle; only tests, the graft smoke check
+and the CPU-baseline leg of bench.py call it.
+"""
+import ctypes
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libqr_oracle.so")
+REF_DIR = os.environ.get("QR_REFERENCE", "/root/reference")
+REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+
+
+def build_oracle():
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "qr_oracle.c")
+    deps = [src, os.path.join(HERE, "qr_oracle.h"), os.path.join(ROOT, "include", "qr_gpu.h")]
+    if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
+        return LIB
+    cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c99", "-fPIC", "-shared",
+           "-ffp-contract=off", "-fno-fast-math", "-I" + HERE,
+           "-I" + os.path.join(ROOT, "include"), src, "-lm", "-o", LIB]
+    subprocess.run(cmd, check=True)
+    return LIB
+
+
+def build_ref():
+    """Build oracle/_ref/ref_driver from the reference sources, if present."""
+    if not os.path.isdir(os.path.join(REF_DIR, "core", "engine")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_DIR], check=True,
+                   stdout=subprocess.DEVNULL)
+    return REF_DRIVER
+
+
+def load_oracle():
+    L = ctypes.CDLL(build_oracle())
+    L.qr_oracle_render.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(ctypes.c_uint64)]
+    return L

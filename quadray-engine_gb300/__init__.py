@@ -1,0 +1,259 @@
+"""GB300 QuadRay engine: Python host bindings.
+
+Thin ctypes layer over ``_build/libquadray_gb300.so`` (built by
+``build.py``): seeded synthetic scenes, the host flattening (no GPU needed),
+the C ABI of ``include/qr_gpu.h`` and the ``rt_Scene`` engine API.  The
+render itself always runs in the CUDA library; there is no CPU fallback and
+loading fails loudly if the library is missing.
+
+The directory name is not a Python identifier, so import it with
+``importlib.import_module("quadray-engine_gb300")`` after putting the repo
+root on ``sys.path``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libquadray_gb300.so")
+
+# scene kinds and generator flags (csrc/scenegen.hpp)
+SCN_PLAIN = 1
+SCN_ANIM = 2
+SCN_PT = 3
+GEN_IDS = 1 << 0
+
+# runtime options (csrc/format.h): -1 selects the default (FULL minus the
+# scene's opt-outs)
+OPTS_DEFAULT = -1
+OPTS_NONE = (1 << 20) | (1 << 21) | (1 << 25)
+
+QR_OK = 0
+
+
+class QrSceneDesc(ctypes.Structure):
+    """qr_scene_desc of include/qr_gpu.h."""
+    _fields_ = [
+        ("nsrf", ctypes.c_int32), ("srf", ctypes.c_void_p),
+        ("nmat", ctypes.c_int32), ("mat", ctypes.c_void_p),
+        ("nlgt", ctypes.c_int32), ("lgt", ctypes.c_void_p),
+        ("nelem", ctypes.c_int32), ("elems", ctypes.c_void_p),
+        ("nlelem", ctypes.c_int32), ("lelems", ctypes.c_void_p),
+        ("ntex", ctypes.c_int32), ("texels", ctypes.c_void_p),
+        ("cam_off", ctypes.c_int32), ("cam_num", ctypes.c_int32),
+    ]
+
+
+class QrFrameParams(ctypes.Structure):
+    """qr_frame_params of include/qr_gpu.h."""
+    _fields_ = [
+        ("org", ctypes.c_float * 3), ("t_min", ctypes.c_float),
+        ("dir", ctypes.c_float * 3), ("t_max", ctypes.c_float),
+        ("hor", ctypes.c_float * 3), ("pad0", ctypes.c_float),
+        ("ver", ctypes.c_float * 3), ("pad1", ctypes.c_float),
+        ("amb", ctypes.c_float * 3), ("l_amb", ctypes.c_float),
+        ("x_res", ctypes.c_int32), ("y_res", ctypes.c_int32),
+        ("x_row", ctypes.c_int32), ("fsaa", ctypes.c_int32),
+        ("depth", ctypes.c_int32), ("ctx_props", ctypes.c_int32),
+        ("pt_on", ctypes.c_int32), ("frame_idx", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+        ("pts_c", ctypes.c_float), ("pad2", ctypes.c_float),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libquadray_gb300.so is not built: run "
+                               "quadray-engine_gb300/build.py (or "
+                               "__graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, i64, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_ulonglong
+        L.qrpy_gen_new.restype = vp
+        L.qrpy_gen_new.argtypes = [i32, u64, i32, i32]
+        L.qrpy_gen_free.argtypes = [vp]
+        L.qrpy_gen_nsurf.argtypes = [vp]
+        L.qrpy_flat_new.restype = vp
+        L.qrpy_flat_new.argtypes = [vp, i32, i32, i32, i32]
+        L.qrpy_flat_update.argtypes = [vp, i64, i32]
+        L.qrpy_flat_desc.argtypes = [vp, ctypes.POINTER(QrSceneDesc),
+                                     ctypes.POINTER(QrFrameParams)]
+        L.qrpy_flat_free.argtypes = [vp]
+        L.qrpy_scene_new.restype = vp
+        L.qrpy_scene_new.argtypes = [vp, i32, i32, i32, i32, i32]
+        L.qrpy_scene_render.argtypes = [vp, i64, vp]
+        L.qrpy_scene_render_device.argtypes = [vp, i64, vp, vp]
+        L.qrpy_scene_ctx.restype = vp
+        L.qrpy_scene_ctx.argtypes = [vp]
+        L.qrpy_scene_free.argtypes = [vp]
+        L.qr_ctx_create.argtypes = [i32, ctypes.POINTER(vp)]
+        L.qr_ctx_destroy.argtypes = [vp]
+        L.qr_last_error.restype = ctypes.c_char_p
+        L.qr_last_error.argtypes = [vp]
+        L.qr_scene_upload.argtypes = [vp, ctypes.POINTER(QrSceneDesc),
+                                      ctypes.POINTER(ctypes.c_int)]
+        L.qr_scene_update.argtypes = [vp, i32, ctypes.POINTER(QrSceneDesc)]
+        L.qr_scene_release.argtypes = [vp, i32]
+        L.qr_render_device.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp, vp]
+        L.qr_render_host.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp]
+        L.qr_sync.argtypes = [vp, vp]
+        L.qr_render_stats.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp,
+                                      ctypes.POINTER(ctypes.c_uint64)]
+        _lib = L
+    return _lib
+
+
+class GenScene:
+    """A seeded synthetic scene in the scene-struct format (scenegen.hpp)."""
+
+    def __init__(self, kind=SCN_PLAIN, seed=1, nq=16, flags=0):
+        self.kind, self.seed, self.nq, self.flags = kind, seed, nq, flags
+        self.h = lib().qrpy_gen_new(kind, seed, nq, flags)
+        if not self.h:
+            raise RuntimeError("scene generation failed")
+
+    @property
+    def nsurf(self):
+        return lib().qrpy_gen_nsurf(self.h)
+
+    def close(self):
+        if self.h:
+            lib().qrpy_gen_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Flat:
+    """Host flattening of a scene (update phases); CPU only."""
+
+    def __init__(self, gen, x_res, y_res, fsaa=0, opts=OPTS_DEFAULT):
+        self.gen = gen
+        self.h = lib().qrpy_flat_new(gen.h, opts, x_res, y_res, fsaa)
+        if not self.h:
+            raise RuntimeError("flattening failed")
+        self.desc = QrSceneDesc()
+        self.params = QrFrameParams()
+
+    def update(self, time=0, depth=10):
+        rc = lib().qrpy_flat_update(self.h, int(time), int(depth))
+        if rc != QR_OK:
+            raise RuntimeError("update failed: %d" % rc)
+        lib().qrpy_flat_desc(self.h, ctypes.byref(self.desc), ctypes.byref(self.params))
+        return self.desc, self.params
+
+    def close(self):
+        if self.h:
+            lib().qrpy_flat_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """A device context of the C ABI (qr_ctx)."""
+
+    def __init__(self, device=0):
+        p = ctypes.c_void_p()
+        rc = lib().qr_ctx_create(device, ctypes.byref(p))
+        if rc != QR_OK:
+            raise RuntimeError("qr_ctx_create failed: %d" % rc)
+        self.h = p
+
+    def error(self):
+        return lib().qr_last_error(self.h).decode()
+
+    def upload(self, desc):
+        sid = ctypes.c_int(-1)
+        rc = lib().qr_scene_upload(self.h, ctypes.byref(desc), ctypes.byref(sid))
+        if rc != QR_OK:
+            raise RuntimeError("qr_scene_upload: %d %s" % (rc, self.error()))
+        return sid.value
+
+    def update(self, sid, desc):
+        rc = lib().qr_scene_update(self.h, sid, ctypes.byref(desc))
+        if rc != QR_OK:
+            raise RuntimeError("qr_scene_update: %d %s" % (rc, self.error()))
+
+    def render_host(self, sid, params):
+        out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+        rc = lib().qr_render_host(self.h, sid, ctypes.byref(params),
+                                  out.ctypes.data_as(ctypes.c_void_p))
+        if rc != QR_OK:
+            raise RuntimeError("qr_render_host: %d %s" % (rc, self.error()))
+        return out[:, :params.x_res]
+
+    def render_device(self, sid, params, dev_ptr, stream=0):
+        rc = lib().qr_render_device(self.h, sid, ctypes.byref(params),
+                                    ctypes.c_void_p(dev_ptr), ctypes.c_void_p(stream))
+        if rc != QR_OK:
+            raise RuntimeError("qr_render_device: %d %s" % (rc, self.error()))
+
+    def sync(self, stream=0):
+        rc = lib().qr_sync(self.h, ctypes.c_void_p(stream))
+        if rc != QR_OK:
+            raise RuntimeError("qr_sync: %d %s" % (rc, self.error()))
+
+    def close(self):
+        if self.h:
+            lib().qr_ctx_destroy(self.h)
+            self.h = None
+
+
+class Engine:
+    """rt_Platform + rt_Scene over a generated scene (the user-facing API)."""
+
+    def __init__(self, gen, x_res, y_res, fsaa=0, opts=OPTS_DEFAULT, depth=10):
+        self.gen = gen
+        self.x_res, self.y_res = x_res, y_res
+        self.h = lib().qrpy_scene_new(gen.h, x_res, y_res, fsaa, opts, depth)
+        if not self.h:
+            raise RuntimeError("rt_Scene construction failed")
+
+    def render(self, time=0, out=None):
+        if out is None:
+            out = np.zeros((self.y_res, self.x_res), dtype=np.uint32)
+        rc = lib().qrpy_scene_render(self.h, int(time), out.ctypes.data_as(ctypes.c_void_p))
+        if rc != QR_OK:
+            raise RuntimeError("render failed: %d" % rc)
+        return out
+
+    def render_device(self, time, dev_ptr, stream=0):
+        rc = lib().qrpy_scene_render_device(self.h, int(time), ctypes.c_void_p(dev_ptr),
+                                            ctypes.c_void_p(stream))
+        if rc != QR_OK:
+            raise RuntimeError("render_device failed: %d" % rc)
+
+    def close(self):
+        if self.h:
+            lib().qrpy_scene_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def build(verbose=False, force=False):
+    """Compile the CUDA library (see build.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("qr_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose, force=force)

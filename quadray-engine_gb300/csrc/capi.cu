@@ -1,0 +1,337 @@
+/*
+ * capi.cu: C ABI of the GB300 render backend (include/qr_gpu.h).
+ *
+ * A context owns device-resident scenes (flattened records copied once and
+ * replaced in place on update) and a device frame buffer for host renders.
+ * Every entry point returns a status code and never throws; CUDA errors are
+ * kept in the context's message buffer.
+ */
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+#include <new>
+#include <vector>
+
+#include "qr_gpu.h"
+#include "tracer.cuh"
+
+/* device stack per thread: the tracer recurses for refracted and reflected
+ * rays, up to the scene's depth (at most QR_MAX_DEPTH levels) */
+#define QR_MAX_DEPTH        10
+#define QR_STACK_BYTES      (24 * 1024)
+
+struct qr_scene_slot
+{
+    int          used;
+    void        *block;     /* one device allocation for all arrays */
+    size_t       bytes;
+    qr_dscene    d;
+    qr_scene_desc shape;    /* sizes of the uploaded arrays */
+};
+
+struct qr_ctx
+{
+    int          device;
+    char         err[256];
+    std::vector<qr_scene_slot> scenes;
+    uint32_t    *dframe;    /* frame buffer for qr_render_host */
+    size_t       dframe_px;
+    cudaStream_t stream;
+};
+
+static int fail(qr_ctx *ctx, int code, const char *what, cudaError_t e)
+{
+    if (ctx != NULL)
+    {
+        snprintf(ctx->err, sizeof(ctx->err), "%s: %s", what,
+                 e == cudaSuccess ? "error" : cudaGetErrorString(e));
+    }
+    return code;
+}
+
+extern "C" int qr_ctx_create(int device, qr_ctx **out)
+{
+    if (out == NULL) return QR_ERR_ARG;
+    *out = NULL;
+    qr_ctx *ctx = new (std::nothrow) qr_ctx();
+    if (ctx == NULL) return QR_ERR_OOM;
+    ctx->device = device;
+    ctx->err[0] = 0;
+    ctx->dframe = NULL;
+    ctx->dframe_px = 0;
+    ctx->stream = 0;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceSetLimit(cudaLimitStackSize, QR_STACK_BYTES);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+    {
+        fprintf(stderr, "qr_ctx_create: %s\n", cudaGetErrorString(e));
+        delete ctx;
+        return QR_ERR_CUDA;
+    }
+    *out = ctx;
+    return QR_OK;
+}
+
+extern "C" int qr_ctx_destroy(qr_ctx *ctx)
+{
+    if (ctx == NULL) return QR_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    for (size_t i = 0; i < ctx->scenes.size(); i++)
+    {
+        if (ctx->scenes[i].used) cudaFree(ctx->scenes[i].block);
+    }
+    if (ctx->dframe) cudaFree(ctx->dframe);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return QR_OK;
+}
+
+extern "C" const char *qr_last_error(qr_ctx *ctx)
+{
+    return ctx == NULL ? "null context" : ctx->err;
+}
+
+static size_t al16(size_t n) { return (n + 255) & ~(size_t)255; }
+
+static int check_desc(const qr_scene_desc *d)
+{
+    if (d == NULL) return QR_ERR_ARG;
+    if (d->nsrf < 0 || d->nmat < 0 || d->nlgt < 0 || d->nelem < 0 ||
+        d->nlelem < 0 || d->ntex < 0) return QR_ERR_ARG;
+    if ((d->nsrf && !d->srf) || (d->nmat && !d->mat) || (d->nlgt && !d->lgt) ||
+        (d->nelem && !d->elems) || (d->nlelem && !d->lelems) ||
+        (d->ntex && !d->texels)) return QR_ERR_ARG;
+    if (d->cam_off < 0 || d->cam_num < 0 || d->cam_off + d->cam_num > d->nelem)
+        return QR_ERR_ARG;
+    /* every index the kernel follows must stay in bounds */
+    for (int i = 0; i < d->nelem; i++)
+    {
+        const qr_elem &e = d->elems[i];
+        if (e.kind == QR_ELM_SURFACE || e.kind == QR_ELM_TRNODE)
+        {
+            if (e.ref < 0 || e.ref >= d->nsrf) return QR_ERR_ARG;
+        }
+        else if (e.kind != QR_ELM_ACC_ENTER && e.kind != QR_ELM_ACC_LEAVE)
+        {
+            return QR_ERR_ARG;
+        }
+    }
+    for (int i = 0; i < d->nsrf; i++)
+    {
+        const qr_srf &s = d->srf[i];
+        if (s.is_node) continue;
+        for (int k = 0; k < 2; k++)
+        {
+            if (s.mat[k] < 0 || s.mat[k] >= d->nmat) return QR_ERR_ARG;
+            if (s.lgt_off[k] < 0 || s.lgt_off[k] + s.lgt_num[k] > d->nlelem) return QR_ERR_ARG;
+            if (s.sec_off[k] < 0 || s.sec_off[k] + s.sec_num[k] > d->nelem) return QR_ERR_ARG;
+        }
+        if (s.clip_off < 0 || s.clip_off + s.clip_num > d->nelem) return QR_ERR_ARG;
+        if (s.trnode >= d->nsrf) return QR_ERR_ARG;
+        for (int k = 0; k < 3; k++)
+            if (s.amap[k] < 0 || s.amap[k] > 2) return QR_ERR_ARG;
+    }
+    for (int i = 0; i < d->nlelem; i++)
+    {
+        const qr_lelem &l = d->lelems[i];
+        if (l.light < 0 || l.light >= d->nlgt) return QR_ERR_ARG;
+        if (l.shd_off < 0 || l.shd_off + l.shd_num > d->nelem) return QR_ERR_ARG;
+    }
+    for (int i = 0; i < d->nmat; i++)
+    {
+        const qr_mat &m = d->mat[i];
+        long span = (long)(m.xmask + 1) * (long)((m.ymask + 1) << m.yshft);
+        if (m.tex_off < 0 || m.tex_off >= d->ntex) return QR_ERR_ARG;
+        if ((m.props & QR_PROP_TEXTURE) && m.tex_off + span > d->ntex) return QR_ERR_ARG;
+    }
+    return QR_OK;
+}
+
+/* copy a scene's arrays into one device block (or into an existing one) */
+static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool fresh)
+{
+    size_t o_srf = 0;
+    size_t o_mat = o_srf + al16(sizeof(qr_srf) * d->nsrf);
+    size_t o_lgt = o_mat + al16(sizeof(qr_mat) * d->nmat);
+    size_t o_elm = o_lgt + al16(sizeof(qr_light) * d->nlgt);
+    size_t o_lel = o_elm + al16(sizeof(qr_elem) * d->nelem);
+    size_t o_tex = o_lel + al16(sizeof(qr_lelem) * d->nlelem);
+    size_t total = o_tex + al16(sizeof(uint32_t) * d->ntex);
+
+    std::vector<unsigned char> h(total, 0);
+    memcpy(&h[o_srf], d->srf, sizeof(qr_srf) * d->nsrf);
+    memcpy(&h[o_mat], d->mat, sizeof(qr_mat) * d->nmat);
+    memcpy(&h[o_lgt], d->lgt, sizeof(qr_light) * d->nlgt);
+    memcpy(&h[o_elm], d->elems, sizeof(qr_elem) * d->nelem);
+    memcpy(&h[o_lel], d->lelems, sizeof(qr_lelem) * d->nlelem);
+    memcpy(&h[o_tex], d->texels, sizeof(uint32_t) * d->ntex);
+
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaSetDevice", e);
+    if (fresh || sl.bytes < total)
+    {
+        if (!fresh && sl.block) cudaFree(sl.block);
+        sl.block = NULL;
+        e = cudaMalloc(&sl.block, total);
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaMalloc scene", e);
+        sl.bytes = total;
+    }
+    e = cudaMemcpyAsync(sl.block, h.data(), total, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "scene copy", e);
+
+    unsigned char *b = (unsigned char *)sl.block;
+    sl.d.srf = (const qr_srf *)(b + o_srf);
+    sl.d.mat = (const qr_mat *)(b + o_mat);
+    sl.d.lgt = (const qr_light *)(b + o_lgt);
+    sl.d.elems = (const qr_elem *)(b + o_elm);
+    sl.d.lelems = (const qr_lelem *)(b + o_lel);
+    sl.d.texels = (const uint32_t *)(b + o_tex);
+    sl.d.nsrf = d->nsrf; sl.d.nmat = d->nmat; sl.d.nlgt = d->nlgt;
+    sl.d.nelem = d->nelem; sl.d.nlelem = d->nlelem; sl.d.ntex = d->ntex;
+    sl.d.cam_off = d->cam_off;
+    sl.d.cam_num = d->cam_num;
+    sl.shape = *d;
+    return QR_OK;
+}
+
+extern "C" int qr_scene_upload(qr_ctx *ctx, const qr_scene_desc *desc, int *scene_id)
+{
+    if (ctx == NULL || scene_id == NULL) return QR_ERR_ARG;
+    int rc = check_desc(desc);
+    if (rc != QR_OK) return rc;
+    qr_scene_slot sl;
+    memset(&sl, 0, sizeof(sl));
+    rc = upload(ctx, sl, desc, true);
+    if (rc != QR_OK) return rc;
+    sl.used = 1;
+    for (size_t i = 0; i < ctx->scenes.size(); i++)
+    {
+        if (!ctx->scenes[i].used)
+        {
+            ctx->scenes[i] = sl;
+            *scene_id = (int)i;
+            return QR_OK;
+        }
+    }
+    ctx->scenes.push_back(sl);
+    *scene_id = (int)ctx->scenes.size() - 1;
+    return QR_OK;
+}
+
+static qr_scene_slot *slot(qr_ctx *ctx, int id)
+{
+    if (ctx == NULL || id < 0 || id >= (int)ctx->scenes.size()) return NULL;
+    if (!ctx->scenes[id].used) return NULL;
+    return &ctx->scenes[id];
+}
+
+extern "C" int qr_scene_update(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    int rc = check_desc(desc);
+    if (rc != QR_OK) return rc;
+    return upload(ctx, *sl, desc, false);
+}
+
+extern "C" int qr_scene_release(qr_ctx *ctx, int scene_id)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    cudaSetDevice(ctx->device);
+    cudaFree(sl->block);
+    memset(sl, 0, sizeof(*sl));
+    return QR_OK;
+}
+
+static int check_fp(const qr_frame_params *fp)
+{
+    if (fp == NULL) return QR_ERR_ARG;
+    if (fp->x_res <= 0 || fp->y_res <= 0 || fp->x_row < fp->x_res) return QR_ERR_ARG;
+    if (fp->x_res > 16384 || fp->y_res > 16384) return QR_ERR_LIMIT;
+    if (fp->fsaa != 0 && fp->fsaa != 2) return QR_ERR_ARG;
+    if (fp->depth < 0 || fp->depth > QR_MAX_DEPTH) return QR_ERR_LIMIT;
+    return QR_OK;
+}
+
+extern "C" int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                                uint32_t *dev_frame, void *stream)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    int rc = check_fp(fp);
+    if (rc != QR_OK) return rc;
+    if (dev_frame == NULL) return QR_ERR_ARG;
+    cudaError_t e = qr_launch_whitted(sl->d, *fp, dev_frame, NULL,
+                                      (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "whitted launch", e);
+    return QR_OK;
+}
+
+extern "C" int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                              uint32_t *host_frame)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    int rc = check_fp(fp);
+    if (rc != QR_OK) return rc;
+    if (host_frame == NULL) return QR_ERR_ARG;
+    size_t px = (size_t)fp->x_row * fp->y_res;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess && ctx->dframe_px < px)
+    {
+        if (ctx->dframe) cudaFree(ctx->dframe);
+        ctx->dframe = NULL;
+        e = cudaMalloc(&ctx->dframe, px * sizeof(uint32_t));
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaMalloc frame", e);
+        ctx->dframe_px = px;
+    }
+    if (e == cudaSuccess) e = qr_launch_whitted(sl->d, *fp, ctx->dframe, NULL, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host_frame, ctx->dframe, px * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "render host", e);
+    return QR_OK;
+}
+
+extern "C" int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                               uint32_t *host_frame, uint64_t *counts)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    int rc = check_fp(fp);
+    if (rc != QR_OK) return rc;
+    if (host_frame == NULL || counts == NULL) return QR_ERR_ARG;
+    size_t px = (size_t)fp->x_row * fp->y_res;
+    uint32_t *dframe = NULL;
+    qr_dstats *dst = NULL;
+    qr_dstats hst;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaMalloc(&dframe, px * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&dst, sizeof(qr_dstats));
+    if (e == cudaSuccess) e = cudaMemsetAsync(dst, 0, sizeof(qr_dstats), ctx->stream);
+    if (e == cudaSuccess) e = qr_launch_whitted(sl->d, *fp, dframe, dst, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host_frame, dframe, px * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&hst, dst, sizeof(qr_dstats), cudaMemcpyDeviceToHost,
+                            ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (dframe) cudaFree(dframe);
+    if (dst) cudaFree(dst);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "render stats", e);
+    for (int k = 0; k < QR_STAT_COUNT; k++) counts[k] = hst.c[k];
+    return QR_OK;
+}
+
+extern "C" int qr_sync(qr_ctx *ctx, void *stream)
+{
+    if (ctx == NULL) return QR_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(stream ? (cudaStream_t)stream : ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "sync", e);
+    return QR_OK;
+}

@@ -1,0 +1,1064 @@
+/*
+ * tracer.cu: sm_103a Whitted ray tracer of the GB300 QuadRay engine.
+ *
+ * One thread traces one pixel (or one AA sample) through the flattened scene
+ * of qr_gpu.h: ray generation, list walk with plane / quadric / two-plane
+ * solvers, clipping (axis boxes, custom clippers, boolean accumulators, conic
+ * apex adjustment), shading with hard shadows to every light, refraction and
+ * reflection with Fresnel, and the 8-bit pack.  The arithmetic restates the
+ * reference's fp32 SIMD tracer (VectorChief/QuadRay-engine
+ * core/tracer/tracer.cpp render0, 2086-7622) operation by operation so the
+ * frames are bit-identical to the reference's CPU render; it is compiled with
+ * -fmad=false -prec-div=true -prec-sqrt=true -ftz=false, and divisions and
+ * square roots use the IEEE round-to-nearest intrinsics.
+ *
+ * Per-lane view of the reference's SIMD masks: the reference shades every
+ * surface that is nearest so far; per lane that is the nearest hit in walk
+ * order (a later hit wins only if strictly nearer), which is what this kernel
+ * keeps and shades once.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <float.h>
+
+#include "tracer.cuh"
+
+#define FLAG_PASS   2
+#define FLAG_SHAD   4
+#define SIDE_OUTER  0
+#define SIDE_INNER  1
+#define D_EPS       0.00000000001f  /* root-sorting threshold, object.h:41 */
+#define T_EPS       0.0000001f      /* root-split threshold, object.h:42 */
+#define SIGN_BIT    0x80000000u
+
+namespace qr_dev
+{
+
+/* work counters of instrumented launches (st == NULL in timed launches) */
+#define CNT(k) do { if (st != NULL) atomicAdd(&st->c[k], 1ull); } while (0)
+
+struct Ray
+{
+    float org[3];
+    float dir[3];
+    float t_min, t_max;
+    int   from;         /* originating surface, -1 for camera rays */
+    int   flags;        /* side | pass | shadow */
+    float phit[3];      /* originating surface's local hit */
+    int   depth;        /* remaining secondary-ray depth */
+};
+
+struct Hit
+{
+    int   srf;
+    int   side;
+    float hit[3];
+    float loc[3];
+};
+
+struct Walk
+{
+    int   shadow;
+    int   occluded;
+    float tbuf;
+    Hit   best;
+};
+
+__device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
+__device__ __forceinline__ float u2f(uint32_t u) { return __uint_as_float(u); }
+__device__ __forceinline__ float fxor(float a, uint32_t m) { return u2f(f2u(a) ^ m); }
+__device__ __forceinline__ uint32_t sgnbit(float a) { return f2u(a) & SIGN_BIT; }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+/* full-precision rsqrt of the reference's compat mode: 1 / sqrt(x) */
+__device__ __forceinline__ float rsq(float x) { return __fdiv_rn(1.0f, __fsqrt_rn(x)); }
+
+/* transform-node matrix times vector, diagonal first (tracer.cpp:2537-2568) */
+__device__ __forceinline__ void xform(const qr_srf *__restrict__ t,
+                                      const float v[3], float o[3])
+{
+    const int am = __ldg(&t->amap[3]);
+    float x = __ldg(&t->tci[0]) * v[0];
+    float y = __ldg(&t->tcj[1]) * v[1];
+    float z = __ldg(&t->tck[2]) * v[2];
+    if (am != 1)
+    {
+        x = x + __ldg(&t->tci[1]) * v[1];
+        x = x + __ldg(&t->tci[2]) * v[2];
+        y = y + __ldg(&t->tcj[0]) * v[0];
+        y = y + __ldg(&t->tcj[2]) * v[2];
+        z = z + __ldg(&t->tck[0]) * v[0];
+        z = z + __ldg(&t->tck[1]) * v[1];
+    }
+    o[0] = x; o[1] = y; o[2] = z;
+}
+
+/* clipping subroutine for one root (tracer.cpp:2686-3249) */
+__device__ int clip_root(const qr_dscene &S, const Ray &r, int si, float t,
+                         float tbuf, const float ldff[3], const float lray[3],
+                         int side, int dmask, uint32_t amask, float hit[3],
+                         float loc[3], qr_dstats *st)
+{
+    CNT(QR_STAT_CLIP_ROOT);
+    const qr_srf *__restrict__ s = &S.srf[si];
+    int valid = (tbuf > t) && (r.t_min < t);
+
+    #pragma unroll
+    for (int k = 0; k < 3; k++) hit[k] = r.dir[k] * t + r.org[k];
+
+    const int am3 = __ldg(&s->amap[3]);
+    if (am3 != 0)
+    {
+        #pragma unroll
+        for (int k = 0; k < 3; k++) loc[k] = lray[k] * t + ldff[k];
+    }
+    else
+    {
+        #pragma unroll
+        for (int k = 0; k < 3; k++) loc[k] = hit[k] - __ldg(&s->pos[k]);
+    }
+
+    const int conic = __ldg(&s->conic);
+    if (conic != 0 && dmask)
+    {
+        /* conic singularity adjustment near the apex (2795-2945) */
+        const int mi = __ldg(&s->amap[0]), mj = __ldg(&s->amap[1]),
+                  mk = __ldg(&s->amap[2]);
+        float r2 = loc[mi] * loc[mi];
+        if (conic != 2) r2 = r2 + loc[mj] * loc[mj];
+        r2 = r2 + loc[mk] * loc[mk];
+        if (r2 < T_EPS)
+        {
+            float li, lj = 0.0f, lk, lr, sk;
+            li = fxor(1.0f, sgnbit(ldff[mi]));
+            sk = __ldg(&s->sci[mi]);
+            lr = 1.0f;
+            if (conic != 2)
+            {
+                lj = fxor(1.0f, sgnbit(ldff[mj]));
+                sk = sk + __ldg(&s->sci[mj]);
+                lr = lr + 1.0f;
+            }
+            sk = fdiv(sk, __ldg(&s->sci[mk]));
+            sk = fxor(sk, SIGN_BIT);
+            lk = fsqrt(sk);
+            float inv = rsq(sk + lr);
+            inv = inv * T_EPS;
+            li = li * inv;
+            lj = lj * inv;
+            lk = lk * inv;
+            const uint32_t tside = side ? SIGN_BIT : 0u;
+            lk = fxor(lk, sgnbit(ldff[mk]));
+            lk = fxor(lk, amask & ~tside);
+            li = fxor(li, tside & ~amask);
+            lj = fxor(lj, tside & ~amask);
+            loc[mi] = li;
+            if (conic != 2) loc[mj] = lj;
+            loc[mk] = lk;
+        }
+    }
+
+    /* axis clippers (2963-3014) */
+    const int mint = __ldg(&s->mint), maxt = __ldg(&s->maxt);
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        if ((mint >> k) & 1) valid = valid && (__ldg(&s->bmin[k]) <= loc[k]);
+        if ((maxt >> k) & 1) valid = valid && (__ldg(&s->bmax[k]) >= loc[k]);
+    }
+
+    /* custom clippers with boolean accumulator segments (3020-3240) */
+    const int cnum = __ldg(&s->clip_num);
+    if (cnum > 0)
+    {
+        const int coff = __ldg(&s->clip_off);
+        int mask = valid, saved = 0, cache_last = -1;
+        float nx[3] = {0.0f, 0.0f, 0.0f};
+        for (int e = 0; e < cnum; e++)
+        {
+            const int ei = coff + e;
+            const qr_elem *__restrict__ el = &S.elems[ei];
+            const int kind = __ldg(&el->kind);
+            if (kind == QR_ELM_ACC_ENTER) { saved = mask; mask = 1; continue; }
+            if (kind == QR_ELM_ACC_LEAVE) { mask = !mask && saved; continue; }
+            const int ref = __ldg(&el->ref);
+            const qr_srf *__restrict__ c = &S.srf[ref];
+            float p[3], v;
+            if (kind == QR_ELM_TRNODE)
+            {
+                if (__ldg(&s->trnode) == ref)
+                {
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++) nx[k] = loc[k] + __ldg(&s->pos[k]);
+                }
+                else
+                {
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++) p[k] = hit[k] - __ldg(&c->pos[k]);
+                    if (__ldg(&c->amap[3]) != 0) xform(c, p, nx);
+                    else { nx[0] = p[0]; nx[1] = p[1]; nx[2] = p[2]; }
+                }
+                cache_last = __ldg(&el->last);
+                continue;
+            }
+            if (cache_last >= 0)
+            {
+                #pragma unroll
+                for (int k = 0; k < 3; k++) p[k] = nx[k] - __ldg(&c->pos[k]);
+                if (ei == cache_last) cache_last = -1;
+            }
+            else
+            {
+                float d[3];
+                #pragma unroll
+                for (int k = 0; k < 3; k++) d[k] = hit[k] - __ldg(&c->pos[k]);
+                if (__ldg(&c->amap[3]) != 0) xform(c, d, p);
+                else { p[0] = d[0]; p[1] = d[1]; p[2] = d[2]; }
+            }
+            CNT(QR_STAT_CLIP_CUSTOM);
+            const int clpk = __ldg(&c->clpk);
+            if (clpk == 1)
+            {
+                v = fxor(p[__ldg(&c->amap[2])], __ldg(&c->asgn[2]) ? SIGN_BIT : 0u);
+            }
+            else
+            {
+                float d2[3];
+                #pragma unroll
+                for (int k = 0; k < 3; k++)
+                {
+                    d2[k] = p[k] * p[k] * __ldg(&c->sci[k]);
+                    if (clpk == 2)
+                    {
+                        const float sj = __ldg(&c->scj[k]);
+                        d2[k] = p[k] * p[k] * __ldg(&c->sci[k]) - (sj + sj) * p[k];
+                    }
+                }
+                v = ((d2[0] - __ldg(&c->sci[3])) + d2[1]) + d2[2];
+            }
+            if (__ldg(&el->rel) < 0) mask = mask && (v >= 0.0f);
+            else                    mask = mask && (v <= 0.0f);
+        }
+        valid = mask;
+    }
+    return valid;
+}
+
+__device__ __forceinline__ void accept_root(const qr_dscene &S, Walk &w, int si,
+                                            int side, float t,
+                                            const float hit[3],
+                                            const float loc[3])
+{
+    if (w.shadow)
+    {
+        /* light sources and transparent non-refractive surfaces do not
+         * occlude (CHECK_SHAD, 576-616) */
+        const int props = __ldg(&S.srf[si].props[side]);
+        if (props & QR_PROP_LIGHT) return;
+        if ((props & QR_PROP_TRANSP) && !(props & QR_PROP_REFRACT)) return;
+        w.occluded = 1;
+        return;
+    }
+    w.tbuf = t;
+    w.best.srf = si;
+    w.best.side = side;
+    #pragma unroll
+    for (int k = 0; k < 3; k++) { w.best.hit[k] = hit[k]; w.best.loc[k] = loc[k]; }
+}
+
+/* CHECK_SIDE (558-567) */
+__device__ __forceinline__ int side_blocked(const Ray &r, int si, int side)
+{
+    if (r.from != si) return 0;
+    const int f = r.flags & 3;
+    return f == 1 - side || f == 2 + side;
+}
+
+/* quadric roots with root sorting and splitting (5785-6206) */
+__device__ void root_pair(const qr_dscene &S, const Ray &r, Walk &w, int si,
+                          const float ldff[3], const float lray[3],
+                          float a, float b, float c, float d, qr_dstats *st)
+{
+    if (!(0.0f <= d)) return;
+    const float nb = fxor(b, SIGN_BIT);
+    const int dmask = d < D_EPS;
+
+    float sd = fsqrt(d);
+    sd = fxor(sd, sgnbit(nb));
+    const float q = nb + sd;
+    const int m_neg = 0.0f > sd;
+    float t1n, t1d, t2n, t2d;
+    if (m_neg) { t1n = q; t1d = a; t2n = c; t2d = q; }
+    else       { t1n = c; t1d = q; t2n = q; t2d = a; }
+    const uint32_t amask = sgnbit(a);
+
+    float t1, t2;
+    int t1m, t2m;
+    if (dmask)
+    {
+        if (t1n == 0.0f) t1d = 1.0f;
+        if (t2n == 0.0f) t2d = 1.0f;
+        t1 = fdiv(t1n, t1d);
+        t2 = fdiv(t2n, t2d);
+        t1m = t1d != 0.0f;
+        t2m = t2d != 0.0f;
+        float tdff = t1 - t2;
+        tdff = fxor(tdff, amask);
+        const int fmask = 0.0f <= tdff;
+        tdff = fmask ? tdff : 0.0f;
+        float teps = fmask ? T_EPS : 0.0f;
+        teps = teps * t1;
+        teps = fabsf(teps);
+        tdff = tdff * -0.5f;
+        tdff = tdff - teps;
+        tdff = fxor(tdff, amask);
+        if (!(t1m && t2m)) tdff = 0.0f;
+        t1 = t1 + tdff;
+        t2 = t2 - tdff;
+    }
+    else
+    {
+        t1 = fdiv(t1n, t1d);
+        t2 = fdiv(t2n, t2d);
+        t1m = t1d != 0.0f;
+        t2m = t2d != 0.0f;
+    }
+
+    const int first = (0.0f > a) ? SIDE_INNER : SIDE_OUTER;
+    float hit[3], loc[3];
+    #pragma unroll 1
+    for (int k = 0; k < 2; k++)
+    {
+        const int side = k == 0 ? first : 1 - first;
+        const float t = side == SIDE_OUTER ? t1 : t2;
+        const int tm = side == SIDE_OUTER ? t1m : t2m;
+        if (side_blocked(r, si, side) || !tm) continue;
+        if (clip_root(S, r, si, t, w.tbuf, ldff, lray, side, dmask, amask, hit, loc, st))
+        {
+            accept_root(S, w, si, side, t, hit, loc);
+            if (w.shadow && w.occluded) return;
+        }
+    }
+}
+
+/* list walk (2413-2680) with the solvers (5522-6497) */
+__device__ void walk(const qr_dscene &S, const Ray &r, int off, int num, Walk &w,
+                     qr_dstats *st)
+{
+    float cdff[3] = {0.0f, 0.0f, 0.0f}, cray[3] = {0.0f, 0.0f, 0.0f};
+    int cache_last = -1;
+
+    #pragma unroll 1
+    for (int e = 0; e < num; e++)
+    {
+        const int ei = off + e;
+        const qr_elem *__restrict__ el = &S.elems[ei];
+        const int kind = __ldg(&el->kind);
+        const int si = __ldg(&el->ref);
+        const qr_srf *__restrict__ s = &S.srf[si];
+        float ldff[3], lray[3];
+
+        if (kind == QR_ELM_TRNODE)
+        {
+            float d[3];
+            #pragma unroll
+            for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&s->pos[k]);
+            if (__ldg(&s->amap[3]) == 0) continue;
+            CNT(QR_STAT_XFORM);
+            xform(s, d, cdff);
+            xform(s, r.dir, cray);
+            cache_last = __ldg(&el->last);
+            continue;
+        }
+
+        const int am3 = __ldg(&s->amap[3]);
+        if (cache_last >= 0)
+        {
+            if (r.from == si)
+            {
+                #pragma unroll
+                for (int k = 0; k < 3; k++) ldff[k] = r.phit[k];
+            }
+            else
+            {
+                #pragma unroll
+                for (int k = 0; k < 3; k++) ldff[k] = cdff[k] - __ldg(&s->pos[k]);
+            }
+            #pragma unroll
+            for (int k = 0; k < 3; k++) lray[k] = cray[k];
+            if (ei == cache_last) cache_last = -1;
+        }
+        else if (r.from == si)
+        {
+            #pragma unroll
+            for (int k = 0; k < 3; k++) ldff[k] = r.phit[k];
+            if (am3 != 0) xform(s, r.dir, lray);
+            else
+            {
+                #pragma unroll
+                for (int k = 0; k < 3; k++) lray[k] = r.dir[k];
+            }
+        }
+        else
+        {
+            float d[3];
+            #pragma unroll
+            for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&s->pos[k]);
+            if (am3 != 0) { CNT(QR_STAT_XFORM); xform(s, d, ldff); xform(s, r.dir, lray); }
+            else
+            {
+                #pragma unroll
+                for (int k = 0; k < 3; k++) { ldff[k] = d[k]; lray[k] = r.dir[k]; }
+            }
+        }
+
+        const int solver = __ldg(&s->solver);
+        if (solver == 1)
+        {
+            /* plane (5545-5634) */
+            if (r.from == si) continue;
+            const int mk = __ldg(&s->amap[2]);
+            const uint32_t sg = __ldg(&s->asgn[2]) ? SIGN_BIT : 0u;
+            float dk = fxor(ldff[mk], sg);
+            const float rk = fxor(lray[mk], sg);
+            dk = fxor(dk, SIGN_BIT);
+            if (!(rk != 0.0f)) continue;
+            const float t = fdiv(dk, rk);
+            float hit[3], loc[3];
+            CNT(QR_STAT_TEST_PLANE);
+            if (!clip_root(S, r, si, t, w.tbuf, ldff, lray, 0, 0, 0u, hit, loc, st)) continue;
+            accept_root(S, w, si, rk < 0.0f ? SIDE_OUTER : SIDE_INNER, t, hit, loc);
+        }
+        else if (solver == 2)
+        {
+            /* quadric coefficients (5722-5783) */
+            float a = 0.0f, b = 0.0f, c = 0.0f;
+            #pragma unroll
+            for (int k = 0; k < 3; k++)
+            {
+                const float sci = __ldg(&s->sci[k]), scj = __ldg(&s->scj[k]);
+                const float sri = sci * lray[k];
+                float sdi = sci * ldff[k];
+                sdi = sdi - scj;
+                const float ax = lray[k] * sri;
+                const float bx = lray[k] * sdi;
+                sdi = sdi - scj;
+                const float cx = ldff[k] * sdi;
+                if (k == 0) { a = ax; b = bx; c = cx; }
+                else { a = a + ax; b = b + bx; c = c + cx; }
+            }
+            c = c - __ldg(&s->sci[3]);
+            const float d = b * b - c * a;
+            CNT(QR_STAT_TEST_QUADRIC);
+            root_pair(S, r, w, si, ldff, lray, a, b, c, d, st);
+        }
+        else
+        {
+            /* two-plane (6349-6402) */
+            const int mi = __ldg(&s->amap[0]), mk = __ldg(&s->amap[2]);
+            const float ri = lray[mi], di = ldff[mi], rk = lray[mk], dk = ldff[mk];
+            const float si_ = __ldg(&s->sci[mi]), sk = __ldg(&s->sci[mk]);
+            float dd = di * rk - dk * ri;
+            dd = dd * dd;
+            dd = dd * si_;
+            dd = dd * sk;
+            dd = fabsf(dd);
+            const float bb = si_ * di * ri + sk * dk * rk;
+            const float cc = di * di * si_ + dk * dk * sk;
+            const float aa = ri * ri * si_ + rk * rk * sk;
+            CNT(QR_STAT_TEST_TWOPLANE);
+            root_pair(S, r, w, si, ldff, lray, aa, bb, cc, dd, st);
+        }
+        if (w.shadow && w.occluded) return;
+    }
+}
+
+__device__ void trace(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                      int off, int num, float col[3], qr_dstats *st);
+
+/* shading (3255-5359): normal, texel, ambient, lights with shadows,
+ * transparency, reflection */
+__device__ void shade(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                      const Hit &h, float col[3], qr_dstats *st)
+{
+    const qr_srf *__restrict__ s = &S.srf[h.srf];
+    const int side = h.side;
+    const int props = __ldg(&s->props[side]);
+    const qr_mat *__restrict__ m = &S.mat[__ldg(&s->mat[side])];
+    const uint32_t tside = side ? SIGN_BIT : 0u;
+    float nrm[3], tex[3], c[3];
+    float tu = 0.0f, tv = 0.0f;
+    const int nrmk = __ldg(&s->nrmk);
+
+    if (nrmk == 1)
+    {
+        const int mk = __ldg(&s->amap[2]);
+        nrm[0] = nrm[1] = nrm[2] = 0.0f;
+        nrm[mk] = fxor(fxor(1.0f, tside), __ldg(&s->asgn[2]) ? SIGN_BIT : 0u);
+        if (props & QR_PROP_TEXTURE)
+        {
+            tu = fxor(h.loc[__ldg(&s->amap[0])], __ldg(&s->asgn[0]) ? SIGN_BIT : 0u);
+            tv = fxor(h.loc[__ldg(&s->amap[1])], __ldg(&s->asgn[1]) ? SIGN_BIT : 0u);
+        }
+    }
+    else
+    {
+        float x = h.loc[0] * __ldg(&s->sci[0]);
+        float y = h.loc[1] * __ldg(&s->sci[1]);
+        float z = h.loc[2] * __ldg(&s->sci[2]);
+        if (nrmk == 2)
+        {
+            x = x - __ldg(&s->scj[0]);
+            y = y - __ldg(&s->scj[1]);
+            z = z - __ldg(&s->scj[2]);
+        }
+        float l2 = x * x + y * y;
+        l2 = l2 + z * z;
+        const float inv = fxor(rsq(l2), tside);
+        nrm[0] = x * inv; nrm[1] = y * inv; nrm[2] = z * inv;
+    }
+
+    if (__ldg(&s->amap[3]) != 0)
+    {
+        /* transposed inverse of the transform node (3273-3352) */
+        const int tn = __ldg(&s->trnode);
+        const qr_srf *__restrict__ t = &S.srf[tn >= 0 ? tn : h.srf];
+        const float n1 = nrm[0], n2 = nrm[1], n3 = nrm[2];
+        float x = __ldg(&t->tci[0]) * n1;
+        float y = __ldg(&t->tcj[1]) * n2;
+        float z = __ldg(&t->tck[2]) * n3;
+        const int tam = __ldg(&t->amap[3]);
+        int renorm = 1;
+        if (tam != 1)
+        {
+            x = x + __ldg(&t->tcj[0]) * n2;
+            x = x + __ldg(&t->tck[0]) * n3;
+            y = y + __ldg(&t->tci[1]) * n1;
+            y = y + __ldg(&t->tck[1]) * n3;
+            z = z + __ldg(&t->tci[2]) * n1;
+            z = z + __ldg(&t->tcj[2]) * n2;
+            if (tam == 2) renorm = 0;
+        }
+        if (renorm)
+        {
+            float l2 = x * x + y * y;
+            l2 = l2 + z * z;
+            const float inv = rsq(l2);
+            x = x * inv; y = y * inv; z = z * inv;
+        }
+        nrm[0] = x; nrm[1] = y; nrm[2] = z;
+    }
+
+    /* texel (3380-3416, PAINT_COLX 970-979) */
+    {
+        int32_t idx = 0;
+        if (props & QR_PROP_TEXTURE)
+        {
+            const float uv[2] = {tu, tv};
+            float tx = uv[__ldg(&m->tmap[0])], ty = uv[__ldg(&m->tmap[1])];
+            tx = tx - __ldg(&m->xoffs);
+            ty = ty - __ldg(&m->yoffs);
+            tx = tx * __ldg(&m->xscal);
+            ty = ty * __ldg(&m->yscal);
+            idx = (__float2int_rd(tx) & __ldg(&m->xmask)) +
+                  ((__float2int_rd(ty) & __ldg(&m->ymask)) << __ldg(&m->yshft));
+        }
+        const uint32_t texel = __ldg(&S.texels[__ldg(&m->tex_off) + idx]);
+        tex[0] = fdiv((float)(int32_t)((texel >> 16) & 0xFF), 255.0f);
+        tex[1] = fdiv((float)(int32_t)((texel >> 8) & 0xFF), 255.0f);
+        tex[2] = fdiv((float)(int32_t)(texel & 0xFF), 255.0f);
+        if (props & QR_PROP_GAMMA)
+        {
+            #pragma unroll
+            for (int k = 0; k < 3; k++) tex[k] = tex[k] * tex[k];
+        }
+    }
+
+    #pragma unroll
+    for (int k = 0; k < 3; k++) c[k] = tex[k];
+
+    const float m_trn = __ldg(&m->c_trn), m_rfl = __ldg(&m->c_rfl);
+    if (!(props & QR_PROP_LIGHT))
+    {
+        /* ambient (3945-3987) */
+        #pragma unroll
+        for (int k = 0; k < 3; k++) c[k] = c[k] * P.amb[k];
+        float f = 1.0f - m_trn;
+        f = f - m_rfl;
+        f = (0.0f <= f) ? f : 0.0f;
+        #pragma unroll
+        for (int k = 0; k < 3; k++) c[k] = c[k] * f;
+
+        /* lights (4002-4391) */
+        const int loff = __ldg(&s->lgt_off[side]), lnum = __ldg(&s->lgt_num[side]);
+        const float l_dff = __ldg(&m->l_dff), l_spc = __ldg(&m->l_spc);
+        const uint32_t l_pow = (uint32_t)__ldg(&m->l_pow);
+        #pragma unroll 1
+        for (int li = 0; li < lnum; li++)
+        {
+            const qr_lelem *__restrict__ le = &S.lelems[loff + li];
+            const qr_light *__restrict__ L = &S.lgt[__ldg(&le->light)];
+            float lv[3];
+            #pragma unroll
+            for (int k = 0; k < 3; k++) lv[k] = __ldg(&L->pos[k]) - h.hit[k];
+            float dot = lv[0] * nrm[0] + lv[1] * nrm[1];
+            dot = dot + lv[2] * nrm[2];
+            if (!(0.0f < dot)) continue;
+
+            {
+                /* shadow ray: origin at the hit, direction L, t in (0, 1) */
+                Ray sr;
+                #pragma unroll
+                for (int k = 0; k < 3; k++)
+                {
+                    sr.org[k] = h.hit[k];
+                    sr.dir[k] = lv[k];
+                    sr.phit[k] = h.loc[k];
+                }
+                sr.t_min = 0.0f;
+                sr.t_max = __ldg(&L->t_max);
+                sr.from = h.srf;
+                sr.flags = side | FLAG_SHAD;
+                sr.depth = r.depth - 1;
+                Walk sw;
+                sw.shadow = 1;
+                sw.occluded = 0;
+                sw.tbuf = sr.t_max;
+                sw.best.srf = -1;
+                CNT(QR_STAT_RAY_SHADOW);
+                walk(S, sr, __ldg(&le->shd_off), __ldg(&le->shd_num), sw, st);
+                if (sw.occluded) continue;
+            }
+
+            CNT(QR_STAT_LIGHT);
+            float r2 = lv[0] * lv[0] + lv[1] * lv[1];
+            r2 = r2 + lv[2] * lv[2];
+
+            float diff, sdot = dot;
+            if (props & QR_PROP_DIFFUSE)
+            {
+                const float inv_r = rsq(r2);
+                float r1 = inv_r * r2;
+                float att = r2 * __ldg(&L->a_qdr);
+                r1 = r1 * __ldg(&L->a_lnr);
+                att = att + __ldg(&L->a_cnt);
+                att = att + r1;
+                const float inv_a = rsq(att);
+                diff = dot * inv_a;
+                diff = diff * inv_r;
+                diff = diff * l_dff;
+            }
+            else
+            {
+                diff = 0.0f;
+            }
+
+            int spec_on = 0;
+            float spec = 0.0f;
+            if (props & QR_PROP_SPECULAR)
+            {
+                float pn, rx, ry, rz;
+                pn = sdot * nrm[0]; rx = lv[0] - pn; rx = rx - pn;
+                pn = sdot * nrm[1]; ry = lv[1] - pn; ry = ry - pn;
+                pn = sdot * nrm[2]; rz = lv[2] - pn; rz = rz - pn;
+                rx = rx * r.dir[0];
+                ry = ry * r.dir[1];
+                rz = rz * r.dir[2];
+                float ray2 = r.dir[2] * r.dir[2];
+                ray2 = ray2 + r.dir[0] * r.dir[0];
+                ray2 = ray2 + r.dir[1] * r.dir[1];
+                float sv = rx + ry;
+                sv = sv + rz;
+                if (0.0f < sv)
+                {
+                    /* power in 28.4 fixed point (4225-4285) */
+                    sv = sv * rsq(ray2);
+                    sv = sv * rsq(r2);
+                    float p1 = 1.0f, p2 = sv;
+                    uint32_t fr = l_pow & 0xF, in = l_pow >> 4;
+                    if (fr != 0)
+                    {
+                        float s4 = sv;
+                        do
+                        {
+                            s4 = fsqrt(s4);
+                            if (fr & 0x8) p1 = p1 * s4;
+                            fr = (fr << 1) & 0xF;
+                        } while (fr != 0);
+                    }
+                    if (in != 0)
+                    {
+                        const float p3 = p1;
+                        p1 = 1.0f;
+                        do
+                        {
+                            if (in & 1) p1 = p1 * p2;
+                            p2 = p2 * p2;
+                            in >>= 1;
+                        } while (in != 0);
+                        p1 = p1 * p3;
+                    }
+                    spec = p1 * l_spc;
+                    spec_on = 1;
+                }
+            }
+
+            float lc[3];
+            if (spec_on && !(props & QR_PROP_METAL))
+            {
+                /* plain: highlight in the light's colour (4323-4355) */
+                #pragma unroll
+                for (int k = 0; k < 3; k++)
+                {
+                    const float lk = __ldg(&L->col[k]);
+                    float t1 = tex[k] * diff;
+                    t1 = t1 * lk;
+                    lc[k] = t1 + lk * spec;
+                }
+            }
+            else
+            {
+                /* metal: highlight tinted by the surface (4287-4317) */
+                if (spec_on) diff = diff + spec;
+                #pragma unroll
+                for (int k = 0; k < 3; k++)
+                {
+                    lc[k] = tex[k] * __ldg(&L->col[k]);
+                    lc[k] = lc[k] * diff;
+                }
+            }
+            #pragma unroll
+            for (int k = 0; k < 3; k++) c[k] = lc[k] + c[k];
+        }
+    }
+
+    /* transparency (4442-4936) */
+    float c_trn = m_trn, c_rfl = m_rfl;
+    if (!(props & QR_PROP_OPAQUE))
+    {
+        const int fres = (props & QR_PROP_FRESNEL) != 0;
+        const int refr = (props & QR_PROP_REFRACT) != 0;
+        const float c_rfr = __ldg(&m->c_rfr), rfr_2 = __ldg(&m->rfr_2);
+        float nw[3];
+        int do_trn = 0, m_ok = 1;
+        if (refr || fres)
+        {
+            CNT(QR_STAT_REFRACT);
+            float l2 = r.dir[0] * r.dir[0];
+            l2 = l2 + r.dir[1] * r.dir[1];
+            l2 = l2 + r.dir[2] * r.dir[2];
+            const float inv = rsq(l2);
+            float dn[3];
+            #pragma unroll
+            for (int k = 0; k < 3; k++) dn[k] = r.dir[k] * inv;
+            float cosi = dn[0] * nrm[0];
+            cosi = cosi + dn[1] * nrm[1];
+            cosi = cosi + dn[2] * nrm[2];
+            float nci = cosi * c_rfr;
+            float kk = nci * nci;
+            kk = kk + 1.0f;
+            kk = kk - rfr_2;
+            if (fres) m_ok = 0.0f <= kk;
+            if (fres && !m_ok)
+            {
+                c_trn = 0.0f;
+                c_rfl = m_rfl + m_trn;
+            }
+            else
+            {
+                const float sq = fsqrt(kk);
+                nci = nci + sq;
+                if (refr)
+                {
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++)
+                    {
+                        const float a1 = nrm[k] * nci;
+                        const float a2 = dn[k] * c_rfr;
+                        nw[k] = a2 - a1;
+                    }
+                }
+                else
+                {
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++) nw[k] = r.dir[k];
+                }
+                if (fres)
+                {
+                    float x1 = cosi, x2, x3;
+                    x2 = x1 * c_rfr;
+                    x2 = x2 - sq;
+                    const float sqn = sq * c_rfr;
+                    x3 = x1;
+                    x1 = x1 + sqn;
+                    x3 = x3 - sqn;
+                    float f0 = fdiv(nci, x2);
+                    float f1 = fdiv(x1, x3);
+                    f0 = f0 * f0;
+                    f1 = f1 * f1;
+                    float fr = f0 + f1;
+                    fr = fabsf(fr * -0.5f);
+                    fr = fr * m_trn;
+                    c_trn = m_trn - fr;
+                    c_rfl = m_rfl + fr;
+                }
+                do_trn = 1;
+            }
+        }
+        else
+        {
+            #pragma unroll
+            for (int k = 0; k < 3; k++) nw[k] = r.dir[k];
+            do_trn = 1;
+        }
+        if (do_trn && m_ok)
+        {
+            float tc[3] = {0.0f, 0.0f, 0.0f};
+            if (r.depth != 0)
+            {
+                Ray cr;
+                #pragma unroll
+                for (int k = 0; k < 3; k++)
+                {
+                    cr.org[k] = h.hit[k];
+                    cr.dir[k] = nw[k];
+                    cr.phit[k] = h.loc[k];
+                }
+                cr.t_min = 0.0f;
+                cr.t_max = FLT_MAX;
+                cr.from = h.srf;
+                cr.flags = side | FLAG_PASS;
+                cr.depth = r.depth - 1;
+                CNT(QR_STAT_RAY_SECONDARY);
+                trace(S, P, cr, __ldg(&s->sec_off[1 - side]),
+                      __ldg(&s->sec_num[1 - side]), tc, st);
+                #pragma unroll
+                for (int k = 0; k < 3; k++) tc[k] = tc[k] * c_trn;
+            }
+            #pragma unroll
+            for (int k = 0; k < 3; k++) c[k] = tc[k] + c[k];
+        }
+    }
+
+    /* reflection (4942-5359) */
+    {
+        const int refl = (props & QR_PROP_REFLECT) != 0;
+        const int do_rfl = refl || (!(props & QR_PROP_OPAQUE) && (props & QR_PROP_FRESNEL));
+        if (do_rfl)
+        {
+            CNT(QR_STAT_REFLECT);
+            float l2 = r.dir[0] * r.dir[0];
+            l2 = l2 + r.dir[1] * r.dir[1];
+            l2 = l2 + r.dir[2] * r.dir[2];
+            const float inv = rsq(l2);
+            float dn[3], rw[3];
+            #pragma unroll
+            for (int k = 0; k < 3; k++) dn[k] = r.dir[k] * inv;
+            float cosi = dn[0] * nrm[0];
+            cosi = cosi + dn[1] * nrm[1];
+            cosi = cosi + dn[2] * nrm[2];
+            #pragma unroll
+            for (int k = 0; k < 3; k++)
+            {
+                const float p = nrm[k] * cosi;
+                rw[k] = dn[k] - p;
+                rw[k] = rw[k] - p;
+            }
+            if ((props & QR_PROP_FRESNEL) && (props & QR_PROP_OPAQUE))
+            {
+                float fr;
+                if (props & QR_PROP_METAL)
+                {
+                    /* fast complex-IOR Fresnel (5067-5089) */
+                    float r6 = __ldg(&m->c_rcp);
+                    float x4 = cosi * r6;
+                    x4 = x4 + x4;
+                    float x0 = cosi * cosi;
+                    r6 = r6 * r6;
+                    r6 = r6 + __ldg(&m->ext_2);
+                    float x1 = x0 * r6;
+                    x0 = x0 + r6;
+                    x1 = x1 + 1.0f;
+                    float x2 = x0, x3 = x1;
+                    x0 = x0 + x4;
+                    x1 = x1 + x4;
+                    x2 = x2 - x4;
+                    x3 = x3 - x4;
+                    x0 = fdiv(x0, x2);
+                    x1 = fdiv(x1, x3);
+                    x0 = x0 + x1;
+                    fr = fabsf(x0 * -0.5f);
+                }
+                else
+                {
+                    /* dielectric Fresnel for opaque surfaces (5108-5134) */
+                    const float n = __ldg(&m->c_rfr);
+                    float x0 = cosi * n;
+                    float x7 = x0 * x0;
+                    x7 = x7 + 1.0f;
+                    x7 = x7 - __ldg(&m->rfr_2);
+                    x7 = fsqrt(x7);
+                    x0 = x0 + x7;
+                    float x1 = cosi;
+                    float x2 = x1 * n;
+                    x2 = x2 - x7;
+                    x7 = x7 * n;
+                    float x3 = x1;
+                    x1 = x1 + x7;
+                    x3 = x3 - x7;
+                    x0 = fdiv(x0, x2);
+                    float f1 = fdiv(x1, x3);
+                    x0 = x0 * x0;
+                    f1 = f1 * f1;
+                    x0 = x0 + f1;
+                    fr = fabsf(x0 * -0.5f);
+                }
+                fr = fr - 1.0f;
+                fr = fr * m_rfl;
+                c_rfl = m_rfl + fr;
+            }
+            float rc[3] = {0.0f, 0.0f, 0.0f};
+            if (r.depth != 0)
+            {
+                Ray cr;
+                #pragma unroll
+                for (int k = 0; k < 3; k++)
+                {
+                    cr.org[k] = h.hit[k];
+                    cr.dir[k] = rw[k];
+                    cr.phit[k] = h.loc[k];
+                }
+                cr.t_min = 0.0f;
+                cr.t_max = FLT_MAX;
+                cr.from = h.srf;
+                cr.flags = side;
+                cr.depth = r.depth - 1;
+                CNT(QR_STAT_RAY_SECONDARY);
+                trace(S, P, cr, __ldg(&s->sec_off[side]), __ldg(&s->sec_num[side]),
+                      rc, st);
+                #pragma unroll
+                for (int k = 0; k < 3; k++) rc[k] = rc[k] * c_rfl;
+            }
+            #pragma unroll
+            for (int k = 0; k < 3; k++) c[k] = rc[k] + c[k];
+        }
+    }
+    #pragma unroll
+    for (int k = 0; k < 3; k++) col[k] = c[k];
+}
+
+__device__ void trace(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                      int off, int num, float col[3], qr_dstats *st)
+{
+    Walk w;
+    w.shadow = 0;
+    w.occluded = 0;
+    w.tbuf = r.t_max;
+    w.best.srf = -1;
+    walk(S, r, off, num, w, st);
+    if (w.best.srf < 0)
+    {
+        col[0] = col[1] = col[2] = 0.0f;
+        return;
+    }
+    CNT(QR_STAT_SHADE);
+    shade(S, P, r, w.best, col, st);
+}
+
+/* sub-sample offsets of the 4x rotated grid (engine.cpp:3572-3606) */
+__constant__ float c_aa4_h[4] = {-0.08f - 0.25f, -0.08f + 0.25f,
+                                 +0.08f - 0.25f, +0.08f + 0.25f};
+__constant__ float c_aa4_v[4] = {+0.08f - 0.25f, -0.08f - 0.25f,
+                                 +0.08f + 0.25f, -0.08f + 0.25f};
+
+__device__ __forceinline__ void primary(const qr_dscene &S, const qr_frame_params &P,
+                                        float hs, float vs, float col[3],
+                                        qr_dstats *st)
+{
+    Ray r;
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        float hx = P.hor[k] * hs;
+        const float vx = P.ver[k] * vs;
+        hx = hx + vx;
+        r.dir[k] = hx + P.dir[k];
+        r.org[k] = P.org[k];
+        r.phit[k] = 0.0f;
+    }
+    r.t_min = P.t_min;
+    r.t_max = P.t_max;
+    r.from = -1;
+    r.flags = 0;
+    r.depth = P.depth;
+    CNT(QR_STAT_RAY_PRIMARY);
+    trace(S, P, r, S.cam_off, S.cam_num, col, st);
+}
+
+__device__ __forceinline__ float clamp1(float v) { return v < 1.0f ? v : 1.0f; }
+
+/* clamp, gamma, x255, round to nearest, pack XRGB (7028-7145, 1922-1940) */
+__device__ __forceinline__ uint32_t pack(const qr_frame_params &P, const float col[3])
+{
+    uint32_t px = 0;
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        float v = col[k];
+        if (P.ctx_props & QR_PROP_GAMMA) v = fsqrt(v);
+        v = v * 255.0f;
+        /* x86 cvtps2dq gives 0x80000000 for NaN / out of range */
+        const int32_t iv = (v != v || v >= 2147483648.0f || v < -2147483648.0f)
+                           ? (int32_t)0x80000000 : __float2int_rn(v);
+        px |= ((uint32_t)iv & 0xFFu) << (16 - 8 * k);
+    }
+    return px;
+}
+
+__global__ void __launch_bounds__(128)
+whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
+               qr_dstats *st)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.x_res || y >= P.y_res) return;
+    float col[3];
+    if (P.fsaa == 2)
+    {
+        float cs[4][3];
+        #pragma unroll 1
+        for (int s = 0; s < 4; s++)
+        {
+            primary(S, P, (float)x + c_aa4_h[s], (float)y + c_aa4_v[s], cs[s], st);
+            #pragma unroll
+            for (int k = 0; k < 3; k++) cs[s][k] = clamp1(cs[s][k]);
+        }
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            const float p01 = cs[0][k] * 0.5f + cs[1][k] * 0.5f;
+            const float p23 = cs[2][k] * 0.5f + cs[3][k] * 0.5f;
+            col[k] = p01 * 0.5f + p23 * 0.5f;
+        }
+    }
+    else
+    {
+        primary(S, P, (float)x, (float)y, col, st);
+        #pragma unroll
+        for (int k = 0; k < 3; k++) col[k] = clamp1(col[k]);
+    }
+    frame[(size_t)y * P.x_row + x] = pack(P, col);
+}
+
+} /* namespace qr_dev */
+
+cudaError_t qr_launch_whitted(const qr_dscene &sc, const qr_frame_params &fp,
+                              uint32_t *dev_frame, qr_dstats *dstats,
+                              cudaStream_t stream)
+{
+    const dim3 block(32, 4);
+    const dim3 grid((fp.x_res + block.x - 1) / block.x,
+                    (fp.y_res + block.y - 1) / block.y);
+    qr_dev::whitted_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, dstats);
+    return cudaGetLastError();
+}

@@ -1,0 +1,34 @@
+/*
+ * tracer.cuh: device-side data of the GB300 QuadRay tracer.
+ */
+#ifndef QR_TRACER_CUH
+#define QR_TRACER_CUH
+
+#include <stdint.h>
+#include "qr_gpu.h"
+
+/* device copy of a flattened scene (qr_scene_desc with device pointers) */
+struct qr_dscene
+{
+    const qr_srf   *srf;
+    const qr_mat   *mat;
+    const qr_light *lgt;
+    const qr_elem  *elems;
+    const qr_lelem *lelems;
+    const uint32_t *texels;
+    int32_t nsrf, nmat, nlgt, nelem, nlelem, ntex;
+    int32_t cam_off, cam_num;
+};
+
+/* per-launch counters (instrumented runs only) */
+struct qr_dstats
+{
+    unsigned long long c[QR_STAT_COUNT];   /* QR_STAT_* counters */
+};
+
+/* launch the per-pixel Whitted kernel for one frame */
+cudaError_t qr_launch_whitted(const qr_dscene &sc, const qr_frame_params &fp,
+                              uint32_t *dev_frame, qr_dstats *dstats,
+                              cudaStream_t stream);
+
+#endif /* QR_TRACER_CUH */

@@ -1,0 +1,53 @@
+"""Shared fixtures: the package, the CPU oracle, and the gpu marker."""
+import ctypes
+import importlib
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+if ORACLE_DIR not in sys.path:
+    sys.path.insert(0, ORACLE_DIR)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+
+
+@pytest.fixture(scope="session")
+def qr():
+    mod = importlib.import_module("quadray-engine_gb300")
+    if not os.path.exists(mod.LIB_PATH):
+        mod.build()
+    return mod
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    import build as oracle_build
+    return oracle_build.load_oracle()
+
+
+def oracle_render(oracle, desc, params, y0=0, y1=None):
+    """Render a frame with the CPU oracle; returns (frame, traced rays)."""
+    y1 = params.y_res if y1 is None else y1
+    out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+    nr = ctypes.c_uint64()
+    rc = oracle.qr_oracle_render(ctypes.addressof(desc), ctypes.addressof(params),
+                                 out.ctypes.data, y0, y1, ctypes.byref(nr))
+    assert rc == 0
+    return out[:, :params.x_res], nr.value
+
+
+def channels(frame):
+    f = frame.astype(np.int64)
+    return np.stack([(f >> 16) & 255, (f >> 8) & 255, f & 255], axis=-1)
+
+
+def max_channel_diff(a, b):
+    return np.abs(channels(a) - channels(b)).max(axis=-1)
