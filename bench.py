@@ -46,6 +46,20 @@ WORKLOADS = {
 }
 
 
+def whole_job(units_per_step, steps, t_local, dist=None, device="cpu"):
+    """Replicas: every rank renders its own frames; the job's time is the
+    slowest rank's and its throughput counts the units of all ranks."""
+    world = 1
+    t = t_local
+    if dist is not None and dist.is_initialized():
+        import torch
+        world = dist.get_world_size()
+        tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return units_per_step * steps * world / t, t
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -237,13 +251,9 @@ def main():
     torch.cuda.synchronize()
     ck = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in ev]
-    t_total = sum(ms) / 1000.0
+    value, t_total = whole_job(rays, args.steps, sum(ms) / 1000.0, dist, "cuda")
     if dist is not None:
-        tt = torch.tensor([t_total], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
         dist.barrier()
-    value = rays * args.steps * world / t_total
     fps = args.steps * world / t_total
 
     # end to end through the engine API with a host frame buffer
@@ -258,7 +268,7 @@ def main():
         eng.render(0, hbuf)
         lat.append(time.perf_counter() - t0)
     e2e_t = sum(lat)
-    h2d = (desc.nsrf * 256 + desc.nmat * 96 + desc.nlgt * 48 + desc.nelem * 16 +
+    h2d = (desc.nsrf * 256 + desc.nmat * 112 + desc.nlgt * 48 + desc.nelem * 16 +
            desc.nlelem * 16 + desc.ntex * 4)
     d2h = wl["w"] * wl["h"] * 4
     eng.close()

@@ -12,14 +12,20 @@
  * reference's own test harness (test/core_test.cpp:976-1094): build scene,
  * set options, render, read the frame.
  *
- * usage: ref_driver KIND SEED NQ W H FSAA FRAMES FLAGS OPTS OUT [THREADS] [DUMP]
+ * usage: ref_driver KIND SEED NQ W H FSAA FRAMES FLAGS OPTS OUT [THREADS]
+ *                   [DEPTH] [DUMP]
  *   KIND    1 plain Whitted, 2 animated, 3 path tracer
  *   FSAA    0 none, 2 4x
  *   FRAMES  frames rendered at t = i*16 ms; all are written (PT: accumulated)
  *   FLAGS   scenegen flags (1 = hit-ID materials)
- *   OPTS    "full" or "none" runtime options
+ *   OPTS    "full", "none" or a number: runtime options (rt_Scene::set_opts)
  *   OUT     output file: FRAMES x H x W little-endian uint32 XRGB
  *   THREADS worker threads (pthread pool), default 1
+ *   DEPTH   secondary-ray depth, default 10 (the compiled-in RT_STACK_DEPTH,
+ *           core/tracer/tracer.h:51); the engine copies its member "depth"
+ *           into every slice's s_inf per frame (core/engine/engine.cpp:2903,
+ *           3667), so a smaller value is set on that member after
+ *           construction (the context stack keeps its 1 + 10 levels)
  *   DUMP    if "dump", print the engine's per-surface backend fields
  */
 #include <stdio.h>
@@ -34,7 +40,7 @@
 #undef private
 #undef protected
 
-#include "scenegen.hpp"
+#include "../quadray-engine_gb300/csrc/scenegen.hpp"
 
 static rt_pntr sys_alloc(rt_size size)
 {
@@ -193,7 +199,7 @@ int main(int argc, char **argv)
     if (argc < 11)
     {
         fprintf(stderr, "usage: %s KIND SEED NQ W H FSAA FRAMES FLAGS OPTS OUT "
-                        "[THREADS] [DUMP]\n", argv[0]);
+                        "[THREADS] [DEPTH] [DUMP]\n", argv[0]);
         return 2;
     }
     int kind = atoi(argv[1]);
@@ -206,7 +212,13 @@ int main(int argc, char **argv)
     const char *opts = argv[9];
     const char *out = argv[10];
     int thnum = argc > 11 ? atoi(argv[11]) : 1;
-    int dump = argc > 12 && strcmp(argv[12], "dump") == 0;
+    int depth = argc > 12 ? atoi(argv[12]) : 10;
+    int dump = argc > 13 && strcmp(argv[13], "dump") == 0;
+    if (depth < 0 || depth > 10)
+    {
+        fprintf(stderr, "DEPTH must be in [0, 10]\n");
+        return 2;
+    }
 
     qr_gen::Scene *sc = qr_gen::build(kind, seed, nq, flags);
 
@@ -229,7 +241,9 @@ int main(int argc, char **argv)
         g_cur = scene;
         if (strcmp(opts, "none") == 0) scene->set_opts(RT_OPTS_NONE);
         else if (strcmp(opts, "full") == 0) scene->set_opts(RT_OPTS_FULL);
+        else scene->set_opts((rt_si32)strtoul(opts, NULL, 0));
         if (kind == QR_SCN_PT) scene->set_pton(1);
+        scene->depth = depth;
 
         for (int f = 0; f < frames; f++)
         {

@@ -38,7 +38,9 @@ void *qrpy_flat_new(void *g, int opts, int x_res, int y_res, int fsaa)
     qr_gen::Scene *sc = (qr_gen::Scene *)g;
     try
     {
-        int o = opts < 0 ? (int)(RT_OPTS_FULL & ~sc->scn.opts) : opts;
+        /* the scene's opt-outs always apply (rt_Scene::set_opts,
+         * core/engine/engine.cpp:3786) */
+        int o = (int)((opts < 0 ? RT_OPTS_FULL : opts) & ~sc->scn.opts);
         return new qr::Flat(&sc->scn, o, x_res, y_res, fsaa);
     }
     catch (rt_Exception &e)

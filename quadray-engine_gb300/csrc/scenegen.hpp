@@ -80,35 +80,45 @@ static inline rt_ui32 pack_rgb(float r, float g, float b)
     return (cr << 16) | (cg << 8) | cb;
 }
 
-/* animator for QR_SCN_ANIM: rotation speed (deg/frame) is taken from the
- * object's scale slot W (encoded in the transform's unused precision via the
- * per-object table below); frames are 16 ms apart */
-struct AnimEntry { rt_TRANSFORM3D *trm; float base[3]; float rate[3]; };
-
-static std::vector<AnimEntry> &anim_table()
+/*
+ * Animator of QR_SCN_ANIM (rt_FUNC_ANIM3D, the reference's f_anim hook): the
+ * object spins about its three axes at a constant rate.  The rotation is a
+ * pure function of the frame time and of the object's position, which the
+ * animator never changes: a SplitMix64 stream seeded by the position bits
+ * gives the base angles U(-180,180) and the rates U[0,2] deg per frame
+ * (frames are 16 ms apart).  Being stateless, it gives the same angles in
+ * every engine instance that holds a copy of the scene.
+ */
+static inline uint64_t pos_hash(const rt_TRANSFORM3D *trm)
 {
-    static std::vector<AnimEntry> t;
-    return t;
+    uint64_t h = 0x51A7u;
+    for (int k = 0; k < 3; k++)
+    {
+        uint32_t b;
+        memcpy(&b, &trm->pos[k], 4);
+        h = h * 0x100000001B3ull ^ b;
+    }
+    return h;
 }
 
-static void anim_rotate(rt_time time, rt_time last_time, rt_TRANSFORM3D *trm,
-                        rt_pntr pobj)
+static inline float spin_angle(uint64_t h, int k, rt_time time)
+{
+    Rng r(h + (uint64_t)k);
+    double base = -180.0 + 360.0 * r.u01();
+    double rate = 2.0 * r.u01();
+    double a = base + rate * ((double)time / 16.0);
+    a = fmod(a + 180.0, 360.0);
+    if (a < 0.0) a += 360.0;
+    return (float)(a - 180.0);
+}
+
+static void anim_spin(rt_time time, rt_time last_time, rt_TRANSFORM3D *trm,
+                      rt_pntr pobj)
 {
     (void)last_time; (void)pobj;
-    std::vector<AnimEntry> &t = anim_table();
-    for (size_t i = 0; i < t.size(); i++)
-    {
-        if (t[i].trm != trm) continue;
-        double f = (double)time / 16.0;   /* frame index at 16 ms per frame */
-        for (int k = 0; k < 3; k++)
-        {
-            double a = (double)t[i].base[k] + (double)t[i].rate[k] * f;
-            a = fmod(a, 360.0);
-            if (a >= 180.0) a -= 360.0;
-            trm->rot[k] = (float)a;
-        }
-        return;
-    }
+    uint64_t h = pos_hash(trm);
+    for (int k = 0; k < 3; k++)
+        trm->rot[k] = spin_angle(h, k, time);
 }
 
 /*
@@ -373,12 +383,161 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
     sc.scn.lock = RT_NULL;
 }
 
+/* material of QR_SCN_ANIM objects: 25% transparent dielectric (relative
+ * index 1/n outside, n inside, n = U[1.3,1.6]), 15% metal, 15% reflective
+ * plain, the rest plain; *inner receives the inner side's material */
+static rt_MATERIAL *random_anim_material(Scene &sc, Rng &r, rt_MATERIAL **inner)
+{
+    double u = r.u01();
+    rt_ui32 col = pack_rgb(r.uf(0.2, 1.0), r.uf(0.2, 1.0), r.uf(0.2, 1.0));
+    float dff = r.uf(0.2, 0.9);
+    float spc = r.uf(0.1, 0.6);
+    float pw  = (float)r.ui(8, 64);
+    if (sc.flags & QR_GEN_NOSPEC) spc = 0.0f;
+    if (u < 0.25)
+    {
+        float n = r.uf(1.3, 1.6), trn = r.uf(0.6, 0.9);
+        rt_MATERIAL *mo = sc.material(RT_MAT_PLAIN, col, dff, spc, pw,
+                                      0.0f, trn, 1.0f / n, 0.0f);
+        *inner = sc.material(RT_MAT_PLAIN, col, dff, spc, pw, 0.0f, trn, n, 0.0f);
+        return mo;
+    }
+    if (u < 0.40)
+    {
+        float rfl = r.uf(0.3, 0.7), ext = r.uf(2.0, 9.0);
+        rt_MATERIAL *mo = sc.material(RT_MAT_METAL, col, 1.0f, spc, pw,
+                                      rfl, 0.0f, 1.0f, ext);
+        *inner = sc.material(RT_MAT_PLAIN, 0x808080, dff, 0.0f, 1.0f,
+                             0.0f, 0.0f, 1.0f, 0.0f);
+        return mo;
+    }
+    float rfl = u < 0.55 ? r.uf(0.2, 0.5) : 0.0f;
+    rt_MATERIAL *mo = sc.material(RT_MAT_PLAIN, col, dff, spc, pw, rfl, 0.0f, 1.0f, 0.0f);
+    *inner = mo;
+    return mo;
+}
+
+/* a transform that is "trivial" in the reference's sense (multiples of 90
+ * degrees and a translation) placing a plane across local axis a (0 I, 1 J,
+ * 2 K) at offset d, facing +a or -a */
+static void axis_plane_trm(rt_TRANSFORM3D *t, int a, int flip, float d)
+{
+    float rx = 0.0f, ry = 0.0f;
+    if (a == 0) ry = flip ? -90.0f : 90.0f;
+    else if (a == 1) rx = flip ? 90.0f : -90.0f;
+    else rx = flip ? 180.0f : 0.0f;
+    Scene::trm_set(t, 1, 1, 1, rx, ry, 0, a == 0 ? d : 0.0f, a == 1 ? d : 0.0f,
+                   a == 2 ? d : 0.0f);
+}
+
+/* QR_SCN_ANIM: ground plane, 4 lights, and a 3-level hierarchy of spinning
+ * arrays (4 clusters x 4 groups x nq/16 items); each item is a quadric cut
+ * by 1-2 axis planes (RT_REL_MINUS_INNER/OUTER) whose caps are clipped back
+ * to the quadric's inside (RT_REL_MINUS_OUTER), and each cluster holds 2
+ * boolean-minus pairs (a sphere drilled by a cylinder) */
+static void build_anim(Scene &sc, uint64_t seed, int nq)
+{
+    Rng r(seed);
+    std::vector<rt_OBJECT> root;
+    root.push_back(look_camera(sc, 0.0f, -25.0f, 8.0f, 60.0f));
+    for (int i = 0; i < 4; i++)
+    {
+        float px = r.uf(-15, 15), py = r.uf(-15, 15), pz = r.uf(8, 15);
+        rt_ui32 col = pack_rgb(r.uf(0.3, 1.0), r.uf(0.3, 1.0), r.uf(0.3, 1.0));
+        if ((sc.flags & QR_GEN_ONELIGHT) && i > 0) continue;
+        root.push_back(sc.light(px, py, pz, col, 0.0f, 0.6f, 0.0f, 0.0f, 0.0f));
+    }
+    rt_MATERIAL *gm = sc.material(RT_MAT_PLAIN, 0xB0B0A8, 0.8f,
+                                  (sc.flags & QR_GEN_NOSPEC) ? 0.0f : 0.2f, 16.0f,
+                                  0.25f, 0.0f, 1.0f, 0.0f);
+    root.push_back(sc.plane(gm, gm));
+
+    int per_group = nq / 16 > 0 ? nq / 16 : 1;
+    for (int c = 0; c < 4; c++)
+    {
+        std::vector<rt_OBJECT> cluster;
+        for (int g = 0; g < 4; g++)
+        {
+            std::vector<rt_OBJECT> group;
+            for (int i = 0; i < per_group; i++)
+            {
+                std::vector<rt_OBJECT> item;
+                std::vector<rt_RELATION> rel;
+                rt_MATERIAL *mi, *mo = random_anim_material(sc, r, &mi);
+                int tag;
+                item.push_back(random_quadric(sc, r, mo, mi, &tag));
+                int np = r.ui(1, 2);
+                for (int j = 0; j < np; j++)
+                {
+                    rt_MATERIAL *pi, *po = random_anim_material(sc, r, &pi);
+                    rt_OBJECT p = sc.plane(po, pi);
+                    int a = r.ui(0, 2), flip = r.ui(0, 1);
+                    axis_plane_trm(&p.trm, a, flip, r.uf(-0.6, 0.6));
+                    rt_PLANE *pl = (rt_PLANE *)p.obj.pobj;
+                    pl->srf.min[RT_I] = -2.5f; pl->srf.max[RT_I] = +2.5f;
+                    pl->srf.min[RT_J] = -2.5f; pl->srf.max[RT_J] = +2.5f;
+                    item.push_back(p);
+                    rt_RELATION cut = {0, r.ui(0, 1) ? RT_REL_MINUS_INNER
+                                                     : RT_REL_MINUS_OUTER, j + 1};
+                    rt_RELATION cap = {j + 1, RT_REL_MINUS_OUTER, 0};
+                    rel.push_back(cut);
+                    rel.push_back(cap);
+                }
+                rt_OBJECT it = sc.array(item, &rel);
+                Scene::trm_set(&it.trm, 1, 1, 1, 0, 0, 0, r.uf(-1.5, 1.5),
+                               r.uf(-1.5, 1.5), r.uf(-1.0, 1.0));
+                it.f_anim = anim_spin;
+                group.push_back(it);
+            }
+            rt_OBJECT go = sc.array(group);
+            Scene::trm_set(&go.trm, 1, 1, 1, 0, 0, 0, r.uf(-3.0, 3.0),
+                           r.uf(-3.0, 3.0), r.uf(-0.5, 0.5));
+            go.f_anim = anim_spin;
+            cluster.push_back(go);
+        }
+        for (int b = 0; b < 2; b++)
+        {
+            std::vector<rt_OBJECT> pair;
+            std::vector<rt_RELATION> rel;
+            rt_MATERIAL *ai, *ao = random_anim_material(sc, r, &ai);
+            rt_MATERIAL *bi, *bo = random_anim_material(sc, r, &bi);
+            float ra = r.uf(0.8, 1.5);
+            pair.push_back(sc.quadric(RT_TAG_SPHERE, ra, 0.0f, -RT_INF, +RT_INF, ao, ai));
+            rt_OBJECT cyl = sc.quadric(RT_TAG_CYLINDER, ra * r.uf(0.3, 0.6), 0.0f,
+                                       -RT_INF, +RT_INF, bo, bi);
+            axis_plane_trm(&cyl.trm, r.ui(0, 2), 0, 0.0f);
+            pair.push_back(cyl);
+            rt_RELATION drill = {0, RT_REL_MINUS_INNER, 1};
+            rt_RELATION wall = {1, RT_REL_MINUS_OUTER, 0};
+            rel.push_back(drill);
+            rel.push_back(wall);
+            rt_OBJECT po = sc.array(pair, &rel);
+            Scene::trm_set(&po.trm, 1, 1, 1, 0, 0, 0, r.uf(-3.0, 3.0),
+                           r.uf(-3.0, 3.0), r.uf(0.5, 1.5));
+            po.f_anim = anim_spin;
+            cluster.push_back(po);
+        }
+        rt_OBJECT co = sc.array(cluster);
+        Scene::trm_set(&co.trm, 1, 1, 1, 0, 0, 0, r.uf(-9.0, 9.0),
+                       r.uf(-9.0, 9.0), r.uf(2.5, 4.0));
+        co.f_anim = anim_spin;
+        root.push_back(co);
+    }
+    rt_OBJECT ro = sc.array(root);
+    sc.scn.root = ro.obj;
+    sc.scn.opts = RT_OPTS_FRESNEL;      /* Fresnel on: opt out of the default */
+    sc.scn.lock = RT_NULL;
+}
+
 static Scene *build(int kind, uint64_t seed, int nq, int flags)
 {
     Scene *sc = new Scene();
     sc->flags = flags;
     switch (kind)
     {
+    case QR_SCN_ANIM:
+        build_anim(*sc, seed, nq > 0 ? nq : 64);
+        break;
     case QR_SCN_PLAIN:
     default:
         build_plain(*sc, seed, nq > 0 ? nq : 16, 2);

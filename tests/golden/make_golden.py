@@ -1,0 +1,70 @@
+"""Generate the golden fixtures of tests/golden/ from the reference engine.
+
+TEST INFRASTRUCTURE ONLY.  Runs the reference's own fp32 CPU renderer
+(VectorChief/QuadRay-engine rt_Scene::render, core/engine/engine.cpp:3014),
+built from the reference sources by ``make -C oracle ref`` into
+``oracle/_ref/ref_driver``, on the seeded synthetic scenes of
+quadray-engine_gb300/csrc/scenegen.hpp and stores each frame as a compressed
+``.npz`` (uint32 XRGB, H x W) plus the case parameters.  The fixtures pin the
+CPU restatement in oracle/qr_oracle.c (tests/test_oracle_golden.py) and the
+CUDA path (tests/test_gpu_parity.py) without the reference being present.
+
+    python tests/golden/make_golden.py            # (re)write all fixtures
+
+The reference is compiled with its SSE4 128-bit target (4 lanes), so the
+frames carry the SIMD-group effects of that target (see the oracle header).
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+# name: (kind, seed, nq, w, h, fsaa, frames, flags, opts)
+#   kind 1 = plain Whitted scene; flags 1 = hit-ID materials; fsaa 2 = 4x
+CASES = {
+    "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
+    "plain_s2_160x96":      (1, 2, 16, 160, 96, 0, 1, 0, "full"),
+    "plain_s3_160x96":      (1, 3, 16, 160, 96, 0, 1, 0, "full"),
+    "plain_s4_160x96":      (1, 4, 16, 160, 96, 0, 1, 0, "full"),
+    "plain_s5_none_160x96": (1, 5, 16, 160, 96, 0, 1, 0, "none"),
+    "plain_s1_ids_160x96":  (1, 1, 16, 160, 96, 0, 1, 1, "full"),
+    "plain_s6_ids_160x96":  (1, 6, 16, 160, 96, 0, 1, 1, "full"),
+    "plain_s2_aa4_128x80":  (1, 2, 16, 128, 80, 2, 1, 0, "full"),
+    "plain_s8_q32_200x120": (1, 8, 32, 200, 120, 0, 1, 0, "full"),
+    "plain_s9_ragged_37x23": (1, 9, 16, 37, 23, 0, 1, 0, "full"),
+}
+
+
+def run_case(name, case):
+    kind, seed, nq, w, h, fsaa, frames, flags, opts = case
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "frame.bin")
+        cmd = [DRIVER, str(kind), str(seed), str(nq), str(w), str(h),
+               str(fsaa), str(frames), str(flags), opts, out, "1"]
+        subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.DEVNULL)
+        data = np.fromfile(out, dtype="<u4").reshape(frames, h, w)
+    meta = dict(kind=kind, seed=seed, nq=nq, w=w, h=h, fsaa=fsaa,
+                frames=frames, flags=flags, opts=opts)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), frames=data,
+                        meta=json.dumps(meta))
+    return data
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        sys.exit("oracle/_ref/ref_driver is missing: run `make -C oracle ref`")
+    for name, case in CASES.items():
+        data = run_case(name, case)
+        print("%-24s %s nonzero=%d" % (name, data.shape, int((data != 0).sum())))
+
+
+if __name__ == "__main__":
+    main()

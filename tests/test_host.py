@@ -1,0 +1,171 @@
+"""Host-side logic without a GPU: the C-ABI library, struct layouts, the
+seeded scene generator and the host flattening.
+
+Nothing here launches a kernel.  The library must load and export every entry
+point include/qr_gpu.h declares; creating a context on a machine without a
+GPU must fail with a status code (the product has no CPU fallback).
+"""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "qr_gpu.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*|void)\s*\*?\s*(qr_\w+)\s*\(",
+                                 src, flags=re.M)))
+
+
+def test_header_declares_entry_points():
+    names = header_functions()
+    for n in ["qr_ctx_create", "qr_ctx_destroy", "qr_last_error", "qr_scene_upload",
+              "qr_scene_update", "qr_scene_release", "qr_render_device",
+              "qr_render_host", "qr_sync", "qr_render_stats"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(qr):
+    L = qr.lib()
+    missing = [n for n in header_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_context_without_gpu_fails_with_status(qr):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    p = ctypes.c_void_p()
+    rc = qr.lib().qr_ctx_create(0, ctypes.byref(p))
+    assert rc != qr.QR_OK
+    assert not p.value
+
+
+def test_null_arguments_rejected(qr):
+    L = qr.lib()
+    assert L.qr_ctx_create(0, None) != qr.QR_OK
+    assert L.qr_render_host(None, 0, None, None) != qr.QR_OK
+    assert L.qr_scene_upload(None, None, None) != qr.QR_OK
+
+
+def _c_layout():
+    """sizeof/offsetof of the ABI structs as a C compiler lays them out."""
+    prog = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "qr_gpu.h"
+#define P(T, F) printf(#T "." #F " %zu\n", offsetof(T, F))
+int main(void) {
+    printf("qr_srf %zu\nqr_mat %zu\nqr_light %zu\nqr_elem %zu\nqr_lelem %zu\n",
+           sizeof(qr_srf), sizeof(qr_mat), sizeof(qr_light), sizeof(qr_elem),
+           sizeof(qr_lelem));
+    printf("qr_scene_desc %zu\nqr_frame_params %zu\n", sizeof(qr_scene_desc),
+           sizeof(qr_frame_params));
+    P(qr_frame_params, x_res); P(qr_frame_params, seed); P(qr_frame_params, pts_c);
+    P(qr_scene_desc, texels); P(qr_scene_desc, cam_num);
+    P(qr_srf, sci); P(qr_srf, amap); P(qr_srf, trnode); P(qr_srf, id);
+    return 0;
+}
+"""
+    with tempfile.TemporaryDirectory() as td:
+        c = os.path.join(td, "l.c")
+        exe = os.path.join(td, "l")
+        open(c, "w").write(prog)
+        subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    return dict((k, int(v)) for k, v in (ln.split() for ln in out.splitlines()))
+
+
+def test_struct_layouts_match_ctypes_mirror(qr):
+    lay = _c_layout()
+    assert lay["qr_srf"] == 256
+    assert lay["qr_srf.sci"] % 16 == 0
+    assert lay["qr_elem"] == 16 and lay["qr_lelem"] == 16
+    assert lay["qr_light"] == 48
+    assert lay["qr_mat"] == 112
+    assert lay["qr_scene_desc"] == ctypes.sizeof(qr.QrSceneDesc)
+    assert lay["qr_frame_params"] == ctypes.sizeof(qr.QrFrameParams)
+    assert lay["qr_frame_params.x_res"] == qr.QrFrameParams.x_res.offset
+    assert lay["qr_frame_params.seed"] == qr.QrFrameParams.seed.offset
+    assert lay["qr_frame_params.pts_c"] == qr.QrFrameParams.pts_c.offset
+    assert lay["qr_scene_desc.texels"] == qr.QrSceneDesc.texels.offset
+    assert lay["qr_scene_desc.cam_num"] == qr.QrSceneDesc.cam_num.offset
+
+
+def _desc_arrays(desc, mat_size=112):
+    def arr(ptr, n, rec):
+        if n == 0:
+            return np.zeros((0, rec // 4), dtype=np.int32)
+        buf = (ctypes.c_char * (n * rec)).from_address(ptr)
+        return np.frombuffer(bytes(buf), dtype=np.int32).reshape(n, rec // 4)
+    return dict(srf=arr(desc.srf, desc.nsrf, 256), mat=arr(desc.mat, desc.nmat, mat_size),
+                lgt=arr(desc.lgt, desc.nlgt, 48), elems=arr(desc.elems, desc.nelem, 16),
+                lelems=arr(desc.lelems, desc.nlelem, 16))
+
+
+def _flat_arrays(qr, seed):
+    f = qr.Flat(qr.GenScene(qr.SCN_PLAIN, seed, 16), 64, 48)
+    return _desc_arrays(f.update(0, 10)[0])     # copied while f is alive
+
+
+def test_generation_is_deterministic(qr):
+    a, b, c = _flat_arrays(qr, 11), _flat_arrays(qr, 11), _flat_arrays(qr, 12)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert not np.array_equal(a["srf"], c["srf"])
+
+
+@pytest.mark.parametrize("nq", [1, 16, 64])
+def test_flattened_lists_are_consistent(qr, nq):
+    g = qr.GenScene(qr.SCN_PLAIN, 3, nq)
+    f = qr.Flat(g, 96, 64)
+    desc, params = f.update(0, 10)
+    A = _desc_arrays(desc)
+    srf, el, le = A["srf"], A["elems"], A["lelems"]
+    nsrf, nel = desc.nsrf, desc.nelem
+    assert 0 <= desc.cam_off and desc.cam_off + desc.cam_num <= nel
+    # qr_elem: kind, ref, last, rel
+    for kind, ref, last, rel in el:
+        assert kind in (0, 1, 2, 3)
+        if kind in (0, 1):
+            assert 0 <= ref < nsrf
+        if kind == 1:
+            assert 0 <= last < nel
+    # surface records: list ranges stay inside the element arrays
+    # int32 words: clip_off 45, clip_num 46, lgt_off 48-49, lgt_num 50-51,
+    # sec_off 52-53, sec_num 54-55, mat 40-41
+    for r in srf:
+        assert r[45] >= 0 and r[45] + r[46] <= nel
+        for s in (0, 1):
+            assert r[48 + s] >= 0 and r[48 + s] + r[50 + s] <= desc.nlelem
+            assert r[52 + s] >= 0 and r[52 + s] + r[54 + s] <= nel
+            assert -1 <= r[40 + s] < desc.nmat
+    for light, off, num, _ in le:
+        assert 0 <= light < desc.nlgt
+        assert 0 <= off and off + num <= nel
+    # the camera sees every surface of the plain scene (1 ground plane + nq)
+    cam = el[desc.cam_off:desc.cam_off + desc.cam_num]
+    seen = set(int(r) for k, r, _, _ in cam if k == 0)
+    assert len(seen) == nq + 1
+    assert params.x_res == 96 and params.y_res == 64 and params.x_row >= 96
+
+
+def test_frame_params_camera(qr):
+    """The ray basis spans the screen: hor/ver are 1/x_res of the camera axes."""
+    g = qr.GenScene(qr.SCN_PLAIN, 1, 16)
+    f = qr.Flat(g, 800, 480)
+    _, p = f.update(0, 10)
+    hor, ver = np.array(p.hor), np.array(p.ver)
+    assert abs(np.linalg.norm(hor) * 800 - 1.0) < 1e-5
+    assert abs(np.linalg.norm(ver) * 800 - 1.0) < 1e-5
+    assert abs(np.dot(hor, ver)) < 1e-6
+    assert np.allclose(p.org, [0.0, -25.0, 8.0])
+    assert abs(p.t_min - 0.5 / np.tan(np.radians(30.0))) < 1e-5
