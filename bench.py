@@ -2,19 +2,23 @@
 
 A step renders one frame of the workload.  ``value`` is rays/s with the scene
 resident in HBM and the frame written to device memory (CUDA events on the
-launching stream, L2 flushed between steps).  ``e2e`` is the same metric
+launching stream, L2 flushed between steps).  For the animated workload every
+step renders the next frame (t = 16 ms apart); the flattened scene of every
+frame is uploaded before the timed region.  ``e2e`` is the same metric
 through the engine API (rt_Scene::render) with a host frame buffer: host
-update phases, scene upload, render and frame download inside the timed
-region.  Rays are traced segments (primary + shadow + reflected/refracted),
-counted in an instrumented launch of the same frame.
+update phases (animation, transforms, lists), scene upload, render and frame
+download inside the timed region.  Rays are traced segments (primary +
+shadow + reflected/refracted), counted per frame by an instrumented build of
+the same kernel.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload plain|anim]
+                    [--workload anim|plain]
 """
 import argparse
 import ctypes
 import importlib
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -41,7 +45,12 @@ STAT_NAMES = ["ray_primary", "ray_shadow", "ray_secondary", "test_plane",
               "clip_custom", "shade", "light", "refract", "reflect"]
 
 WORKLOADS = {
-    # 800x480, 1 spp, 1 ground plane + 16 quadrics, 2 lights, shadows
+    # animated Whitted frame: 1920x1080, 4x AA, 64 quadrics cut by 1-2 planes
+    # each plus 8 boolean-minus pairs, 3-level spinning hierarchy, 4 lights,
+    # reflection + refraction with Fresnel to depth 4
+    "anim": dict(kind=2, seed=1, nq=64, w=1920, h=1080, fsaa=2, depth=4, anim=True),
+    # plain Whitted frame: 800x480, 1 spp, 1 ground plane + 16 quadrics,
+    # 2 lights, shadows
     "plain": dict(kind=1, seed=1, nq=16, w=800, h=480, fsaa=0, depth=10, anim=False),
 }
 
@@ -125,7 +134,8 @@ class ClockSampler:
 
 def cpu_baseline(qr, wl, seconds=12.0):
     """The CPU restatement of the reference tracer on the host cores, on a
-    bounded band of rows of the same frame; returns rays/s and the setup."""
+    bounded sample of rows of the workload's first frame; returns rays/s and
+    the setup."""
     import build as oracle_build
     O = oracle_build.load_oracle()
     g = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)
@@ -133,25 +143,32 @@ def cpu_baseline(qr, wl, seconds=12.0):
     desc, params = f.update(0, wl["depth"])
     cores = os.cpu_count() or 1
     out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+    # rows in a stride order spread over the whole frame (the top rows of a
+    # frame are mostly background and would flatter the CPU)
+    stride = 7919
+    while math.gcd(stride, params.y_res) != 1:
+        stride += 2
+    nxt = [0]
     rows_done = [0]
     rays = [0]
     lock = threading.Lock()
     t_end = time.perf_counter() + seconds
 
-    def worker(k):
-        y = k
+    def worker():
         while time.perf_counter() < t_end:
-            yy = y % params.y_res
+            with lock:
+                i = nxt[0]
+                nxt[0] += 1
+            yy = (i * stride) % params.y_res
             nr = ctypes.c_uint64()
             O.qr_oracle_render(ctypes.addressof(desc), ctypes.addressof(params),
                                out.ctypes.data, yy, yy + 1, ctypes.byref(nr))
             with lock:
                 rows_done[0] += 1
                 rays[0] += nr.value
-            y += cores
 
     t0 = time.perf_counter()
-    th = [threading.Thread(target=worker, args=(k,)) for k in range(cores)]
+    th = [threading.Thread(target=worker) for _ in range(cores)]
     for t in th:
         t.start()
     for t in th:
@@ -189,7 +206,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plain", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="anim", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -214,26 +231,40 @@ def main():
     qr = importlib.import_module("quadray-engine_gb300")
     gen = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)
     flat = qr.Flat(gen, wl["w"], wl["h"], wl["fsaa"])
-    desc, params = flat.update(0, wl["depth"])
     ctx = qr.Context(local)
-    sid = ctx.upload(desc)
+    nframes = args.warmup + args.steps if wl["anim"] else 1
+    sids, scene_bytes = [], 0
+    for j in range(nframes):
+        desc, params = flat.update(16 * j, wl["depth"])
+        sids.append(ctx.upload(desc))
+        scene_bytes = (desc.nsrf * 256 + desc.nmat * 112 + desc.nlgt * 48 +
+                       desc.nelem * 16 + desc.nlelem * 16 + desc.ntex * 4)
 
-    # instrumented launch: rays and work counters of one frame
-    counts = (ctypes.c_uint64 * 13)()
+    def sid_of(j):
+        return sids[j] if wl["anim"] else sids[0]
+
+    # instrumented launches: rays and work counters of every timed frame
     host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
-    rc = qr.lib().qr_render_stats(ctx.h, sid, ctypes.byref(params),
-                                  host.ctypes.data_as(ctypes.c_void_p), counts)
-    assert rc == 0, ctx.error()
-    stats = dict(zip(STAT_NAMES, [int(c) for c in counts]))
-    rays = stats["ray_primary"] + stats["ray_shadow"] + stats["ray_secondary"]
-    flops = sum(stats[k] * v for k, v in FLOPS.items())
+    stats = dict((k, 0) for k in STAT_NAMES)
+    frame_rays = []
+    for i in range(args.steps if wl["anim"] else 1):
+        counts = (ctypes.c_uint64 * 13)()
+        rc = qr.lib().qr_render_stats(ctx.h, sid_of(args.warmup + i), ctypes.byref(params),
+                                      host.ctypes.data_as(ctypes.c_void_p), counts)
+        assert rc == 0, ctx.error()
+        for k, c in zip(STAT_NAMES, counts):
+            stats[k] += int(c)
+        frame_rays.append(int(counts[0]) + int(counts[1]) + int(counts[2]))
+    nstat = len(frame_rays)
+    rays = sum(frame_rays) / nstat                      # per frame (mean)
+    flops = sum(stats[k] * v for k, v in FLOPS.items()) / nstat
 
     frame = torch.empty((params.y_res, params.x_row), dtype=torch.int32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
-    for _ in range(args.warmup):
-        ctx.render_device(sid, params, frame.data_ptr(), sp)
+    for j in range(args.warmup):
+        ctx.render_device(sid_of(j), params, frame.data_ptr(), sp)
     torch.cuda.synchronize()
 
     if dist is not None:
@@ -246,7 +277,7 @@ def main():
     for i in range(args.steps):
         flush.zero_()
         ev[i][0].record(stream)
-        ctx.render_device(sid, params, frame.data_ptr(), sp)
+        ctx.render_device(sid_of(args.warmup + i), params, frame.data_ptr(), sp)
         ev[i][1].record(stream)
     torch.cuda.synchronize()
     ck = clocks.stop()
@@ -260,16 +291,16 @@ def main():
     eng = qr.Engine(qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0), wl["w"], wl["h"],
                     fsaa=wl["fsaa"], depth=wl["depth"])
     hbuf = np.zeros((wl["h"], wl["w"]), dtype=np.uint32)
-    for i in range(args.warmup):
-        eng.render(0, hbuf)
+    step_t = (lambda j: 16 * j) if wl["anim"] else (lambda j: 0)
+    for j in range(args.warmup):
+        eng.render(step_t(j), hbuf)
     lat = []
     for i in range(args.steps):
         t0 = time.perf_counter()
-        eng.render(0, hbuf)
+        eng.render(step_t(args.warmup + i), hbuf)
         lat.append(time.perf_counter() - t0)
     e2e_t = sum(lat)
-    h2d = (desc.nsrf * 256 + desc.nmat * 112 + desc.nlgt * 48 + desc.nelem * 16 +
-           desc.nlelem * 16 + desc.ntex * 4)
+    h2d = scene_bytes
     d2h = wl["w"] * wl["h"] * 4
     eng.close()
 
@@ -285,7 +316,8 @@ def main():
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "width": wl["w"], "height": wl["h"],
                    "fsaa": wl["fsaa"], "quadrics": wl["nq"], "seed": wl["seed"],
-                   "depth": wl["depth"], "rays_per_frame": rays,
+                   "depth": wl["depth"], "animated": wl["anim"],
+                   "surfaces": int(desc.nsrf), "rays_per_frame": rays,
                    "l2": "256 MiB buffer written between timed steps",
                    "parallelism": "replicas" if world > 1 else "single"},
         "frames_per_s": fps,
@@ -299,7 +331,7 @@ def main():
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
                      "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x max clock)",
                      "flops_per_frame": flops},
-        "work": stats,
+        "work_per_frame": dict((k, v / nstat) for k, v in stats.items()),
         "gpu_launches": args.steps,
         "clocks": ck,
     }

@@ -23,6 +23,7 @@ SCN_PLAIN = 1
 SCN_ANIM = 2
 SCN_PT = 3
 GEN_IDS = 1 << 0
+GEN_TARRAY = 1 << 3      # animated scene keeps RT_OPTS_TARRAY on
 
 # runtime options (csrc/format.h): -1 selects the default (FULL minus the
 # scene's opt-outs)

@@ -23,7 +23,10 @@ DEV_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-prec-div=true",
 HOST_FLAGS = ["-Xcompiler", "-fPIC,-O2,-ffp-contract=off,-fno-fast-math"]
 INCS = ["-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
 
-SOURCES = ["tracer.cu", "capi.cu", "flatten.cpp", "engine.cpp", "pyshim.cpp"]
+SOURCES = ["tracer.cu", "tracer_stats.cu", "capi.cu", "flatten.cpp", "engine.cpp",
+           "pyshim.cpp"]
+# sources that textually include another translation unit
+INCLUDES = {"tracer_stats.cu": ["tracer.cu"]}
 
 
 def _nvcc():
@@ -61,7 +64,8 @@ def build(verbose=False, force=False):
         path = os.path.join(CSRC, src)
         obj = os.path.join(OUT, src + ".o")
         objs.append(obj)
-        if force or _stale(obj, [path] + headers):
+        extra = [os.path.join(CSRC, f) for f in INCLUDES.get(src, [])]
+        if force or _stale(obj, [path] + headers + extra):
             cmd = [nvcc] + ARCH + DEV_FLAGS + HOST_FLAGS + INCS + \
                   ["-c", path, "-o", obj]
             if src.endswith(".cu"):

@@ -15,10 +15,6 @@
 #include "qr_gpu.h"
 #include "tracer.cuh"
 
-/* device stack per thread: the tracer recurses for refracted and reflected
- * rays, up to the scene's depth (at most QR_MAX_DEPTH levels) */
-#define QR_MAX_DEPTH        10
-#define QR_STACK_BYTES      (24 * 1024)
 
 struct qr_scene_slot
 {
@@ -61,7 +57,6 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
     ctx->dframe_px = 0;
     ctx->stream = 0;
     cudaError_t e = cudaSetDevice(device);
-    if (e == cudaSuccess) e = cudaDeviceSetLimit(cudaLimitStackSize, QR_STACK_BYTES);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess)
     {
@@ -264,7 +259,7 @@ extern "C" int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params
     int rc = check_fp(fp);
     if (rc != QR_OK) return rc;
     if (dev_frame == NULL) return QR_ERR_ARG;
-    cudaError_t e = qr_launch_whitted(sl->d, *fp, dev_frame, NULL,
+    cudaError_t e = qr_launch_whitted(sl->d, *fp, dev_frame,
                                       (cudaStream_t)stream);
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "whitted launch", e);
     return QR_OK;
@@ -288,7 +283,7 @@ extern "C" int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *
         if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaMalloc frame", e);
         ctx->dframe_px = px;
     }
-    if (e == cudaSuccess) e = qr_launch_whitted(sl->d, *fp, ctx->dframe, NULL, ctx->stream);
+    if (e == cudaSuccess) e = qr_launch_whitted(sl->d, *fp, ctx->dframe, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(host_frame, ctx->dframe, px * sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, ctx->stream);
@@ -313,7 +308,7 @@ extern "C" int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params 
     if (e == cudaSuccess) e = cudaMalloc(&dframe, px * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&dst, sizeof(qr_dstats));
     if (e == cudaSuccess) e = cudaMemsetAsync(dst, 0, sizeof(qr_dstats), ctx->stream);
-    if (e == cudaSuccess) e = qr_launch_whitted(sl->d, *fp, dframe, dst, ctx->stream);
+    if (e == cudaSuccess) e = qr_launch_whitted_stats(sl->d, *fp, dframe, dst, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(host_frame, dframe, px * sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, ctx->stream);

@@ -46,6 +46,7 @@
 #define QR_GEN_IDS      (1 << 0)   /* hit-ID materials */
 #define QR_GEN_NOSPEC   (1 << 1)   /* debug: no specular */
 #define QR_GEN_ONELIGHT (1 << 2)   /* debug: a single light */
+#define QR_GEN_TARRAY   (1 << 3)   /* QR_SCN_ANIM: keep RT_OPTS_TARRAY on */
 
 namespace qr_gen
 {
@@ -78,6 +79,26 @@ static inline rt_ui32 pack_rgb(float r, float g, float b)
     if (cg > 255) cg = 255;
     if (cb > 255) cb = 255;
     return (cr << 16) | (cg << 8) | cb;
+}
+
+/* a random colour, channels drawn in the order r, g, b (separate statements:
+ * the evaluation order of function arguments differs between compilers and
+ * targets, so no call below takes two draws as arguments) */
+static inline rt_ui32 rand_rgb(Rng &r, double lo, double hi)
+{
+    float cr = r.uf(lo, hi);
+    float cg = r.uf(lo, hi);
+    float cb = r.uf(lo, hi);
+    return pack_rgb(cr, cg, cb);
+}
+
+/* a random position in a box, drawn x, y, z */
+static inline void rand_pos(Rng &r, float p[3], double x0, double x1, double y0,
+                            double y1, double z0, double z1)
+{
+    p[0] = r.uf(x0, x1);
+    p[1] = r.uf(y0, y1);
+    p[2] = r.uf(z0, z1);
 }
 
 /*
@@ -331,7 +352,7 @@ static rt_OBJECT random_quadric(Scene &sc, Rng &r, rt_MATERIAL *mo,
 
 static rt_MATERIAL *random_plain(Scene &sc, Rng &r)
 {
-    rt_ui32 col = pack_rgb(r.uf(0.2, 1.0), r.uf(0.2, 1.0), r.uf(0.2, 1.0));
+    rt_ui32 col = rand_rgb(r, 0.2, 1.0);
     float dff = r.uf(0.2, 0.9);
     float spc = r.uf(0.1, 0.6);
     float pw  = (float)r.ui(8, 64);
@@ -359,7 +380,7 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
     for (int i = 0; i < nl; i++)
     {
         float px = r.uf(-15, 15), py = r.uf(-15, 15), pz = r.uf(8, 15);
-        rt_ui32 col = pack_rgb(r.uf(0.3, 1.0), r.uf(0.3, 1.0), r.uf(0.3, 1.0));
+        rt_ui32 col = rand_rgb(r, 0.3, 1.0);
         if ((sc.flags & QR_GEN_ONELIGHT) && i > 0) continue;
         root.push_back(sc.light(px, py, pz, col, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f));
     }
@@ -389,7 +410,7 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
 static rt_MATERIAL *random_anim_material(Scene &sc, Rng &r, rt_MATERIAL **inner)
 {
     double u = r.u01();
-    rt_ui32 col = pack_rgb(r.uf(0.2, 1.0), r.uf(0.2, 1.0), r.uf(0.2, 1.0));
+    rt_ui32 col = rand_rgb(r, 0.2, 1.0);
     float dff = r.uf(0.2, 0.9);
     float spc = r.uf(0.1, 0.6);
     float pw  = (float)r.ui(8, 64);
@@ -443,7 +464,7 @@ static void build_anim(Scene &sc, uint64_t seed, int nq)
     for (int i = 0; i < 4; i++)
     {
         float px = r.uf(-15, 15), py = r.uf(-15, 15), pz = r.uf(8, 15);
-        rt_ui32 col = pack_rgb(r.uf(0.3, 1.0), r.uf(0.3, 1.0), r.uf(0.3, 1.0));
+        rt_ui32 col = rand_rgb(r, 0.3, 1.0);
         if ((sc.flags & QR_GEN_ONELIGHT) && i > 0) continue;
         root.push_back(sc.light(px, py, pz, col, 0.0f, 0.6f, 0.0f, 0.0f, 0.0f));
     }
@@ -484,14 +505,16 @@ static void build_anim(Scene &sc, uint64_t seed, int nq)
                     rel.push_back(cap);
                 }
                 rt_OBJECT it = sc.array(item, &rel);
-                Scene::trm_set(&it.trm, 1, 1, 1, 0, 0, 0, r.uf(-1.5, 1.5),
-                               r.uf(-1.5, 1.5), r.uf(-1.0, 1.0));
+                float ip[3];
+                rand_pos(r, ip, -1.5, 1.5, -1.5, 1.5, -1.0, 1.0);
+                Scene::trm_set(&it.trm, 1, 1, 1, 0, 0, 0, ip[0], ip[1], ip[2]);
                 it.f_anim = anim_spin;
                 group.push_back(it);
             }
             rt_OBJECT go = sc.array(group);
-            Scene::trm_set(&go.trm, 1, 1, 1, 0, 0, 0, r.uf(-3.0, 3.0),
-                           r.uf(-3.0, 3.0), r.uf(-0.5, 0.5));
+            float gp[3];
+            rand_pos(r, gp, -3.0, 3.0, -3.0, 3.0, -0.5, 0.5);
+            Scene::trm_set(&go.trm, 1, 1, 1, 0, 0, 0, gp[0], gp[1], gp[2]);
             go.f_anim = anim_spin;
             cluster.push_back(go);
         }
@@ -512,20 +535,28 @@ static void build_anim(Scene &sc, uint64_t seed, int nq)
             rel.push_back(drill);
             rel.push_back(wall);
             rt_OBJECT po = sc.array(pair, &rel);
-            Scene::trm_set(&po.trm, 1, 1, 1, 0, 0, 0, r.uf(-3.0, 3.0),
-                           r.uf(-3.0, 3.0), r.uf(0.5, 1.5));
+            float pp[3];
+            rand_pos(r, pp, -3.0, 3.0, -3.0, 3.0, 0.5, 1.5);
+            Scene::trm_set(&po.trm, 1, 1, 1, 0, 0, 0, pp[0], pp[1], pp[2]);
             po.f_anim = anim_spin;
             cluster.push_back(po);
         }
         rt_OBJECT co = sc.array(cluster);
-        Scene::trm_set(&co.trm, 1, 1, 1, 0, 0, 0, r.uf(-9.0, 9.0),
-                       r.uf(-9.0, 9.0), r.uf(2.5, 4.0));
+        float cp[3];
+        rand_pos(r, cp, -9.0, 9.0, -9.0, 9.0, 2.5, 4.0);
+        Scene::trm_set(&co.trm, 1, 1, 1, 0, 0, 0, cp[0], cp[1], cp[2]);
         co.f_anim = anim_spin;
         root.push_back(co);
     }
     rt_OBJECT ro = sc.array(root);
     sc.scn.root = ro.obj;
-    sc.scn.opts = RT_OPTS_FRESNEL;      /* Fresnel on: opt out of the default */
+    /* opt-outs of the reference's default options (rt_SCENE.opts): Fresnel
+     * on, and no array-level transform nodes (RT_OPTS_TARRAY), under which
+     * the reference's per-surface shadow and secondary-ray lists of this
+     * spinning hierarchy lose occluders and candidates (its frame then
+     * departs from its own unculled render); QR_GEN_TARRAY keeps it on */
+    sc.scn.opts = RT_OPTS_FRESNEL;
+    if ((sc.flags & QR_GEN_TARRAY) == 0) sc.scn.opts |= RT_OPTS_TARRAY;
     sc.scn.lock = RT_NULL;
 }
 

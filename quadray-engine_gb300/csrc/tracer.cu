@@ -31,11 +31,30 @@
 #define T_EPS       0.0000001f      /* root-split threshold, object.h:42 */
 #define SIGN_BIT    0x80000000u
 
-namespace qr_dev
+/*
+ * Work counters.  This file is compiled twice: as namespace qr_dev (the
+ * timed kernel, no counter code at all) and, from tracer_stats.cu with
+ * QR_STATS defined, as namespace qr_dev_stats, where every counted event
+ * increments a per-thread counter that is warp-reduced into the global
+ * totals once at the end of the kernel.
+ */
+#ifdef QR_STATS
+#define QR_NS qr_dev_stats
+#else
+#define QR_NS qr_dev
+#endif
+
+namespace QR_NS
 {
 
-/* work counters of instrumented launches (st == NULL in timed launches) */
-#define CNT(k) do { if (st != NULL) atomicAdd(&st->c[k], 1ull); } while (0)
+#ifdef QR_STATS
+struct TCnt { uint32_t c[QR_STAT_COUNT]; };
+typedef TCnt *StP;
+#define CNT(k) (st->c[k]++)
+#else
+typedef void *StP;
+#define CNT(k) ((void)0)
+#endif
 
 struct Ray
 {
@@ -97,7 +116,7 @@ __device__ __forceinline__ void xform(const qr_srf *__restrict__ t,
 __device__ int clip_root(const qr_dscene &S, const Ray &r, int si, float t,
                          float tbuf, const float ldff[3], const float lray[3],
                          int side, int dmask, uint32_t amask, float hit[3],
-                         float loc[3], qr_dstats *st)
+                         float loc[3], StP st)
 {
     CNT(QR_STAT_CLIP_ROOT);
     const qr_srf *__restrict__ s = &S.srf[si];
@@ -277,7 +296,7 @@ __device__ __forceinline__ int side_blocked(const Ray &r, int si, int side)
 /* quadric roots with root sorting and splitting (5785-6206) */
 __device__ void root_pair(const qr_dscene &S, const Ray &r, Walk &w, int si,
                           const float ldff[3], const float lray[3],
-                          float a, float b, float c, float d, qr_dstats *st)
+                          float a, float b, float c, float d, StP st)
 {
     if (!(0.0f <= d)) return;
     const float nb = fxor(b, SIGN_BIT);
@@ -343,7 +362,7 @@ __device__ void root_pair(const qr_dscene &S, const Ray &r, Walk &w, int si,
 
 /* list walk (2413-2680) with the solvers (5522-6497) */
 __device__ void walk(const qr_dscene &S, const Ray &r, int off, int num, Walk &w,
-                     qr_dstats *st)
+                     StP st)
 {
     float cdff[3] = {0.0f, 0.0f, 0.0f}, cray[3] = {0.0f, 0.0f, 0.0f};
     int cache_last = -1;
@@ -473,20 +492,27 @@ __device__ void walk(const qr_dscene &S, const Ray &r, int off, int num, Walk &w
     }
 }
 
-__device__ void trace(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
-                      int off, int num, float col[3], qr_dstats *st);
+/* what a shaded hit asks of its children: a refracted ray (weight c_trn)
+ * and a reflected ray (weight c_rfl), traced in that order (4820-4883,
+ * 5235-5298) */
+struct Sec
+{
+    int   trn, rfl;             /* child wanted (before the depth check) */
+    float c_trn, c_rfl;
+    float nw[3], rw[3];         /* refracted / reflected directions */
+};
 
-/* shading (3255-5359): normal, texel, ambient, lights with shadows,
- * transparency, reflection */
-__device__ void shade(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
-                      const Hit &h, float col[3], qr_dstats *st)
+/* shading of one hit (3255-5359): normal, texel, ambient, lights with
+ * shadows; computes (but does not trace) the refracted and reflected rays */
+__device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                            const Hit &h, float c[3], Sec &o, StP st)
 {
     const qr_srf *__restrict__ s = &S.srf[h.srf];
     const int side = h.side;
     const int props = __ldg(&s->props[side]);
     const qr_mat *__restrict__ m = &S.mat[__ldg(&s->mat[side])];
     const uint32_t tside = side ? SIGN_BIT : 0u;
-    float nrm[3], tex[3], c[3];
+    float nrm[3], tex[3];
     float tu = 0.0f, tv = 0.0f;
     const int nrmk = __ldg(&s->nrmk);
 
@@ -734,6 +760,7 @@ __device__ void shade(const qr_dscene &S, const qr_frame_params &P, const Ray &r
 
     /* transparency (4442-4936) */
     float c_trn = m_trn, c_rfl = m_rfl;
+    o.trn = 0;
     if (!(props & QR_PROP_OPAQUE))
     {
         const int fres = (props & QR_PROP_FRESNEL) != 0;
@@ -811,33 +838,9 @@ __device__ void shade(const qr_dscene &S, const qr_frame_params &P, const Ray &r
             for (int k = 0; k < 3; k++) nw[k] = r.dir[k];
             do_trn = 1;
         }
-        if (do_trn && m_ok)
-        {
-            float tc[3] = {0.0f, 0.0f, 0.0f};
-            if (r.depth != 0)
-            {
-                Ray cr;
-                #pragma unroll
-                for (int k = 0; k < 3; k++)
-                {
-                    cr.org[k] = h.hit[k];
-                    cr.dir[k] = nw[k];
-                    cr.phit[k] = h.loc[k];
-                }
-                cr.t_min = 0.0f;
-                cr.t_max = FLT_MAX;
-                cr.from = h.srf;
-                cr.flags = side | FLAG_PASS;
-                cr.depth = r.depth - 1;
-                CNT(QR_STAT_RAY_SECONDARY);
-                trace(S, P, cr, __ldg(&s->sec_off[1 - side]),
-                      __ldg(&s->sec_num[1 - side]), tc, st);
-                #pragma unroll
-                for (int k = 0; k < 3; k++) tc[k] = tc[k] * c_trn;
-            }
-            #pragma unroll
-            for (int k = 0; k < 3; k++) c[k] = tc[k] + c[k];
-        }
+        o.trn = do_trn && m_ok;
+        #pragma unroll
+        for (int k = 0; k < 3; k++) o.nw[k] = nw[k];
     }
 
     /* reflection (4942-5359) */
@@ -917,52 +920,181 @@ __device__ void shade(const qr_dscene &S, const qr_frame_params &P, const Ray &r
                 fr = fr * m_rfl;
                 c_rfl = m_rfl + fr;
             }
-            float rc[3] = {0.0f, 0.0f, 0.0f};
-            if (r.depth != 0)
+            #pragma unroll
+            for (int k = 0; k < 3; k++) o.rw[k] = rw[k];
+        }
+        o.rfl = do_rfl;
+    }
+    o.c_trn = c_trn;
+    o.c_rfl = c_rfl;
+}
+
+/* a shaded hit waiting for the colour of its refracted child (stage 0) or
+ * reflected child (stage 1) */
+struct Pend
+{
+    float c[3];
+    float c_trn, c_rfl;
+    float hit[3], loc[3], rw[3];
+    int   srf, side, depth, stage, rfl;
+};
+
+__device__ __forceinline__ void child_ray(Ray &cr, const float hit[3], const float dir[3],
+                                          const float loc[3], int srf, int flags,
+                                          int depth)
+{
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        cr.org[k] = hit[k];
+        cr.dir[k] = dir[k];
+        cr.phit[k] = loc[k];
+    }
+    cr.t_min = 0.0f;
+    cr.t_max = FLT_MAX;
+    cr.from = srf;
+    cr.flags = flags;
+    cr.depth = depth;
+}
+
+/*
+ * The Whitted ray tree of one camera ray, without recursion.  The reference
+ * recurses through its context stack (tracer.cpp:4820-4860, 5235-5275); here
+ * a shaded hit that spawns a child is parked on a small per-thread stack and
+ * combined when the child's colour is known, in the reference's order:
+ * colour = rc * c_rfl + (tc * c_trn + local).
+ */
+__device__ void trace_tree(const qr_dscene &S, const qr_frame_params &P, Ray r,
+                           int off, int num, float col[3], StP st)
+{
+    Pend stk[QR_MAX_DEPTH];
+    int sp = 0;
+    float ret[3];
+    #pragma unroll 1
+    for (;;)
+    {
+        Walk w;
+        w.shadow = 0;
+        w.occluded = 0;
+        w.tbuf = r.t_max;
+        w.best.srf = -1;
+        walk(S, r, off, num, w, st);
+        if (w.best.srf < 0)
+        {
+            ret[0] = ret[1] = ret[2] = 0.0f;
+        }
+        else
+        {
+            CNT(QR_STAT_SHADE);
+            float c[3];
+            Sec o;
+            shade_local(S, P, r, w.best, c, o, st);
+            const qr_srf *__restrict__ s = &S.srf[w.best.srf];
+            const int side = w.best.side;
+            int spawned = 0;
+            if (o.trn)
             {
-                Ray cr;
+                if (r.depth != 0)
+                {
+                    Pend &p = stk[sp++];
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++)
+                    {
+                        p.c[k] = c[k];
+                        p.hit[k] = w.best.hit[k];
+                        p.loc[k] = w.best.loc[k];
+                        p.rw[k] = o.rw[k];
+                    }
+                    p.c_trn = o.c_trn;
+                    p.c_rfl = o.c_rfl;
+                    p.srf = w.best.srf;
+                    p.side = side;
+                    p.depth = r.depth;
+                    p.stage = 0;
+                    p.rfl = o.rfl;
+                    CNT(QR_STAT_RAY_SECONDARY);
+                    const int d = r.depth - 1;
+                    child_ray(r, w.best.hit, o.nw, w.best.loc, w.best.srf,
+                              side | FLAG_PASS, d);
+                    off = __ldg(&s->sec_off[1 - side]);
+                    num = __ldg(&s->sec_num[1 - side]);
+                    spawned = 1;
+                }
+                else
+                {
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++) c[k] = 0.0f + c[k];
+                }
+            }
+            if (!spawned && o.rfl)
+            {
+                if (r.depth != 0)
+                {
+                    Pend &p = stk[sp++];
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++) p.c[k] = c[k];
+                    p.c_rfl = o.c_rfl;
+                    p.stage = 1;
+                    CNT(QR_STAT_RAY_SECONDARY);
+                    const int d = r.depth - 1;
+                    child_ray(r, w.best.hit, o.rw, w.best.loc, w.best.srf, side, d);
+                    off = __ldg(&s->sec_off[side]);
+                    num = __ldg(&s->sec_num[side]);
+                    spawned = 1;
+                }
+                else
+                {
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++) c[k] = 0.0f + c[k];
+                }
+            }
+            if (spawned) continue;
+            #pragma unroll
+            for (int k = 0; k < 3; k++) ret[k] = c[k];
+        }
+
+        /* fold finished children into their parents */
+        int more = 0;
+        while (sp > 0)
+        {
+            Pend &p = stk[sp - 1];
+            if (p.stage == 0)
+            {
                 #pragma unroll
                 for (int k = 0; k < 3; k++)
                 {
-                    cr.org[k] = h.hit[k];
-                    cr.dir[k] = rw[k];
-                    cr.phit[k] = h.loc[k];
+                    const float tc = ret[k] * p.c_trn;
+                    p.c[k] = tc + p.c[k];
                 }
-                cr.t_min = 0.0f;
-                cr.t_max = FLT_MAX;
-                cr.from = h.srf;
-                cr.flags = side;
-                cr.depth = r.depth - 1;
-                CNT(QR_STAT_RAY_SECONDARY);
-                trace(S, P, cr, __ldg(&s->sec_off[side]), __ldg(&s->sec_num[side]),
-                      rc, st);
+                if (p.rfl)
+                {
+                    const qr_srf *__restrict__ s = &S.srf[p.srf];
+                    p.stage = 1;
+                    CNT(QR_STAT_RAY_SECONDARY);
+                    child_ray(r, p.hit, p.rw, p.loc, p.srf, p.side, p.depth - 1);
+                    off = __ldg(&s->sec_off[p.side]);
+                    num = __ldg(&s->sec_num[p.side]);
+                    more = 1;
+                    break;
+                }
+            }
+            else
+            {
                 #pragma unroll
-                for (int k = 0; k < 3; k++) rc[k] = rc[k] * c_rfl;
+                for (int k = 0; k < 3; k++)
+                {
+                    const float rc = ret[k] * p.c_rfl;
+                    p.c[k] = rc + p.c[k];
+                }
             }
             #pragma unroll
-            for (int k = 0; k < 3; k++) c[k] = rc[k] + c[k];
+            for (int k = 0; k < 3; k++) ret[k] = p.c[k];
+            sp--;
         }
+        if (!more) break;
     }
     #pragma unroll
-    for (int k = 0; k < 3; k++) col[k] = c[k];
-}
-
-__device__ void trace(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
-                      int off, int num, float col[3], qr_dstats *st)
-{
-    Walk w;
-    w.shadow = 0;
-    w.occluded = 0;
-    w.tbuf = r.t_max;
-    w.best.srf = -1;
-    walk(S, r, off, num, w, st);
-    if (w.best.srf < 0)
-    {
-        col[0] = col[1] = col[2] = 0.0f;
-        return;
-    }
-    CNT(QR_STAT_SHADE);
-    shade(S, P, r, w.best, col, st);
+    for (int k = 0; k < 3; k++) col[k] = ret[k];
 }
 
 /* sub-sample offsets of the 4x rotated grid (engine.cpp:3572-3606) */
@@ -973,7 +1105,7 @@ __constant__ float c_aa4_v[4] = {+0.08f - 0.25f, -0.08f - 0.25f,
 
 __device__ __forceinline__ void primary(const qr_dscene &S, const qr_frame_params &P,
                                         float hs, float vs, float col[3],
-                                        qr_dstats *st)
+                                        StP st)
 {
     Ray r;
     #pragma unroll
@@ -992,7 +1124,7 @@ __device__ __forceinline__ void primary(const qr_dscene &S, const qr_frame_param
     r.flags = 0;
     r.depth = P.depth;
     CNT(QR_STAT_RAY_PRIMARY);
-    trace(S, P, r, S.cam_off, S.cam_num, col, st);
+    trace_tree(S, P, r, S.cam_off, S.cam_num, col, st);
 }
 
 __device__ __forceinline__ float clamp1(float v) { return v < 1.0f ? v : 1.0f; }
@@ -1017,11 +1149,20 @@ __device__ __forceinline__ uint32_t pack(const qr_frame_params &P, const float c
 
 __global__ void __launch_bounds__(128)
 whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
-               qr_dstats *st)
+               qr_dstats *gst)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= P.x_res || y >= P.y_res) return;
+#ifdef QR_STATS
+    TCnt cnt;
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
+    StP st = &cnt;
+#else
+    StP st = NULL;
+    (void)gst;
+#endif
     float col[3];
     if (P.fsaa == 2)
     {
@@ -1048,17 +1189,37 @@ whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
         for (int k = 0; k < 3; k++) col[k] = clamp1(col[k]);
     }
     frame[(size_t)y * P.x_row + x] = pack(P, col);
+#ifdef QR_STATS
+    const unsigned am = __activemask();
+    const int leader = __ffs(am) - 1;
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++)
+    {
+        const unsigned v = __reduce_add_sync(am, cnt.c[k]);
+        if ((int)(threadIdx.x & 31) == leader && v != 0)
+            atomicAdd(&gst->c[k], (unsigned long long)v);
+    }
+#endif
 }
 
-} /* namespace qr_dev */
+} /* namespace QR_NS */
 
+#ifdef QR_STATS
+cudaError_t qr_launch_whitted_stats(const qr_dscene &sc, const qr_frame_params &fp,
+                                    uint32_t *dev_frame, qr_dstats *dstats,
+                                    cudaStream_t stream)
+#else
 cudaError_t qr_launch_whitted(const qr_dscene &sc, const qr_frame_params &fp,
-                              uint32_t *dev_frame, qr_dstats *dstats,
-                              cudaStream_t stream)
+                              uint32_t *dev_frame, cudaStream_t stream)
+#endif
 {
     const dim3 block(32, 4);
     const dim3 grid((fp.x_res + block.x - 1) / block.x,
                     (fp.y_res + block.y - 1) / block.y);
-    qr_dev::whitted_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, dstats);
+#ifdef QR_STATS
+    QR_NS::whitted_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, dstats);
+#else
+    QR_NS::whitted_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, NULL);
+#endif
     return cudaGetLastError();
 }

@@ -7,6 +7,11 @@
 #include <stdint.h>
 #include "qr_gpu.h"
 
+/* secondary-ray depth limit: the reference's context stack depth
+ * (RT_STACK_DEPTH, core/tracer/tracer.h:51); the tracer keeps one pending
+ * shaded hit per level */
+#define QR_MAX_DEPTH        10
+
 /* device copy of a flattened scene (qr_scene_desc with device pointers) */
 struct qr_dscene
 {
@@ -28,7 +33,12 @@ struct qr_dstats
 
 /* launch the per-pixel Whitted kernel for one frame */
 cudaError_t qr_launch_whitted(const qr_dscene &sc, const qr_frame_params &fp,
-                              uint32_t *dev_frame, qr_dstats *dstats,
-                              cudaStream_t stream);
+                              uint32_t *dev_frame, cudaStream_t stream);
+
+/* the same kernel built with work counters (tracer_stats.cu); dstats must
+ * hold zeros before the launch */
+cudaError_t qr_launch_whitted_stats(const qr_dscene &sc, const qr_frame_params &fp,
+                                    uint32_t *dev_frame, qr_dstats *dstats,
+                                    cudaStream_t stream);
 
 #endif /* QR_TRACER_CUH */

@@ -26,8 +26,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
-# name: (kind, seed, nq, w, h, fsaa, frames, flags, opts)
-#   kind 1 = plain Whitted scene; flags 1 = hit-ID materials; fsaa 2 = 4x
+# name: (kind, seed, nq, w, h, fsaa, frames, flags, opts[, depth])
+#   kind 1 = plain Whitted scene, 2 = animated scene (clippers, booleans,
+#   3-level spinning hierarchy, reflection/refraction with Fresnel; frames
+#   at t = 0, 16, 32 ms); flags 1 = hit-ID materials, 8 = animated scene
+#   that keeps RT_OPTS_TARRAY on (see test_oracle_golden.py); fsaa 2 = 4x;
+#   opts "none" renders the reference without its list optimisations
 CASES = {
     "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
     "plain_s2_160x96":      (1, 2, 16, 160, 96, 0, 1, 0, "full"),
@@ -39,20 +43,31 @@ CASES = {
     "plain_s2_aa4_128x80":  (1, 2, 16, 128, 80, 2, 1, 0, "full"),
     "plain_s8_q32_200x120": (1, 8, 32, 200, 120, 0, 1, 0, "full"),
     "plain_s9_ragged_37x23": (1, 9, 16, 37, 23, 0, 1, 0, "full"),
+    "anim_s1_none_160x90_d4":     (2, 1, 64, 160, 90, 0, 2, 0, "none", 4),
+    "anim_s2_none_aa4_128x72_d4": (2, 2, 64, 128, 72, 2, 2, 0, "none", 4),
+    "anim_s4_none_96x54_d10":     (2, 4, 64, 96, 54, 0, 1, 0, "none", 10),
+    "anim_s5_ids_160x90":         (2, 5, 64, 160, 90, 0, 2, 1, "full", 4),
+    "anim_s1_full_160x90_d4":     (2, 1, 64, 160, 90, 0, 2, 0, "full", 4),
+    "anim_s3_full_aa4_128x72_d4": (2, 3, 64, 128, 72, 2, 1, 0, "full", 4),
+    "anim_s1_tarray_160x90_d4":   (2, 1, 64, 160, 90, 0, 1, 8, "full", 4),
+    "anim_s1_tarray_none_160x90_d4": (2, 1, 64, 160, 90, 0, 1, 8, "none", 4),
 }
 
 
 def run_case(name, case):
-    kind, seed, nq, w, h, fsaa, frames, flags, opts = case
+    kind, seed, nq, w, h, fsaa, frames, flags, opts = case[:9]
+    depth = case[9] if len(case) > 9 else 10
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "frame.bin")
+        # the frame does not depend on the worker count (rows are independent)
         cmd = [DRIVER, str(kind), str(seed), str(nq), str(w), str(h),
-               str(fsaa), str(frames), str(flags), opts, out, "1"]
+               str(fsaa), str(frames), str(flags), opts, out,
+               str(min(8, os.cpu_count() or 1)), str(depth)]
         subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL,
                        stderr=subprocess.DEVNULL)
         data = np.fromfile(out, dtype="<u4").reshape(frames, h, w)
     meta = dict(kind=kind, seed=seed, nq=nq, w=w, h=h, fsaa=fsaa,
-                frames=frames, flags=flags, opts=opts)
+                frames=frames, flags=flags, opts=opts, depth=depth)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), frames=data,
                         meta=json.dumps(meta))
     return data
