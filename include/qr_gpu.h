@@ -150,7 +150,8 @@ typedef struct qr_frame_params
 {
     float   org[3];     float t_min;        /* camera position, near clip */
     float   dir[3];     float t_max;        /* ray to pixel (0,0) centre */
-    float   hor[3];     float pad0;         /* per-pixel horizontal step */
+    float   hor[3];     int32_t flags;      /* per-pixel horizontal step;
+                                               QR_FP_* bits */
     float   ver[3];     float pad1;         /* per-pixel vertical step */
     float   amb[3];     float l_amb;        /* accumulated ambient colour */
     int32_t x_res, y_res, x_row;            /* frame size, row stride (px) */
@@ -162,6 +163,11 @@ typedef struct qr_frame_params
     uint64_t seed;                          /* PT seed */
     float   pts_c;  float pad2;             /* PT samples so far */
 } qr_frame_params;
+
+/* qr_frame_params.flags */
+#define QR_FP_LINEAR_WALK   1   /* walk every surface list in order instead of
+                                   the scene's bounding-volume hierarchy (the
+                                   frame is the same; for tests) */
 
 typedef struct qr_ctx qr_ctx;
 

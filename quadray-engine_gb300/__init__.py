@@ -31,6 +31,7 @@ OPTS_DEFAULT = -1
 OPTS_NONE = (1 << 20) | (1 << 21) | (1 << 25)
 
 QR_OK = 0
+FP_LINEAR_WALK = 1        # qr_frame_params.flags: no BVH (same frame)
 
 
 class QrSceneDesc(ctypes.Structure):
@@ -51,7 +52,7 @@ class QrFrameParams(ctypes.Structure):
     _fields_ = [
         ("org", ctypes.c_float * 3), ("t_min", ctypes.c_float),
         ("dir", ctypes.c_float * 3), ("t_max", ctypes.c_float),
-        ("hor", ctypes.c_float * 3), ("pad0", ctypes.c_float),
+        ("hor", ctypes.c_float * 3), ("flags", ctypes.c_int32),
         ("ver", ctypes.c_float * 3), ("pad1", ctypes.c_float),
         ("amb", ctypes.c_float * 3), ("l_amb", ctypes.c_float),
         ("x_res", ctypes.c_int32), ("y_res", ctypes.c_int32),

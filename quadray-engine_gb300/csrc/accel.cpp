@@ -1,0 +1,571 @@
+/*
+ * accel.cpp: conservative world boxes of a flattened scene's surfaces and a
+ * binned-SAH bounding-volume hierarchy over its camera list (see accel.h).
+ */
+#include "accel.h"
+
+#include <math.h>
+#include <string.h>
+#include <algorithm>
+
+namespace
+{
+
+const double INF = HUGE_VAL;
+
+struct Box
+{
+    double lo[3], hi[3];
+    void inf()
+    {
+        for (int k = 0; k < 3; k++) { lo[k] = -INF; hi[k] = +INF; }
+    }
+    bool finite() const
+    {
+        for (int k = 0; k < 3; k++)
+            if (!(lo[k] > -INF && hi[k] < INF)) return false;
+        return true;
+    }
+    bool empty() const
+    {
+        for (int k = 0; k < 3; k++)
+            if (lo[k] > hi[k]) return true;
+        return false;
+    }
+    void meet(const Box &b)
+    {
+        for (int k = 0; k < 3; k++)
+        {
+            lo[k] = std::max(lo[k], b.lo[k]);
+            hi[k] = std::min(hi[k], b.hi[k]);
+        }
+    }
+};
+
+/* a record's 3x3 transform as the tracer applies it (xform in tracer.cu:
+ * diagonal only for amap[3] == 1, "scaling only") */
+void record_matrix(const qr_srf &t, double m[3][3])
+{
+    const float *row[3] = {t.tci, t.tcj, t.tck};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            m[i][j] = (t.amap[3] == 1 && i != j) ? 0.0 : (double)row[i][j];
+}
+
+bool invert3(const double m[3][3], double r[3][3])
+{
+    double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1];
+    double c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2];
+    double c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+    double det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
+    if (!(fabs(det) > 1e-30)) return false;
+    double id = 1.0 / det;
+    r[0][0] = c00 * id;
+    r[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+    r[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+    r[1][0] = c01 * id;
+    r[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+    r[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
+    r[2][0] = c02 * id;
+    r[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
+    r[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
+    return true;
+}
+
+/* interval image of box u under h = a * u + o */
+Box affine_image(const double a[3][3], const double o[3], const Box &u)
+{
+    Box h;
+    for (int i = 0; i < 3; i++)
+    {
+        double lo = o[i], hi = o[i];
+        for (int j = 0; j < 3; j++)
+        {
+            const double c = a[i][j];
+            if (c == 0.0) continue;
+            const double p = c * u.lo[j], q = c * u.hi[j];
+            if (isnan(p) || isnan(q)) { lo = -INF; hi = INF; break; }
+            lo += std::min(p, q);
+            hi += std::max(p, q);
+        }
+        h.lo[i] = lo;
+        h.hi[i] = hi;
+    }
+    return h;
+}
+
+/* minimum of g(x) = a x^2 - 2 b x over [lo, hi] */
+double gmin(double a, double b, double lo, double hi)
+{
+    if (a > 0.0)
+    {
+        double x = std::min(std::max(b / a, lo), hi);
+        return a * x * x - 2.0 * b * x;
+    }
+    if (a == 0.0)
+    {
+        if (b == 0.0) return 0.0;
+        double x = b > 0.0 ? hi : lo;
+        if (!(x > -INF && x < INF)) return -INF;
+        return -2.0 * b * x;
+    }
+    if (!(lo > -INF && hi < INF)) return -INF;
+    return std::min(a * lo * lo - 2.0 * b * lo, a * hi * hi - 2.0 * b * hi);
+}
+
+/* tighten box u to the sublevel set  sum_k (a_k x_k^2 - 2 b_k x_k) <= w  */
+void quadric_tighten(const double a[3], const double b[3], double w, Box &u)
+{
+    for (int it = 0; it < 4; it++)
+    {
+        for (int j = 0; j < 3; j++)
+        {
+            double U = w;
+            for (int k = 0; k < 3; k++)
+            {
+                if (k == j) continue;
+                U -= gmin(a[k], b[k], u.lo[k], u.hi[k]);
+            }
+            if (!(U < INF)) continue;
+            if (a[j] > 0.0)
+            {
+                double rhs = U + b[j] * b[j] / a[j];
+                if (rhs < 0.0) rhs = 0.0;
+                const double c = b[j] / a[j], r = sqrt(rhs / a[j]);
+                u.lo[j] = std::max(u.lo[j], c - r);
+                u.hi[j] = std::min(u.hi[j], c + r);
+            }
+            else if (a[j] == 0.0 && b[j] != 0.0)
+            {
+                if (b[j] > 0.0) u.lo[j] = std::max(u.lo[j], -U / (2.0 * b[j]));
+                else            u.hi[j] = std::min(u.hi[j], U / (-2.0 * b[j]));
+            }
+        }
+    }
+}
+
+/*
+ * Rounding allowance.  The tracer evaluates the quadric (its c coefficient,
+ * the discriminant) and the hit position in float on local coordinates of
+ * magnitude up to D; far from the surface those values are dominated by
+ * rounding, and the reference's arithmetic, which the tracer reproduces,
+ * then reports hits the exact geometry does not have.  A box must contain
+ * them too: the quadric is widened to {f <= eta} with eta = G (sum |sci| D^2
+ * + 2 sum |scj| D + |w|), and positions by G D, where G = 32 float epsilons
+ * is several times the rounding of those few operations.  Rays whose origin
+ * is farther than D allows are walked in list order instead (qr_dscene
+ * ray_c / ray_r2).
+ */
+const double G_ROUND = 32.0 * 1.1920928955078125e-7;
+
+double quadric_eta(const float sci[4], const float scj[3], double D)
+{
+    double e = fabs((double)sci[3]);
+    for (int k = 0; k < 3; k++)
+        e += fabs((double)sci[k]) * D * D + 2.0 * fabs((double)scj[k]) * D;
+    return G_ROUND * e;
+}
+
+/* surface in its local coordinates: quadric {f <= eta} (or the plane k = 0)
+ * within the active axis clippers (clip_root, tracer.cu), for local
+ * coordinates up to D in magnitude */
+Box local_surface_box(const qr_srf &s, double D)
+{
+    const double m = G_ROUND * D + 1e-6;
+    Box u;
+    u.inf();
+    for (int k = 0; k < 3; k++)
+    {
+        if ((s.mint >> k) & 1) u.lo[k] = s.bmin[k] - m;
+        if ((s.maxt >> k) & 1) u.hi[k] = s.bmax[k] + m;
+    }
+    if (s.solver == 1)
+    {
+        const int mk = s.amap[2];
+        u.lo[mk] = std::max(u.lo[mk], -m);
+        u.hi[mk] = std::min(u.hi[mk], +m);
+        return u;
+    }
+    double a[3], b[3];
+    for (int k = 0; k < 3; k++) { a[k] = s.sci[k]; b[k] = s.scj[k]; }
+    quadric_tighten(a, b, (double)s.sci[3] + quadric_eta(s.sci, s.scj, D), u);
+    for (int k = 0; k < 3; k++) { u.lo[k] -= m; u.hi[k] += m; }
+    return u;
+}
+
+/* region a clipper keeps when it subtracts its outer subspace (v <= 0 in the
+ * clipper evaluation of clip_root, tracer.cu), with the rounding allowance */
+Box local_clip_region(const qr_srf &c, double D)
+{
+    const double m = G_ROUND * D + 1e-6;
+    Box u;
+    u.inf();
+    if (c.clpk == 1)
+    {
+        const int mk = c.amap[2];
+        if (c.asgn[2]) u.lo[mk] = -m;       /* -p_k <= 0 */
+        else           u.hi[mk] = +m;       /*  p_k <= 0 */
+        return u;
+    }
+    double a[3], b[3];
+    float scj0[3] = {0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < 3; k++)
+    {
+        a[k] = c.sci[k];
+        b[k] = c.clpk == 2 ? c.scj[k] : 0.0;
+    }
+    quadric_tighten(a, b, (double)c.sci[3] +
+                    quadric_eta(c.sci, c.clpk == 2 ? c.scj : scj0, D), u);
+    for (int k = 0; k < 3; k++) { u.lo[k] -= m; u.hi[k] += m; }
+    return u;
+}
+
+/* largest row norm of a record's 3x3 transform (1 without one): local
+ * coordinates are at most this times the world distance */
+double record_gain(const qr_srf &t)
+{
+    if (t.amap[3] == 0) return 1.0;
+    double m[3][3], g = 0.0;
+    record_matrix(t, m);
+    for (int i = 0; i < 3; i++)
+        g = std::max(g, sqrt(m[i][0] * m[i][0] + m[i][1] * m[i][1] + m[i][2] * m[i][2]));
+    return std::max(g, 1.0);
+}
+
+/*
+ * world box of local box u of record s, where the local coordinates are
+ *   xf >= 0 (transform node T, am3(T) != 0): loc = M_T (h - T.pos) - s.pos
+ *   own transform (am3(s) != 0):             loc = M_s (h - s.pos)
+ *   translation only:                        loc = h - s.pos
+ * and node_only selects the transform-node form loc = X_T(h) - s.pos with
+ * X_T(h) = am3(T) ? M_T (h - T.pos) : h - T.pos (clip-list groups)
+ */
+bool world_box(const qr_scene_desc *d, const qr_srf &s, int xf, bool node_only,
+               const Box &u, Box &w)
+{
+    double a[3][3], o[3];
+    if (xf >= 0 && (node_only || d->srf[xf].amap[3] != 0))
+    {
+        const qr_srf &t = d->srf[xf];
+        Box v = u;
+        for (int k = 0; k < 3; k++) { v.lo[k] += s.pos[k]; v.hi[k] += s.pos[k]; }
+        if (t.amap[3] != 0)
+        {
+            double m[3][3];
+            record_matrix(t, m);
+            if (!invert3(m, a)) return false;
+        }
+        else
+        {
+            memset(a, 0, sizeof(a));
+            a[0][0] = a[1][1] = a[2][2] = 1.0;
+        }
+        for (int k = 0; k < 3; k++) o[k] = t.pos[k];
+        w = affine_image(a, o, v);
+        return true;
+    }
+    if (s.amap[3] != 0)
+    {
+        double m[3][3];
+        record_matrix(s, m);
+        if (!invert3(m, a)) return false;
+    }
+    else
+    {
+        memset(a, 0, sizeof(a));
+        a[0][0] = a[1][1] = a[2][2] = 1.0;
+    }
+    for (int k = 0; k < 3; k++) o[k] = s.pos[k];
+    w = affine_image(a, o, u);
+    return true;
+}
+
+void pad(Box &b)
+{
+    for (int k = 0; k < 3; k++)
+    {
+        const double m = 1e-3 + 1e-4 * (fabs(b.lo[k]) + fabs(b.hi[k]));
+        b.lo[k] -= m;
+        b.hi[k] += m;
+    }
+}
+
+/* transform node of each element of a list (-1 outside groups), following
+ * the element layout of qr_elem (QR_ELM_TRNODE with `last`) */
+void list_groups(const qr_scene_desc *d, int off, int num, std::vector<int> &xf)
+{
+    xf.assign(num, -1);
+    int node = -1, last = -1;
+    for (int e = 0; e < num; e++)
+    {
+        const qr_elem &el = d->elems[off + e];
+        if (node >= 0 && off + e > last) node = -1;
+        if (el.kind == QR_ELM_TRNODE)
+        {
+            node = el.ref;
+            last = el.last;
+            continue;
+        }
+        xf[e] = node;
+    }
+}
+
+/* ---- binned SAH ---------------------------------------------------------- */
+
+struct Prim
+{
+    Box b;
+    double c[3];
+    qr_bitem it;
+};
+
+double area(const Box &b)
+{
+    double dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    return 2.0 * (dx * dy + dy * dz + dz * dx);
+}
+
+Box merge(const Box &a, const Box &b)
+{
+    Box r;
+    for (int k = 0; k < 3; k++)
+    {
+        r.lo[k] = std::min(a.lo[k], b.lo[k]);
+        r.hi[k] = std::max(a.hi[k], b.hi[k]);
+    }
+    return r;
+}
+
+int build_node(std::vector<Prim> &p, int lo, int hi, int depth, qr_accel_host *out)
+{
+    const int idx = (int)out->nodes.size();
+    out->nodes.push_back(qr_bnode());
+    Box bb = p[lo].b, cb;
+    for (int k = 0; k < 3; k++) cb.lo[k] = cb.hi[k] = p[lo].c[k];
+    for (int i = lo + 1; i < hi; i++)
+    {
+        bb = merge(bb, p[i].b);
+        for (int k = 0; k < 3; k++)
+        {
+            cb.lo[k] = std::min(cb.lo[k], p[i].c[k]);
+            cb.hi[k] = std::max(cb.hi[k], p[i].c[k]);
+        }
+    }
+    if (depth > out->depth) out->depth = depth;
+    const int n = hi - lo;
+    int mid = -1;
+    if (n > 2 && depth < QR_BVH_STACK - 8)
+    {
+        /* binned SAH over the centroid box */
+        const int NB = 12;
+        double best = area(bb) * n;     /* cost of a leaf */
+        int bax = -1, bsplit = -1;
+        for (int ax = 0; ax < 3; ax++)
+        {
+            const double ext = cb.hi[ax] - cb.lo[ax];
+            if (!(ext > 0.0)) continue;
+            Box bin[NB];
+            int cnt[NB] = {0};
+            for (int i = lo; i < hi; i++)
+            {
+                int q = (int)((p[i].c[ax] - cb.lo[ax]) / ext * NB);
+                q = std::min(std::max(q, 0), NB - 1);
+                bin[q] = cnt[q] ? merge(bin[q], p[i].b) : p[i].b;
+                cnt[q]++;
+            }
+            for (int s = 1; s < NB; s++)
+            {
+                Box l, r;
+                int nl = 0, nr = 0;
+                for (int q = 0; q < s; q++)
+                    if (cnt[q]) { l = nl ? merge(l, bin[q]) : bin[q]; nl += cnt[q]; }
+                for (int q = s; q < NB; q++)
+                    if (cnt[q]) { r = nr ? merge(r, bin[q]) : bin[q]; nr += cnt[q]; }
+                if (nl == 0 || nr == 0) continue;
+                const double cost = 0.5 * area(bb) + area(l) * nl + area(r) * nr;
+                if (cost < best) { best = cost; bax = ax; bsplit = s; }
+            }
+        }
+        if (bax >= 0)
+        {
+            const double ext = cb.hi[bax] - cb.lo[bax];
+            Prim *m = std::partition(&p[lo], &p[lo] + n, [&](const Prim &x) {
+                int q = (int)((x.c[bax] - cb.lo[bax]) / ext * NB);
+                q = std::min(std::max(q, 0), NB - 1);
+                return q < bsplit;
+            });
+            mid = (int)(m - &p[0]);
+            if (mid <= lo || mid >= hi) mid = -1;
+        }
+    }
+    qr_bnode nd;
+    memset(&nd, 0, sizeof(nd));
+    for (int k = 0; k < 3; k++)
+    {
+        nd.lo[k] = (float)bb.lo[k];
+        nd.hi[k] = (float)bb.hi[k];
+        /* round outwards to float */
+        if ((double)nd.lo[k] > bb.lo[k]) nd.lo[k] = nextafterf(nd.lo[k], -HUGE_VALF);
+        if ((double)nd.hi[k] < bb.hi[k]) nd.hi[k] = nextafterf(nd.hi[k], +HUGE_VALF);
+    }
+    if (mid < 0)
+    {
+        nd.a = (int)out->items.size();
+        nd.count = n;
+        for (int i = lo; i < hi; i++) out->items.push_back(p[i].it);
+        out->nodes[idx] = nd;
+        return idx;
+    }
+    nd.count = 0;
+    out->nodes[idx] = nd;
+    const int l = build_node(p, lo, mid, depth + 1, out);
+    const int r = build_node(p, mid, hi, depth + 1, out);
+    out->nodes[idx].a = l;
+    out->nodes[idx].b = r;
+    return idx;
+}
+
+} /* namespace */
+
+int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out)
+{
+    out->nodes.clear();
+    out->items.clear();
+    out->always.clear();
+    out->depth = 0;
+    out->boxes.assign((size_t)d->nsrf * 6, 0.0f);
+    out->bounded.assign(d->nsrf, 0);
+
+    /* transform node of each surface in the camera list */
+    std::vector<int> xf;
+    list_groups(d, d->cam_off, d->cam_num, xf);
+    std::vector<int> srf_xf(d->nsrf, -2);
+    for (int e = 0; e < d->cam_num; e++)
+    {
+        const qr_elem &el = d->elems[d->cam_off + e];
+        if (el.kind == QR_ELM_SURFACE) srf_xf[el.ref] = xf[e];
+    }
+
+    /* the scene's extent: boxes without rounding allowance, and the gain
+     * from world distances to local coordinates */
+    double gain = 1.0;
+    for (int i = 0; i < d->nsrf; i++) gain = std::max(gain, record_gain(d->srf[i]));
+    double clo[3] = {INF, INF, INF}, chi[3] = {-INF, -INF, -INF};
+    for (int i = 0; i < d->nsrf; i++)
+    {
+        const qr_srf &s = d->srf[i];
+        if (s.is_node || srf_xf[i] == -2) continue;
+        Box u = local_surface_box(s, 0.0), w;
+        if (u.empty() || !world_box(d, s, srf_xf[i], false, u, w) || !w.finite()) continue;
+        for (int k = 0; k < 3; k++)
+        {
+            clo[k] = std::min(clo[k], w.lo[k]);
+            chi[k] = std::max(chi[k], w.hi[k]);
+        }
+    }
+    /* record positions too (transform nodes, surfaces): the local
+     * coordinates the walk forms start from them */
+    for (int i = 0; i < d->nsrf; i++)
+        for (int k = 0; k < 3; k++)
+        {
+            clo[k] = std::min(clo[k], (double)d->srf[i].pos[k]);
+            chi[k] = std::max(chi[k], (double)d->srf[i].pos[k]);
+        }
+    double rs = 0.0;
+    for (int k = 0; k < 3; k++)
+    {
+        if (!(clo[k] <= chi[k])) { clo[k] = chi[k] = 0.0; }
+        out->ray_c[k] = (float)(0.5 * (clo[k] + chi[k]));
+        rs += 0.25 * (chi[k] - clo[k]) * (chi[k] - clo[k]);
+    }
+    rs = sqrt(rs);
+    /* rays starting within ray_r of the centre use the hierarchy; their
+     * local coordinates stay below D */
+    const double ray_r = 6.0 * rs + 8.0;
+    const double D = gain * (ray_r + 2.0 * rs + 1.0) + 1.0;
+    out->ray_r2 = (float)(ray_r * ray_r);
+
+    /* world boxes of the surfaces (unclipped by custom clippers) */
+    std::vector<Box> wbox(d->nsrf);
+    std::vector<char> ok(d->nsrf, 0);
+    for (int i = 0; i < d->nsrf; i++)
+    {
+        const qr_srf &s = d->srf[i];
+        if (s.is_node || srf_xf[i] == -2) continue;
+        Box u = local_surface_box(s, D), w;
+        if (u.empty()) { wbox[i] = u; ok[i] = 0; continue; }
+        ok[i] = world_box(d, s, srf_xf[i], false, u, w) ? 1 : 0;
+        wbox[i] = w;
+    }
+
+    /* clippers that keep only the inside of a surface (v <= 0, relation
+     * "minus outer", outside accumulator segments) bound the clipped one */
+    for (int i = 0; i < d->nsrf; i++)
+    {
+        const qr_srf &s = d->srf[i];
+        if (!ok[i] || s.clip_num <= 0) continue;
+        std::vector<int> cxf;
+        list_groups(d, s.clip_off, s.clip_num, cxf);
+        int acc = 0;
+        for (int e = 0; e < s.clip_num; e++)
+        {
+            const qr_elem &el = d->elems[s.clip_off + e];
+            if (el.kind == QR_ELM_ACC_ENTER) { acc = 1; continue; }
+            if (el.kind == QR_ELM_ACC_LEAVE) { acc = 0; continue; }
+            if (el.kind != QR_ELM_SURFACE || acc || el.rel <= 0) continue;
+            const qr_srf &c = d->srf[el.ref];
+            Box u = local_clip_region(c, D), w;
+            if (!world_box(d, c, cxf[e], true, u, w)) continue;
+            wbox[i].meet(w);
+        }
+    }
+
+    for (int e = 0; e < d->cam_num; e++)
+    {
+        const qr_elem &el = d->elems[d->cam_off + e];
+        if (el.kind != QR_ELM_SURFACE) continue;
+        const int i = el.ref;
+        qr_bitem it;
+        it.pos = e;
+        it.srf = i;
+        it.xf = (xf[e] >= 0 && d->srf[xf[e]].amap[3] != 0) ? xf[e] : -1;
+        it.pad = 0;
+        Box b = wbox[i];
+        if (ok[i] && !b.empty() && b.finite())
+        {
+            pad(b);
+            for (int k = 0; k < 3; k++)
+            {
+                out->boxes[6 * i + k] = (float)b.lo[k];
+                out->boxes[6 * i + 3 + k] = (float)b.hi[k];
+            }
+            out->bounded[i] = 1;
+        }
+        else
+        {
+            out->always.push_back(it);
+        }
+    }
+
+    std::vector<Prim> prims;
+    for (int e = 0; e < d->cam_num; e++)
+    {
+        const qr_elem &el = d->elems[d->cam_off + e];
+        if (el.kind != QR_ELM_SURFACE || out->bounded[el.ref] != 1) continue;
+        Prim p;
+        const int i = el.ref;
+        for (int k = 0; k < 3; k++)
+        {
+            p.b.lo[k] = out->boxes[6 * i + k];
+            p.b.hi[k] = out->boxes[6 * i + 3 + k];
+            p.c[k] = 0.5 * (p.b.lo[k] + p.b.hi[k]);
+        }
+        p.it.pos = e;
+        p.it.srf = i;
+        p.it.xf = (xf[e] >= 0 && d->srf[xf[e]].amap[3] != 0) ? xf[e] : -1;
+        p.it.pad = 0;
+        prims.push_back(p);
+    }
+    if (!prims.empty()) build_node(prims, 0, (int)prims.size(), 1, out);
+    return 0;
+}

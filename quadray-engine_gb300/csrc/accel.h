@@ -1,0 +1,70 @@
+/*
+ * accel.h: bounding-volume hierarchy over a flattened scene's surface list.
+ *
+ * The reference tests every surface of a (per-tile, culled) list for every
+ * ray (core/tracer/tracer.cpp:2413-2680).  The GB300 tracer replaces the
+ * walk of the full camera / shadow / secondary list with a traversal of a
+ * BVH built over conservative world-space boxes of the list's surfaces;
+ * surfaces without a finite box are tested by every ray.  A hit is accepted
+ * by (t, list position): among equal distances the surface earlier in the
+ * list wins, which is exactly what the in-order walk with its strict depth
+ * test keeps, so frames are bit-identical to the walk.
+ *
+ * Boxes are derived from the records the tracer itself uses (qr_srf): the
+ * surface's local coordinates as the walk forms them (transform node, own
+ * transform or translation only), bounded by the quadric's sublevel set
+ * {f <= 0}, the active axis clippers and the clippers that keep only the
+ * inside of a surface (RT_REL_MINUS_OUTER outside accumulator segments), and
+ * mapped back to world space in double precision with a safety margin.
+ */
+#ifndef QR_ACCEL_H
+#define QR_ACCEL_H
+
+#include <stdint.h>
+#include <vector>
+#include "qr_gpu.h"
+
+/* BVH node: inner nodes have count == 0 and children a, b; leaves hold
+ * items [a, a + count) */
+struct qr_bnode
+{
+    float   lo[3];
+    int32_t a;
+    float   hi[3];
+    int32_t count;
+    int32_t b;
+    int32_t pad[3];
+};
+
+/* one surface of the list: its position in the list (tie order), record
+ * index, and the transform node whose cached transform the walk applies
+ * (-1: the surface's own transform or translation) */
+struct qr_bitem
+{
+    int32_t pos;
+    int32_t srf;
+    int32_t xf;
+    int32_t pad;
+};
+
+struct qr_accel_host
+{
+    std::vector<qr_bnode> nodes;        /* nodes[0] is the root */
+    std::vector<qr_bitem> items;        /* leaf items (BVH order) */
+    std::vector<qr_bitem> always;       /* unbounded surfaces (list order) */
+    std::vector<float>    boxes;        /* per record: lo[3], hi[3] (debug) */
+    std::vector<int32_t>  bounded;      /* per record */
+    int depth;
+    /* rays whose origin lies within sqrt(ray_r2) of ray_c may use the
+     * hierarchy (the boxes allow for their rounding); others walk the list */
+    float ray_c[3], ray_r2;
+};
+
+/* build the hierarchy over the camera list of `d` (which the flattening
+ * also uses, in the same order, for shadow and secondary rays); returns 0 */
+int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out);
+
+/* deepest traversal stack the tracer supports */
+#define QR_BVH_STACK 48
+
+#endif /* QR_ACCEL_H */

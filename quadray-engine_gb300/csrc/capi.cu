@@ -14,6 +14,7 @@
 
 #include "qr_gpu.h"
 #include "tracer.cuh"
+#include "accel.h"
 
 
 struct qr_scene_slot
@@ -143,16 +144,50 @@ static int check_desc(const qr_scene_desc *d)
     return QR_OK;
 }
 
-/* copy a scene's arrays into one device block (or into an existing one) */
+/* the shadow list that every light shares, if it holds the camera list's
+ * surfaces in the camera list's order (then the hierarchy serves it) */
+static void shadow_list(const qr_scene_desc *d, int *off, int *num)
+{
+    *off = -1;
+    *num = -1;
+    if (d->nlelem == 0) return;
+    const int so = d->lelems[0].shd_off, sn = d->lelems[0].shd_num;
+    for (int i = 1; i < d->nlelem; i++)
+        if (d->lelems[i].shd_off != so || d->lelems[i].shd_num != sn) return;
+    if (sn != d->cam_num) return;
+    for (int e = 0; e < sn; e++)
+    {
+        const qr_elem &a = d->elems[so + e], &b = d->elems[d->cam_off + e];
+        if (a.kind != b.kind || a.ref != b.ref) return;
+        if (a.kind == QR_ELM_TRNODE && a.last - so != b.last - d->cam_off) return;
+    }
+    *off = so;
+    *num = sn;
+}
+
+/* copy a scene's arrays, and the hierarchy built over them, into one device
+ * block (or into an existing one) */
 static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool fresh)
 {
+    qr_accel_host acc;
+    qr_accel_build(d, &acc);
+    const bool use_bvh = acc.depth < QR_BVH_STACK - 2;
+    if (!use_bvh)
+    {
+        acc.nodes.clear();
+        acc.items.clear();
+    }
+
     size_t o_srf = 0;
     size_t o_mat = o_srf + al16(sizeof(qr_srf) * d->nsrf);
     size_t o_lgt = o_mat + al16(sizeof(qr_mat) * d->nmat);
     size_t o_elm = o_lgt + al16(sizeof(qr_light) * d->nlgt);
     size_t o_lel = o_elm + al16(sizeof(qr_elem) * d->nelem);
     size_t o_tex = o_lel + al16(sizeof(qr_lelem) * d->nlelem);
-    size_t total = o_tex + al16(sizeof(uint32_t) * d->ntex);
+    size_t o_nod = o_tex + al16(sizeof(uint32_t) * d->ntex);
+    size_t o_itm = o_nod + al16(sizeof(qr_bnode) * acc.nodes.size());
+    size_t o_alw = o_itm + al16(sizeof(qr_bitem) * acc.items.size());
+    size_t total = o_alw + al16(sizeof(qr_bitem) * acc.always.size());
 
     std::vector<unsigned char> h(total, 0);
     memcpy(&h[o_srf], d->srf, sizeof(qr_srf) * d->nsrf);
@@ -161,6 +196,12 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     memcpy(&h[o_elm], d->elems, sizeof(qr_elem) * d->nelem);
     memcpy(&h[o_lel], d->lelems, sizeof(qr_lelem) * d->nlelem);
     memcpy(&h[o_tex], d->texels, sizeof(uint32_t) * d->ntex);
+    if (!acc.nodes.empty())
+        memcpy(&h[o_nod], acc.nodes.data(), sizeof(qr_bnode) * acc.nodes.size());
+    if (!acc.items.empty())
+        memcpy(&h[o_itm], acc.items.data(), sizeof(qr_bitem) * acc.items.size());
+    if (!acc.always.empty())
+        memcpy(&h[o_alw], acc.always.data(), sizeof(qr_bitem) * acc.always.size());
 
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaSetDevice", e);
@@ -187,6 +228,15 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     sl.d.nelem = d->nelem; sl.d.nlelem = d->nlelem; sl.d.ntex = d->ntex;
     sl.d.cam_off = d->cam_off;
     sl.d.cam_num = d->cam_num;
+    sl.d.nodes = (const qr_bnode *)(b + o_nod);
+    sl.d.items = (const qr_bitem *)(b + o_itm);
+    sl.d.always = (const qr_bitem *)(b + o_alw);
+    sl.d.nnodes = use_bvh ? (int32_t)acc.nodes.size() : -1;
+    sl.d.nitems = (int32_t)acc.items.size();
+    sl.d.nalways = (int32_t)acc.always.size();
+    shadow_list(d, &sl.d.shd_off, &sl.d.shd_num);
+    for (int k = 0; k < 3; k++) sl.d.ray_c[k] = acc.ray_c[k];
+    sl.d.ray_r2 = acc.ray_r2;
     sl.shape = *d;
     return QR_OK;
 }

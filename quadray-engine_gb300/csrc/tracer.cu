@@ -80,6 +80,7 @@ struct Walk
     int   shadow;
     int   occluded;
     float tbuf;
+    int   bestp;        /* list position of the nearest hit (-1: none) */
     Hit   best;
 };
 
@@ -114,13 +115,15 @@ __device__ __forceinline__ void xform(const qr_srf *__restrict__ t,
 
 /* clipping subroutine for one root (tracer.cpp:2686-3249) */
 __device__ int clip_root(const qr_dscene &S, const Ray &r, int si, float t,
-                         float tbuf, const float ldff[3], const float lray[3],
+                         const Walk &w, int p, const float ldff[3], const float lray[3],
                          int side, int dmask, uint32_t amask, float hit[3],
                          float loc[3], StP st)
 {
     CNT(QR_STAT_CLIP_ROOT);
     const qr_srf *__restrict__ s = &S.srf[si];
-    int valid = (tbuf > t) && (r.t_min < t);
+    /* depth test (2688-2699); an equal distance wins only from a surface
+     * earlier in the list, which is what the in-order walk keeps */
+    int valid = ((w.tbuf > t) || (w.tbuf == t && p < w.bestp)) && (r.t_min < t);
 
     #pragma unroll
     for (int k = 0; k < 3; k++) hit[k] = r.dir[k] * t + r.org[k];
@@ -264,7 +267,7 @@ __device__ int clip_root(const qr_dscene &S, const Ray &r, int si, float t,
 }
 
 __device__ __forceinline__ void accept_root(const qr_dscene &S, Walk &w, int si,
-                                            int side, float t,
+                                            int p, int side, float t,
                                             const float hit[3],
                                             const float loc[3])
 {
@@ -279,6 +282,7 @@ __device__ __forceinline__ void accept_root(const qr_dscene &S, Walk &w, int si,
         return;
     }
     w.tbuf = t;
+    w.bestp = p;
     w.best.srf = si;
     w.best.side = side;
     #pragma unroll
@@ -294,7 +298,7 @@ __device__ __forceinline__ int side_blocked(const Ray &r, int si, int side)
 }
 
 /* quadric roots with root sorting and splitting (5785-6206) */
-__device__ void root_pair(const qr_dscene &S, const Ray &r, Walk &w, int si,
+__device__ void root_pair(const qr_dscene &S, const Ray &r, Walk &w, int si, int p,
                           const float ldff[3], const float lray[3],
                           float a, float b, float c, float d, StP st)
 {
@@ -352,15 +356,126 @@ __device__ void root_pair(const qr_dscene &S, const Ray &r, Walk &w, int si,
         const float t = side == SIDE_OUTER ? t1 : t2;
         const int tm = side == SIDE_OUTER ? t1m : t2m;
         if (side_blocked(r, si, side) || !tm) continue;
-        if (clip_root(S, r, si, t, w.tbuf, ldff, lray, side, dmask, amask, hit, loc, st))
+        if (clip_root(S, r, si, t, w, p, ldff, lray, side, dmask, amask, hit, loc, st))
         {
-            accept_root(S, w, si, side, t, hit, loc);
+            accept_root(S, w, si, p, side, t, hit, loc);
             if (w.shadow && w.occluded) return;
         }
     }
 }
 
-/* list walk (2413-2680) with the solvers (5522-6497) */
+/* plane / quadric / two-plane solvers for one surface (5522-6497) on the
+ * ray in the surface's local coordinates; p is the surface's list position */
+__device__ __forceinline__ void solve_surface(const qr_dscene &S, const Ray &r, Walk &w,
+                                              int si, int p, const float ldff[3],
+                                              const float lray[3], StP st)
+{
+    const qr_srf *__restrict__ s = &S.srf[si];
+    const int solver = __ldg(&s->solver);
+    if (solver == 1)
+    {
+        /* plane (5545-5634) */
+        if (r.from == si) return;
+        const int mk = __ldg(&s->amap[2]);
+        const uint32_t sg = __ldg(&s->asgn[2]) ? SIGN_BIT : 0u;
+        float dk = fxor(ldff[mk], sg);
+        const float rk = fxor(lray[mk], sg);
+        dk = fxor(dk, SIGN_BIT);
+        if (!(rk != 0.0f)) return;
+        const float t = fdiv(dk, rk);
+        float hit[3], loc[3];
+        CNT(QR_STAT_TEST_PLANE);
+        if (!clip_root(S, r, si, t, w, p, ldff, lray, 0, 0, 0u, hit, loc, st)) return;
+        accept_root(S, w, si, p, rk < 0.0f ? SIDE_OUTER : SIDE_INNER, t, hit, loc);
+    }
+    else if (solver == 2)
+    {
+        /* quadric coefficients (5722-5783) */
+        float a = 0.0f, b = 0.0f, c = 0.0f;
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            const float sci = __ldg(&s->sci[k]), scj = __ldg(&s->scj[k]);
+            const float sri = sci * lray[k];
+            float sdi = sci * ldff[k];
+            sdi = sdi - scj;
+            const float ax = lray[k] * sri;
+            const float bx = lray[k] * sdi;
+            sdi = sdi - scj;
+            const float cx = ldff[k] * sdi;
+            if (k == 0) { a = ax; b = bx; c = cx; }
+            else { a = a + ax; b = b + bx; c = c + cx; }
+        }
+        c = c - __ldg(&s->sci[3]);
+        const float d = b * b - c * a;
+        CNT(QR_STAT_TEST_QUADRIC);
+        root_pair(S, r, w, si, p, ldff, lray, a, b, c, d, st);
+    }
+    else
+    {
+        /* two-plane (6349-6402) */
+        const int mi = __ldg(&s->amap[0]), mk = __ldg(&s->amap[2]);
+        const float ri = lray[mi], di = ldff[mi], rk = lray[mk], dk = ldff[mk];
+        const float si_ = __ldg(&s->sci[mi]), sk = __ldg(&s->sci[mk]);
+        float dd = di * rk - dk * ri;
+        dd = dd * dd;
+        dd = dd * si_;
+        dd = dd * sk;
+        dd = fabsf(dd);
+        const float bb = si_ * di * ri + sk * dk * rk;
+        const float cc = di * di * si_ + dk * dk * sk;
+        const float aa = ri * ri * si_ + rk * rk * sk;
+        CNT(QR_STAT_TEST_TWOPLANE);
+        root_pair(S, r, w, si, p, ldff, lray, aa, bb, cc, dd, st);
+    }
+}
+
+/* the surface's local ray without the walk's per-node cache: through
+ * transform node xf (>= 0), the surface's own transform, or a translation
+ * (2518-2645) */
+__device__ __forceinline__ void local_ray(const qr_dscene &S, const Ray &r, int si,
+                                          int xf, float ldff[3], float lray[3], StP st)
+{
+    const qr_srf *__restrict__ s = &S.srf[si];
+    if (xf >= 0)
+    {
+        const qr_srf *__restrict__ t = &S.srf[xf];
+        float d[3], cdff[3];
+        #pragma unroll
+        for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&t->pos[k]);
+        CNT(QR_STAT_XFORM);
+        xform(t, d, cdff);
+        xform(t, r.dir, lray);
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+            ldff[k] = r.from == si ? r.phit[k] : cdff[k] - __ldg(&s->pos[k]);
+        return;
+    }
+    const int am3 = __ldg(&s->amap[3]);
+    if (r.from == si)
+    {
+        #pragma unroll
+        for (int k = 0; k < 3; k++) ldff[k] = r.phit[k];
+        if (am3 != 0) xform(s, r.dir, lray);
+        else
+        {
+            #pragma unroll
+            for (int k = 0; k < 3; k++) lray[k] = r.dir[k];
+        }
+        return;
+    }
+    float d[3];
+    #pragma unroll
+    for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&s->pos[k]);
+    if (am3 != 0) { CNT(QR_STAT_XFORM); xform(s, d, ldff); xform(s, r.dir, lray); }
+    else
+    {
+        #pragma unroll
+        for (int k = 0; k < 3; k++) { ldff[k] = d[k]; lray[k] = r.dir[k]; }
+    }
+}
+
+/* list walk (2413-2680): in list order, with the per-node transform cache */
 __device__ void walk(const qr_dscene &S, const Ray &r, int off, int num, Walk &w,
                      StP st)
 {
@@ -390,106 +505,128 @@ __device__ void walk(const qr_dscene &S, const Ray &r, int off, int num, Walk &w
             continue;
         }
 
-        const int am3 = __ldg(&s->amap[3]);
         if (cache_last >= 0)
         {
-            if (r.from == si)
-            {
-                #pragma unroll
-                for (int k = 0; k < 3; k++) ldff[k] = r.phit[k];
-            }
-            else
-            {
-                #pragma unroll
-                for (int k = 0; k < 3; k++) ldff[k] = cdff[k] - __ldg(&s->pos[k]);
-            }
-            #pragma unroll
-            for (int k = 0; k < 3; k++) lray[k] = cray[k];
-            if (ei == cache_last) cache_last = -1;
-        }
-        else if (r.from == si)
-        {
-            #pragma unroll
-            for (int k = 0; k < 3; k++) ldff[k] = r.phit[k];
-            if (am3 != 0) xform(s, r.dir, lray);
-            else
-            {
-                #pragma unroll
-                for (int k = 0; k < 3; k++) lray[k] = r.dir[k];
-            }
-        }
-        else
-        {
-            float d[3];
-            #pragma unroll
-            for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&s->pos[k]);
-            if (am3 != 0) { CNT(QR_STAT_XFORM); xform(s, d, ldff); xform(s, r.dir, lray); }
-            else
-            {
-                #pragma unroll
-                for (int k = 0; k < 3; k++) { ldff[k] = d[k]; lray[k] = r.dir[k]; }
-            }
-        }
-
-        const int solver = __ldg(&s->solver);
-        if (solver == 1)
-        {
-            /* plane (5545-5634) */
-            if (r.from == si) continue;
-            const int mk = __ldg(&s->amap[2]);
-            const uint32_t sg = __ldg(&s->asgn[2]) ? SIGN_BIT : 0u;
-            float dk = fxor(ldff[mk], sg);
-            const float rk = fxor(lray[mk], sg);
-            dk = fxor(dk, SIGN_BIT);
-            if (!(rk != 0.0f)) continue;
-            const float t = fdiv(dk, rk);
-            float hit[3], loc[3];
-            CNT(QR_STAT_TEST_PLANE);
-            if (!clip_root(S, r, si, t, w.tbuf, ldff, lray, 0, 0, 0u, hit, loc, st)) continue;
-            accept_root(S, w, si, rk < 0.0f ? SIDE_OUTER : SIDE_INNER, t, hit, loc);
-        }
-        else if (solver == 2)
-        {
-            /* quadric coefficients (5722-5783) */
-            float a = 0.0f, b = 0.0f, c = 0.0f;
             #pragma unroll
             for (int k = 0; k < 3; k++)
             {
-                const float sci = __ldg(&s->sci[k]), scj = __ldg(&s->scj[k]);
-                const float sri = sci * lray[k];
-                float sdi = sci * ldff[k];
-                sdi = sdi - scj;
-                const float ax = lray[k] * sri;
-                const float bx = lray[k] * sdi;
-                sdi = sdi - scj;
-                const float cx = ldff[k] * sdi;
-                if (k == 0) { a = ax; b = bx; c = cx; }
-                else { a = a + ax; b = b + bx; c = c + cx; }
+                ldff[k] = r.from == si ? r.phit[k] : cdff[k] - __ldg(&s->pos[k]);
+                lray[k] = cray[k];
             }
-            c = c - __ldg(&s->sci[3]);
-            const float d = b * b - c * a;
-            CNT(QR_STAT_TEST_QUADRIC);
-            root_pair(S, r, w, si, ldff, lray, a, b, c, d, st);
+            if (ei == cache_last) cache_last = -1;
         }
         else
         {
-            /* two-plane (6349-6402) */
-            const int mi = __ldg(&s->amap[0]), mk = __ldg(&s->amap[2]);
-            const float ri = lray[mi], di = ldff[mi], rk = lray[mk], dk = ldff[mk];
-            const float si_ = __ldg(&s->sci[mi]), sk = __ldg(&s->sci[mk]);
-            float dd = di * rk - dk * ri;
-            dd = dd * dd;
-            dd = dd * si_;
-            dd = dd * sk;
-            dd = fabsf(dd);
-            const float bb = si_ * di * ri + sk * dk * rk;
-            const float cc = di * di * si_ + dk * dk * sk;
-            const float aa = ri * ri * si_ + rk * rk * sk;
-            CNT(QR_STAT_TEST_TWOPLANE);
-            root_pair(S, r, w, si, ldff, lray, aa, bb, cc, dd, st);
+            local_ray(S, r, si, -1, ldff, lray, st);
         }
+        solve_surface(S, r, w, si, e, ldff, lray, st);
         if (w.shadow && w.occluded) return;
     }
+}
+
+/* ray / box slab test against the node's box, for t in (t_min, tmax] */
+__device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray &r,
+                                       const float inv[3], float tmax, float &tn)
+{
+    float t0 = -FLT_MAX, t1 = FLT_MAX;
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const float lo = __ldg(&n->lo[k]), hi = __ldg(&n->hi[k]);
+        if (r.dir[k] == 0.0f)
+        {
+            if (r.org[k] < lo || r.org[k] > hi) return 0;
+            continue;
+        }
+        const float a = (lo - r.org[k]) * inv[k], b = (hi - r.org[k]) * inv[k];
+        t0 = fmaxf(t0, fminf(a, b));
+        t1 = fminf(t1, fmaxf(a, b));
+    }
+    tn = t0;
+    return t0 <= t1 && t1 >= r.t_min && t0 <= tmax;
+}
+
+__device__ __forceinline__ void test_item(const qr_dscene &S, const Ray &r, Walk &w,
+                                          const qr_bitem *__restrict__ it, StP st)
+{
+    const int si = __ldg(&it->srf);
+    float ldff[3], lray[3];
+    local_ray(S, r, si, __ldg(&it->xf), ldff, lray, st);
+    solve_surface(S, r, w, si, __ldg(&it->pos), ldff, lray, st);
+}
+
+/*
+ * The full surface list through the bounding-volume hierarchy: unbounded
+ * surfaces first, then the tree, near child first, skipping boxes that start
+ * beyond the nearest hit so far.  Hits are accepted by (distance, list
+ * position), so the result is the in-order walk's.
+ */
+__device__ void bvh_walk(const qr_dscene &S, const Ray &r, Walk &w, StP st)
+{
+    #pragma unroll 1
+    for (int i = 0; i < S.nalways; i++)
+    {
+        test_item(S, r, w, &S.always[i], st);
+        if (w.shadow && w.occluded) return;
+    }
+    if (S.nnodes == 0) return;
+    float inv[3];
+    #pragma unroll
+    for (int k = 0; k < 3; k++) inv[k] = r.dir[k] != 0.0f ? fdiv(1.0f, r.dir[k]) : 0.0f;
+    int stk[QR_BVH_STACK];
+    float stt[QR_BVH_STACK];
+    int sp = 0;
+    float tn;
+    if (box_hit(&S.nodes[0], r, inv, w.tbuf, tn)) { stk[0] = 0; stt[0] = tn; sp = 1; }
+    #pragma unroll 1
+    while (sp > 0)
+    {
+        --sp;
+        if (stt[sp] > w.tbuf) continue;
+        const qr_bnode *__restrict__ n = &S.nodes[stk[sp]];
+        const int cnt = __ldg(&n->count);
+        const int a = __ldg(&n->a);
+        if (cnt > 0)
+        {
+            #pragma unroll 1
+            for (int i = 0; i < cnt; i++)
+            {
+                test_item(S, r, w, &S.items[a + i], st);
+                if (w.shadow && w.occluded) return;
+            }
+            continue;
+        }
+        const int b = __ldg(&n->b);
+        float ta, tb;
+        const int ha = box_hit(&S.nodes[a], r, inv, w.tbuf, ta);
+        const int hb = box_hit(&S.nodes[b], r, inv, w.tbuf, tb);
+        if (ha && hb)
+        {
+            const int near_a = ta <= tb;
+            stk[sp] = near_a ? b : a; stt[sp] = near_a ? tb : ta; sp++;
+            stk[sp] = near_a ? a : b; stt[sp] = near_a ? ta : tb; sp++;
+        }
+        else if (ha) { stk[sp] = a; stt[sp] = ta; sp++; }
+        else if (hb) { stk[sp] = b; stt[sp] = tb; sp++; }
+    }
+}
+
+/* the list walk or, for the scene's full camera / shadow list and a ray
+ * that starts near the scene (where the boxes allow for the rounding of the
+ * solvers), the BVH */
+__device__ __forceinline__ void trace_walk(const qr_dscene &S, const qr_frame_params &P,
+                                           const Ray &r, int off, int num, Walk &w,
+                                           StP st)
+{
+    const float dx = r.org[0] - S.ray_c[0], dy = r.org[1] - S.ray_c[1],
+                dz = r.org[2] - S.ray_c[2];
+    if (S.nnodes >= 0 && !(P.flags & QR_FP_LINEAR_WALK) &&
+        dx * dx + dy * dy + dz * dz <= S.ray_r2 &&
+        ((off == S.cam_off && num == S.cam_num) ||
+         (off == S.shd_off && num == S.shd_num)))
+        bvh_walk(S, r, w, st);
+    else
+        walk(S, r, off, num, w, st);
 }
 
 /* what a shaded hit asks of its children: a refracted ray (weight c_trn)
@@ -650,9 +787,10 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
                 sw.shadow = 1;
                 sw.occluded = 0;
                 sw.tbuf = sr.t_max;
+                sw.bestp = -1;
                 sw.best.srf = -1;
                 CNT(QR_STAT_RAY_SHADOW);
-                walk(S, sr, __ldg(&le->shd_off), __ldg(&le->shd_num), sw, st);
+                trace_walk(S, P, sr, __ldg(&le->shd_off), __ldg(&le->shd_num), sw, st);
                 if (sw.occluded) continue;
             }
 
@@ -977,8 +1115,9 @@ __device__ void trace_tree(const qr_dscene &S, const qr_frame_params &P, Ray r,
         w.shadow = 0;
         w.occluded = 0;
         w.tbuf = r.t_max;
+        w.bestp = -1;
         w.best.srf = -1;
-        walk(S, r, off, num, w, st);
+        trace_walk(S, P, r, off, num, w, st);
         if (w.best.srf < 0)
         {
             ret[0] = ret[1] = ret[2] = 0.0f;

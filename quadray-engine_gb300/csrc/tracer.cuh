@@ -6,6 +6,7 @@
 
 #include <stdint.h>
 #include "qr_gpu.h"
+#include "accel.h"
 
 /* secondary-ray depth limit: the reference's context stack depth
  * (RT_STACK_DEPTH, core/tracer/tracer.h:51); the tracer keeps one pending
@@ -23,6 +24,16 @@ struct qr_dscene
     const uint32_t *texels;
     int32_t nsrf, nmat, nlgt, nelem, nlelem, ntex;
     int32_t cam_off, cam_num;
+    /* bounding-volume hierarchy over the camera list (accel.h); nnodes < 0
+     * when the scene has none.  The shadow list [shd_off, shd_off + shd_num)
+     * holds the same surfaces, so shadow rays use it too */
+    const qr_bnode *nodes;
+    const qr_bitem *items;
+    const qr_bitem *always;
+    int32_t nnodes, nitems, nalways;
+    int32_t shd_off, shd_num;
+    /* rays starting within sqrt(ray_r2) of ray_c use the hierarchy */
+    float   ray_c[3], ray_r2;
 };
 
 /* per-launch counters (instrumented runs only) */

@@ -143,3 +143,21 @@ def test_gpu_matches_reference_goldens(qr, ctx):
             sid = ctx.upload(desc)
             img = ctx.render_host(sid, params)
             check_against_golden(img, frames[k], meta)
+
+
+# ---- bounding-volume hierarchy: the same frames as the in-order list walk
+
+@pytest.mark.parametrize("kind,seed,nq,w,h,fsaa,t,depth", [
+    (2, 1, 64, 320, 180, 2, 0, 4), (2, 8, 64, 256, 144, 0, 48, 10),
+    (2, 9, 128, 192, 108, 2, 32, 4), (1, 3, 16, 320, 192, 0, 0, 10),
+    (1, 4, 64, 256, 160, 2, 0, 10)])
+def test_bvh_equals_linear_walk(qr, ctx, kind, seed, nq, w, h, fsaa, t, depth):
+    g = qr.GenScene(kind, seed, nq, 0)
+    f = qr.Flat(g, w, h, fsaa)
+    desc, params = f.update(t, depth)
+    sid = ctx.upload(desc)
+    a = ctx.render_host(sid, params).copy()
+    lin = qr.QrFrameParams.from_buffer_copy(params)
+    lin.flags = qr.FP_LINEAR_WALK
+    b = ctx.render_host(sid, lin)
+    assert (a != b).sum() == 0
