@@ -475,55 +475,6 @@ __device__ __forceinline__ void local_ray(const qr_dscene &S, const Ray &r, int 
     }
 }
 
-/* list walk (2413-2680): in list order, with the per-node transform cache */
-__device__ void walk(const qr_dscene &S, const Ray &r, int off, int num, Walk &w,
-                     StP st)
-{
-    float cdff[3] = {0.0f, 0.0f, 0.0f}, cray[3] = {0.0f, 0.0f, 0.0f};
-    int cache_last = -1;
-
-    #pragma unroll 1
-    for (int e = 0; e < num; e++)
-    {
-        const int ei = off + e;
-        const qr_elem *__restrict__ el = &S.elems[ei];
-        const int kind = __ldg(&el->kind);
-        const int si = __ldg(&el->ref);
-        const qr_srf *__restrict__ s = &S.srf[si];
-        float ldff[3], lray[3];
-
-        if (kind == QR_ELM_TRNODE)
-        {
-            float d[3];
-            #pragma unroll
-            for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&s->pos[k]);
-            if (__ldg(&s->amap[3]) == 0) continue;
-            CNT(QR_STAT_XFORM);
-            xform(s, d, cdff);
-            xform(s, r.dir, cray);
-            cache_last = __ldg(&el->last);
-            continue;
-        }
-
-        if (cache_last >= 0)
-        {
-            #pragma unroll
-            for (int k = 0; k < 3; k++)
-            {
-                ldff[k] = r.from == si ? r.phit[k] : cdff[k] - __ldg(&s->pos[k]);
-                lray[k] = cray[k];
-            }
-            if (ei == cache_last) cache_last = -1;
-        }
-        else
-        {
-            local_ray(S, r, si, -1, ldff, lray, st);
-        }
-        solve_surface(S, r, w, si, e, ldff, lray, st);
-        if (w.shadow && w.occluded) return;
-    }
-}
-
 /* ray / box slab test against the node's box, for t in (t_min, tmax] */
 __device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray &r,
                                        const float inv[3], float tmax, float &tn)
@@ -546,103 +497,165 @@ __device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray
     return t0 <= t1 && t1 >= r.t_min && t0 <= tmax;
 }
 
-__device__ __forceinline__ void test_item(const qr_dscene &S, const Ray &r, Walk &w,
-                                          const qr_bitem *__restrict__ it, StP st)
-{
-    const int si = __ldg(&it->srf);
-    float ldff[3], lray[3];
-    local_ray(S, r, si, __ldg(&it->xf), ldff, lray, st);
-    solve_surface(S, r, w, si, __ldg(&it->pos), ldff, lray, st);
-}
-
 /*
- * The full surface list through the bounding-volume hierarchy: unbounded
- * surfaces first, then the tree, near child first, skipping boxes that start
- * beyond the nearest hit so far.  Hits are accepted by (distance, list
- * position), so the result is the in-order walk's.
+ * One surface list, nearest hit or any occluder.  The surfaces come either
+ * from the list in order (2413-2680, with the per-node transform cache) or,
+ * for the scene's full camera / shadow list and a ray that starts near the
+ * scene (where the boxes allow for the solvers' rounding), from the
+ * bounding-volume hierarchy: unbounded surfaces first, then the tree, near
+ * child first, skipping boxes that start beyond the nearest hit so far.
+ * Hits are accepted by (distance, list position), so both give the in-order
+ * walk's result.  There is one solver site for both sources.
  */
-__device__ void bvh_walk(const qr_dscene &S, const Ray &r, Walk &w, StP st)
-{
-    #pragma unroll 1
-    for (int i = 0; i < S.nalways; i++)
-    {
-        test_item(S, r, w, &S.always[i], st);
-        if (w.shadow && w.occluded) return;
-    }
-    if (S.nnodes == 0) return;
-    float inv[3];
-    #pragma unroll
-    for (int k = 0; k < 3; k++) inv[k] = r.dir[k] != 0.0f ? fdiv(1.0f, r.dir[k]) : 0.0f;
-    int stk[QR_BVH_STACK];
-    float stt[QR_BVH_STACK];
-    int sp = 0;
-    float tn;
-    if (box_hit(&S.nodes[0], r, inv, w.tbuf, tn)) { stk[0] = 0; stt[0] = tn; sp = 1; }
-    #pragma unroll 1
-    while (sp > 0)
-    {
-        --sp;
-        if (stt[sp] > w.tbuf) continue;
-        const qr_bnode *__restrict__ n = &S.nodes[stk[sp]];
-        const int cnt = __ldg(&n->count);
-        const int a = __ldg(&n->a);
-        if (cnt > 0)
-        {
-            #pragma unroll 1
-            for (int i = 0; i < cnt; i++)
-            {
-                test_item(S, r, w, &S.items[a + i], st);
-                if (w.shadow && w.occluded) return;
-            }
-            continue;
-        }
-        const int b = __ldg(&n->b);
-        float ta, tb;
-        const int ha = box_hit(&S.nodes[a], r, inv, w.tbuf, ta);
-        const int hb = box_hit(&S.nodes[b], r, inv, w.tbuf, tb);
-        if (ha && hb)
-        {
-            const int near_a = ta <= tb;
-            stk[sp] = near_a ? b : a; stt[sp] = near_a ? tb : ta; sp++;
-            stk[sp] = near_a ? a : b; stt[sp] = near_a ? ta : tb; sp++;
-        }
-        else if (ha) { stk[sp] = a; stt[sp] = ta; sp++; }
-        else if (hb) { stk[sp] = b; stt[sp] = tb; sp++; }
-    }
-}
-
-/* the list walk or, for the scene's full camera / shadow list and a ray
- * that starts near the scene (where the boxes allow for the rounding of the
- * solvers), the BVH */
-__device__ __forceinline__ void trace_walk(const qr_dscene &S, const qr_frame_params &P,
-                                           const Ray &r, int off, int num, Walk &w,
-                                           StP st)
+__device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                     int off, int num, Walk &w, StP st)
 {
     const float dx = r.org[0] - S.ray_c[0], dy = r.org[1] - S.ray_c[1],
                 dz = r.org[2] - S.ray_c[2];
-    if (S.nnodes >= 0 && !(P.flags & QR_FP_LINEAR_WALK) &&
-        dx * dx + dy * dy + dz * dz <= S.ray_r2 &&
-        ((off == S.cam_off && num == S.cam_num) ||
-         (off == S.shd_off && num == S.shd_num)))
-        bvh_walk(S, r, w, st);
-    else
-        walk(S, r, off, num, w, st);
+    const int use_bvh = S.nnodes >= 0 && !(P.flags & QR_FP_LINEAR_WALK) &&
+                        dx * dx + dy * dy + dz * dz <= S.ray_r2 &&
+                        ((off == S.cam_off && num == S.cam_num) ||
+                         (off == S.shd_off && num == S.shd_num));
+    /* list source */
+    int e = 0, cache_last = -1;
+    float cdff[3] = {0.0f, 0.0f, 0.0f}, cray[3] = {0.0f, 0.0f, 0.0f};
+    /* hierarchy source */
+    int ai = 0, ia = 0, ib = 0, sp = 0;
+    int stk[QR_BVH_STACK];
+    float stt[QR_BVH_STACK];
+    float inv[3];
+    if (use_bvh)
+    {
+        #pragma unroll
+        for (int k = 0; k < 3; k++) inv[k] = r.dir[k] != 0.0f ? fdiv(1.0f, r.dir[k]) : 0.0f;
+        float tn;
+        if (S.nnodes > 0 && box_hit(&S.nodes[0], r, inv, w.tbuf, tn))
+        {
+            stk[0] = 0;
+            stt[0] = tn;
+            sp = 1;
+        }
+    }
+
+    #pragma unroll 1
+    for (;;)
+    {
+        int si, p, xf = -1, cached = 0;
+        if (!use_bvh)
+        {
+            int found = 0;
+            #pragma unroll 1
+            while (e < num)
+            {
+                const int ei = off + e;
+                const qr_elem *__restrict__ el = &S.elems[ei];
+                const int kind = __ldg(&el->kind);
+                const int ref = __ldg(&el->ref);
+                e++;
+                if (kind == QR_ELM_TRNODE)
+                {
+                    const qr_srf *__restrict__ t = &S.srf[ref];
+                    float d[3];
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&t->pos[k]);
+                    if (__ldg(&t->amap[3]) == 0) continue;
+                    CNT(QR_STAT_XFORM);
+                    xform(t, d, cdff);
+                    xform(t, r.dir, cray);
+                    cache_last = __ldg(&el->last);
+                    continue;
+                }
+                si = ref;
+                p = e - 1;
+                if (cache_last >= 0)
+                {
+                    cached = 1;
+                    if (ei == cache_last) cache_last = -1;
+                }
+                found = 1;
+                break;
+            }
+            if (!found) break;
+        }
+        else
+        {
+            const qr_bitem *__restrict__ it;
+            if (ai < S.nalways)
+            {
+                it = &S.always[ai++];
+            }
+            else
+            {
+                #pragma unroll 1
+                while (ia >= ib && sp > 0)
+                {
+                    --sp;
+                    if (stt[sp] > w.tbuf) continue;
+                    const qr_bnode *__restrict__ n = &S.nodes[stk[sp]];
+                    const int cnt = __ldg(&n->count);
+                    const int a = __ldg(&n->a);
+                    if (cnt > 0)
+                    {
+                        ia = a;
+                        ib = a + cnt;
+                        continue;
+                    }
+                    const int b = __ldg(&n->b);
+                    float ta, tb;
+                    const int ha = box_hit(&S.nodes[a], r, inv, w.tbuf, ta);
+                    const int hb = box_hit(&S.nodes[b], r, inv, w.tbuf, tb);
+                    if (ha && hb)
+                    {
+                        const int near_a = ta <= tb;
+                        stk[sp] = near_a ? b : a; stt[sp] = near_a ? tb : ta; sp++;
+                        stk[sp] = near_a ? a : b; stt[sp] = near_a ? ta : tb; sp++;
+                    }
+                    else if (ha) { stk[sp] = a; stt[sp] = ta; sp++; }
+                    else if (hb) { stk[sp] = b; stt[sp] = tb; sp++; }
+                }
+                if (ia >= ib) break;
+                it = &S.items[ia++];
+            }
+            si = __ldg(&it->srf);
+            p = __ldg(&it->pos);
+            xf = __ldg(&it->xf);
+        }
+
+        float ldff[3], lray[3];
+        if (cached)
+        {
+            const qr_srf *__restrict__ s = &S.srf[si];
+            #pragma unroll
+            for (int k = 0; k < 3; k++)
+            {
+                ldff[k] = r.from == si ? r.phit[k] : cdff[k] - __ldg(&s->pos[k]);
+                lray[k] = cray[k];
+            }
+        }
+        else
+        {
+            local_ray(S, r, si, xf, ldff, lray, st);
+        }
+        solve_surface(S, r, w, si, p, ldff, lray, st);
+        if (w.shadow && w.occluded) return;
+    }
 }
 
-/* what a shaded hit asks of its children: a refracted ray (weight c_trn)
- * and a reflected ray (weight c_rfl), traced in that order (4820-4883,
- * 5235-5298) */
-struct Sec
+/* shading state of one hit, kept while its shadow rays are traced */
+struct Shade
 {
-    int   trn, rfl;             /* child wanted (before the depth check) */
-    float c_trn, c_rfl;
-    float nw[3], rw[3];         /* refracted / reflected directions */
+    int   srf, side, props;
+    float hit[3], loc[3];
+    float nrm[3], tex[3];
+    float c[3];             /* colour so far: ambient, then lights */
+    float dir[3];           /* direction of the shaded ray */
+    int   depth;            /* its remaining secondary depth */
+    int   loff, lnum;       /* light list of the hit side */
 };
 
-/* shading of one hit (3255-5359): normal, texel, ambient, lights with
- * shadows; computes (but does not trace) the refracted and reflected rays */
-__device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
-                            const Hit &h, float c[3], Sec &o, StP st)
+/* normal, texel and ambient of a hit (3255-3416, 3945-3987) */
+__device__ void shade_begin(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                            const Hit &h, Shade &sh)
 {
     const qr_srf *__restrict__ s = &S.srf[h.srf];
     const int side = h.side;
@@ -652,6 +665,18 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
     float nrm[3], tex[3];
     float tu = 0.0f, tv = 0.0f;
     const int nrmk = __ldg(&s->nrmk);
+
+    sh.srf = h.srf;
+    sh.side = side;
+    sh.props = props;
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        sh.hit[k] = h.hit[k];
+        sh.loc[k] = h.loc[k];
+        sh.dir[k] = r.dir[k];
+    }
+    sh.depth = r.depth;
 
     if (nrmk == 1)
     {
@@ -738,165 +763,211 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
     }
 
     #pragma unroll
-    for (int k = 0; k < 3; k++) c[k] = tex[k];
-
-    const float m_trn = __ldg(&m->c_trn), m_rfl = __ldg(&m->c_rfl);
+    for (int k = 0; k < 3; k++)
+    {
+        sh.nrm[k] = nrm[k];
+        sh.tex[k] = tex[k];
+        sh.c[k] = tex[k];
+    }
+    sh.loff = 0;
+    sh.lnum = 0;
     if (!(props & QR_PROP_LIGHT))
     {
         /* ambient (3945-3987) */
+        const float m_trn = __ldg(&m->c_trn), m_rfl = __ldg(&m->c_rfl);
         #pragma unroll
-        for (int k = 0; k < 3; k++) c[k] = c[k] * P.amb[k];
+        for (int k = 0; k < 3; k++) sh.c[k] = sh.c[k] * P.amb[k];
         float f = 1.0f - m_trn;
         f = f - m_rfl;
         f = (0.0f <= f) ? f : 0.0f;
         #pragma unroll
-        for (int k = 0; k < 3; k++) c[k] = c[k] * f;
+        for (int k = 0; k < 3; k++) sh.c[k] = sh.c[k] * f;
+        sh.loff = __ldg(&s->lgt_off[side]);
+        sh.lnum = __ldg(&s->lgt_num[side]);
+    }
+}
 
-        /* lights (4002-4391) */
-        const int loff = __ldg(&s->lgt_off[side]), lnum = __ldg(&s->lgt_num[side]);
-        const float l_dff = __ldg(&m->l_dff), l_spc = __ldg(&m->l_spc);
-        const uint32_t l_pow = (uint32_t)__ldg(&m->l_pow);
-        #pragma unroll 1
-        for (int li = 0; li < lnum; li++)
+/* light vector and its dot with the normal (4008-4050) */
+__device__ __forceinline__ float light_dot(const qr_dscene &S, const Shade &sh, int li,
+                                           float lv[3])
+{
+    const qr_lelem *__restrict__ le = &S.lelems[sh.loff + li];
+    const qr_light *__restrict__ L = &S.lgt[__ldg(&le->light)];
+    #pragma unroll
+    for (int k = 0; k < 3; k++) lv[k] = __ldg(&L->pos[k]) - sh.hit[k];
+    float dot = lv[0] * sh.nrm[0] + lv[1] * sh.nrm[1];
+    dot = dot + lv[2] * sh.nrm[2];
+    return dot;
+}
+
+/* the next light at or after li that faces the surface (lnum if none) */
+__device__ __forceinline__ int next_light(const qr_dscene &S, const Shade &sh, int li)
+{
+    #pragma unroll 1
+    for (; li < sh.lnum; li++)
+    {
+        float lv[3];
+        if (0.0f < light_dot(S, sh, li, lv)) break;
+    }
+    return li;
+}
+
+/* shadow ray of light li: origin at the hit, direction L, t in (0, 1) */
+__device__ __forceinline__ void shadow_ray(const qr_dscene &S, const Shade &sh, int li,
+                                           Ray &sr, int &off, int &num)
+{
+    const qr_lelem *__restrict__ le = &S.lelems[sh.loff + li];
+    const qr_light *__restrict__ L = &S.lgt[__ldg(&le->light)];
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        sr.org[k] = sh.hit[k];
+        sr.dir[k] = __ldg(&L->pos[k]) - sh.hit[k];
+        sr.phit[k] = sh.loc[k];
+    }
+    sr.t_min = 0.0f;
+    sr.t_max = __ldg(&L->t_max);
+    sr.from = sh.srf;
+    sr.flags = sh.side | FLAG_SHAD;
+    sr.depth = sh.depth - 1;
+    off = __ldg(&le->shd_off);
+    num = __ldg(&le->shd_num);
+}
+
+/* diffuse, attenuation and specular of an unshadowed light (4100-4391) */
+__device__ void light_add(const qr_dscene &S, Shade &sh, int li)
+{
+    const qr_srf *__restrict__ s = &S.srf[sh.srf];
+    const qr_mat *__restrict__ m = &S.mat[__ldg(&s->mat[sh.side])];
+    const int props = sh.props;
+    const qr_lelem *__restrict__ le = &S.lelems[sh.loff + li];
+    const qr_light *__restrict__ L = &S.lgt[__ldg(&le->light)];
+    float lv[3];
+    const float dot = light_dot(S, sh, li, lv);
+    const float l_dff = __ldg(&m->l_dff), l_spc = __ldg(&m->l_spc);
+    const uint32_t l_pow = (uint32_t)__ldg(&m->l_pow);
+
+    float r2 = lv[0] * lv[0] + lv[1] * lv[1];
+    r2 = r2 + lv[2] * lv[2];
+
+    float diff, sdot = dot;
+    if (props & QR_PROP_DIFFUSE)
+    {
+        const float inv_r = rsq(r2);
+        float r1 = inv_r * r2;
+        float att = r2 * __ldg(&L->a_qdr);
+        r1 = r1 * __ldg(&L->a_lnr);
+        att = att + __ldg(&L->a_cnt);
+        att = att + r1;
+        const float inv_a = rsq(att);
+        diff = dot * inv_a;
+        diff = diff * inv_r;
+        diff = diff * l_dff;
+    }
+    else
+    {
+        diff = 0.0f;
+    }
+
+    int spec_on = 0;
+    float spec = 0.0f;
+    if (props & QR_PROP_SPECULAR)
+    {
+        float pn, rx, ry, rz;
+        pn = sdot * sh.nrm[0]; rx = lv[0] - pn; rx = rx - pn;
+        pn = sdot * sh.nrm[1]; ry = lv[1] - pn; ry = ry - pn;
+        pn = sdot * sh.nrm[2]; rz = lv[2] - pn; rz = rz - pn;
+        rx = rx * sh.dir[0];
+        ry = ry * sh.dir[1];
+        rz = rz * sh.dir[2];
+        float ray2 = sh.dir[2] * sh.dir[2];
+        ray2 = ray2 + sh.dir[0] * sh.dir[0];
+        ray2 = ray2 + sh.dir[1] * sh.dir[1];
+        float sv = rx + ry;
+        sv = sv + rz;
+        if (0.0f < sv)
         {
-            const qr_lelem *__restrict__ le = &S.lelems[loff + li];
-            const qr_light *__restrict__ L = &S.lgt[__ldg(&le->light)];
-            float lv[3];
-            #pragma unroll
-            for (int k = 0; k < 3; k++) lv[k] = __ldg(&L->pos[k]) - h.hit[k];
-            float dot = lv[0] * nrm[0] + lv[1] * nrm[1];
-            dot = dot + lv[2] * nrm[2];
-            if (!(0.0f < dot)) continue;
-
+            /* power in 28.4 fixed point (4225-4285) */
+            sv = sv * rsq(ray2);
+            sv = sv * rsq(r2);
+            float p1 = 1.0f, p2 = sv;
+            uint32_t fr = l_pow & 0xF, in = l_pow >> 4;
+            if (fr != 0)
             {
-                /* shadow ray: origin at the hit, direction L, t in (0, 1) */
-                Ray sr;
-                #pragma unroll
-                for (int k = 0; k < 3; k++)
+                float s4 = sv;
+                do
                 {
-                    sr.org[k] = h.hit[k];
-                    sr.dir[k] = lv[k];
-                    sr.phit[k] = h.loc[k];
-                }
-                sr.t_min = 0.0f;
-                sr.t_max = __ldg(&L->t_max);
-                sr.from = h.srf;
-                sr.flags = side | FLAG_SHAD;
-                sr.depth = r.depth - 1;
-                Walk sw;
-                sw.shadow = 1;
-                sw.occluded = 0;
-                sw.tbuf = sr.t_max;
-                sw.bestp = -1;
-                sw.best.srf = -1;
-                CNT(QR_STAT_RAY_SHADOW);
-                trace_walk(S, P, sr, __ldg(&le->shd_off), __ldg(&le->shd_num), sw, st);
-                if (sw.occluded) continue;
+                    s4 = fsqrt(s4);
+                    if (fr & 0x8) p1 = p1 * s4;
+                    fr = (fr << 1) & 0xF;
+                } while (fr != 0);
             }
-
-            CNT(QR_STAT_LIGHT);
-            float r2 = lv[0] * lv[0] + lv[1] * lv[1];
-            r2 = r2 + lv[2] * lv[2];
-
-            float diff, sdot = dot;
-            if (props & QR_PROP_DIFFUSE)
+            if (in != 0)
             {
-                const float inv_r = rsq(r2);
-                float r1 = inv_r * r2;
-                float att = r2 * __ldg(&L->a_qdr);
-                r1 = r1 * __ldg(&L->a_lnr);
-                att = att + __ldg(&L->a_cnt);
-                att = att + r1;
-                const float inv_a = rsq(att);
-                diff = dot * inv_a;
-                diff = diff * inv_r;
-                diff = diff * l_dff;
-            }
-            else
-            {
-                diff = 0.0f;
-            }
-
-            int spec_on = 0;
-            float spec = 0.0f;
-            if (props & QR_PROP_SPECULAR)
-            {
-                float pn, rx, ry, rz;
-                pn = sdot * nrm[0]; rx = lv[0] - pn; rx = rx - pn;
-                pn = sdot * nrm[1]; ry = lv[1] - pn; ry = ry - pn;
-                pn = sdot * nrm[2]; rz = lv[2] - pn; rz = rz - pn;
-                rx = rx * r.dir[0];
-                ry = ry * r.dir[1];
-                rz = rz * r.dir[2];
-                float ray2 = r.dir[2] * r.dir[2];
-                ray2 = ray2 + r.dir[0] * r.dir[0];
-                ray2 = ray2 + r.dir[1] * r.dir[1];
-                float sv = rx + ry;
-                sv = sv + rz;
-                if (0.0f < sv)
+                const float p3 = p1;
+                p1 = 1.0f;
+                do
                 {
-                    /* power in 28.4 fixed point (4225-4285) */
-                    sv = sv * rsq(ray2);
-                    sv = sv * rsq(r2);
-                    float p1 = 1.0f, p2 = sv;
-                    uint32_t fr = l_pow & 0xF, in = l_pow >> 4;
-                    if (fr != 0)
-                    {
-                        float s4 = sv;
-                        do
-                        {
-                            s4 = fsqrt(s4);
-                            if (fr & 0x8) p1 = p1 * s4;
-                            fr = (fr << 1) & 0xF;
-                        } while (fr != 0);
-                    }
-                    if (in != 0)
-                    {
-                        const float p3 = p1;
-                        p1 = 1.0f;
-                        do
-                        {
-                            if (in & 1) p1 = p1 * p2;
-                            p2 = p2 * p2;
-                            in >>= 1;
-                        } while (in != 0);
-                        p1 = p1 * p3;
-                    }
-                    spec = p1 * l_spc;
-                    spec_on = 1;
-                }
+                    if (in & 1) p1 = p1 * p2;
+                    p2 = p2 * p2;
+                    in >>= 1;
+                } while (in != 0);
+                p1 = p1 * p3;
             }
-
-            float lc[3];
-            if (spec_on && !(props & QR_PROP_METAL))
-            {
-                /* plain: highlight in the light's colour (4323-4355) */
-                #pragma unroll
-                for (int k = 0; k < 3; k++)
-                {
-                    const float lk = __ldg(&L->col[k]);
-                    float t1 = tex[k] * diff;
-                    t1 = t1 * lk;
-                    lc[k] = t1 + lk * spec;
-                }
-            }
-            else
-            {
-                /* metal: highlight tinted by the surface (4287-4317) */
-                if (spec_on) diff = diff + spec;
-                #pragma unroll
-                for (int k = 0; k < 3; k++)
-                {
-                    lc[k] = tex[k] * __ldg(&L->col[k]);
-                    lc[k] = lc[k] * diff;
-                }
-            }
-            #pragma unroll
-            for (int k = 0; k < 3; k++) c[k] = lc[k] + c[k];
+            spec = p1 * l_spc;
+            spec_on = 1;
         }
     }
 
-    /* transparency (4442-4936) */
+    float lc[3];
+    if (spec_on && !(props & QR_PROP_METAL))
+    {
+        /* plain: highlight in the light's colour (4323-4355) */
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            const float lk = __ldg(&L->col[k]);
+            float t1 = sh.tex[k] * diff;
+            t1 = t1 * lk;
+            lc[k] = t1 + lk * spec;
+        }
+    }
+    else
+    {
+        /* metal: highlight tinted by the surface (4287-4317) */
+        if (spec_on) diff = diff + spec;
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            lc[k] = sh.tex[k] * __ldg(&L->col[k]);
+            lc[k] = lc[k] * diff;
+        }
+    }
+    #pragma unroll
+    for (int k = 0; k < 3; k++) sh.c[k] = lc[k] + sh.c[k];
+}
+
+/* what a shaded hit asks of its children: a refracted ray (weight c_trn)
+ * and a reflected ray (weight c_rfl), traced in that order (4820-4883,
+ * 5235-5298) */
+struct Sec
+{
+    int   trn, rfl;             /* child wanted (before the depth check) */
+    float c_trn, c_rfl;
+    float nw[3], rw[3];         /* refracted / reflected directions */
+};
+
+/* transparency (4442-4936) and reflection (4942-5359): weights and
+ * directions of the children */
+__device__ void shade_end(const qr_dscene &S, const Shade &sh, Sec &o, StP st)
+{
+    const qr_srf *__restrict__ s = &S.srf[sh.srf];
+    const qr_mat *__restrict__ m = &S.mat[__ldg(&s->mat[sh.side])];
+    const int props = sh.props;
+    const float *nrm = sh.nrm;
+    const float *dir = sh.dir;
+    const float m_trn = __ldg(&m->c_trn), m_rfl = __ldg(&m->c_rfl);
+
     float c_trn = m_trn, c_rfl = m_rfl;
     o.trn = 0;
     if (!(props & QR_PROP_OPAQUE))
@@ -909,13 +980,13 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
         if (refr || fres)
         {
             CNT(QR_STAT_REFRACT);
-            float l2 = r.dir[0] * r.dir[0];
-            l2 = l2 + r.dir[1] * r.dir[1];
-            l2 = l2 + r.dir[2] * r.dir[2];
+            float l2 = dir[0] * dir[0];
+            l2 = l2 + dir[1] * dir[1];
+            l2 = l2 + dir[2] * dir[2];
             const float inv = rsq(l2);
             float dn[3];
             #pragma unroll
-            for (int k = 0; k < 3; k++) dn[k] = r.dir[k] * inv;
+            for (int k = 0; k < 3; k++) dn[k] = dir[k] * inv;
             float cosi = dn[0] * nrm[0];
             cosi = cosi + dn[1] * nrm[1];
             cosi = cosi + dn[2] * nrm[2];
@@ -946,7 +1017,7 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
                 else
                 {
                     #pragma unroll
-                    for (int k = 0; k < 3; k++) nw[k] = r.dir[k];
+                    for (int k = 0; k < 3; k++) nw[k] = dir[k];
                 }
                 if (fres)
                 {
@@ -973,7 +1044,7 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
         else
         {
             #pragma unroll
-            for (int k = 0; k < 3; k++) nw[k] = r.dir[k];
+            for (int k = 0; k < 3; k++) nw[k] = dir[k];
             do_trn = 1;
         }
         o.trn = do_trn && m_ok;
@@ -985,16 +1056,17 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
     {
         const int refl = (props & QR_PROP_REFLECT) != 0;
         const int do_rfl = refl || (!(props & QR_PROP_OPAQUE) && (props & QR_PROP_FRESNEL));
+        o.rfl = do_rfl;
         if (do_rfl)
         {
             CNT(QR_STAT_REFLECT);
-            float l2 = r.dir[0] * r.dir[0];
-            l2 = l2 + r.dir[1] * r.dir[1];
-            l2 = l2 + r.dir[2] * r.dir[2];
+            float l2 = dir[0] * dir[0];
+            l2 = l2 + dir[1] * dir[1];
+            l2 = l2 + dir[2] * dir[2];
             const float inv = rsq(l2);
-            float dn[3], rw[3];
+            float dn[3];
             #pragma unroll
-            for (int k = 0; k < 3; k++) dn[k] = r.dir[k] * inv;
+            for (int k = 0; k < 3; k++) dn[k] = dir[k] * inv;
             float cosi = dn[0] * nrm[0];
             cosi = cosi + dn[1] * nrm[1];
             cosi = cosi + dn[2] * nrm[2];
@@ -1002,8 +1074,8 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
             for (int k = 0; k < 3; k++)
             {
                 const float p = nrm[k] * cosi;
-                rw[k] = dn[k] - p;
-                rw[k] = rw[k] - p;
+                float rw = dn[k] - p;
+                o.rw[k] = rw - p;
             }
             if ((props & QR_PROP_FRESNEL) && (props & QR_PROP_OPAQUE))
             {
@@ -1058,10 +1130,7 @@ __device__ void shade_local(const qr_dscene &S, const qr_frame_params &P, const 
                 fr = fr * m_rfl;
                 c_rfl = m_rfl + fr;
             }
-            #pragma unroll
-            for (int k = 0; k < 3; k++) o.rw[k] = rw[k];
         }
-        o.rfl = do_rfl;
     }
     o.c_trn = c_trn;
     o.c_rfl = c_rfl;
@@ -1096,9 +1165,12 @@ __device__ __forceinline__ void child_ray(Ray &cr, const float hit[3], const flo
 }
 
 /*
- * The Whitted ray tree of one camera ray, without recursion.  The reference
- * recurses through its context stack (tracer.cpp:4820-4860, 5235-5275); here
- * a shaded hit that spawns a child is parked on a small per-thread stack and
+ * The Whitted ray tree of one camera ray as one loop with a single list walk.
+ * Each turn of the loop traces one segment: a camera or secondary ray
+ * (nearest hit), or one shadow ray of the hit being shaded (any occluder).
+ * The reference recurses through its context stack (tracer.cpp:4820-4860,
+ * 5235-5275) and loops over lights inside the shading (4008-4096); here a
+ * shaded hit that spawns a child is parked on a small per-thread stack and
  * combined when the child's colour is known, in the reference's order:
  * colour = rc * c_rfl + (tc * c_trn + local).
  */
@@ -1108,53 +1180,87 @@ __device__ void trace_tree(const qr_dscene &S, const qr_frame_params &P, Ray r,
     Pend stk[QR_MAX_DEPTH];
     int sp = 0;
     float ret[3];
+    Shade sh;
+    int shadow = 0, li = 0;
     #pragma unroll 1
     for (;;)
     {
         Walk w;
-        w.shadow = 0;
+        w.shadow = shadow;
         w.occluded = 0;
         w.tbuf = r.t_max;
         w.bestp = -1;
         w.best.srf = -1;
-        trace_walk(S, P, r, off, num, w, st);
-        if (w.best.srf < 0)
+        walk(S, P, r, off, num, w, st);
+
+        int finish = 0;         /* the shading of sh is complete */
+        if (shadow)
+        {
+            if (!w.occluded)
+            {
+                CNT(QR_STAT_LIGHT);
+                light_add(S, sh, li);
+            }
+            li = next_light(S, sh, li + 1);
+            if (li < sh.lnum)
+            {
+                CNT(QR_STAT_RAY_SHADOW);
+                shadow_ray(S, sh, li, r, off, num);
+                continue;
+            }
+            shadow = 0;
+            finish = 1;
+        }
+        else if (w.best.srf < 0)
         {
             ret[0] = ret[1] = ret[2] = 0.0f;
         }
         else
         {
             CNT(QR_STAT_SHADE);
-            float c[3];
+            shade_begin(S, P, r, w.best, sh);
+            li = next_light(S, sh, 0);
+            if (li < sh.lnum)
+            {
+                CNT(QR_STAT_RAY_SHADOW);
+                shadow = 1;
+                shadow_ray(S, sh, li, r, off, num);
+                continue;
+            }
+            finish = 1;
+        }
+
+        if (finish)
+        {
             Sec o;
-            shade_local(S, P, r, w.best, c, o, st);
-            const qr_srf *__restrict__ s = &S.srf[w.best.srf];
-            const int side = w.best.side;
+            shade_end(S, sh, o, st);
+            const qr_srf *__restrict__ s = &S.srf[sh.srf];
+            const int side = sh.side;
+            float c[3] = {sh.c[0], sh.c[1], sh.c[2]};
             int spawned = 0;
             if (o.trn)
             {
-                if (r.depth != 0)
+                if (sh.depth != 0)
                 {
                     Pend &p = stk[sp++];
                     #pragma unroll
                     for (int k = 0; k < 3; k++)
                     {
                         p.c[k] = c[k];
-                        p.hit[k] = w.best.hit[k];
-                        p.loc[k] = w.best.loc[k];
+                        p.hit[k] = sh.hit[k];
+                        p.loc[k] = sh.loc[k];
                         p.rw[k] = o.rw[k];
                     }
                     p.c_trn = o.c_trn;
                     p.c_rfl = o.c_rfl;
-                    p.srf = w.best.srf;
+                    p.srf = sh.srf;
                     p.side = side;
-                    p.depth = r.depth;
+                    p.depth = sh.depth;
                     p.stage = 0;
                     p.rfl = o.rfl;
                     CNT(QR_STAT_RAY_SECONDARY);
-                    const int d = r.depth - 1;
-                    child_ray(r, w.best.hit, o.nw, w.best.loc, w.best.srf,
-                              side | FLAG_PASS, d);
+                    child_ray(r, sh.hit, o.nw, sh.loc, sh.srf, side | FLAG_PASS,
+                              sh.depth - 1);
                     off = __ldg(&s->sec_off[1 - side]);
                     num = __ldg(&s->sec_num[1 - side]);
                     spawned = 1;
@@ -1167,7 +1273,7 @@ __device__ void trace_tree(const qr_dscene &S, const qr_frame_params &P, Ray r,
             }
             if (!spawned && o.rfl)
             {
-                if (r.depth != 0)
+                if (sh.depth != 0)
                 {
                     Pend &p = stk[sp++];
                     #pragma unroll
@@ -1175,8 +1281,7 @@ __device__ void trace_tree(const qr_dscene &S, const qr_frame_params &P, Ray r,
                     p.c_rfl = o.c_rfl;
                     p.stage = 1;
                     CNT(QR_STAT_RAY_SECONDARY);
-                    const int d = r.depth - 1;
-                    child_ray(r, w.best.hit, o.rw, w.best.loc, w.best.srf, side, d);
+                    child_ray(r, sh.hit, o.rw, sh.loc, sh.srf, side, sh.depth - 1);
                     off = __ldg(&s->sec_off[side]);
                     num = __ldg(&s->sec_num[side]);
                     spawned = 1;
@@ -1194,6 +1299,7 @@ __device__ void trace_tree(const qr_dscene &S, const qr_frame_params &P, Ray r,
 
         /* fold finished children into their parents */
         int more = 0;
+        #pragma unroll 1
         while (sp > 0)
         {
             Pend &p = stk[sp - 1];
