@@ -1392,7 +1392,15 @@ __device__ __forceinline__ uint32_t pack(const qr_frame_params &P, const float c
     return px;
 }
 
-__global__ void __launch_bounds__(128)
+/* blocks of 32x4 threads; QR_MIN_BLOCKS resident blocks per SM bound the
+ * registers per thread (65536 / (128 * QR_MIN_BLOCKS)).  Measured on the
+ * 1920x1080 4x AA animated frame: 1 (152 registers) 55.0 ms, unbounded (128)
+ * 48.0 ms, 5 (96) 44.8 ms, 6 (80) 44.0 ms, 8 (64) 46.5 ms */
+#ifndef QR_MIN_BLOCKS
+#define QR_MIN_BLOCKS 6
+#endif
+
+__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
 whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
                qr_dstats *gst)
 {
