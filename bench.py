@@ -52,6 +52,10 @@ WORKLOADS = {
     # plain Whitted frame: 800x480, 1 spp, 1 ground plane + 16 quadrics,
     # 2 lights, shadows
     "plain": dict(kind=1, seed=1, nq=16, w=800, h=480, fsaa=0, depth=10, anim=False),
+    # path tracer: 1280x720, 64 samples a pixel per step, depth 8 (roulette
+    # after 3 bounces), 32 quadrics in a closed box of 5 planes, light
+    # cluster with an emitting sphere
+    "pt": dict(kind=3, seed=1, nq=32, w=1280, h=720, fsaa=0, depth=8, anim=False, pt=64),
 }
 
 
@@ -141,6 +145,10 @@ def cpu_baseline(qr, wl, seconds=12.0):
     g = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)
     f = qr.Flat(g, wl["w"], wl["h"], wl["fsaa"])
     desc, params = f.update(0, wl["depth"])
+    spp = wl.get("pt", 0)
+    if spp:
+        params.pt_on, params.pts_c, params.seed, params.frame_idx = spp, 0.0, 1, 0
+    acc = np.zeros((params.y_res, params.x_row, 3), dtype=np.float32)
     cores = os.cpu_count() or 1
     out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
     # rows in a stride order spread over the whole frame (the top rows of a
@@ -161,8 +169,13 @@ def cpu_baseline(qr, wl, seconds=12.0):
                 nxt[0] += 1
             yy = (i * stride) % params.y_res
             nr = ctypes.c_uint64()
-            O.qr_oracle_render(ctypes.addressof(desc), ctypes.addressof(params),
-                               out.ctypes.data, yy, yy + 1, ctypes.byref(nr))
+            if spp:
+                O.qr_oracle_pt(ctypes.addressof(desc), ctypes.addressof(params),
+                               acc.ctypes.data, out.ctypes.data, yy, yy + 1,
+                               ctypes.byref(nr))
+            else:
+                O.qr_oracle_render(ctypes.addressof(desc), ctypes.addressof(params),
+                                   out.ctypes.data, yy, yy + 1, ctypes.byref(nr))
             with lock:
                 rows_done[0] += 1
                 rays[0] += nr.value
@@ -243,6 +256,10 @@ def main():
     def sid_of(j):
         return sids[j] if wl["anim"] else sids[0]
 
+    spp = wl.get("pt", 0)
+    if spp:
+        params.pt_on, params.pts_c, params.seed, params.frame_idx = spp, 0.0, 1, 0
+
     # instrumented launches: rays and work counters of every timed frame
     host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
     stats = dict((k, 0) for k in STAT_NAMES)
@@ -289,7 +306,7 @@ def main():
 
     # end to end through the engine API with a host frame buffer
     eng = qr.Engine(qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0), wl["w"], wl["h"],
-                    fsaa=wl["fsaa"], depth=wl["depth"])
+                    fsaa=wl["fsaa"], depth=wl["depth"], pton=spp)
     hbuf = np.zeros((wl["h"], wl["w"]), dtype=np.uint32)
     step_t = (lambda j: 16 * j) if wl["anim"] else (lambda j: 0)
     for j in range(args.warmup):
@@ -317,6 +334,7 @@ def main():
         "config": {"workload": args.workload, "width": wl["w"], "height": wl["h"],
                    "fsaa": wl["fsaa"], "quadrics": wl["nq"], "seed": wl["seed"],
                    "depth": wl["depth"], "animated": wl["anim"],
+                   "samples_per_pixel": spp if spp else (4 if wl["fsaa"] == 2 else 1),
                    "surfaces": int(desc.nsrf), "rays_per_frame": rays,
                    "l2": "256 MiB buffer written between timed steps",
                    "parallelism": "replicas" if world > 1 else "single"},

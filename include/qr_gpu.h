@@ -164,6 +164,9 @@ typedef struct qr_frame_params
     float   pts_c;  float pad2;             /* PT samples so far */
 } qr_frame_params;
 
+/* most path-tracer samples per pixel in one render call */
+#define QR_MAX_PT_SAMPLES   65536
+
 /* qr_frame_params.flags */
 #define QR_FP_LINEAR_WALK   1   /* walk every surface list in order instead of
                                    the scene's bounding-volume hierarchy (the
@@ -183,9 +186,21 @@ int qr_scene_update(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc);
 int qr_scene_release(qr_ctx *ctx, int scene_id);
 
 /* render one frame into a device frame buffer (uint32 XRGB, x_row stride),
- * asynchronously on `stream` (a cudaStream_t, 0 = default stream) */
+ * asynchronously on `stream` (a cudaStream_t, 0 = default stream).
+ * With fp->pt_on > 0 the frame is path traced: pt_on samples per pixel are
+ * added to the context's running sums (reset when fp->pts_c == 0, which
+ * counts the samples already summed) and the frame shows the mean over
+ * pts_c + pt_on samples; the samples come from PCG32 streams seeded by
+ * (fp->seed, fp->frame_idx, pixel).  This replaces the reference's
+ * path-tracer accumulation planes (rt_Scene::render with set_pton,
+ * core/engine/engine.cpp:2914-2919, 3674; tracer.cpp:2115-2139) */
 int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                      uint32_t *dev_frame, void *stream);
+
+/* path tracer with caller-owned running sums: dev_acc holds 3 floats per
+ * pixel (x_row stride) and is overwritten when fp->pts_c == 0 */
+int qr_render_pt(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                 float *dev_acc, uint32_t *dev_frame, void *stream);
 /* render one frame into host memory: copies in, renders, copies out, syncs */
 int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                    uint32_t *host_frame);

@@ -17,21 +17,26 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libqr_oracle.so")
+LIB64 = os.path.join(OUT, "libqr_oracle64.so")     # QR_ORACLE_FP64 build
 REF_DIR = os.environ.get("QR_REFERENCE", "/root/reference")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
 
 
-def build_oracle():
+def build_oracle(fp64=False):
+    """Compile qr_oracle.c in float (the checker, the CPU baseline) or, with
+    fp64, in double (the FP64 path-tracer oracle)."""
     os.makedirs(OUT, exist_ok=True)
+    lib = LIB64 if fp64 else LIB
     src = os.path.join(HERE, "qr_oracle.c")
     deps = [src, os.path.join(HERE, "qr_oracle.h"), os.path.join(ROOT, "include", "qr_gpu.h")]
-    if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
-        return LIB
+    if os.path.exists(lib) and all(os.path.getmtime(d) <= os.path.getmtime(lib) for d in deps):
+        return lib
     cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c99", "-fPIC", "-shared",
            "-ffp-contract=off", "-fno-fast-math", "-I" + HERE,
-           "-I" + os.path.join(ROOT, "include"), src, "-lm", "-o", LIB]
+           "-I" + os.path.join(ROOT, "include")] + (["-DQR_ORACLE_FP64"] if fp64 else []) + \
+          [src, "-lm", "-o", lib]
     subprocess.run(cmd, check=True)
-    return LIB
+    return lib
 
 
 def build_ref():
@@ -43,9 +48,12 @@ def build_ref():
     return REF_DRIVER
 
 
-def load_oracle():
-    L = ctypes.CDLL(build_oracle())
+def load_oracle(fp64=False):
+    L = ctypes.CDLL(build_oracle(fp64))
     L.qr_oracle_render.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_int, ctypes.c_int,
                                    ctypes.POINTER(ctypes.c_uint64)]
+    L.qr_oracle_pt.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                               ctypes.POINTER(ctypes.c_uint64)]
     return L

@@ -32,6 +32,26 @@
 #include "qr_gpu.h"
 #include "qr_oracle.h"
 
+/* precision of the restatement: float (the checker of the GPU tracer and
+ * the CPU baseline) or, built with QR_ORACLE_FP64, double (the FP64 oracle
+ * of the path tracer); both builds come from this one source.  The scene
+ * records stay float either way. */
+#ifdef QR_ORACLE_FP64
+typedef double real;
+#define R_SQRT  sqrt
+#define R_FABS  fabs
+#define R_FLOOR floor
+#define R_LRINT lrint
+#define R_FMA   fma
+#else
+typedef float real;
+#define R_SQRT  sqrtf
+#define R_FABS  fabsf
+#define R_FLOOR floorf
+#define R_LRINT lrintf
+#define R_FMA   fmaf
+#endif
+
 #define TAG_ARRAY   (-1)
 #define FLAG_SIDE   1
 #define FLAG_PASS   2           /* 0 pass back (reflect), 2 pass thru */
@@ -50,7 +70,7 @@ typedef struct scene_s
     const qr_elem  *elems;
     const qr_lelem *lelems;
     const uint32_t *texels;
-    float amb[3];
+    real amb[3];
     int   ctx_props;
     uint64_t nrays;         /* traced segments (stats) */
 } scene_t;
@@ -58,13 +78,13 @@ typedef struct scene_s
 /* a ray context (rt_SIMD_CONTEXT fields used per lane) */
 typedef struct ray_s
 {
-    float org[3];
-    float ray[3];
-    float t_min;
-    float t_max;
+    real org[3];
+    real ray[3];
+    real t_min;
+    real t_max;
     int   from;             /* originating surface (ctx PARAM OBJ), -1 none */
     int   flags;            /* side | pass | shadow bits of ctx PARAM FLG */
-    float phit[3];          /* originating surface's local hit (parent NRM_IJK) */
+    real phit[3];          /* originating surface's local hit (parent NRM_IJK) */
     int   depth;            /* remaining secondary-ray depth (inf_DEPTH) */
 } ray_t;
 
@@ -73,28 +93,28 @@ typedef struct hit_s
 {
     int   srf;
     int   side;
-    float t;
-    float hit[3];           /* world hit point (ctx HIT) */
-    float loc[3];           /* local hit in the solver's frame (ctx NEW) */
-    float amask;            /* sign of the quadric's a (for the record) */
+    real t;
+    real hit[3];           /* world hit point (ctx HIT) */
+    real loc[3];           /* local hit in the solver's frame (ctx NEW) */
+    real amask;            /* sign of the quadric's a (for the record) */
 } hit_t;
 
-static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
-static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
-static inline float fxor(float a, uint32_t m) { return u2f(f2u(a) ^ m); }
-static inline uint32_t sgnbit(float a) { return f2u(a) & 0x80000000u; }
+/* sign-bit operations of the reference's SIMD code (xor with the sign
+ * mask), written as negation so they hold in either precision */
+static inline real fxor(real a, uint32_t m) { return (m & 0x80000000u) ? -a : a; }
+static inline uint32_t sgnbit(real a) { return signbit(a) ? 0x80000000u : 0u; }
 
 /* reciprocal square root and reciprocal in the reference's full-precision
  * compat mode (core/config/rtconf.h: rsq = 1/sqrt, rcp = 1/x) */
-static inline float rsq(float x) { return 1.0f / sqrtf(x); }
+static inline real rsq(real x) { return 1.0f / R_SQRT(x); }
 
 /* M * v with the transform-node coefficients, diagonal terms first
  * (tracer.cpp:2537-2568); fast path keeps only the diagonal (2546) */
-static void xform(const qr_srf *t, const float v[3], float o[3])
+static void xform(const qr_srf *t, const real v[3], real o[3])
 {
-    float x = t->tci[0] * v[0];
-    float y = t->tcj[1] * v[1];
-    float z = t->tck[2] * v[2];
+    real x = t->tci[0] * v[0];
+    real y = t->tcj[1] * v[1];
+    real z = t->tck[2] * v[2];
     if (t->amap[3] != 1)
     {
         x = x + t->tci[1] * v[1];
@@ -117,10 +137,10 @@ static void xform(const qr_srf *t, const float v[3], float o[3])
  *   tbuf   current depth buffer
  *   dmask  this lane's near-zero-determinant flag, amask sign of a
  */
-static int clip_root(const scene_t *sc, const ray_t *r, int si, float t,
-                     float tbuf, const float ldff[3], const float lray[3],
-                     int side, int dmask, uint32_t amask, float hit[3],
-                     float loc[3])
+static int clip_root(const scene_t *sc, const ray_t *r, int si, real t,
+                     real tbuf, const real ldff[3], const real lray[3],
+                     int side, int dmask, uint32_t amask, real hit[3],
+                     real loc[3])
 {
     const qr_srf *s = &sc->srf[si];
     int valid = 1;
@@ -152,7 +172,7 @@ static int clip_root(const scene_t *sc, const ray_t *r, int si, float t,
     if (s->conic != 0 && dmask)
     {
         int mi = s->amap[0], mj = s->amap[1], mk = s->amap[2];
-        float r2 = loc[mi] * loc[mi];
+        real r2 = loc[mi] * loc[mi];
         if (s->conic != 2)
         {
             r2 = r2 + loc[mj] * loc[mj];
@@ -160,7 +180,7 @@ static int clip_root(const scene_t *sc, const ray_t *r, int si, float t,
         r2 = r2 + loc[mk] * loc[mk];
         if (r2 < T_EPS)
         {
-            float li, lj = 0.0f, lk, lr, sk;
+            real li, lj = 0.0f, lk, lr, sk;
             li = fxor(1.0f, sgnbit(ldff[mi]));
             sk = s->sci[mi];
             lr = 1.0f;
@@ -172,9 +192,9 @@ static int clip_root(const scene_t *sc, const ray_t *r, int si, float t,
             }
             sk = sk / s->sci[mk];
             sk = fxor(sk, 0x80000000u);
-            lk = sqrtf(sk);
+            lk = R_SQRT(sk);
             {
-                float inv = rsq(sk + lr);
+                real inv = rsq(sk + lr);
                 inv = inv * T_EPS;
                 li = li * inv;
                 lj = lj * inv;
@@ -214,13 +234,13 @@ static int clip_root(const scene_t *sc, const ray_t *r, int si, float t,
     {
         int mask = valid, saved = 0, cache_last = -1;
         int e;
-        float nx[3] = {0, 0, 0};    /* ctx NRM_X/Y/Z used as scratch */
+        real nx[3] = {0, 0, 0};    /* ctx NRM_X/Y/Z used as scratch */
         for (e = 0; e < s->clip_num; e++)
         {
             int ei = s->clip_off + e;
             const qr_elem *el = &sc->elems[ei];
             const qr_srf *c;
-            float p[3], v;
+            real p[3], v;
             if (el->kind == QR_ELM_ACC_ENTER)
             {
                 saved = mask;
@@ -258,7 +278,7 @@ static int clip_root(const scene_t *sc, const ray_t *r, int si, float t,
             }
             else
             {
-                float d[3];
+                real d[3];
                 for (k = 0; k < 3; k++) d[k] = hit[k] - c->pos[k];
                 if (c->amap[3] != 0) xform(c, d, p);
                 else { p[0] = d[0]; p[1] = d[1]; p[2] = d[2]; }
@@ -271,17 +291,17 @@ static int clip_root(const scene_t *sc, const ray_t *r, int si, float t,
             }
             else if (c->clpk == 2)
             {
-                float d2[3];
+                real d2[3];
                 for (k = 0; k < 3; k++)
                 {
-                    float d1 = (c->scj[k] + c->scj[k]) * p[k];
+                    real d1 = (c->scj[k] + c->scj[k]) * p[k];
                     d2[k] = p[k] * p[k] * c->sci[k] - d1;
                 }
                 v = ((d2[0] - c->sci[3]) + d2[1]) + d2[2];
             }
             else
             {
-                float d2[3];
+                real d2[3];
                 for (k = 0; k < 3; k++) d2[k] = p[k] * p[k] * c->sci[k];
                 v = ((d2[0] - c->sci[3]) + d2[1]) + d2[2];
             }
@@ -302,13 +322,13 @@ typedef struct walk_s
 {
     int     shadow;         /* 1: any-hit test for shadow rays */
     int     occluded;
-    float   tbuf;
+    real   tbuf;
     hit_t   best;
 } walk_t;
 
 /* record a root that passed the clipper; shadow rays test occlusion */
 static void accept_root(const scene_t *sc, walk_t *w, int si, int side,
-                        float t, const float hit[3], const float loc[3],
+                        real t, const real hit[3], const real loc[3],
                         uint32_t amask)
 {
     if (w->shadow)
@@ -327,7 +347,7 @@ static void accept_root(const scene_t *sc, walk_t *w, int si, int side,
     w->best.t = t;
     memcpy(w->best.hit, hit, sizeof(w->best.hit));
     memcpy(w->best.loc, loc, sizeof(w->best.loc));
-    w->best.amask = u2f(amask);
+    w->best.amask = amask ? (real)-0.0f : (real)0.0f;
 }
 
 /* CHECK_SIDE (558-567): a ray leaving surface s cannot hit it again from
@@ -341,14 +361,14 @@ static int side_blocked(const ray_t *r, int si, int side)
 }
 
 static void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
-                      const float ldff[3], const float lray[3],
-                      float a, float b, float c, float d)
+                      const real ldff[3], const real lray[3],
+                      real a, real b, real c, real d)
 {
     const qr_srf *s = &sc->srf[si];
-    float nb, sd, q, t1n, t1d, t2n, t2d, t1, t2;
+    real nb, sd, q, t1n, t1d, t2n, t2d, t1, t2;
     int dmask, m_pos, m_neg, t1m, t2m, first, k;
     uint32_t amask;
-    float hit[3], loc[3];
+    real hit[3], loc[3];
 
     /* QD_rts (5785-5799) */
     if (!(0.0f <= d)) return;               /* xmask */
@@ -356,7 +376,7 @@ static void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
     dmask = d < D_EPS;
 
     /* b-mixed roots (5854-5883) */
-    sd = sqrtf(d);
+    sd = R_SQRT(d);
     sd = fxor(sd, sgnbit(nb));
     q = nb + sd;
     m_pos = 0.0f <= sd;
@@ -371,7 +391,7 @@ static void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
     {
         /* near-zero determinant: zero numerators give t = 0 and the two
          * roots are equated and split by T_EPS (5908-5959) */
-        float tdff, teps;
+        real tdff, teps;
         int fmask;
         if (t1n == 0.0f) t1d = 1.0f;
         if (t2n == 0.0f) t2d = 1.0f;
@@ -385,7 +405,7 @@ static void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
         tdff = fmask ? tdff : 0.0f;
         teps = fmask ? T_EPS : 0.0f;
         teps = teps * t1;
-        teps = fabsf(teps);
+        teps = R_FABS(teps);
         tdff = tdff * -0.5f;
         tdff = tdff - teps;
         tdff = fxor(tdff, amask);
@@ -408,7 +428,7 @@ static void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
     for (k = 0; k < 2; k++)
     {
         int side = k == 0 ? first : 1 - first;
-        float t = side == SIDE_OUTER ? t1 : t2;
+        real t = side == SIDE_OUTER ? t1 : t2;
         int tm = side == SIDE_OUTER ? t1m : t2m;
         if (side_blocked(r, si, side)) continue;
         if (!tm) continue;
@@ -424,7 +444,7 @@ static void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
 
 static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
 {
-    float cdff[3] = {0, 0, 0}, cray[3] = {0, 0, 0};
+    real cdff[3] = {0, 0, 0}, cray[3] = {0, 0, 0};
     int cache_last = -1;
     int e, k;
 
@@ -433,13 +453,13 @@ static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
         int ei = off + e;
         const qr_elem *el = &sc->elems[ei];
         const qr_srf *s = &sc->srf[el->ref];
-        float ldff[3], lray[3];
+        real ldff[3], lray[3];
 
         if (el->kind == QR_ELM_TRNODE)
         {
             /* transform node: cache its diff and ray (2466-2510,
              * 2574-2589, 2599-2643) */
-            float d[3];
+            real d[3];
             for (k = 0; k < 3; k++) d[k] = r->org[k] - s->pos[k];
             if (s->amap[3] == 0) continue;
             xform(s, d, cdff);
@@ -471,7 +491,7 @@ static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
             }
             else
             {
-                float d[3];
+                real d[3];
                 for (k = 0; k < 3; k++) d[k] = r->org[k] - s->pos[k];
                 if (s->amap[3] != 0)
                 {
@@ -491,8 +511,8 @@ static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
             /* plane (5545-5634) */
             int mk = s->amap[2];
             uint32_t sg = s->asgn[2] ? 0x80000000u : 0u;
-            float dk, rk, t;
-            float hit[3], loc[3];
+            real dk, rk, t;
+            real hit[3], loc[3];
             if (r->from == el->ref) continue;
             dk = fxor(ldff[mk], sg);
             rk = fxor(lray[mk], sg);
@@ -510,7 +530,7 @@ static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
         else if (s->solver == 2)
         {
             /* quadric coefficients (5722-5783) */
-            float a, b, c, d, ax, bx, cx, sri, sdi;
+            real a, b, c, d, ax, bx, cx, sri, sdi;
             a = b = c = 0.0f;
             for (k = 0; k < 3; k++)
             {
@@ -532,14 +552,14 @@ static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
         {
             /* two-plane (6349-6402) */
             int mi = s->amap[0], mk = s->amap[2];
-            float ri = lray[mi], di = ldff[mi], rk2 = lray[mk], dk2 = ldff[mk];
-            float si_ = s->sci[mi], sk = s->sci[mk];
-            float dd, bb, cc, aa;
+            real ri = lray[mi], di = ldff[mi], rk2 = lray[mk], dk2 = ldff[mk];
+            real si_ = s->sci[mi], sk = s->sci[mk];
+            real dd, bb, cc, aa;
             dd = di * rk2 - dk2 * ri;
             dd = dd * dd;
             dd = dd * si_;
             dd = dd * sk;
-            dd = fabsf(dd);
+            dd = R_FABS(dd);
             bb = si_ * di * ri + sk * dk2 * rk2;
             cc = di * di * si_ + dk2 * dk2 * sk;
             aa = ri * ri * si_ + rk2 * rk2 * sk;
@@ -553,28 +573,28 @@ static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
  *      transform (3273-3352), material (3356-3416), lights (3929-4436),
  *      transparency (4438-4936), reflection (4938-5359) -------------------- */
 
-static void trace(scene_t *sc, const ray_t *r, int off, int num, float col[3]);
+static void trace(scene_t *sc, const ray_t *r, int off, int num, real col[3]);
 
-static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
+/* normal (side-oriented, world frame) and texel colour of a hit */
+static void hit_surface(const scene_t *sc, const hit_t *h, real nrm[3], real tex[3])
 {
     const qr_srf *s = &sc->srf[h->srf];
     int side = h->side;
     int props = s->props[side];
     const qr_mat *m = &sc->mat[s->mat[side]];
     uint32_t tside = side ? 0x80000000u : 0u;
-    float nrm[3], tex[3], c[3];
-    float tu = 0.0f, tv = 0.0f;
+    real tu = 0.0f, tv = 0.0f;
     int k;
 
     /* normal in the solver's frame */
     if (s->nrmk == 1)
     {
-        float n[3] = {0.0f, 0.0f, 0.0f};
+        real n[3] = {0.0f, 0.0f, 0.0f};
         int mk = s->amap[2];
         n[s->amap[0]] = 0.0f;
         n[s->amap[1]] = 0.0f;
         n[mk] = fxor(fxor(1.0f, tside), s->asgn[2] ? 0x80000000u : 0u);
-        memcpy(nrm, n, sizeof(nrm));
+        memcpy(nrm, n, 3 * sizeof(real));
         if (props & QR_PROP_TEXTURE)
         {
             tu = fxor(h->loc[s->amap[0]], s->asgn[0] ? 0x80000000u : 0u);
@@ -583,10 +603,10 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
     }
     else
     {
-        float x = h->loc[0] * s->sci[0];
-        float y = h->loc[1] * s->sci[1];
-        float z = h->loc[2] * s->sci[2];
-        float l2, inv;
+        real x = h->loc[0] * s->sci[0];
+        real y = h->loc[1] * s->sci[1];
+        real z = h->loc[2] * s->sci[2];
+        real l2, inv;
         if (s->nrmk == 2)
         {
             x = x - s->scj[0];
@@ -606,10 +626,10 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
     {
         /* node's transposed inverse (3273-3352) */
         const qr_srf *t = &sc->srf[s->trnode >= 0 ? s->trnode : h->srf];
-        float n1 = nrm[0], n2 = nrm[1], n3 = nrm[2];
-        float x = t->tci[0] * n1;
-        float y = t->tcj[1] * n2;
-        float z = t->tck[2] * n3;
+        real n1 = nrm[0], n2 = nrm[1], n3 = nrm[2];
+        real x = t->tci[0] * n1;
+        real y = t->tcj[1] * n2;
+        real z = t->tck[2] * n3;
         int renorm = 1;
         if (t->amap[3] != 1)
         {
@@ -623,8 +643,8 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
         }
         if (renorm)
         {
-            float l2 = x * x + y * y;
-            float inv;
+            real l2 = x * x + y * y;
+            real inv;
             l2 = l2 + z * z;
             inv = rsq(l2);
             x = x * inv;
@@ -640,30 +660,43 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
         int32_t idx = 0;
         if (props & QR_PROP_TEXTURE)
         {
-            float uv[2] = {tu, tv};
-            float tx = uv[m->tmap[0]], ty = uv[m->tmap[1]];
+            real uv[2] = {tu, tv};
+            real tx = uv[m->tmap[0]], ty = uv[m->tmap[1]];
             tx = tx - m->xoffs;
             ty = ty - m->yoffs;
             tx = tx * m->xscal;
             ty = ty * m->yscal;
-            idx = ((int32_t)floorf(tx) & m->xmask) +
-                  (((int32_t)floorf(ty) & m->ymask) << m->yshft);
+            idx = ((int32_t)R_FLOOR(tx) & m->xmask) +
+                  (((int32_t)R_FLOOR(ty) & m->ymask) << m->yshft);
         }
         texel = sc->texels[m->tex_off + idx];
-        tex[0] = (float)(int32_t)((texel >> 16) & 0xFF) / 255.0f;
-        tex[1] = (float)(int32_t)((texel >> 8) & 0xFF) / 255.0f;
-        tex[2] = (float)(int32_t)(texel & 0xFF) / 255.0f;
+        tex[0] = (real)(int32_t)((texel >> 16) & 0xFF) / 255.0f;
+        tex[1] = (real)(int32_t)((texel >> 8) & 0xFF) / 255.0f;
+        tex[2] = (real)(int32_t)(texel & 0xFF) / 255.0f;
         if (props & QR_PROP_GAMMA)
         {
             for (k = 0; k < 3; k++) tex[k] = tex[k] * tex[k];
         }
     }
 
+}
+
+static void shade(scene_t *sc, const ray_t *r, const hit_t *h, real col[3])
+{
+    const qr_srf *s = &sc->srf[h->srf];
+    int side = h->side;
+    int props = s->props[side];
+    const qr_mat *m = &sc->mat[s->mat[side]];
+    real nrm[3], tex[3], c[3];
+    int k;
+
+    hit_surface(sc, h, nrm, tex);
+
     /* ambient (3931-3996) */
     for (k = 0; k < 3; k++) c[k] = tex[k];
     if (!(props & QR_PROP_LIGHT))
     {
-        float f;
+        real f;
         for (k = 0; k < 3; k++) c[k] = c[k] * sc->amb[k];
         f = 1.0f - m->c_trn;
         f = f - m->c_rfl;
@@ -678,9 +711,9 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
             {
                 const qr_lelem *le = &sc->lelems[loff + li];
                 const qr_light *L = &sc->lgt[le->light];
-                float lv[3], dot, r2, diff, sdot, lc[3];
+                real lv[3], dot, r2, diff, sdot, lc[3];
                 int spec_on = 0;
-                float spec = 0.0f;
+                real spec = 0.0f;
                 for (k = 0; k < 3; k++) lv[k] = L->pos[k] - h->hit[k];
                 dot = lv[0] * nrm[0] + lv[1] * nrm[1];
                 dot = dot + lv[2] * nrm[2];
@@ -712,7 +745,7 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
 
                 if (props & QR_PROP_DIFFUSE)
                 {
-                    float inv_r, r1, att, inv_a;
+                    real inv_r, r1, att, inv_a;
                     inv_r = rsq(r2);
                     r1 = inv_r * r2;
                     att = r2 * L->a_qdr;
@@ -733,8 +766,8 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
 
                 if (props & QR_PROP_SPECULAR)
                 {
-                    float rx, ry, rz, sv, ray2;
-                    float pn;
+                    real rx, ry, rz, sv, ray2;
+                    real pn;
                     pn = sdot * nrm[0];
                     rx = lv[0] - pn; rx = rx - pn;
                     pn = sdot * nrm[1];
@@ -752,7 +785,7 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                     if (0.0f < sv)
                     {
                         /* power in 28.4 fixed point (4225-4285) */
-                        float p1 = 1.0f, p2, p3;
+                        real p1 = 1.0f, p2, p3;
                         uint32_t lp = (uint32_t)m->l_pow;
                         uint32_t fr = lp & 0xF, in = lp >> 4;
                         sv = sv * rsq(ray2);
@@ -760,10 +793,10 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                         p2 = sv;
                         if (fr != 0)
                         {
-                            float s4 = sv;
+                            real s4 = sv;
                             do
                             {
-                                s4 = sqrtf(s4);
+                                s4 = R_SQRT(s4);
                                 if (fr & 0x8) p1 = p1 * s4;
                                 fr = (fr << 1) & 0xF;
                             } while (fr != 0);
@@ -791,7 +824,7 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                      * (LT_mtl, 4323-4355) */
                     for (k = 0; k < 3; k++)
                     {
-                        float t1 = tex[k] * diff;
+                        real t1 = tex[k] * diff;
                         t1 = t1 * L->col[k];
                         lc[k] = t1 + L->col[k] * spec;
                     }
@@ -817,14 +850,14 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
 
     /* transparency (4442-4936) */
     {
-        float c_trn = m->c_trn, c_rfl = m->c_rfl;
+        real c_trn = m->c_trn, c_rfl = m->c_rfl;
         int m_trn = 1;
-        float nw[3];
+        real nw[3];
         int do_trn = 0;
 
         if (!(props & QR_PROP_OPAQUE))
         {
-            float dn[3], l2, inv, cosi, nci, kk, sq = 0.0f;
+            real dn[3], l2, inv, cosi, nci, kk, sq = 0.0f;
             int fres = (props & QR_PROP_FRESNEL) != 0;
             int refr = (props & QR_PROP_REFRACT) != 0;
             if (refr || fres)
@@ -853,14 +886,14 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                 }
                 else
                 {
-                    sq = sqrtf(kk);
+                    sq = R_SQRT(kk);
                     nci = nci + sq;
                     if (refr)
                     {
                         for (k = 0; k < 3; k++)
                         {
-                            float a1 = nrm[k] * nci;
-                            float a2 = dn[k] * m->c_rfr;
+                            real a1 = nrm[k] * nci;
+                            real a2 = dn[k] * m->c_rfr;
                             nw[k] = a2 - a1;
                         }
                     }
@@ -870,8 +903,8 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                     }
                     if (fres)
                     {
-                        float x1 = cosi, x2, x3, f0, f1, fr;
-                        float sqn;
+                        real x1 = cosi, x2, x3, f0, f1, fr;
+                        real sqn;
                         x2 = x1 * m->c_rfr;
                         x2 = x2 - sq;
                         sqn = sq * m->c_rfr;
@@ -883,7 +916,7 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                         f0 = f0 * f0;
                         f1 = f1 * f1;
                         fr = f0 + f1;
-                        fr = fabsf(fr * -0.5f);
+                        fr = R_FABS(fr * -0.5f);
                         fr = fr * m->c_trn;
                         c_trn = m->c_trn - fr;
                         c_rfl = m->c_rfl + fr;
@@ -899,7 +932,7 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
 
             if (do_trn && m_trn)
             {
-                float tc[3] = {0.0f, 0.0f, 0.0f};
+                real tc[3] = {0.0f, 0.0f, 0.0f};
                 if (r->depth != 0)
                 {
                     ray_t cr;
@@ -928,7 +961,7 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
             }
             if (do_rfl)
             {
-                float dn[3], l2, inv, cosi, rw[3];
+                real dn[3], l2, inv, cosi, rw[3];
                 l2 = r->ray[0] * r->ray[0];
                 l2 = l2 + r->ray[1] * r->ray[1];
                 l2 = l2 + r->ray[2] * r->ray[2];
@@ -939,17 +972,17 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                 cosi = cosi + dn[2] * nrm[2];
                 for (k = 0; k < 3; k++)
                 {
-                    float p = nrm[k] * cosi;
+                    real p = nrm[k] * cosi;
                     rw[k] = dn[k] - p;
                     rw[k] = rw[k] - p;
                 }
                 if ((props & QR_PROP_FRESNEL) && (props & QR_PROP_OPAQUE))
                 {
-                    float fr;
+                    real fr;
                     if (props & QR_PROP_METAL)
                     {
                         /* fast complex-IOR Fresnel (5067-5089) */
-                        float r6 = m->c_rcp, x4, x0, x1, x2, x3;
+                        real r6 = m->c_rcp, x4, x0, x1, x2, x3;
                         x4 = cosi * r6;
                         x4 = x4 + x4;
                         x0 = cosi * cosi;
@@ -967,17 +1000,17 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                         x0 = x0 / x2;
                         x1 = x1 / x3;
                         x0 = x0 + x1;
-                        fr = fabsf(x0 * -0.5f);
+                        fr = R_FABS(x0 * -0.5f);
                     }
                     else
                     {
                         /* dielectric Fresnel for opaque (5108-5134) */
-                        float x4 = cosi, n = m->c_rfr, x0, x7, x1, x2, x3, f1;
+                        real x4 = cosi, n = m->c_rfr, x0, x7, x1, x2, x3, f1;
                         x0 = cosi * n;
                         x7 = x0 * x0;
                         x7 = x7 + 1.0f;
                         x7 = x7 - m->rfr_2;
-                        x7 = sqrtf(x7);
+                        x7 = R_SQRT(x7);
                         x0 = x0 + x7;
                         x1 = x4;
                         x2 = x1 * n;
@@ -991,14 +1024,14 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
                         x0 = x0 * x0;
                         f1 = f1 * f1;
                         x0 = x0 + f1;
-                        fr = fabsf(x0 * -0.5f);
+                        fr = R_FABS(x0 * -0.5f);
                     }
                     fr = fr - 1.0f;
                     fr = fr * m->c_rfl;
                     c_rfl = m->c_rfl + fr;
                 }
                 {
-                    float rc[3] = {0.0f, 0.0f, 0.0f};
+                    real rc[3] = {0.0f, 0.0f, 0.0f};
                     if (r->depth != 0)
                     {
                         ray_t cr;
@@ -1021,7 +1054,7 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, float col[3])
     memcpy(col, c, sizeof(c));
 }
 
-static void trace(scene_t *sc, const ray_t *r, int off, int num, float col[3])
+static void trace(scene_t *sc, const ray_t *r, int off, int num, real col[3])
 {
     walk_t w;
     memset(&w, 0, sizeof(w));
@@ -1040,18 +1073,18 @@ static void trace(scene_t *sc, const ray_t *r, int off, int num, float col[3])
 /* ---- frame (ray generation 2348-2411, AA offsets engine.cpp:3521-3606,
  *      clamp/AA/gamma/pack 7028-7145 and FRAME_SIMD 1922-1940) ----------- */
 
-static const float aa4_h[4] = {-0.08f - 0.25f, -0.08f + 0.25f,
+static const real aa4_h[4] = {-0.08f - 0.25f, -0.08f + 0.25f,
                                +0.08f - 0.25f, +0.08f + 0.25f};
-static const float aa4_v[4] = {+0.08f - 0.25f, -0.08f - 0.25f,
+static const real aa4_v[4] = {+0.08f - 0.25f, -0.08f - 0.25f,
                                +0.08f + 0.25f, -0.08f + 0.25f};
 
 static void primary(scene_t *sc, const qr_scene_desc *d,
-                    const qr_frame_params *fp, float hs, float vs,
-                    float col[3])
+                    const qr_frame_params *fp, real hs, real vs,
+                    real col[3])
 {
     ray_t r;
     int k;
-    float hx[3], vx[3];
+    real hx[3], vx[3];
     for (k = 0; k < 3; k++)
     {
         hx[k] = fp->hor[k] * hs;
@@ -1069,25 +1102,25 @@ static void primary(scene_t *sc, const qr_scene_desc *d,
     trace(sc, &r, d->cam_off, d->cam_num, col);
 }
 
-static uint32_t pack(const qr_frame_params *fp, const float col[3])
+static uint32_t pack(const qr_frame_params *fp, const real col[3])
 {
     uint32_t px = 0;
     int k;
     static const int sh[3] = {16, 8, 0};
     for (k = 0; k < 3; k++)
     {
-        float v = col[k];
+        real v = col[k];
         int32_t iv;
-        if (fp->ctx_props & QR_PROP_GAMMA) v = sqrtf(v);
+        if (fp->ctx_props & QR_PROP_GAMMA) v = R_SQRT(v);
         v = v * 255.0f;
         iv = (isnan(v) || v >= 2147483648.0f || v < -2147483648.0f) ?
-             (int32_t)0x80000000 : (int32_t)lrintf(v);
+             (int32_t)0x80000000 : (int32_t)R_LRINT(v);
         px |= ((uint32_t)iv & 0xFF) << sh[k];
     }
     return px;
 }
 
-static inline float clamp1(float v) { return v < 1.0f ? v : 1.0f; }
+static inline real clamp1(real v) { return v < 1.0f ? v : 1.0f; }
 
 int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
                      uint32_t *frame, int y0, int y1, uint64_t *nrays)
@@ -1110,27 +1143,27 @@ int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
     {
         for (x = 0; x < fp->x_res; x++)
         {
-            float col[3];
+            real col[3];
             if (fp->fsaa == 2)
             {
-                float cs[4][3];
+                real cs[4][3];
                 int s;
                 for (s = 0; s < 4; s++)
                 {
-                    primary(&sc, d, fp, (float)x + aa4_h[s],
-                            (float)y + aa4_v[s], cs[s]);
+                    primary(&sc, d, fp, (real)x + aa4_h[s],
+                            (real)y + aa4_v[s], cs[s]);
                     for (k = 0; k < 3; k++) cs[s][k] = clamp1(cs[s][k]);
                 }
                 for (k = 0; k < 3; k++)
                 {
-                    float p01 = cs[0][k] * 0.5f + cs[1][k] * 0.5f;
-                    float p23 = cs[2][k] * 0.5f + cs[3][k] * 0.5f;
+                    real p01 = cs[0][k] * 0.5f + cs[1][k] * 0.5f;
+                    real p23 = cs[2][k] * 0.5f + cs[3][k] * 0.5f;
                     col[k] = p01 * 0.5f + p23 * 0.5f;
                 }
             }
             else
             {
-                primary(&sc, d, fp, (float)x, (float)y, col);
+                primary(&sc, d, fp, (real)x, (real)y, col);
                 for (k = 0; k < 3; k++) col[k] = clamp1(col[k]);
             }
             frame[(size_t)y * fp->x_row + x] = pack(fp, col);
@@ -1138,4 +1171,504 @@ int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
     }
     if (nrays) *nrays = sc.nrays;
     return QR_OK;
+}
+
+/* ==== path tracer ==========================================================
+ *
+ * The estimator of the reference's path-tracer mode (tracer.cpp built with
+ * RT_FEAT_PT, rt_Scene::set_pton, RT_FEAT_BUFFERS=0), per sample:
+ *   camera ray with a tent-filter jitter of +-0.5 pixel (2267-2342);
+ *   at a hit: colour = emission of the material (mat_COL, the light colour
+ *   x 100 of a LIGHT material, object.cpp:1346-1375) plus, for a diffuse
+ *   material and depth left, l_dff * tex * the colour of a cosine-weighted
+ *   bounce (3470-3930, power-series sin/cos 1979-2007), with Russian
+ *   roulette at probability max(tex) once the depth left is at most 5
+ *   (3484-3528); then the refracted and reflected children of the Whitted
+ *   path (4438-5359), where a dielectric, once the depth left is at most
+ *   8, follows only one of the two: reflection with
+ *   probability P = 0.25 + 0.5 Re, weight c_rfl / P, else refraction with
+ *   weight c_trn / (1 - P) (4685-4723); point lights and ambient are not
+ *   used (no next-event estimation); colour = rc c_rfl + (tc c_trn + local);
+ *   the pixel is the mean of its samples (2115-2139, 2250-2263).
+ * Random numbers come from one PCG32 stream (O'Neill 2014) per pixel and
+ * launch, seeded from (seed, frame index, pixel index), in the order the
+ * samples and their depth-first ray trees use them; the CUDA path tracer
+ * draws the same stream in the same order.
+ */
+
+/* depth left at which roulette and the dielectric split start: the
+ * reference compares its depth counter with RT_STACK_DEPTH - 5 and - 2
+ * (tracer.cpp:3486, 4690; RT_STACK_DEPTH = 10, tracer.h:51) whatever the
+ * scene's depth */
+#define PT_RR_DEPTH     (10 - 5)
+#define PT_SPLIT_DEPTH  (10 - 2)
+
+typedef struct pcg_s { uint64_t state, inc; } pcg_t;
+
+static uint32_t pcg_next(pcg_t *g)
+{
+    uint64_t old = g->state;
+    uint32_t xs, rot;
+    g->state = old * 6364136223846793005ull + g->inc;
+    xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+}
+
+static void pcg_seed(pcg_t *g, uint64_t seed, int frame, uint64_t pixel)
+{
+    g->state = 0u;
+    g->inc = (pixel << 1) | 1u;
+    pcg_next(g);
+    g->state += seed ^ ((uint64_t)(uint32_t)frame * 0x9E3779B97F4A7C15ull);
+    pcg_next(g);
+}
+
+/* uniform in [0, 1) with 24 bits, exact in either precision */
+static real pcg_unit(pcg_t *g)
+{
+    return (real)(int32_t)(pcg_next(g) >> 8) * (real)(1.0f / 16777216.0f);
+}
+
+/* power series of sin and cos on [-pi, pi], evaluated with fused
+ * multiply-adds like the reference's sinps/cosps (Taylor terms to x^9 and
+ * x^8) */
+static real pt_sin(real x)
+{
+    real t = x * x, s = x, p = x * t;
+    s = R_FMA(p, (real)(-1.0 / 6.0), s);
+    p = p * t;
+    s = R_FMA(p, (real)(1.0 / 120.0), s);
+    p = p * t;
+    s = R_FMA(p, (real)(-1.0 / 5040.0), s);
+    p = p * t;
+    s = R_FMA(p, (real)(1.0 / 362880.0), s);
+    return s;
+}
+
+static real pt_cos(real x)
+{
+    real t = x * x, c = 1.0f, p = t;
+    c = R_FMA(p, (real)(-0.5), c);
+    p = p * t;
+    c = R_FMA(p, (real)(1.0 / 24.0), c);
+    p = p * t;
+    c = R_FMA(p, (real)(-1.0 / 720.0), c);
+    p = p * t;
+    c = R_FMA(p, (real)(1.0 / 40320.0), c);
+    return c;
+}
+
+#ifdef QR_ORACLE_FP64
+#define PT_PI 3.14159265358979323846
+#else
+#define PT_PI 3.14159265358979323846f
+#endif
+
+/* cosine-weighted direction about the unit normal w */
+static void pt_bounce(const real w[3], real u1, real u2, real d[3])
+{
+    real a[3] = {0.0f, 0.0f, 0.0f}, u[3], v[3], l, inv, s0, s1, ph, cp, sp;
+    int k;
+    if (R_FABS(w[0]) > 0.1f) a[1] = 1.0f; else a[0] = 1.0f;
+    u[0] = a[1] * w[2] - a[2] * w[1];
+    u[1] = a[2] * w[0] - a[0] * w[2];
+    u[2] = a[0] * w[1] - a[1] * w[0];
+    l = u[0] * u[0] + u[1] * u[1];
+    l = l + u[2] * u[2];
+    inv = rsq(l);
+    for (k = 0; k < 3; k++) u[k] = u[k] * inv;
+    v[0] = w[1] * u[2] - w[2] * u[1];
+    v[1] = w[2] * u[0] - w[0] * u[2];
+    v[2] = w[0] * u[1] - w[1] * u[0];
+    s1 = R_SQRT(u1);
+    s0 = R_SQRT(1.0f - u1);
+    ph = u2 + u2;
+    ph = ph * PT_PI;
+    ph = ph - PT_PI;
+    cp = pt_cos(ph) * s1;
+    sp = pt_sin(ph) * s1;
+    for (k = 0; k < 3; k++)
+    {
+        d[k] = w[k] * s0;
+        d[k] = d[k] + u[k] * cp;
+        d[k] = d[k] + v[k] * sp;
+    }
+}
+
+/* refracted / reflected children of a hit: the Whitted weights (4442-5359) */
+typedef struct pt_sec_s
+{
+    int  trn, rfl, split;
+    real c_trn, c_rfl;
+    real nw[3], rw[3];
+} pt_sec_t;
+
+static void pt_secondary(const scene_t *sc, const ray_t *r, const hit_t *h,
+                         const real nrm[3], pt_sec_t *o)
+{
+    const qr_srf *s = &sc->srf[h->srf];
+    int props = s->props[h->side];
+    const qr_mat *m = &sc->mat[s->mat[h->side]];
+    real c_trn = m->c_trn, c_rfl = m->c_rfl;
+    int k;
+    o->trn = 0;
+    o->rfl = 0;
+    o->split = 0;
+    if (!(props & QR_PROP_OPAQUE))
+    {
+        int fres = (props & QR_PROP_FRESNEL) != 0;
+        int refr = (props & QR_PROP_REFRACT) != 0;
+        int do_trn = 0, m_ok = 1;
+        real nw[3];
+        if (refr || fres)
+        {
+            real dn[3], l2, inv, cosi, nci, kk;
+            l2 = r->ray[0] * r->ray[0];
+            l2 = l2 + r->ray[1] * r->ray[1];
+            l2 = l2 + r->ray[2] * r->ray[2];
+            inv = rsq(l2);
+            for (k = 0; k < 3; k++) dn[k] = r->ray[k] * inv;
+            cosi = dn[0] * nrm[0];
+            cosi = cosi + dn[1] * nrm[1];
+            cosi = cosi + dn[2] * nrm[2];
+            nci = cosi * m->c_rfr;
+            kk = nci * nci;
+            kk = kk + 1.0f;
+            kk = kk - m->rfr_2;
+            if (fres) m_ok = 0.0f <= kk;
+            if (fres && !m_ok)
+            {
+                c_trn = 0.0f;
+                c_rfl = m->c_rfl + m->c_trn;
+            }
+            else
+            {
+                real sq = R_SQRT(kk);
+                nci = nci + sq;
+                if (refr)
+                {
+                    for (k = 0; k < 3; k++)
+                    {
+                        real a1 = nrm[k] * nci;
+                        real a2 = dn[k] * m->c_rfr;
+                        nw[k] = a2 - a1;
+                    }
+                }
+                else
+                {
+                    for (k = 0; k < 3; k++) nw[k] = r->ray[k];
+                }
+                if (fres)
+                {
+                    real x1 = cosi, x2, x3, f0, f1, fr, sqn;
+                    x2 = x1 * m->c_rfr;
+                    x2 = x2 - sq;
+                    sqn = sq * m->c_rfr;
+                    x3 = x1;
+                    x1 = x1 + sqn;
+                    x3 = x3 - sqn;
+                    f0 = nci / x2;
+                    f1 = x1 / x3;
+                    f0 = f0 * f0;
+                    f1 = f1 * f1;
+                    fr = f0 + f1;
+                    fr = R_FABS(fr * -0.5f);
+                    fr = fr * m->c_trn;
+                    c_trn = m->c_trn - fr;
+                    c_rfl = m->c_rfl + fr;
+                    o->split = 1;
+                }
+                do_trn = 1;
+            }
+        }
+        else
+        {
+            for (k = 0; k < 3; k++) nw[k] = r->ray[k];
+            do_trn = 1;
+        }
+        o->trn = do_trn && m_ok;
+        for (k = 0; k < 3; k++) o->nw[k] = nw[k];
+    }
+    {
+        int refl = (props & QR_PROP_REFLECT) != 0;
+        int do_rfl = refl || (!(props & QR_PROP_OPAQUE) && (props & QR_PROP_FRESNEL));
+        o->rfl = do_rfl;
+        if (do_rfl)
+        {
+            real dn[3], l2, inv, cosi;
+            l2 = r->ray[0] * r->ray[0];
+            l2 = l2 + r->ray[1] * r->ray[1];
+            l2 = l2 + r->ray[2] * r->ray[2];
+            inv = rsq(l2);
+            for (k = 0; k < 3; k++) dn[k] = r->ray[k] * inv;
+            cosi = dn[0] * nrm[0];
+            cosi = cosi + dn[1] * nrm[1];
+            cosi = cosi + dn[2] * nrm[2];
+            for (k = 0; k < 3; k++)
+            {
+                real p = nrm[k] * cosi;
+                real x = dn[k] - p;
+                o->rw[k] = x - p;
+            }
+            if ((props & QR_PROP_FRESNEL) && (props & QR_PROP_OPAQUE))
+            {
+                real fr;
+                if (props & QR_PROP_METAL)
+                {
+                    real r6 = m->c_rcp, x4, x0, x1, x2, x3;
+                    x4 = cosi * r6;
+                    x4 = x4 + x4;
+                    x0 = cosi * cosi;
+                    r6 = r6 * r6;
+                    r6 = r6 + m->ext_2;
+                    x1 = x0 * r6;
+                    x0 = x0 + r6;
+                    x1 = x1 + 1.0f;
+                    x2 = x0;
+                    x3 = x1;
+                    x0 = x0 + x4;
+                    x1 = x1 + x4;
+                    x2 = x2 - x4;
+                    x3 = x3 - x4;
+                    x0 = x0 / x2;
+                    x1 = x1 / x3;
+                    x0 = x0 + x1;
+                    fr = R_FABS(x0 * -0.5f);
+                }
+                else
+                {
+                    real n = m->c_rfr, x0, x7, x1, x2, x3, f1;
+                    x0 = cosi * n;
+                    x7 = x0 * x0;
+                    x7 = x7 + 1.0f;
+                    x7 = x7 - m->rfr_2;
+                    x7 = R_SQRT(x7);
+                    x0 = x0 + x7;
+                    x1 = cosi;
+                    x2 = x1 * n;
+                    x2 = x2 - x7;
+                    x7 = x7 * n;
+                    x3 = x1;
+                    x1 = x1 + x7;
+                    x3 = x3 - x7;
+                    x0 = x0 / x2;
+                    f1 = x1 / x3;
+                    x0 = x0 * x0;
+                    f1 = f1 * f1;
+                    x0 = x0 + f1;
+                    fr = R_FABS(x0 * -0.5f);
+                }
+                fr = fr - 1.0f;
+                fr = fr * m->c_rfl;
+                c_rfl = m->c_rfl + fr;
+            }
+        }
+    }
+    o->c_trn = c_trn;
+    o->c_rfl = c_rfl;
+}
+
+static void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
+                     pcg_t *g, real col[3]);
+
+static void child(ray_t *cr, const hit_t *h, const real dir[3], int flags, int depth)
+{
+    int k;
+    for (k = 0; k < 3; k++)
+    {
+        cr->org[k] = h->hit[k];
+        cr->ray[k] = dir[k];
+        cr->phit[k] = h->loc[k];
+    }
+    cr->t_min = 0.0f;
+    cr->t_max = FLT_MAX;
+    cr->from = h->srf;
+    cr->flags = flags;
+    cr->depth = depth;
+}
+
+static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
+                     pcg_t *g, real col[3])
+{
+    const qr_srf *s = &sc->srf[h->srf];
+    int side = h->side;
+    int props = s->props[side];
+    const qr_mat *m = &sc->mat[s->mat[side]];
+    real nrm[3], tex[3], c[3], ddir[3] = {0.0f, 0.0f, 0.0f};
+    int dif, k;
+    pt_sec_t o;
+
+    hit_surface(sc, h, nrm, tex);
+
+    /* random draws in a fixed order: roulette, bounce, dielectric split */
+    dif = (props & QR_PROP_DIFFUSE) && r->depth != 0;
+    if (dif && r->depth <= PT_RR_DEPTH)
+    {
+        real p = tex[0] > tex[1] ? tex[0] : tex[1];
+        real u;
+        p = p > tex[2] ? p : tex[2];
+        u = pcg_unit(g);
+        if (!(u < p)) dif = 0;
+        else
+        {
+            real rc = 1.0f / p;
+            for (k = 0; k < 3; k++) tex[k] = tex[k] * rc;
+        }
+    }
+    if (dif)
+    {
+        real u1 = pcg_unit(g);
+        real u2 = pcg_unit(g);
+        pt_bounce(nrm, u1, u2, ddir);
+    }
+    pt_secondary(sc, r, h, nrm, &o);
+    if (o.split && o.trn && o.rfl && r->depth != 0 && r->depth <= PT_SPLIT_DEPTH)
+    {
+        real u = pcg_unit(g);
+        real re = o.c_rfl / (o.c_trn + o.c_rfl);
+        real pr = re * 0.5f;
+        pr = pr + 0.25f;
+        if (u < pr)
+        {
+            o.trn = 0;
+            o.c_rfl = o.c_rfl / pr;
+        }
+        else
+        {
+            o.rfl = 0;
+            o.c_trn = o.c_trn / (1.0f - pr);
+        }
+    }
+
+    /* diffuse child, then emission */
+    for (k = 0; k < 3; k++) c[k] = 0.0f;
+    if (dif)
+    {
+        ray_t cr;
+        real lc[3];
+        child(&cr, h, ddir, side, r->depth - 1);
+        pt_trace(sc, &cr, s->sec_off[side], s->sec_num[side], dmax, g, lc);
+        for (k = 0; k < 3; k++)
+        {
+            c[k] = lc[k] * m->l_dff;
+            c[k] = c[k] * tex[k];
+        }
+    }
+    for (k = 0; k < 3; k++) c[k] = c[k] + m->emit[k];
+
+    if (o.trn)
+    {
+        real tc[3] = {0.0f, 0.0f, 0.0f};
+        if (r->depth != 0)
+        {
+            ray_t cr;
+            child(&cr, h, o.nw, side | FLAG_PASS, r->depth - 1);
+            pt_trace(sc, &cr, s->sec_off[1 - side], s->sec_num[1 - side], dmax, g, tc);
+            for (k = 0; k < 3; k++) tc[k] = tc[k] * o.c_trn;
+        }
+        for (k = 0; k < 3; k++) c[k] = tc[k] + c[k];
+    }
+    if (o.rfl)
+    {
+        real rc[3] = {0.0f, 0.0f, 0.0f};
+        if (r->depth != 0)
+        {
+            ray_t cr;
+            child(&cr, h, o.rw, side, r->depth - 1);
+            pt_trace(sc, &cr, s->sec_off[side], s->sec_num[side], dmax, g, rc);
+            for (k = 0; k < 3; k++) rc[k] = rc[k] * o.c_rfl;
+        }
+        for (k = 0; k < 3; k++) c[k] = rc[k] + c[k];
+    }
+    for (k = 0; k < 3; k++) col[k] = c[k];
+}
+
+static void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
+                     pcg_t *g, real col[3])
+{
+    walk_t w;
+    memset(&w, 0, sizeof(w));
+    w.tbuf = r->t_max;
+    w.best.srf = -1;
+    sc->nrays++;
+    walk(sc, r, off, num, &w);
+    if (w.best.srf < 0)
+    {
+        col[0] = col[1] = col[2] = 0.0f;
+        return;
+    }
+    pt_shade(sc, r, &w.best, dmax, g, col);
+}
+
+/* tent filter on [-1, 1] from one uniform number (2267-2342), halved */
+static real pt_tent(real u)
+{
+    real r = u + u, d;
+    if (r < 1.0f) d = R_SQRT(r) - 1.0f;
+    else d = 1.0f - R_SQRT(2.0f - r);
+    return d * 0.5f;
+}
+
+int qr_oracle_pt(const qr_scene_desc *d, const qr_frame_params *fp, void *acc_,
+                 uint32_t *frame, int y0, int y1, uint64_t *nrays)
+{
+    scene_t sc;
+    real *acc = (real *)acc_;
+    int x, y, k, n, spp = fp->pt_on;
+    int n0 = (int)fp->pts_c;
+    memset(&sc, 0, sizeof(sc));
+    sc.srf = d->srf;
+    sc.mat = d->mat;
+    sc.lgt = d->lgt;
+    sc.elems = d->elems;
+    sc.lelems = d->lelems;
+    sc.texels = d->texels;
+    for (k = 0; k < 3; k++) sc.amb[k] = fp->amb[k];
+    sc.ctx_props = fp->ctx_props;
+    if (spp <= 0) return 1;
+    for (y = y0; y < y1; y++)
+    {
+        for (x = 0; x < fp->x_res; x++)
+        {
+            pcg_t g;
+            real sum[3] = {0.0f, 0.0f, 0.0f}, mean[3];
+            real *a = &acc[3 * ((size_t)y * fp->x_row + x)];
+            pcg_seed(&g, fp->seed, fp->frame_idx, (uint64_t)y * fp->x_res + x);
+            for (n = 0; n < spp; n++)
+            {
+                real hs, vs, col[3];
+                ray_t r;
+                hs = pt_tent(pcg_unit(&g));
+                vs = pt_tent(pcg_unit(&g));
+                hs = (real)x + hs;
+                vs = (real)y + vs;
+                for (k = 0; k < 3; k++)
+                {
+                    real hx = fp->hor[k] * hs;
+                    real vx = fp->ver[k] * vs;
+                    hx = hx + vx;
+                    r.ray[k] = hx + fp->dir[k];
+                    r.org[k] = fp->org[k];
+                    r.phit[k] = 0.0f;
+                }
+                r.t_min = fp->t_min;
+                r.t_max = fp->t_max;
+                r.from = -1;
+                r.flags = 0;
+                r.depth = fp->depth;
+                pt_trace(&sc, &r, d->cam_off, d->cam_num, fp->depth, &g, col);
+                for (k = 0; k < 3; k++) sum[k] = sum[k] + col[k];
+            }
+            for (k = 0; k < 3; k++)
+            {
+                a[k] = (n0 == 0 ? 0.0f : a[k]) + sum[k];
+                mean[k] = a[k] / (real)(n0 + spp);
+                mean[k] = clamp1(mean[k]);
+            }
+            if (frame != NULL) frame[(size_t)y * fp->x_row + x] = pack(fp, mean);
+        }
+    }
+    if (nrays != NULL) *nrays = sc.nrays;
+    return 0;
 }

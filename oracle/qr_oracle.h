@@ -17,6 +17,14 @@ extern "C" {
 int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
                      uint32_t *frame, int y0, int y1, uint64_t *nrays);
 
+/* path tracer: add fp->pt_on samples per pixel of rows [y0, y1) to the
+ * running sums acc[3 * (y * x_row + x)] (reset first when fp->pts_c == 0;
+ * the element type is the build's precision: float, or double with
+ * QR_ORACLE_FP64) and, when frame is not NULL, write the mean over
+ * pts_c + pt_on samples as XRGB */
+int qr_oracle_pt(const qr_scene_desc *d, const qr_frame_params *fp, void *acc,
+                 uint32_t *frame, int y0, int y1, uint64_t *nrays);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,7 @@ def lib():
         L.qrpy_scene_ctx.restype = vp
         L.qrpy_scene_ctx.argtypes = [vp]
         L.qrpy_scene_free.argtypes = [vp]
+        L.qrpy_scene_set_pton.argtypes = [vp, i32]
         L.qr_ctx_create.argtypes = [i32, ctypes.POINTER(vp)]
         L.qr_ctx_destroy.argtypes = [vp]
         L.qr_last_error.restype = ctypes.c_char_p
@@ -104,6 +105,7 @@ def lib():
         L.qr_scene_release.argtypes = [vp, i32]
         L.qr_render_device.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp, vp]
         L.qr_render_host.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp]
+        L.qr_render_pt.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp, vp, vp]
         L.qr_sync.argtypes = [vp, vp]
         L.qr_render_stats.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp,
                                       ctypes.POINTER(ctypes.c_uint64)]
@@ -205,6 +207,14 @@ class Context:
         if rc != QR_OK:
             raise RuntimeError("qr_render_device: %d %s" % (rc, self.error()))
 
+    def render_pt(self, sid, params, dev_acc, dev_frame, stream=0):
+        """Path-trace params.pt_on samples per pixel into caller-owned device
+        sums (3 floats a pixel) and the device frame."""
+        rc = lib().qr_render_pt(self.h, sid, ctypes.byref(params), ctypes.c_void_p(dev_acc),
+                                ctypes.c_void_p(dev_frame), ctypes.c_void_p(stream))
+        if rc != QR_OK:
+            raise RuntimeError("qr_render_pt: %d %s" % (rc, self.error()))
+
     def sync(self, stream=0):
         rc = lib().qr_sync(self.h, ctypes.c_void_p(stream))
         if rc != QR_OK:
@@ -219,12 +229,19 @@ class Context:
 class Engine:
     """rt_Platform + rt_Scene over a generated scene (the user-facing API)."""
 
-    def __init__(self, gen, x_res, y_res, fsaa=0, opts=OPTS_DEFAULT, depth=10):
+    def __init__(self, gen, x_res, y_res, fsaa=0, opts=OPTS_DEFAULT, depth=10, pton=0):
         self.gen = gen
         self.x_res, self.y_res = x_res, y_res
         self.h = lib().qrpy_scene_new(gen.h, x_res, y_res, fsaa, opts, depth)
         if not self.h:
             raise RuntimeError("rt_Scene construction failed")
+        self.pton = lib().qrpy_scene_set_pton(self.h, pton) if pton else 0
+
+    def set_pton(self, pton):
+        """Path-tracer samples per render (rt_Scene::set_pton); returns the
+        value in effect (0 when the scene's options prohibit the tracer)."""
+        self.pton = lib().qrpy_scene_set_pton(self.h, pton)
+        return self.pton
 
     def render(self, time=0, out=None):
         if out is None:

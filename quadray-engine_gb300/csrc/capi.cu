@@ -33,6 +33,8 @@ struct qr_ctx
     std::vector<qr_scene_slot> scenes;
     uint32_t    *dframe;    /* frame buffer for qr_render_host */
     size_t       dframe_px;
+    float       *dacc;      /* path-tracer running sums (3 floats a pixel) */
+    size_t       dacc_px;
     cudaStream_t stream;
 };
 
@@ -56,6 +58,8 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
     ctx->err[0] = 0;
     ctx->dframe = NULL;
     ctx->dframe_px = 0;
+    ctx->dacc = NULL;
+    ctx->dacc_px = 0;
     ctx->stream = 0;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -78,6 +82,7 @@ extern "C" int qr_ctx_destroy(qr_ctx *ctx)
         if (ctx->scenes[i].used) cudaFree(ctx->scenes[i].block);
     }
     if (ctx->dframe) cudaFree(ctx->dframe);
+    if (ctx->dacc) cudaFree(ctx->dacc);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return QR_OK;
@@ -298,7 +303,31 @@ static int check_fp(const qr_frame_params *fp)
     if (fp->x_res > 16384 || fp->y_res > 16384) return QR_ERR_LIMIT;
     if (fp->fsaa != 0 && fp->fsaa != 2) return QR_ERR_ARG;
     if (fp->depth < 0 || fp->depth > QR_MAX_DEPTH) return QR_ERR_LIMIT;
+    if (fp->pt_on < 0 || fp->pt_on > QR_MAX_PT_SAMPLES) return QR_ERR_LIMIT;
+    if (!(fp->pts_c >= 0.0f) || fp->pts_c > 16777216.0f) return QR_ERR_ARG;
     return QR_OK;
+}
+
+/* the context's path-tracer sums, kept across renders of one frame size */
+static int ensure_acc(qr_ctx *ctx, size_t px)
+{
+    if (ctx->dacc_px >= px) return QR_OK;
+    if (ctx->dacc) cudaFree(ctx->dacc);
+    ctx->dacc = NULL;
+    ctx->dacc_px = 0;
+    cudaError_t e = cudaMalloc(&ctx->dacc, px * 3 * sizeof(float));
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaMalloc path-tracer sums", e);
+    ctx->dacc_px = px;
+    return QR_OK;
+}
+
+/* Whitted frame, or path-tracer samples when fp->pt_on > 0 */
+static cudaError_t launch(qr_ctx *ctx, const qr_scene_slot *sl, const qr_frame_params *fp,
+                          float *acc, uint32_t *dev_frame, cudaStream_t stream)
+{
+    (void)ctx;
+    if (fp->pt_on > 0) return qr_launch_pt(sl->d, *fp, acc, dev_frame, stream);
+    return qr_launch_whitted(sl->d, *fp, dev_frame, stream);
 }
 
 extern "C" int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
@@ -309,9 +338,30 @@ extern "C" int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params
     int rc = check_fp(fp);
     if (rc != QR_OK) return rc;
     if (dev_frame == NULL) return QR_ERR_ARG;
-    cudaError_t e = qr_launch_whitted(sl->d, *fp, dev_frame,
-                                      (cudaStream_t)stream);
-    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "whitted launch", e);
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaSetDevice", e);
+    if (fp->pt_on > 0)
+    {
+        rc = ensure_acc(ctx, (size_t)fp->x_row * fp->y_res);
+        if (rc != QR_OK) return rc;
+    }
+    e = launch(ctx, sl, fp, ctx->dacc, dev_frame, (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "render launch", e);
+    return QR_OK;
+}
+
+extern "C" int qr_render_pt(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                            float *dev_acc, uint32_t *dev_frame, void *stream)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    int rc = check_fp(fp);
+    if (rc != QR_OK) return rc;
+    if (fp->pt_on <= 0 || dev_acc == NULL || dev_frame == NULL) return QR_ERR_ARG;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess)
+        e = qr_launch_pt(sl->d, *fp, dev_acc, dev_frame, (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "path-tracer launch", e);
     return QR_OK;
 }
 
@@ -333,7 +383,12 @@ extern "C" int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *
         if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaMalloc frame", e);
         ctx->dframe_px = px;
     }
-    if (e == cudaSuccess) e = qr_launch_whitted(sl->d, *fp, ctx->dframe, ctx->stream);
+    if (e == cudaSuccess && fp->pt_on > 0)
+    {
+        rc = ensure_acc(ctx, px);
+        if (rc != QR_OK) return rc;
+    }
+    if (e == cudaSuccess) e = launch(ctx, sl, fp, ctx->dacc, ctx->dframe, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(host_frame, ctx->dframe, px * sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, ctx->stream);
@@ -357,8 +412,17 @@ extern "C" int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params 
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaMalloc(&dframe, px * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&dst, sizeof(qr_dstats));
+    float *dacc = NULL;
+    if (e == cudaSuccess && fp->pt_on > 0)
+        e = cudaMalloc(&dacc, px * 3 * sizeof(float));
+    if (e == cudaSuccess && dacc != NULL)
+        e = cudaMemsetAsync(dacc, 0, px * 3 * sizeof(float), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(dst, 0, sizeof(qr_dstats), ctx->stream);
-    if (e == cudaSuccess) e = qr_launch_whitted_stats(sl->d, *fp, dframe, dst, ctx->stream);
+    if (e == cudaSuccess)
+    {
+        if (fp->pt_on > 0) e = qr_launch_pt_stats(sl->d, *fp, dacc, dframe, dst, ctx->stream);
+        else e = qr_launch_whitted_stats(sl->d, *fp, dframe, dst, ctx->stream);
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(host_frame, dframe, px * sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, ctx->stream);
@@ -367,6 +431,7 @@ extern "C" int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params 
                             ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (dframe) cudaFree(dframe);
+    if (dacc) cudaFree(dacc);
     if (dst) cudaFree(dst);
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "render stats", e);
     for (int k = 0; k < QR_STAT_COUNT; k++) counts[k] = hst.c[k];

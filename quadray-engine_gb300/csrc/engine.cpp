@@ -7,6 +7,7 @@
  * per-thread render0 calls.
  */
 #include <math.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -94,7 +95,8 @@ rt_void rt_Scene::operator delete(rt_pntr ptr)
 rt_Scene::rt_Scene(rt_SCENE *scn_, rt_si32 x_res_, rt_si32 y_res_,
                    rt_si32 x_row_, rt_ui32 *frame_, rt_Platform *pfm_)
     : pfm(pfm_), scn(scn_), x_res(x_res_), y_res(y_res_), x_row(x_row_),
-      frame(frame_), own_frame(RT_NULL), opts(0), pt_on(0), depth(10),
+      frame(frame_), own_frame(RT_NULL), opts(0), pt_on(0), pts_c(0), pt_frame(0),
+      depth(10),
       fl(RT_NULL), scene_id(-1), print(0), next(RT_NULL)
 {
     if (scn == RT_NULL) throw rt_Exception("null-pointer in scene");
@@ -208,12 +210,41 @@ rt_void rt_Scene::prepare(rt_time time)
     }
 }
 
+/* frame parameters of this render; in path-tracer mode the samples
+ * accumulate over frames until the scene changes (rt_Scene::render,
+ * core/engine/engine.cpp:3054), each render adding pt_on per pixel */
+rt_void rt_Scene::frame_setup(qr_frame_params *fp)
+{
+    fl->frame_params(fp);
+    fp->x_row = x_row;
+    if (pt_on <= 0) return;
+    qr_scene_desc d;
+    fl->desc(&d);
+    std::vector<unsigned char> key;
+    key.insert(key.end(), (const unsigned char *)d.srf,
+               (const unsigned char *)(d.srf + d.nsrf));
+    key.insert(key.end(), (const unsigned char *)d.mat,
+               (const unsigned char *)(d.mat + d.nmat));
+    key.insert(key.end(), (const unsigned char *)fp,
+               (const unsigned char *)fp + offsetof(qr_frame_params, x_res));
+    key.push_back((unsigned char)fl->fsaa);
+    if (key != pt_key)
+    {
+        pts_c = 0;
+        pt_key.swap(key);
+    }
+    fp->pt_on = pt_on;
+    fp->pts_c = (float)pts_c;
+    fp->frame_idx = pt_frame++;
+    fp->seed = 0x5A17F00Dull;
+    pts_c += pt_on;
+}
+
 rt_void rt_Scene::render(rt_time time)
 {
     prepare(time);
     qr_frame_params fp;
-    fl->frame_params(&fp);
-    fp.x_row = x_row;
+    frame_setup(&fp);
     int rc = qr_render_host(pfm->get_ctx(), scene_id, &fp, frame);
     if (rc != QR_OK)
     {
@@ -226,8 +257,7 @@ rt_void rt_Scene::render_device(rt_time time, rt_ui32 *dev_frame, rt_pntr stream
 {
     prepare(time);
     qr_frame_params fp;
-    fl->frame_params(&fp);
-    fp.x_row = x_row;
+    frame_setup(&fp);
     int rc = qr_render_device(pfm->get_ctx(), scene_id, &fp, dev_frame, stream);
     if (rc != QR_OK) throw rt_Exception("GPU render failed");
 }
@@ -250,12 +280,17 @@ rt_si32 rt_Scene::set_opts(rt_si32 o)
     return opts;
 }
 rt_si32 rt_Scene::get_pton() { return pt_on; }
+/* path-tracer samples per render (0 off); refused while the options
+ * prohibit the path tracer (RT_OPTS_PT, rt_Scene::set_pton,
+ * core/engine/engine.cpp:3807-3822) */
 rt_si32 rt_Scene::set_pton(rt_si32 pton)
 {
-    /* the path tracer is not part of this build's render path yet; the
-     * Whitted tracer keeps rendering */
-    (void)pton;
-    pt_on = 0;
+    if ((opts & RT_OPTS_PT) == 0)
+    {
+        rt_si32 was = pt_on;
+        pt_on = pton > 0 ? pton : 0;
+        if (pt_on && !was) pts_c = 0;
+    }
     return pt_on;
 }
 rt_si32 rt_Scene::get_cam_idx() { return fl->cam_idx; }

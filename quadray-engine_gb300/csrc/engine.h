@@ -12,6 +12,7 @@
 #ifndef QR_ENGINE_H
 #define QR_ENGINE_H
 
+#include <vector>
 #include "format.h"
 #include "rt_exception.h"
 #include "qr_gpu.h"
@@ -146,6 +147,9 @@ private:
     rt_ui32     *own_frame;
     rt_si32      opts;
     rt_si32      pt_on;
+    rt_si32      pts_c;         /* path-tracer samples accumulated */
+    rt_si32      pt_frame;      /* path-tracer launches (stream index) */
+    std::vector<unsigned char> pt_key;  /* scene records of the last frame */
     rt_si32      depth;
     qr::Flat    *fl;
     int          scene_id;
@@ -153,6 +157,7 @@ private:
     rt_Scene    *next;
 
     rt_void     prepare(rt_time time);
+    rt_void     frame_setup(qr_frame_params *fp);
     friend class rt_Platform;
 };
 

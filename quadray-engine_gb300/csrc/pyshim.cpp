@@ -154,6 +154,11 @@ void *qrpy_scene_ctx(void *h)
     return ((qrpy_engine *)h)->pfm->get_ctx();
 }
 
+int qrpy_scene_set_pton(void *h, int pton)
+{
+    return ((qrpy_engine *)h)->scn->set_pton(pton);
+}
+
 void qrpy_scene_free(void *h)
 {
     qrpy_engine *e = (qrpy_engine *)h;

@@ -560,6 +560,114 @@ static void build_anim(Scene &sc, uint64_t seed, int nq)
     sc.scn.lock = RT_NULL;
 }
 
+/* camera at p looking at t, both in one x = const plane (rotation about X
+ * only, as look_camera) */
+static rt_OBJECT camera_at(Scene &sc, float px, float py, float pz, float ty,
+                           float tz, float fov_deg, float amb_lum)
+{
+    double dy = ty - py, dz = tz - pz;
+    double ang = atan2(-dy, dz) * 180.0 / RT_PI;
+    float pov = (float)(0.5 / tan(0.5 * fov_deg * RT_PI / 180.0));
+    return sc.camera(px, py, pz, (float)ang, 0.0f, 0.0f, pov, 0xFFFFFF, amb_lum);
+}
+
+/* a box wall: plane through p with rotation r (multiples of 90 degrees, so
+ * the surface maps to the axes), clipped to [-a, a] x [-b, b] in its I, J */
+static rt_OBJECT wall(Scene &sc, rt_MATERIAL *m, float rx, float ry, float px,
+                      float py, float pz, float a, float b)
+{
+    rt_OBJECT o = sc.plane(m, m);
+    rt_PLANE *pl = (rt_PLANE *)o.obj.pobj;
+    pl->srf.min[RT_I] = -a; pl->srf.max[RT_I] = +a;
+    pl->srf.min[RT_J] = -b; pl->srf.max[RT_J] = +b;
+    Scene::trm_set(&o.trm, 1, 1, 1, rx, ry, 0, px, py, pz);
+    return o;
+}
+
+/* QR_SCN_PT: path-tracer scene.  A closed box of 5 planes (x = +-10,
+ * y = 20, z = 0, z = 12; the front y = 0 is where the camera looks in) with
+ * red / green side walls, nq quadrics inside (60% Lambertian, 25% mirror,
+ * 15% dielectric of index 1.5) and a light cluster: one array holding 16
+ * point lights and a LIGHT-material sphere, whose emission is the cluster's
+ * accumulated light colour x 100 (core/engine/object.cpp:1346-1375) */
+static void build_pt(Scene &sc, uint64_t seed, int nq)
+{
+    Rng r(seed);
+    const float bw = 10.0f, bd = 20.0f, bh = 12.0f;
+    std::vector<rt_OBJECT> root;
+    root.push_back(camera_at(sc, 0.0f, -14.0f, 6.0f, 10.0f, 6.0f, 60.0f, 0.05f));
+
+    rt_MATERIAL *white = sc.material(RT_MAT_PLAIN, 0xC8C8C8, 0.9f, 0.0f, 1.0f,
+                                     0.0f, 0.0f, 1.0f, 0.0f);
+    rt_MATERIAL *red = sc.material(RT_MAT_PLAIN, 0xC03028, 0.9f, 0.0f, 1.0f,
+                                   0.0f, 0.0f, 1.0f, 0.0f);
+    rt_MATERIAL *green = sc.material(RT_MAT_PLAIN, 0x30B040, 0.9f, 0.0f, 1.0f,
+                                     0.0f, 0.0f, 1.0f, 0.0f);
+    root.push_back(wall(sc, white, 0.0f, 0.0f, 0.0f, 0.5f * bd, 0.0f, bw, 0.5f * bd));
+    root.push_back(wall(sc, white, 180.0f, 0.0f, 0.0f, 0.5f * bd, bh, bw, 0.5f * bd));
+    root.push_back(wall(sc, red, 0.0f, 90.0f, -bw, 0.5f * bd, 0.5f * bh, 0.5f * bh, 0.5f * bd));
+    root.push_back(wall(sc, green, 0.0f, -90.0f, bw, 0.5f * bd, 0.5f * bh, 0.5f * bh, 0.5f * bd));
+    root.push_back(wall(sc, white, 90.0f, 0.0f, 0.0f, bd, 0.5f * bh, bw, 0.5f * bh));
+
+    /* light cluster */
+    std::vector<rt_OBJECT> cluster;
+    for (int i = 0; i < 16; i++)
+    {
+        float lx = -0.6f + 0.4f * (float)(i & 3);
+        float ly = -0.6f + 0.4f * (float)(i >> 2);
+        if ((sc.flags & QR_GEN_ONELIGHT) && i > 0) continue;
+        cluster.push_back(sc.light(lx, ly, 0.0f, 0xFFF4E8, 0.0f, 0.025f,
+                                   0.0f, 0.0f, 0.0f));
+    }
+    rt_MATERIAL *lm = sc.material(RT_MAT_LIGHT, 0xFFFFFF, 1.0f, 0.0f, 1.0f,
+                                  0.0f, 0.0f, 1.0f, 0.0f);
+    cluster.push_back(sc.quadric(RT_TAG_SPHERE, 1.2f, 0.0f, -RT_INF, +RT_INF, lm, lm));
+    rt_OBJECT co = sc.array(cluster);
+    Scene::trm_set(&co.trm, 1, 1, 1, 0, 0, 0, 0.0f, 0.55f * bd, bh - 1.6f);
+    root.push_back(co);
+
+    for (int i = 0; i < nq; i++)
+    {
+        double u = r.u01();
+        rt_ui32 col = rand_rgb(r, 0.3, 1.0);
+        rt_MATERIAL *mo, *mi;
+        if (u < 0.60)
+        {
+            mo = mi = sc.material(RT_MAT_PLAIN, col, 1.0f, 0.0f, 1.0f,
+                                  0.0f, 0.0f, 1.0f, 0.0f);
+        }
+        else if (u < 0.85)
+        {
+            mo = sc.material(RT_MAT_METAL, col, 0.0f, 0.0f, 1.0f,
+                             1.0f, 0.0f, 1.0f, 9.0f);
+            mi = sc.material(RT_MAT_PLAIN, 0x808080, 1.0f, 0.0f, 1.0f,
+                             0.0f, 0.0f, 1.0f, 0.0f);
+        }
+        else
+        {
+            mo = sc.material(RT_MAT_PLAIN, 0xF0F8FF, 0.0f, 0.0f, 1.0f,
+                             0.0f, 1.0f, 1.0f / 1.5f, 0.0f);
+            mi = sc.material(RT_MAT_PLAIN, 0xF0F8FF, 0.0f, 0.0f, 1.0f,
+                             0.0f, 1.0f, 1.5f, 0.0f);
+        }
+        int tag;
+        rt_OBJECT q = random_quadric(sc, r, mo, mi, &tag);
+        float p[3];
+        rand_pos(r, p, -bw + 2.5, bw - 2.5, 3.0, bd - 2.5, 1.5, bh - 4.0);
+        float rx = r.uf(-180, 180);
+        float ry = r.uf(-180, 180);
+        float rz = r.uf(-180, 180);
+        Scene::trm_set(&q.trm, 1, 1, 1, rx, ry, rz, p[0], p[1], p[2]);
+        root.push_back(q);
+    }
+    rt_OBJECT ro = sc.array(root);
+    sc.scn.root = ro.obj;
+    /* opt-outs of the default options: Fresnel on, and the path tracer
+     * allowed (RT_OPTS_PT prohibits it, core/engine/format.h:64) */
+    sc.scn.opts = RT_OPTS_FRESNEL | RT_OPTS_PT;
+    sc.scn.lock = RT_NULL;
+}
+
 static Scene *build(int kind, uint64_t seed, int nq, int flags)
 {
     Scene *sc = new Scene();
@@ -568,6 +676,9 @@ static Scene *build(int kind, uint64_t seed, int nq, int flags)
     {
     case QR_SCN_ANIM:
         build_anim(*sc, seed, nq > 0 ? nq : 64);
+        break;
+    case QR_SCN_PT:
+        build_pt(*sc, seed, nq > 0 ? nq : 32);
         break;
     case QR_SCN_PLAIN:
     default:

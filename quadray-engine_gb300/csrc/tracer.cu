@@ -653,30 +653,19 @@ struct Shade
     int   loff, lnum;       /* light list of the hit side */
 };
 
-/* normal, texel and ambient of a hit (3255-3416, 3945-3987) */
-__device__ void shade_begin(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
-                            const Hit &h, Shade &sh)
+/* side-oriented normal in world axes (PL 5669-5687, QD 6237-6283,
+ * TP 6415-6457, node transform 3273-3352) and texel colour (3380-3416,
+ * PAINT_COLX 970-979) of a hit */
+__device__ __forceinline__ void hit_surface(const qr_dscene &S, const Hit &h,
+                                            float nrm[3], float tex[3])
 {
     const qr_srf *__restrict__ s = &S.srf[h.srf];
     const int side = h.side;
     const int props = __ldg(&s->props[side]);
     const qr_mat *__restrict__ m = &S.mat[__ldg(&s->mat[side])];
     const uint32_t tside = side ? SIGN_BIT : 0u;
-    float nrm[3], tex[3];
     float tu = 0.0f, tv = 0.0f;
     const int nrmk = __ldg(&s->nrmk);
-
-    sh.srf = h.srf;
-    sh.side = side;
-    sh.props = props;
-    #pragma unroll
-    for (int k = 0; k < 3; k++)
-    {
-        sh.hit[k] = h.hit[k];
-        sh.loc[k] = h.loc[k];
-        sh.dir[k] = r.dir[k];
-    }
-    sh.depth = r.depth;
 
     if (nrmk == 1)
     {
@@ -761,6 +750,32 @@ __device__ void shade_begin(const qr_dscene &S, const qr_frame_params &P, const 
             for (int k = 0; k < 3; k++) tex[k] = tex[k] * tex[k];
         }
     }
+
+}
+
+/* normal, texel and ambient of a hit (3255-3416, 3945-3987) */
+__device__ void shade_begin(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                            const Hit &h, Shade &sh)
+{
+    const qr_srf *__restrict__ s = &S.srf[h.srf];
+    const int side = h.side;
+    const int props = __ldg(&s->props[side]);
+    const qr_mat *__restrict__ m = &S.mat[__ldg(&s->mat[side])];
+    float nrm[3], tex[3];
+
+    sh.srf = h.srf;
+    sh.side = side;
+    sh.props = props;
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        sh.hit[k] = h.hit[k];
+        sh.loc[k] = h.loc[k];
+        sh.dir[k] = r.dir[k];
+    }
+    sh.depth = r.depth;
+
+    hit_surface(S, h, nrm, tex);
 
     #pragma unroll
     for (int k = 0; k < 3; k++)
@@ -953,6 +968,7 @@ __device__ void light_add(const qr_dscene &S, Shade &sh, int li)
 struct Sec
 {
     int   trn, rfl;             /* child wanted (before the depth check) */
+    int   split;                /* Fresnel weights were computed (no TIR) */
     float c_trn, c_rfl;
     float nw[3], rw[3];         /* refracted / reflected directions */
 };
@@ -970,6 +986,7 @@ __device__ void shade_end(const qr_dscene &S, const Shade &sh, Sec &o, StP st)
 
     float c_trn = m_trn, c_rfl = m_rfl;
     o.trn = 0;
+    o.split = 0;
     if (!(props & QR_PROP_OPAQUE))
     {
         const int fres = (props & QR_PROP_FRESNEL) != 0;
@@ -1037,6 +1054,7 @@ __device__ void shade_end(const qr_dscene &S, const Shade &sh, Sec &o, StP st)
                     fr = fr * m_trn;
                     c_trn = m_trn - fr;
                     c_rfl = m_rfl + fr;
+                    o.split = 1;
                 }
                 do_trn = 1;
             }
@@ -1455,7 +1473,446 @@ whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
 #endif
 }
 
+
+/* ==== path tracer (the reference's RT_FEAT_PT estimator) ====================
+ *
+ * Per sample: a camera ray with a tent-filter jitter of +-0.5 pixel
+ * (2267-2342); at each hit the material's emission (the light colour x 100
+ * of a LIGHT material, object.cpp:1346-1375) plus, for a diffuse material
+ * with depth left, l_dff * tex * the colour of one cosine-weighted bounce
+ * (3470-3930; power-series sin/cos, 1979-2007) under Russian roulette at
+ * probability max(tex) once the depth left is at most RT_STACK_DEPTH - 5
+ * (3484-3528); then the refracted and reflected children of the Whitted path,
+ * where a dielectric, once the depth left is at most RT_STACK_DEPTH - 2,
+ * follows only one: reflection with probability P = 0.25 + 0.5 Re (weight
+ * c_rfl / P) or refraction (weight c_trn / (1 - P)) (4685-4723).  Both
+ * thresholds use the reference's compile-time stack depth (10, tracer.h:51,
+ * QR_MAX_DEPTH here), not the scene's depth.  No point lights, no
+ * ambient.  colour = rc c_rfl + (tc c_trn + (bounce l_dff tex + emission)).
+ * Random numbers: one PCG32 stream (O'Neill 2014) per pixel and launch,
+ * seeded from (seed, frame index, pixel), drawn in sample order and, within
+ * a sample, in depth-first order of its ray tree.
+ */
+
+struct Pcg
+{
+    unsigned long long state, inc;
+};
+
+__device__ __forceinline__ uint32_t pcg_next(Pcg &g)
+{
+    const unsigned long long old = g.state;
+    g.state = old * 6364136223846793005ull + g.inc;
+    const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    const uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+}
+
+__device__ __forceinline__ void pcg_seed(Pcg &g, unsigned long long seed, int frame,
+                                         unsigned long long pixel)
+{
+    g.state = 0ull;
+    g.inc = (pixel << 1) | 1ull;
+    pcg_next(g);
+    g.state += seed ^ ((unsigned long long)(uint32_t)frame * 0x9E3779B97F4A7C15ull);
+    pcg_next(g);
+}
+
+/* uniform in [0, 1), 24 bits */
+__device__ __forceinline__ float pcg_unit(Pcg &g)
+{
+    return (float)(int32_t)(pcg_next(g) >> 8) * (1.0f / 16777216.0f);
+}
+
+/* Taylor series of sin and cos on [-pi, pi] with fused multiply-adds, as the
+ * reference's sinps / cosps (terms to x^9 and x^8) */
+__device__ __forceinline__ float pt_sin(float x)
+{
+    const float t = x * x;
+    float s = x, p = x * t;
+    s = __fmaf_rn(p, (float)(-1.0 / 6.0), s);
+    p = p * t;
+    s = __fmaf_rn(p, (float)(1.0 / 120.0), s);
+    p = p * t;
+    s = __fmaf_rn(p, (float)(-1.0 / 5040.0), s);
+    p = p * t;
+    s = __fmaf_rn(p, (float)(1.0 / 362880.0), s);
+    return s;
+}
+
+__device__ __forceinline__ float pt_cos(float x)
+{
+    const float t = x * x;
+    float c = 1.0f, p = t;
+    c = __fmaf_rn(p, -0.5f, c);
+    p = p * t;
+    c = __fmaf_rn(p, (float)(1.0 / 24.0), c);
+    p = p * t;
+    c = __fmaf_rn(p, (float)(-1.0 / 720.0), c);
+    p = p * t;
+    c = __fmaf_rn(p, (float)(1.0 / 40320.0), c);
+    return c;
+}
+
+/* cosine-weighted direction about the unit normal w */
+__device__ __forceinline__ void pt_bounce(const float w[3], float u1, float u2, float d[3])
+{
+    float a[3] = {0.0f, 0.0f, 0.0f}, u[3], v[3];
+    if (fabsf(w[0]) > 0.1f) a[1] = 1.0f; else a[0] = 1.0f;
+    u[0] = a[1] * w[2] - a[2] * w[1];
+    u[1] = a[2] * w[0] - a[0] * w[2];
+    u[2] = a[0] * w[1] - a[1] * w[0];
+    float l = u[0] * u[0] + u[1] * u[1];
+    l = l + u[2] * u[2];
+    const float inv = rsq(l);
+    #pragma unroll
+    for (int k = 0; k < 3; k++) u[k] = u[k] * inv;
+    v[0] = w[1] * u[2] - w[2] * u[1];
+    v[1] = w[2] * u[0] - w[0] * u[2];
+    v[2] = w[0] * u[1] - w[1] * u[0];
+    const float s1 = fsqrt(u1);
+    const float s0 = fsqrt(1.0f - u1);
+    float ph = u2 + u2;
+    ph = ph * 3.14159265358979323846f;
+    ph = ph - 3.14159265358979323846f;
+    const float cp = pt_cos(ph) * s1;
+    const float sp = pt_sin(ph) * s1;
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        float x = w[k] * s0;
+        x = x + u[k] * cp;
+        d[k] = x + v[k] * sp;
+    }
+}
+
+/* tent filter on [-1, 1] from one uniform number, halved */
+__device__ __forceinline__ float pt_tent(float u)
+{
+    const float r = u + u;
+    const float d = r < 1.0f ? fsqrt(r) - 1.0f : 1.0f - fsqrt(2.0f - r);
+    return d * 0.5f;
+}
+
+/* a shaded path-tracer hit with its children: 0 awaits the bounce, 1 may
+ * spawn the refracted child, 2 awaits it, 3 may spawn the reflected child,
+ * 4 awaits it */
+struct PtPend
+{
+    float c[3], tex[3], emit[3];
+    float l_dff, c_trn, c_rfl;
+    float hit[3], loc[3], nw[3], rw[3];
+    int   srf, side, depth, stage, trn, rfl;
+};
+
+/* shade a hit: normal, texel, the random draws (roulette, bounce, split)
+ * and the children's weights; returns whether the bounce is taken (its
+ * direction in ddir) */
+__device__ int pt_begin(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                        const Hit &h, PtPend &p, Pcg &g, float ddir[3], StP st)
+{
+    const qr_srf *__restrict__ s = &S.srf[h.srf];
+    const int side = h.side;
+    const int props = __ldg(&s->props[side]);
+    const qr_mat *__restrict__ m = &S.mat[__ldg(&s->mat[side])];
+    float nrm[3], tex[3];
+    hit_surface(S, h, nrm, tex);
+
+    int dif = (props & QR_PROP_DIFFUSE) && r.depth != 0;
+    if (dif && r.depth <= QR_MAX_DEPTH - 5)
+    {
+        float pr = tex[0] > tex[1] ? tex[0] : tex[1];
+        pr = pr > tex[2] ? pr : tex[2];
+        const float u = pcg_unit(g);
+        if (!(u < pr)) dif = 0;
+        else
+        {
+            const float rc = fdiv(1.0f, pr);
+            #pragma unroll
+            for (int k = 0; k < 3; k++) tex[k] = tex[k] * rc;
+        }
+    }
+    if (dif)
+    {
+        const float u1 = pcg_unit(g);
+        const float u2 = pcg_unit(g);
+        pt_bounce(nrm, u1, u2, ddir);
+    }
+
+    Shade sh;
+    sh.srf = h.srf;
+    sh.side = side;
+    sh.props = props;
+    #pragma unroll
+    for (int k = 0; k < 3; k++) { sh.nrm[k] = nrm[k]; sh.dir[k] = r.dir[k]; }
+    Sec o;
+    shade_end(S, sh, o, st);
+    if (o.split && o.trn && o.rfl && r.depth != 0 && r.depth <= QR_MAX_DEPTH - 2)
+    {
+        const float u = pcg_unit(g);
+        const float re = fdiv(o.c_rfl, o.c_trn + o.c_rfl);
+        float pr = re * 0.5f;
+        pr = pr + 0.25f;
+        if (u < pr)
+        {
+            o.trn = 0;
+            o.c_rfl = fdiv(o.c_rfl, pr);
+        }
+        else
+        {
+            o.rfl = 0;
+            o.c_trn = fdiv(o.c_trn, 1.0f - pr);
+        }
+    }
+
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        p.c[k] = 0.0f;
+        p.tex[k] = tex[k];
+        p.emit[k] = __ldg(&m->emit[k]);
+        p.hit[k] = h.hit[k];
+        p.loc[k] = h.loc[k];
+        p.nw[k] = o.nw[k];
+        p.rw[k] = o.rw[k];
+    }
+    p.l_dff = __ldg(&m->l_dff);
+    p.c_trn = o.c_trn;
+    p.c_rfl = o.c_rfl;
+    p.srf = h.srf;
+    p.side = side;
+    p.depth = r.depth;
+    p.trn = o.trn;
+    p.rfl = o.rfl;
+    return dif;
+}
+
+/* fold the finished child's colour ret into p and spawn its next child
+ * into (r, off, num); returns 1 when a child was spawned, else 0 with the
+ * node's colour in ret */
+__device__ int pt_advance(const qr_dscene &S, PtPend &p, float ret[3], Ray &r,
+                          int &off, int &num, StP st)
+{
+    const qr_srf *__restrict__ s = &S.srf[p.srf];
+    if (p.stage == 0)
+    {
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            float c = ret[k] * p.l_dff;
+            c = c * p.tex[k];
+            p.c[k] = c + p.emit[k];
+        }
+        p.stage = 1;
+    }
+    if (p.stage == 1)
+    {
+        if (p.trn)
+        {
+            if (p.depth != 0)
+            {
+                CNT(QR_STAT_RAY_SECONDARY);
+                child_ray(r, p.hit, p.nw, p.loc, p.srf, p.side | FLAG_PASS, p.depth - 1);
+                off = __ldg(&s->sec_off[1 - p.side]);
+                num = __ldg(&s->sec_num[1 - p.side]);
+                p.stage = 2;
+                return 1;
+            }
+            #pragma unroll
+            for (int k = 0; k < 3; k++) p.c[k] = 0.0f + p.c[k];
+        }
+        p.stage = 3;
+    }
+    else if (p.stage == 2)
+    {
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            const float tc = ret[k] * p.c_trn;
+            p.c[k] = tc + p.c[k];
+        }
+        p.stage = 3;
+    }
+    if (p.stage == 3)
+    {
+        if (p.rfl)
+        {
+            if (p.depth != 0)
+            {
+                CNT(QR_STAT_RAY_SECONDARY);
+                child_ray(r, p.hit, p.rw, p.loc, p.srf, p.side, p.depth - 1);
+                off = __ldg(&s->sec_off[p.side]);
+                num = __ldg(&s->sec_num[p.side]);
+                p.stage = 4;
+                return 1;
+            }
+            #pragma unroll
+            for (int k = 0; k < 3; k++) p.c[k] = 0.0f + p.c[k];
+        }
+        #pragma unroll
+        for (int k = 0; k < 3; k++) ret[k] = p.c[k];
+        return 0;
+    }
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const float rc = ret[k] * p.c_rfl;
+        p.c[k] = rc + p.c[k];
+        ret[k] = p.c[k];
+    }
+    return 0;
+}
+
+/* one path-tracer sample: the ray tree as one loop over traced segments */
+__device__ void trace_pt(const qr_dscene &S, const qr_frame_params &P, Ray r,
+                         Pcg &g, float col[3], StP st)
+{
+    PtPend stk[QR_MAX_DEPTH + 1];
+    int sp = 0, off = S.cam_off, num = S.cam_num;
+    float ret[3];
+    #pragma unroll 1
+    for (;;)
+    {
+        Walk w;
+        w.shadow = 0;
+        w.occluded = 0;
+        w.tbuf = r.t_max;
+        w.bestp = -1;
+        w.best.srf = -1;
+        walk(S, P, r, off, num, w, st);
+        if (w.best.srf < 0)
+        {
+            ret[0] = ret[1] = ret[2] = 0.0f;
+        }
+        else
+        {
+            CNT(QR_STAT_SHADE);
+            PtPend &p = stk[sp++];
+            float ddir[3];
+            if (pt_begin(S, P, r, w.best, p, g, ddir, st))
+            {
+                const qr_srf *__restrict__ s = &S.srf[p.srf];
+                p.stage = 0;
+                CNT(QR_STAT_RAY_SECONDARY);
+                child_ray(r, p.hit, ddir, p.loc, p.srf, p.side, p.depth - 1);
+                off = __ldg(&s->sec_off[p.side]);
+                num = __ldg(&s->sec_num[p.side]);
+                continue;
+            }
+            /* no bounce: the node starts with its emission, and stage 1
+             * folds nothing */
+            #pragma unroll
+            for (int k = 0; k < 3; k++) p.c[k] = p.c[k] + p.emit[k];
+            p.stage = 1;
+        }
+
+        int spawned = 0;
+        #pragma unroll 1
+        while (sp > 0)
+        {
+            if (pt_advance(S, stk[sp - 1], ret, r, off, num, st)) { spawned = 1; break; }
+            sp--;
+        }
+        if (!spawned) break;
+    }
+    #pragma unroll
+    for (int k = 0; k < 3; k++) col[k] = ret[k];
+}
+
+__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
+pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *frame,
+          qr_dstats *gst)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.x_res || y >= P.y_res) return;
+#ifdef QR_STATS
+    TCnt cnt;
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
+    StP st = &cnt;
+#else
+    StP st = NULL;
+    (void)gst;
+#endif
+    Pcg g;
+    pcg_seed(g, P.seed, P.frame_idx, (unsigned long long)y * P.x_res + x);
+    const int spp = P.pt_on;
+    const int n0 = (int)P.pts_c;
+    float sum[3] = {0.0f, 0.0f, 0.0f};
+    #pragma unroll 1
+    for (int n = 0; n < spp; n++)
+    {
+        float hs = pt_tent(pcg_unit(g));
+        float vs = pt_tent(pcg_unit(g));
+        hs = (float)x + hs;
+        vs = (float)y + vs;
+        Ray r;
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            float hx = P.hor[k] * hs;
+            const float vx = P.ver[k] * vs;
+            hx = hx + vx;
+            r.dir[k] = hx + P.dir[k];
+            r.org[k] = P.org[k];
+            r.phit[k] = 0.0f;
+        }
+        r.t_min = P.t_min;
+        r.t_max = P.t_max;
+        r.from = -1;
+        r.flags = 0;
+        r.depth = P.depth;
+        CNT(QR_STAT_RAY_PRIMARY);
+        float col[3];
+        trace_pt(S, P, r, g, col, st);
+        #pragma unroll
+        for (int k = 0; k < 3; k++) sum[k] = sum[k] + col[k];
+    }
+    float *a = acc + 3 * ((size_t)y * P.x_row + x);
+    float mean[3];
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        a[k] = (n0 == 0 ? 0.0f : a[k]) + sum[k];
+        mean[k] = fdiv(a[k], (float)(n0 + spp));
+        mean[k] = clamp1(mean[k]);
+    }
+    frame[(size_t)y * P.x_row + x] = pack(P, mean);
+#ifdef QR_STATS
+    const unsigned am = __activemask();
+    const int leader = __ffs(am) - 1;
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++)
+    {
+        const unsigned v = __reduce_add_sync(am, cnt.c[k]);
+        if ((int)(threadIdx.x & 31) == leader && v != 0)
+            atomicAdd(&gst->c[k], (unsigned long long)v);
+    }
+#endif
+}
+
 } /* namespace QR_NS */
+
+#ifdef QR_STATS
+cudaError_t qr_launch_pt_stats(const qr_dscene &sc, const qr_frame_params &fp, float *acc,
+                               uint32_t *dev_frame, qr_dstats *dstats,
+                               cudaStream_t stream)
+#else
+cudaError_t qr_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *acc,
+                         uint32_t *dev_frame, cudaStream_t stream)
+#endif
+{
+    const dim3 block(32, 4);
+    const dim3 grid((fp.x_res + block.x - 1) / block.x,
+                    (fp.y_res + block.y - 1) / block.y);
+#ifdef QR_STATS
+    QR_NS::pt_kernel<<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, dstats);
+#else
+    QR_NS::pt_kernel<<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, NULL);
+#endif
+    return cudaGetLastError();
+}
 
 #ifdef QR_STATS
 cudaError_t qr_launch_whitted_stats(const qr_dscene &sc, const qr_frame_params &fp,

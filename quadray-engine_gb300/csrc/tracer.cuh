@@ -52,4 +52,13 @@ cudaError_t qr_launch_whitted_stats(const qr_dscene &sc, const qr_frame_params &
                                     uint32_t *dev_frame, qr_dstats *dstats,
                                     cudaStream_t stream);
 
+/* path tracer: add fp.pt_on samples per pixel to the running sums acc
+ * (3 floats per pixel, x_row stride; reset when fp.pts_c == 0) and write the
+ * mean over pts_c + pt_on samples into dev_frame */
+cudaError_t qr_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *acc,
+                         uint32_t *dev_frame, cudaStream_t stream);
+cudaError_t qr_launch_pt_stats(const qr_dscene &sc, const qr_frame_params &fp, float *acc,
+                               uint32_t *dev_frame, qr_dstats *dstats,
+                               cudaStream_t stream);
+
 #endif /* QR_TRACER_CUH */

@@ -51,12 +51,17 @@ CASES = {
     "anim_s3_full_aa4_128x72_d4": (2, 3, 64, 128, 72, 2, 1, 0, "full", 4),
     "anim_s1_tarray_160x90_d4":   (2, 1, 64, 160, 90, 0, 1, 8, "full", 4),
     "anim_s1_tarray_none_160x90_d4": (2, 1, 64, 160, 90, 0, 1, 8, "none", 4),
+    # path tracer (kind 3): the reference's running mean after 256 frames of
+    # one sample each (its own random streams); only the last frame is kept
+    "pt_s1_ref256_80x45_d8":      (3, 1, 32, 80, 45, 0, 256, 0, "full", 8, "last"),
+    "pt_s2_ref256_64x36_d8":      (3, 2, 32, 64, 36, 0, 256, 0, "full", 8, "last"),
 }
 
 
 def run_case(name, case):
     kind, seed, nq, w, h, fsaa, frames, flags, opts = case[:9]
     depth = case[9] if len(case) > 9 else 10
+    last_only = len(case) > 10 and case[10] == "last"
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "frame.bin")
         # the frame does not depend on the worker count (rows are independent)
@@ -68,6 +73,10 @@ def run_case(name, case):
         data = np.fromfile(out, dtype="<u4").reshape(frames, h, w)
     meta = dict(kind=kind, seed=seed, nq=nq, w=w, h=h, fsaa=fsaa,
                 frames=frames, flags=flags, opts=opts, depth=depth)
+    if last_only:
+        data = data[-1:]
+        meta["samples"] = frames
+        meta["frames"] = 1
     np.savez_compressed(os.path.join(HERE, name + ".npz"), frames=data,
                         meta=json.dumps(meta))
     return data

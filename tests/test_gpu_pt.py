@@ -1,0 +1,156 @@
+"""Path tracer on the GPU (the reference's RT_FEAT_PT estimator), through the
+C ABI.
+
+* Bit for bit against the float oracle (oracle/qr_oracle.c qr_oracle_pt):
+  the same PCG32 streams drawn in the same order, the same fp32 arithmetic,
+  over two accumulating launches.
+* Against the FP64 oracle (the same source in double, the same streams):
+  per-pixel means clamped to [0, 1] within RMSE 0.05 at 64 samples a pixel
+  and below 15% of the RMSE between two independent FP64 renders; mean bias
+  below 0.002.
+* Against the reference's own CPU path tracer (tests/golden, 256 samples a
+  pixel, its own LCG streams): statistically the same image.
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+import pytest
+
+from conftest import channels
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def ctx(qr):
+    c = qr.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def oracle64():
+    import build as oracle_build
+    return oracle_build.load_oracle(fp64=True)
+
+
+def pt_scene(qr, seed, w, h, depth=8, nq=32):
+    g = qr.GenScene(qr.SCN_PT, seed, nq, 0)
+    f = qr.Flat(g, w, h, 0)
+    desc, params = f.update(0, depth)
+    return g, f, desc, params
+
+
+def oracle_pt(O, desc, params, acc, frame=None):
+    nt = min(8, os.cpu_count() or 1)
+    bands = np.linspace(0, params.y_res, nt + 1).astype(int)
+    fr = frame.ctypes.data if frame is not None else None
+    th = [threading.Thread(target=O.qr_oracle_pt, args=(
+        ctypes.addressof(desc), ctypes.addressof(params), acc.ctypes.data, fr,
+        int(bands[i]), int(bands[i + 1]), None)) for i in range(nt)]
+    [t.start() for t in th]
+    [t.join() for t in th]
+
+
+def gpu_means(qr, ctx, sid, params):
+    import torch
+    acc = torch.zeros((params.y_res, params.x_row, 3), dtype=torch.float32, device="cuda")
+    frame = torch.zeros((params.y_res, params.x_row), dtype=torch.int32, device="cuda")
+    ctx.render_pt(sid, params, acc.data_ptr(), frame.data_ptr(),
+                  torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return acc.cpu().numpy()[:, :params.x_res] / params.pt_on
+
+
+@pytest.mark.parametrize("seed", [1, 3])
+def test_pt_bit_exact_vs_float_oracle(qr, oracle, ctx, seed):
+    g, f, desc, params = pt_scene(qr, seed, 96, 54)
+    sid = ctx.upload(desc)
+    acc = np.zeros((params.y_res, params.x_row, 3), dtype=np.float32)
+    for launch in range(2):
+        p = qr.QrFrameParams.from_buffer_copy(params)
+        p.pt_on, p.pts_c, p.seed, p.frame_idx = 8, 8.0 * launch, 4242, launch
+        gpu = ctx.render_host(sid, p)
+        ref = np.zeros((p.y_res, p.x_row), dtype=np.uint32)
+        oracle_pt(oracle, desc, p, acc, ref)
+        assert (gpu != ref[:, :p.x_res]).sum() == 0, launch
+
+
+def test_pt_bvh_equals_linear_walk(qr, ctx):
+    g, f, desc, params = pt_scene(qr, 5, 128, 72)
+    sid = ctx.upload(desc)
+    p = qr.QrFrameParams.from_buffer_copy(params)
+    p.pt_on, p.pts_c, p.seed, p.frame_idx = 16, 0.0, 7, 0
+    a = ctx.render_host(sid, p).copy()
+    p.flags = qr.FP_LINEAR_WALK
+    b = ctx.render_host(sid, p)
+    assert (a != b).sum() == 0
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_pt_vs_fp64_oracle(qr, ctx, oracle64, seed):
+    g, f, desc, params = pt_scene(qr, seed, 96, 54)
+    sid = ctx.upload(desc)
+    p = qr.QrFrameParams.from_buffer_copy(params)
+    p.pt_on, p.pts_c, p.seed, p.frame_idx = 64, 0.0, 99, 0
+    gm = np.minimum(gpu_means(qr, ctx, sid, p), 1.0)
+    acc = np.zeros((p.y_res, p.x_row, 3), dtype=np.float64)
+    oracle_pt(oracle64, desc, p, acc)
+    om = np.minimum(acc[:, :p.x_res] / p.pt_on, 1.0)
+    p2 = qr.QrFrameParams.from_buffer_copy(p)
+    p2.seed = 100
+    acc2 = np.zeros_like(acc)
+    oracle_pt(oracle64, desc, p2, acc2)
+    om2 = np.minimum(acc2[:, :p.x_res] / p.pt_on, 1.0)
+    rmse = float(np.sqrt(((gm - om) ** 2).mean()))
+    noise = float(np.sqrt(((om - om2) ** 2).mean()))
+    bias = float((gm - om).mean())
+    assert rmse < 0.05, rmse
+    assert rmse < 0.15 * noise, (rmse, noise)
+    assert abs(bias) < 0.002, bias
+
+
+def test_pt_vs_reference_path_tracer(qr, ctx):
+    from test_oracle_golden import load_golden, pt_agreement
+    frames, meta = load_golden(os.path.join(GOLDEN, "pt_s1_ref256_80x45_d8.npz"))
+    g, f, desc, params = pt_scene(qr, meta["seed"], meta["w"], meta["h"], meta["depth"])
+    sid = ctx.upload(desc)
+    out = []
+    for sd in (21, 22):
+        p = qr.QrFrameParams.from_buffer_copy(params)
+        p.pt_on, p.pts_c, p.seed, p.frame_idx = meta["samples"], 0.0, sd, 0
+        out.append(ctx.render_host(sid, p).copy())
+    ratio, z = pt_agreement(out[0], out[1], frames[0])
+    assert ratio < 1.35, ratio
+    assert z < 4.0, z
+
+
+def test_engine_pt_accumulates_over_renders(qr, oracle):
+    """rt_Scene with set_pton(4): each render adds 4 samples a pixel to the
+    running mean (launch index = stream index), as two oracle launches do."""
+    g = qr.GenScene(qr.SCN_PT, 2, 32, 0)
+    eng = qr.Engine(g, 80, 45, depth=8, pton=4)
+    assert eng.pton == 4
+    a = eng.render(0).copy()
+    b = eng.render(16).copy()
+    eng.close()
+    g2, f, desc, params = pt_scene(qr, 2, 80, 45)
+    acc = np.zeros((params.y_res, params.x_row, 3), dtype=np.float32)
+    for launch, img in enumerate((a, b)):
+        p = qr.QrFrameParams.from_buffer_copy(params)
+        p.pt_on, p.pts_c, p.seed, p.frame_idx = 4, 4.0 * launch, 0x5A17F00D, launch
+        ref = np.zeros((p.y_res, p.x_row), dtype=np.uint32)
+        oracle_pt(oracle, desc, p, acc, ref)
+        assert (img != ref[:, :p.x_res]).sum() == 0, launch
+
+
+def test_engine_pt_refused_when_prohibited(qr):
+    """Scenes that keep RT_OPTS_PT in their options cannot path trace."""
+    g = qr.GenScene(qr.SCN_PLAIN, 1, 16, 0)
+    eng = qr.Engine(g, 32, 24)
+    assert eng.set_pton(4) == 0
+    eng.close()

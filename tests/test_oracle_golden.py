@@ -77,6 +77,7 @@ def check_against_golden(img, ref, meta):
 
 
 CULLED = {"anim_s1_tarray_160x90_d4"}
+PT = set(os.path.basename(p)[:-4] for p in FIXTURES if os.path.basename(p).startswith("pt_"))
 
 
 def _id(p):
@@ -84,11 +85,13 @@ def _id(p):
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) >= 18
+    assert len(FIXTURES) >= 20
 
 
-@pytest.mark.parametrize("path", [p for p in FIXTURES if _id(p) not in CULLED],
-                         ids=[_id(p) for p in FIXTURES if _id(p) not in CULLED])
+EXACT = [p for p in FIXTURES if _id(p) not in CULLED and _id(p) not in PT]
+
+
+@pytest.mark.parametrize("path", EXACT, ids=[_id(p) for p in EXACT])
 def test_oracle_matches_reference(qr, oracle, path):
     frames, meta = load_golden(path)
     for k, (desc, params) in enumerate(frames_of(qr, meta)):
@@ -136,3 +139,64 @@ def test_planted_error_is_caught(qr, oracle):
     img[::4, :] ^= 2                   # 25% of hit IDs moved to the other side
     with pytest.raises(AssertionError):
         check_against_golden(img, frames[0], meta)
+
+
+# ---- path tracer: same estimator as the reference, different random streams
+
+def pt_frames(qr, oracle, meta, seeds, spp):
+    """oracle path-traced frames (XRGB) of a fixture's scene, one per seed,
+    rendered by row bands on all cores"""
+    import ctypes
+    import threading
+    g = qr.GenScene(meta["kind"], meta["seed"], meta["nq"], meta["flags"])
+    f = qr.Flat(g, meta["w"], meta["h"], 0)
+    desc, params = f.update(0, meta["depth"])
+    out = []
+    for sd in seeds:
+        p = qr.QrFrameParams.from_buffer_copy(params)
+        p.pt_on, p.pts_c, p.seed, p.frame_idx = spp, 0.0, sd, 0
+        acc = np.zeros((p.y_res, p.x_row, 3), dtype=np.float32)
+        fr = np.zeros((p.y_res, p.x_row), dtype=np.uint32)
+        nt = min(8, os.cpu_count() or 1)
+        bands = np.linspace(0, p.y_res, nt + 1).astype(int)
+        th = [threading.Thread(target=oracle.qr_oracle_pt, args=(
+            ctypes.addressof(desc), ctypes.addressof(p), acc.ctypes.data, fr.ctypes.data,
+            int(bands[i]), int(bands[i + 1]), None)) for i in range(nt)]
+        [t.start() for t in th]
+        [t.join() for t in th]
+        out.append(fr[:, :p.x_res].copy())
+    return out
+
+
+def pt_agreement(a, b, ref):
+    """mean squared error of a against ref, over that of a against b (an
+    independent frame of the same estimator: the noise); and the difference
+    of mean brightness in units of its standard error"""
+    A, B, R = (channels(x).astype(np.float64) / 255.0 for x in (a, b, ref))
+    noise = np.mean((A - B) ** 2)
+    ratio = np.mean((A - R) ** 2) / noise
+    se = np.sqrt(noise / A.size)
+    return ratio, abs(A.mean() - R.mean()) / se
+
+
+def test_pt_oracle_agrees_with_reference_path_tracer(qr, oracle):
+    """The oracle's path tracer and the reference's (tests/golden, 256
+    samples a pixel, its own LCG streams) converge to the same image: their
+    distance matches the distance between two independent oracle frames
+    (ratio 1 up to sampling error), and mean brightness agrees."""
+    frames, meta = load_golden(os.path.join(GOLDEN, "pt_s2_ref256_64x36_d8.npz"))
+    a, b = pt_frames(qr, oracle, meta, [11, 12], meta["samples"])
+    ratio, z = pt_agreement(a, b, frames[0])
+    assert ratio < 1.35, ratio
+    assert z < 4.0, z
+
+
+def test_pt_agreement_catches_a_biased_estimator(qr, oracle):
+    """The same check fails for an image 10% too bright (planted on the CPU)."""
+    frames, meta = load_golden(os.path.join(GOLDEN, "pt_s2_ref256_64x36_d8.npz"))
+    a, b = pt_frames(qr, oracle, meta, [11, 12], meta["samples"])
+    c = channels(a).astype(np.float64)
+    c = np.minimum(np.rint(c * 1.1), 255).astype(np.uint32)
+    biased = (c[..., 0] << 16) | (c[..., 1] << 8) | c[..., 2]
+    ratio, z = pt_agreement(biased, b, frames[0])
+    assert ratio > 1.35 or z > 4.0
