@@ -130,10 +130,8 @@ def test_anim_full_size_frame_properties(qr, ctx):
 # ---- the reference's own frames (tests/golden), through the GPU
 
 def test_gpu_matches_reference_goldens(qr, ctx):
-    from test_oracle_golden import FIXTURES, CULLED, _id, load_golden, check_against_golden
-    for path in FIXTURES:
-        if _id(path) in CULLED:
-            continue
+    from test_oracle_golden import EXACT, load_golden, check_against_golden
+    for path in EXACT:
         frames, meta = load_golden(path)
         g = qr.GenScene(meta["kind"], meta["seed"], meta["nq"], meta["flags"])
         opts = qr.OPTS_NONE if meta["opts"] == "none" else qr.OPTS_DEFAULT
