@@ -201,6 +201,19 @@ int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
  * pixel (x_row stride) and is overwritten when fp->pts_c == 0 */
 int qr_render_pt(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                  float *dev_acc, uint32_t *dev_frame, void *stream);
+/* path tracer without any device allocation.  This entry point has no
+ * counterpart in the reference: it is qr_render_pt with its running sums in
+ * a fixed array inside the library (QR_NOALLOC_MAX_PX pixels of 3 floats,
+ * x_row * y_res may not exceed it: QR_ERR_LIMIT).  The first call on a
+ * device looks the array up (cudaGetSymbolAddress) and should come before
+ * any stream capture.  A call with pts_c == 0 starts the sums for its frame
+ * size, later calls of that size add to them (QR_ERR_STATE if none were
+ * started); nothing has to be cleared first.  The array is shared by every
+ * context and scene on a device: overlapping calls race on it. */
+#define QR_NOALLOC_MAX_PX   (1 << 20)
+int qr_render_pt_noalloc(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
+                         uint32_t *dev_frame, void *stream);
+
 /* render one frame into host memory: copies in, renders, copies out, syncs */
 int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                    uint32_t *host_frame);

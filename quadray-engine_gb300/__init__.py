@@ -106,6 +106,7 @@ def lib():
         L.qr_render_device.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp, vp]
         L.qr_render_host.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp]
         L.qr_render_pt.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp, vp, vp]
+        L.qr_render_pt_noalloc.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp, vp]
         L.qr_sync.argtypes = [vp, vp]
         L.qr_render_stats.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp,
                                       ctypes.POINTER(ctypes.c_uint64)]

@@ -445,3 +445,29 @@ extern "C" int qr_sync(qr_ctx *ctx, void *stream)
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "sync", e);
     return QR_OK;
 }
+
+/* ---- internal accessors for other translation units of the library ---- */
+
+int qr_internal_scene(qr_ctx *ctx, int scene_id, const qr_dscene **sc, int *device)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    *sc = &sl->d;
+    *device = ctx->device;
+    return QR_OK;
+}
+
+int qr_internal_check_fp(const qr_frame_params *fp)
+{
+    return check_fp(fp);
+}
+
+int qr_internal_fail(qr_ctx *ctx, int code, const char *what, cudaError_t e)
+{
+    return fail(ctx, code, what, e);
+}
+
+void qr_internal_message(qr_ctx *ctx, const char *msg)
+{
+    if (ctx != NULL) snprintf(ctx->err, sizeof(ctx->err), "%s", msg);
+}
