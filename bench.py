@@ -321,10 +321,18 @@ def main():
     d2h = wl["w"] * wl["h"] * 4
     eng.close()
 
+    # FP32 issue rate: the bit-exact arithmetic issues no fused multiply-add,
+    # so one FP32 operation per lane and clock (152 SMs x 128 lanes); the
+    # clock is the median sampled during the timed region
     pk, pk_kind = peaks()
-    sm_mhz = pk.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12   # TFLOP/s, FMA = 2
+    sm_mhz = ck.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * sm_mhz * 1e6 / 1e12   # TFLOP/s
     achieved = flops * args.steps / t_total / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh).get(args.workload, {}).get("bytes_per_launch")
     line = {
         "metric": "rays_per_s", "value": value, "unit": "rays/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -346,8 +354,10 @@ def main():
                 "frame_ms_p50": 1000.0 * float(np.percentile(lat, 50)),
                 "frame_ms_p99": 1000.0 * float(np.percentile(lat, 99))},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
-                     "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x max clock)",
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
+                     "peak_source": "nominal FP32 issue rate, no FMA (152 SMs x 128 "
+                                    "lanes x sampled SM clock); MEASURED_PEAKS.json "
+                                    "has no FP32 figure",
                      "flops_per_frame": flops},
         "work_per_frame": dict((k, v / nstat) for k, v in stats.items()),
         "gpu_launches": args.steps,
