@@ -56,7 +56,145 @@ WORKLOADS = {
     # after 3 bounces), 32 quadrics in a closed box of 5 planes, light
     # cluster with an emitting sphere
     "pt": dict(kind=3, seed=1, nq=32, w=1280, h=720, fsaa=0, depth=8, anim=False, pt=64),
+    # batched persistent launch: 256 requests (seeds 1000..1255), 8-512
+    # quadrics (log-uniform), 320x240 / 640x480 / 1280x720 / 1920x1080,
+    # Whitted depth 1-6 (plain scene) or path tracer 4-32 samples (box scene)
+    "batch": dict(kind=0, seed=1000, nq=0, w=0, h=0, fsaa=0, depth=0, anim=False,
+                  batch=256),
 }
+
+RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
+
+
+def batch_requests(n, seed0):
+    """the seeded request mix of the batched workload"""
+    rng = np.random.default_rng(seed0)
+    out = []
+    for i in range(n):
+        nq = int(round(math.exp(rng.uniform(math.log(8), math.log(512)))))
+        w, h = RESOLUTIONS[int(rng.integers(0, 4))]
+        if rng.uniform() < 0.5:
+            out.append(dict(kind=1, seed=seed0 + i, nq=nq, w=w, h=h,
+                            depth=int(rng.integers(1, 7)), spp=0))
+        else:
+            out.append(dict(kind=3, seed=seed0 + i, nq=nq, w=w, h=h, depth=8,
+                            spp=int(rng.integers(4, 33))))
+    return out
+
+
+def run_batch(args, wl, rank, world, dist, local):
+    import torch
+    qr = importlib.import_module("quadray-engine_gb300")
+    ctx = qr.Context(local)
+    spec = batch_requests(wl["batch"], wl["seed"])
+    keep, reqs, bufs = [], [], []
+    rays = 0
+    for i, rq in enumerate(spec):
+        g = qr.GenScene(rq["kind"], rq["seed"], rq["nq"], 0)
+        f = qr.Flat(g, rq["w"], rq["h"], 0)
+        desc, params = f.update(0, rq["depth"])
+        sid = ctx.upload(desc)
+        r = qr.QrRequest()
+        r.scene_id = sid
+        r.fp = params
+        r.fp.pt_on, r.fp.pts_c, r.fp.seed, r.fp.frame_idx = rq["spp"], 0.0, rq["seed"], 0
+        fr = torch.empty((rq["h"], params.x_row), dtype=torch.int32, device="cuda")
+        acc = (torch.empty((rq["h"], params.x_row, 3), dtype=torch.float32, device="cuda")
+               if rq["spp"] else None)
+        r.dev_frame = fr.data_ptr()
+        r.dev_acc = acc.data_ptr() if acc is not None else None
+        keep.append((g, f))
+        bufs.append((fr, acc))
+        reqs.append(r)
+        counts = (ctypes.c_uint64 * 13)()
+        host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+        rc = qr.lib().qr_render_stats(ctx.h, sid, ctypes.byref(r.fp),
+                                      host.ctypes.data_as(ctypes.c_void_p), counts)
+        assert rc == 0, ctx.error()
+        rays += int(counts[0]) + int(counts[1]) + int(counts[2])
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    # the per-frame path: one launch per request, in order
+    def per_frame():
+        for r, (fr, acc) in zip(reqs, bufs):
+            if r.fp.pt_on:
+                ctx.render_pt(r.scene_id, r.fp, acc.data_ptr(), fr.data_ptr(), sp)
+            else:
+                ctx.render_device(r.scene_id, r.fp, fr.data_ptr(), sp)
+    per_frame()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    per_frame()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_frames = e0.elapsed_time(e1) / 1000.0
+
+    b = qr.Batch(ctx, len(reqs))
+    b.set(reqs[:32])                # the autotuner times a 32-request sample
+    tw, grab, tune_ms = b.tune()
+    b.set(reqs)
+    for _ in range(args.warmup):
+        b.launch(sp)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        b.launch(sp)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = [a.elapsed_time(c) for a, c in ev]
+    value, t_total = whole_job(rays, args.steps, sum(ms) / 1000.0, dist, "cuda")
+
+    # end to end: request table in, batch, every frame out to pinned memory
+    hosts = [torch.empty(fr.shape, dtype=torch.int32, pin_memory=True) for fr, _ in bufs]
+    d2h = sum(h.numel() * 4 for h in hosts)
+    h2d = ctypes.sizeof(qr.QrRequest) * len(reqs)
+    lat = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        b.set(reqs)
+        b.launch(sp)
+        for (fr, _), hb in zip(bufs, hosts):
+            hb.copy_(fr, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            lat.append(time.perf_counter() - t0)
+    b.close()
+    npx = sum(rq["w"] * rq["h"] for rq in spec)
+    line = {
+        "metric": "rays_per_s", "value": value, "unit": "rays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * t_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch", "requests": len(reqs),
+                   "whitted": sum(1 for q in spec if not q["spp"]),
+                   "path_traced": sum(1 for q in spec if q["spp"]),
+                   "pixels": npx, "rays_per_batch": rays, "seeds": [wl["seed"], wl["seed"] + len(reqs) - 1],
+                   "tile": [tw, 32 // tw], "tiles_per_claim": grab,
+                   "l2": "inputs (scenes, frames, sums) far larger than L2",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "per_frame_path": {"value": rays / t_frames, "unit": "rays/s",
+                           "ms": 1000.0 * t_frames, "launches": len(reqs)},
+        "batch_over_per_frame": (rays / (t_total / args.steps)) / (rays / t_frames),
+        "e2e": {"value": rays * len(lat) / sum(lat), "unit": "rays/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_p50": 1000.0 * float(np.percentile(lat, 50))},
+        "gpu_launches": 2 * args.steps,
+        "clocks": ck,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+
 
 
 def whole_job(units_per_step, steps, t_local, dist=None, device="cpu"):
@@ -240,6 +378,12 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+
+    if wl.get("batch"):
+        run_batch(args, wl, rank, world, dist, local)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
 
     qr = importlib.import_module("quadray-engine_gb300")
     gen = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)

@@ -43,6 +43,7 @@ extern "C" {
 #define QR_ERR_STATE        5   /* call out of order (e.g. render w/o scene) */
 #define QR_ERR_NOSCENE      6   /* unknown scene id */
 #define QR_ERR_LIMIT        7   /* request exceeds a compiled-in limit */
+#define QR_ERR_BUSY         8   /* launched work still running (poll) */
 
 /* ---- material / context property bits (tracer.h:66-77) ----------------- */
 #define QR_PROP_LIGHT       0x00000010
@@ -240,6 +241,43 @@ int qr_sync(qr_ctx *ctx, void *stream);
 #define QR_STAT_COUNT           13
 int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                     uint32_t *host_frame, uint64_t *counts);
+
+/*
+ * Batched rendering: many frame requests on resident scenes of one context,
+ * Whitted or path-traced (fp.pt_on > 0), of any sizes, rendered by one
+ * persistent launch per mode over all their pixel tiles, captured in a CUDA
+ * graph.  The reference renders one frame per rt_Scene::render call
+ * (core/engine/engine.cpp:3014) with a CPU thread pool; it has no batch.
+ * Each frame is the same as the frame of qr_render_device / qr_render_pt for
+ * the same request.
+ */
+typedef struct qr_request
+{
+    int32_t         scene_id;
+    int32_t         pad;
+    qr_frame_params fp;             /* frame size, camera, depth, pt_on ... */
+    uint32_t       *dev_frame;      /* output, x_row stride */
+    float          *dev_acc;        /* path tracer: running sums (3 floats a
+                                       pixel), NULL for Whitted frames */
+} qr_request;
+
+typedef struct qr_batch qr_batch;
+
+int qr_batch_create(qr_ctx *ctx, int max_requests, qr_batch **out);
+int qr_batch_destroy(qr_batch *b);
+/* replace the batch's requests (validated; scenes must stay resident) */
+int qr_batch_set(qr_batch *b, const qr_request *reqs, int n);
+/* tile width (4, 8, 16 or 32; tiles are 32 pixels) and tiles a warp claims
+ * at once (1-64) */
+int qr_batch_config(qr_batch *b, int tile_w, int grab);
+/* time every tile configuration on the batch and keep the fastest;
+ * tile_w, grab and ms (optional) receive the choice and its time */
+int qr_batch_tune(qr_batch *b, int *tile_w, int *grab, float *ms);
+/* render every request on `stream` (asynchronous) */
+int qr_batch_launch(qr_batch *b, void *stream);
+/* QR_OK once the last launch finished, QR_ERR_BUSY while it runs */
+int qr_batch_poll(qr_batch *b);
+int qr_batch_wait(qr_batch *b);
 
 #ifdef __cplusplus
 }

@@ -64,6 +64,17 @@ class QrFrameParams(ctypes.Structure):
     ]
 
 
+class QrRequest(ctypes.Structure):
+    """qr_request of include/qr_gpu.h (one frame of a batch)."""
+    _fields_ = [
+        ("scene_id", ctypes.c_int32), ("pad", ctypes.c_int32),
+        ("fp", QrFrameParams),
+        ("dev_frame", ctypes.c_void_p), ("dev_acc", ctypes.c_void_p),
+    ]
+
+
+QR_ERR_BUSY = 8
+
 _lib = None
 
 
@@ -107,6 +118,15 @@ def lib():
         L.qr_render_host.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp]
         L.qr_render_pt.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp, vp, vp]
         L.qr_render_pt_noalloc.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp, vp]
+        L.qr_batch_create.argtypes = [vp, i32, ctypes.POINTER(vp)]
+        L.qr_batch_destroy.argtypes = [vp]
+        L.qr_batch_set.argtypes = [vp, ctypes.POINTER(QrRequest), i32]
+        L.qr_batch_config.argtypes = [vp, i32, i32]
+        L.qr_batch_tune.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                    ctypes.POINTER(ctypes.c_float)]
+        L.qr_batch_launch.argtypes = [vp, vp]
+        L.qr_batch_poll.argtypes = [vp]
+        L.qr_batch_wait.argtypes = [vp]
         L.qr_sync.argtypes = [vp, vp]
         L.qr_render_stats.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp,
                                       ctypes.POINTER(ctypes.c_uint64)]
@@ -224,6 +244,52 @@ class Context:
     def close(self):
         if self.h:
             lib().qr_ctx_destroy(self.h)
+            self.h = None
+
+
+class Batch:
+    """Batched persistent rendering of many requests (qr_batch_*)."""
+
+    def __init__(self, ctx, max_requests):
+        self.ctx = ctx
+        p = ctypes.c_void_p()
+        rc = lib().qr_batch_create(ctx.h, max_requests, ctypes.byref(p))
+        if rc != QR_OK:
+            raise RuntimeError("qr_batch_create: %d %s" % (rc, ctx.error()))
+        self.h = p
+
+    def _check(self, rc, what):
+        if rc != QR_OK:
+            raise RuntimeError("%s: %d %s" % (what, rc, self.ctx.error()))
+
+    def set(self, requests):
+        arr = (QrRequest * len(requests))(*requests)
+        self._check(lib().qr_batch_set(self.h, arr, len(requests)), "qr_batch_set")
+
+    def config(self, tile_w, grab):
+        self._check(lib().qr_batch_config(self.h, tile_w, grab), "qr_batch_config")
+
+    def tune(self):
+        tw, gr, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        self._check(lib().qr_batch_tune(self.h, ctypes.byref(tw), ctypes.byref(gr),
+                                        ctypes.byref(ms)), "qr_batch_tune")
+        return tw.value, gr.value, ms.value
+
+    def launch(self, stream=0):
+        self._check(lib().qr_batch_launch(self.h, ctypes.c_void_p(stream)), "qr_batch_launch")
+
+    def poll(self):
+        rc = lib().qr_batch_poll(self.h)
+        if rc not in (QR_OK, QR_ERR_BUSY):
+            self._check(rc, "qr_batch_poll")
+        return rc == QR_OK
+
+    def wait(self):
+        self._check(lib().qr_batch_wait(self.h), "qr_batch_wait")
+
+    def close(self):
+        if self.h:
+            lib().qr_batch_destroy(self.h)
             self.h = None
 
 

@@ -1,0 +1,294 @@
+/*
+ * batch.cu: batched persistent rendering of many frame requests (qr_batch_*
+ * of include/qr_gpu.h).
+ *
+ * A batch holds up to max_requests requests on resident scenes of one
+ * context, Whitted or path-traced, of any size.  Each request is cut into
+ * warp tiles; one persistent kernel per mode walks the tiles of all its
+ * requests (tracer.cu batch_kernel), the path-tracer kernel on a second
+ * stream so the two overlap in each other's tail.  The counter reset and the
+ * two launches are captured once into a CUDA graph and replayed by every
+ * launch until the requests or the tile configuration change.  The tile
+ * shape and the tiles a warp claims at once come from qr_batch_tune, which
+ * times each configuration on the batch itself and keeps the fastest.
+ */
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+#include <new>
+#include <vector>
+
+#include "qr_gpu.h"
+#include "tracer.cuh"
+
+int qr_internal_scene(qr_ctx *ctx, int scene_id, const qr_dscene **sc, int *device);
+int qr_internal_check_fp(const qr_frame_params *fp);
+int qr_internal_device(qr_ctx *ctx);
+int qr_internal_fail(qr_ctx *ctx, int code, const char *what, cudaError_t e);
+void qr_internal_message(qr_ctx *ctx, const char *msg);
+
+struct qr_batch
+{
+    qr_ctx      *ctx;
+    int          device;
+    int          max;
+    qr_job      *djobs;         /* Whitted jobs, then path-tracer jobs */
+    int         *dcount;        /* claim counters of the two kernels */
+    std::vector<qr_request> reqs;
+    int          nw, np;        /* jobs per mode */
+    int          tiles[2];      /* tiles per mode */
+    int          tw, th, grab;
+    int          blocks[2];
+    cudaStream_t main, side;
+    cudaEvent_t  fork, join, done;
+    cudaGraphExec_t exec;
+    int          graph_ok;
+    int          launched;
+};
+
+static int bfail(qr_batch *b, int code, const char *what, cudaError_t e)
+{
+    return qr_internal_fail(b->ctx, code, what, e);
+}
+
+extern "C" int qr_batch_create(qr_ctx *ctx, int max_requests, qr_batch **out)
+{
+    if (ctx == NULL || out == NULL || max_requests <= 0 || max_requests > (1 << 20))
+        return QR_ERR_ARG;
+    *out = NULL;
+    qr_batch *b = new (std::nothrow) qr_batch();
+    if (b == NULL) return QR_ERR_OOM;
+    b->ctx = ctx;
+    b->max = max_requests;
+    b->tw = 8;
+    b->th = 4;
+    b->grab = 1;
+    b->device = qr_internal_device(ctx);
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e == cudaSuccess) e = cudaMalloc(&b->djobs, sizeof(qr_job) * (size_t)max_requests);
+    if (e == cudaSuccess) e = cudaMalloc(&b->dcount, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    if (e != cudaSuccess)
+    {
+        int rc = qr_internal_fail(ctx, QR_ERR_CUDA, "batch create", e);
+        qr_batch_destroy(b);
+        return rc;
+    }
+    for (int m = 0; m < 2; m++)
+    {
+        int per = qr_batch_blocks_per_sm(m);
+        b->blocks[m] = sms * (per > 0 ? per : 1);
+    }
+    *out = b;
+    return QR_OK;
+}
+
+extern "C" int qr_batch_destroy(qr_batch *b)
+{
+    if (b == NULL) return QR_ERR_ARG;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->djobs) cudaFree(b->djobs);
+    if (b->dcount) cudaFree(b->dcount);
+    if (b->main) cudaStreamDestroy(b->main);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    if (b->done) cudaEventDestroy(b->done);
+    delete b;
+    return QR_OK;
+}
+
+/* job table of the current requests and tile configuration */
+static int upload_jobs(qr_batch *b)
+{
+    std::vector<qr_job> jobs;
+    jobs.reserve(b->reqs.size());
+    for (int pass = 0; pass < 2; pass++)
+    {
+        int tile = 0;
+        for (size_t i = 0; i < b->reqs.size(); i++)
+        {
+            const qr_request &r = b->reqs[i];
+            const int pt = r.fp.pt_on > 0;
+            if (pt != pass) continue;
+            const qr_dscene *sc = NULL;
+            int dev = 0;
+            if (qr_internal_scene(b->ctx, r.scene_id, &sc, &dev) != QR_OK) return QR_ERR_NOSCENE;
+            qr_job j;
+            memset(&j, 0, sizeof(j));
+            j.S = *sc;
+            j.P = r.fp;
+            j.frame = r.dev_frame;
+            j.acc = r.dev_acc;
+            j.tiles_x = (r.fp.x_res + b->tw - 1) / b->tw;
+            const int ty = (r.fp.y_res + b->th - 1) / b->th;
+            j.tile0 = tile;
+            tile += j.tiles_x * ty;
+            jobs.push_back(j);
+        }
+        b->tiles[pass] = tile;
+        if (pass == 0) b->nw = (int)jobs.size();
+        else b->np = (int)jobs.size() - b->nw;
+    }
+    if (!jobs.empty())
+    {
+        cudaError_t e = cudaMemcpy(b->djobs, jobs.data(), sizeof(qr_job) * jobs.size(),
+                                   cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch job upload", e);
+    }
+    if (b->exec)
+    {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = NULL;
+    }
+    b->graph_ok = 0;
+    return QR_OK;
+}
+
+extern "C" int qr_batch_set(qr_batch *b, const qr_request *reqs, int n)
+{
+    if (b == NULL || (n > 0 && reqs == NULL) || n < 0) return QR_ERR_ARG;
+    if (n > b->max) return QR_ERR_LIMIT;
+    for (int i = 0; i < n; i++)
+    {
+        const qr_dscene *sc;
+        int dev;
+        int rc = qr_internal_scene(b->ctx, reqs[i].scene_id, &sc, &dev);
+        if (rc != QR_OK) return rc;
+        rc = qr_internal_check_fp(&reqs[i].fp);
+        if (rc != QR_OK) return rc;
+        if (reqs[i].dev_frame == NULL) return QR_ERR_ARG;
+        if (reqs[i].fp.pt_on > 0 && reqs[i].dev_acc == NULL) return QR_ERR_ARG;
+    }
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "cudaSetDevice", e);
+    b->reqs.assign(reqs, reqs + n);
+    return upload_jobs(b);
+}
+
+extern "C" int qr_batch_config(qr_batch *b, int tile_w, int grab)
+{
+    if (b == NULL) return QR_ERR_ARG;
+    if (tile_w != 4 && tile_w != 8 && tile_w != 16 && tile_w != 32) return QR_ERR_ARG;
+    if (grab < 1 || grab > 64) return QR_ERR_ARG;
+    b->tw = tile_w;
+    b->th = 32 / tile_w;
+    b->grab = grab;
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "cudaSetDevice", e);
+    return upload_jobs(b);
+}
+
+/* the two persistent launches on b->main (and b->side) */
+static cudaError_t enqueue(qr_batch *b)
+{
+    cudaError_t e = cudaMemsetAsync(b->dcount, 0, 2 * sizeof(int), b->main);
+    if (e == cudaSuccess) e = cudaEventRecord(b->fork, b->main);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork, 0);
+    if (e == cudaSuccess)
+        e = qr_launch_batch(0, b->djobs, b->nw, b->tiles[0], b->dcount, b->tw, b->th,
+                            b->grab, b->blocks[0], b->main);
+    if (e == cudaSuccess)
+        e = qr_launch_batch(1, b->djobs + b->nw, b->np, b->tiles[1], b->dcount + 1,
+                            b->tw, b->th, b->grab, b->blocks[1], b->side);
+    if (e == cudaSuccess) e = cudaEventRecord(b->join, b->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->main, b->join, 0);
+    return e;
+}
+
+extern "C" int qr_batch_launch(qr_batch *b, void *stream)
+{
+    if (b == NULL) return QR_ERR_ARG;
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "cudaSetDevice", e);
+    if (!b->graph_ok)
+    {
+        cudaGraph_t g = NULL;
+        e = cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess)
+        {
+            cudaError_t e2 = enqueue(b);
+            e = cudaStreamEndCapture(b->main, &g);
+            if (e2 != cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch graph capture", e);
+        b->graph_ok = 1;
+    }
+    e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->done, (cudaStream_t)stream);
+    if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch graph launch", e);
+    b->launched = 1;
+    return QR_OK;
+}
+
+extern "C" int qr_batch_poll(qr_batch *b)
+{
+    if (b == NULL) return QR_ERR_ARG;
+    if (!b->launched) return QR_OK;
+    cudaError_t e = cudaEventQuery(b->done);
+    if (e == cudaSuccess) return QR_OK;
+    if (e == cudaErrorNotReady) return QR_ERR_BUSY;
+    return bfail(b, QR_ERR_CUDA, "batch poll", e);
+}
+
+extern "C" int qr_batch_wait(qr_batch *b)
+{
+    if (b == NULL) return QR_ERR_ARG;
+    if (!b->launched) return QR_OK;
+    cudaError_t e = cudaEventSynchronize(b->done);
+    if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch wait", e);
+    return QR_OK;
+}
+
+extern "C" int qr_batch_tune(qr_batch *b, int *tile_w, int *grab, float *ms)
+{
+    if (b == NULL) return QR_ERR_ARG;
+    static const int tws[4] = {8, 16, 32, 4};
+    static const int grabs[2] = {1, 4};
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "cudaSetDevice", e);
+    cudaEvent_t t0, t1;
+    e = cudaEventCreate(&t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&t1);
+    if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "tune events", e);
+    float best = -1.0f;
+    int bw = 8, bg = 1;
+    for (int i = 0; i < 4 && e == cudaSuccess; i++)
+    {
+        for (int j = 0; j < 2 && e == cudaSuccess; j++)
+        {
+            int rc = qr_batch_config(b, tws[i], grabs[j]);
+            if (rc != QR_OK) { cudaEventDestroy(t0); cudaEventDestroy(t1); return rc; }
+            e = enqueue(b);                         /* warm-up */
+            if (e == cudaSuccess) e = cudaEventRecord(t0, b->main);
+            if (e == cudaSuccess) e = enqueue(b);
+            if (e == cudaSuccess) e = cudaEventRecord(t1, b->main);
+            if (e == cudaSuccess) e = cudaEventSynchronize(t1);
+            float t = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, t0, t1);
+            if (e == cudaSuccess && (best < 0.0f || t < best))
+            {
+                best = t;
+                bw = tws[i];
+                bg = grabs[j];
+            }
+        }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch tune", e);
+    int rc = qr_batch_config(b, bw, bg);
+    if (rc != QR_OK) return rc;
+    if (tile_w) *tile_w = bw;
+    if (grab) *grab = bg;
+    if (ms) *ms = best;
+    return QR_OK;
+}

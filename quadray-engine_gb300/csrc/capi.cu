@@ -457,6 +457,11 @@ int qr_internal_scene(qr_ctx *ctx, int scene_id, const qr_dscene **sc, int *devi
     return QR_OK;
 }
 
+int qr_internal_device(qr_ctx *ctx)
+{
+    return ctx->device;
+}
+
 int qr_internal_check_fp(const qr_frame_params *fp)
 {
     return check_fp(fp);

@@ -1418,22 +1418,11 @@ __device__ __forceinline__ uint32_t pack(const qr_frame_params &P, const float c
 #define QR_MIN_BLOCKS 6
 #endif
 
-__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
-whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
-               qr_dstats *gst)
+/* one pixel of a Whitted frame: the camera ray, or the 4 sub-samples of
+ * 4x AA combined in the reference's tree order, then clamp and pack */
+__device__ __forceinline__ void whitted_pixel(const qr_dscene &S, const qr_frame_params &P,
+                                              int x, int y, uint32_t *frame, StP st)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= P.x_res || y >= P.y_res) return;
-#ifdef QR_STATS
-    TCnt cnt;
-    #pragma unroll
-    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
-    StP st = &cnt;
-#else
-    StP st = NULL;
-    (void)gst;
-#endif
     float col[3];
     if (P.fsaa == 2)
     {
@@ -1460,6 +1449,25 @@ whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
         for (int k = 0; k < 3; k++) col[k] = clamp1(col[k]);
     }
     frame[(size_t)y * P.x_row + x] = pack(P, col);
+}
+
+__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
+whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
+               qr_dstats *gst)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.x_res || y >= P.y_res) return;
+#ifdef QR_STATS
+    TCnt cnt;
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
+    StP st = &cnt;
+#else
+    StP st = NULL;
+    (void)gst;
+#endif
+    whitted_pixel(S, P, x, y, frame, st);
 #ifdef QR_STATS
     const unsigned am = __activemask();
     const int leader = __ffs(am) - 1;
@@ -1819,22 +1827,11 @@ __device__ void trace_pt(const qr_dscene &S, const qr_frame_params &P, Ray r,
     for (int k = 0; k < 3; k++) col[k] = ret[k];
 }
 
-__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
-pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *frame,
-          qr_dstats *gst)
+/* one pixel of a path-traced frame: pt_on samples added to the running
+ * sums, the mean clamped and packed */
+__device__ __forceinline__ void pt_pixel(const qr_dscene &S, const qr_frame_params &P,
+                                         int x, int y, float *acc, uint32_t *frame, StP st)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= P.x_res || y >= P.y_res) return;
-#ifdef QR_STATS
-    TCnt cnt;
-    #pragma unroll
-    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
-    StP st = &cnt;
-#else
-    StP st = NULL;
-    (void)gst;
-#endif
     Pcg g;
     pcg_seed(g, P.seed, P.frame_idx, (unsigned long long)y * P.x_res + x);
     const int spp = P.pt_on;
@@ -1879,6 +1876,25 @@ pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *fram
         mean[k] = clamp1(mean[k]);
     }
     frame[(size_t)y * P.x_row + x] = pack(P, mean);
+}
+
+__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
+pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *frame,
+          qr_dstats *gst)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.x_res || y >= P.y_res) return;
+#ifdef QR_STATS
+    TCnt cnt;
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
+    StP st = &cnt;
+#else
+    StP st = NULL;
+    (void)gst;
+#endif
+    pt_pixel(S, P, x, y, acc, frame, st);
 #ifdef QR_STATS
     const unsigned am = __activemask();
     const int leader = __ffs(am) - 1;
@@ -1892,7 +1908,100 @@ pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *fram
 #endif
 }
 
+
+#ifndef QR_STATS
+/*
+ * Batched persistent launch: every request of a batch is cut into warp
+ * tiles of tw x th pixels (tw * th = 32), numbered request after request;
+ * each warp claims `grab` tiles at a time from a global counter until none
+ * are left, staging the request's scene and frame parameters in shared
+ * memory when it moves to another request.  One kernel per mode (Whitted or
+ * path tracer), so each keeps only its own code.
+ */
+template <int MODE>
+__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
+batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter,
+             int tw, int th, int grab)
+{
+    __shared__ qr_dscene sS[4];
+    __shared__ qr_frame_params sP[4];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.y;
+    int cur = -1;
+    #pragma unroll 1
+    for (;;)
+    {
+        int t0 = 0;
+        if (lane == 0) t0 = atomicAdd(counter, grab);
+        t0 = __shfl_sync(0xFFFFFFFFu, t0, 0);
+        if (t0 >= total) break;
+        const int t1 = min(t0 + grab, total);
+        #pragma unroll 1
+        for (int t = t0; t < t1; t++)
+        {
+            /* request of tile t: the last job whose first tile is <= t */
+            int lo = 0, hi = njobs - 1;
+            while (lo < hi)
+            {
+                const int mid = (lo + hi + 1) >> 1;
+                if (__ldg(&jobs[mid].tile0) <= t) lo = mid; else hi = mid - 1;
+            }
+            if (lo != cur)
+            {
+                __syncwarp();
+                const uint32_t *src = (const uint32_t *)&jobs[lo].S;
+                uint32_t *dst = (uint32_t *)&sS[wid];
+                for (int i = lane; i < (int)(sizeof(qr_dscene) / 4); i += 32) dst[i] = __ldg(&src[i]);
+                src = (const uint32_t *)&jobs[lo].P;
+                dst = (uint32_t *)&sP[wid];
+                for (int i = lane; i < (int)(sizeof(qr_frame_params) / 4); i += 32) dst[i] = __ldg(&src[i]);
+                __syncwarp();
+                cur = lo;
+            }
+            const qr_job *__restrict__ J = &jobs[lo];
+            const int local = t - __ldg(&J->tile0);
+            const int tx = __ldg(&J->tiles_x);
+            const int x = (local % tx) * tw + lane % tw;
+            const int y = (local / tx) * th + lane / tw;
+            if (x < sP[wid].x_res && y < sP[wid].y_res)
+            {
+                if (MODE == 0)
+                    whitted_pixel(sS[wid], sP[wid], x, y, J->frame, NULL);
+                else
+                    pt_pixel(sS[wid], sP[wid], x, y, J->acc, J->frame, NULL);
+            }
+        }
+    }
+}
+#endif
+
 } /* namespace QR_NS */
+
+#ifndef QR_STATS
+cudaError_t qr_launch_batch(int mode, const qr_job *jobs, int njobs, int total_tiles,
+                            int *counter, int tw, int th, int grab, int blocks,
+                            cudaStream_t stream)
+{
+    if (njobs <= 0 || total_tiles <= 0) return cudaSuccess;
+    const dim3 block(32, 4);
+    if (mode == 0)
+        QR_NS::batch_kernel<0><<<blocks, block, 0, stream>>>(jobs, njobs, total_tiles,
+                                                            counter, tw, th, grab);
+    else
+        QR_NS::batch_kernel<1><<<blocks, block, 0, stream>>>(jobs, njobs, total_tiles,
+                                                            counter, tw, th, grab);
+    return cudaGetLastError();
+}
+
+int qr_batch_blocks_per_sm(int mode)
+{
+    int n = 0;
+    cudaError_t e = mode == 0
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, QR_NS::batch_kernel<0>, 128, 0)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, QR_NS::batch_kernel<1>, 128, 0);
+    return e == cudaSuccess ? n : 0;
+}
+#endif
 
 #ifdef QR_STATS
 cudaError_t qr_launch_pt_stats(const qr_dscene &sc, const qr_frame_params &fp, float *acc,

@@ -61,4 +61,23 @@ cudaError_t qr_launch_pt_stats(const qr_dscene &sc, const qr_frame_params &fp, f
                                uint32_t *dev_frame, qr_dstats *dstats,
                                cudaStream_t stream);
 
+/* one request of a batched launch: its scene, frame parameters, output
+ * frame (and path-tracer sums) and its first tile in the batch's numbering */
+struct qr_job
+{
+    qr_dscene       S;
+    qr_frame_params P;
+    uint32_t       *frame;
+    float          *acc;
+    int32_t         tile0, tiles_x, pad[2];
+};
+
+/* persistent launch over the tiles of njobs requests of one mode (0
+ * Whitted, 1 path tracer); *counter must hold 0 */
+cudaError_t qr_launch_batch(int mode, const qr_job *jobs, int njobs, int total_tiles,
+                            int *counter, int tw, int th, int grab, int blocks,
+                            cudaStream_t stream);
+/* resident blocks of 128 threads per SM of the batch kernel of a mode */
+int qr_batch_blocks_per_sm(int mode);
+
 #endif /* QR_TRACER_CUH */
