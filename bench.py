@@ -61,9 +61,17 @@ WORKLOADS = {
     # Whitted depth 1-6 (plain scene) or path tracer 4-32 samples (box scene)
     "batch": dict(kind=0, seed=1000, nq=0, w=0, h=0, fsaa=0, depth=0, anim=False,
                   batch=256),
+    "serve": dict(kind=0, seed=2000, nq=0, w=0, h=0, fsaa=0, depth=0, anim=True,
+                  serve=(120, 500, 2000), seconds=10.0),
 }
 
 RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
+
+# served stream: 32 resident scenes (24 animated plain scenes with spinning
+# quadrics, 16-256 quadrics; 8 path-traced box scenes), Poisson arrivals,
+# 640x480 / 1280x720 / 1920x1080, 1-16 samples (Whitted: 1 sample or 4x AA;
+# path tracer: that many samples), HBM budget 120 GB
+SERVE_SIZES = [(640, 480), (1280, 720), (1920, 1080)]
 
 
 def batch_requests(n, seed0):
@@ -80,6 +88,95 @@ def batch_requests(n, seed0):
             out.append(dict(kind=3, seed=seed0 + i, nq=nq, w=w, h=h, depth=8,
                             spp=int(rng.integers(4, 33))))
     return out
+
+
+def run_serve(args, wl, rank, world, dist, local):
+    """served stream: rays/s sustained and latency at each arrival rate"""
+    import torch
+    qr = importlib.import_module("quadray-engine_gb300")
+    serve = importlib.import_module("quadray-engine_gb300.serve")
+    ctx = qr.Context(local)
+    rng = np.random.default_rng(wl["seed"])
+    scenes = []
+    for i in range(32):
+        if i < 24:
+            nq = int(round(math.exp(rng.uniform(math.log(16), math.log(256)))))
+            scenes.append(dict(gen=qr.GenScene(qr.SCN_PLAIN, wl["seed"] + i, nq, qr.GEN_SPIN),
+                               pt=False, depth=10, nq=nq, kind=1))
+        else:
+            nq = int(rng.integers(16, 65))
+            scenes.append(dict(gen=qr.GenScene(qr.SCN_PT, wl["seed"] + i, nq, 0),
+                               pt=True, depth=8, nq=nq, kind=3))
+    # rays per request class from instrumented frames at t = 0
+    rays_of = {}
+
+    def rays(req):
+        sc = scenes[req.scene]
+        fsaa = 0 if (sc["pt"] or req.spp <= 1) else 2
+        key = (req.scene, req.w, req.h, fsaa)
+        if key not in rays_of:
+            g = qr.GenScene(sc["kind"], wl["seed"] + req.scene, sc["nq"],
+                            0 if sc["pt"] else qr.GEN_SPIN)
+            f = qr.Flat(g, req.w, req.h, fsaa)
+            desc, params = f.update(0, sc["depth"])
+            sid = ctx.upload(desc)
+            if sc["pt"]:
+                params.pt_on, params.pts_c = 1, 0.0
+            counts = (ctypes.c_uint64 * 13)()
+            host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+            rc = qr.lib().qr_render_stats(ctx.h, sid, ctypes.byref(params),
+                                          host.ctypes.data_as(ctypes.c_void_p), counts)
+            assert rc == 0, ctx.error()
+            ctx.release(sid)
+            rays_of[key] = int(counts[0]) + int(counts[1]) + int(counts[2])
+        return rays_of[key] * (req.spp if sc["pt"] else 1)
+
+    srv = serve.Server(qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
+                       prep_threads=min(8, os.cpu_count() or 1))
+    # warm-up: every scene once at every size
+    warm = [serve.Request(i, s, 0, w, h, 1, 0.0)
+            for i, (s, (w, h)) in enumerate((s, sz) for s in range(32) for sz in SERVE_SIZES)]
+    srv.run(warm)
+    results = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    for rate in wl["serve"]:
+        reqs = serve.poisson_requests(32, rate, wl["seconds"], SERVE_SIZES, 16,
+                                      wl["seed"] + int(rate))
+        total = sum(rays(r) for r in reqs)
+        done, wall = srv.run(reqs)
+        lat = np.array([r.done - r.arrival for r in done]) * 1000.0
+        big = np.array([r.done - r.arrival for r in done
+                        if (r.w, r.h) == (1920, 1080) and not scenes[r.scene]["pt"]]) * 1000.0
+        results.append({"rate_per_s": rate, "requests": len(reqs), "seconds": wall,
+                        "rays_per_s": total / wall,
+                        "frames_per_s": len(reqs) / wall,
+                        "latency_ms_p50": float(np.percentile(lat, 50)),
+                        "latency_ms_p99": float(np.percentile(lat, 99)),
+                        "whitted_1080p_ms_p99": float(np.percentile(big, 99)) if len(big) else None})
+    ck = clocks.stop()
+    srv.close()
+    top = results[-1]
+    line = {
+        "metric": "rays_per_s", "value": top["rays_per_s"], "unit": "rays/s",
+        "n_gpus": world, "steps": len(results), "warmup": 1,
+        "ms_per_step": 1000.0 * top["seconds"] / max(1, top["requests"]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "serve", "scenes": 32, "animated_plain": 24,
+                   "path_traced": 8, "sizes": SERVE_SIZES, "spp": [1, 16],
+                   "budget_bytes": 120 << 30, "seconds_per_rate": wl["seconds"],
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "rates": results,
+        "e2e": {"value": top["rays_per_s"], "unit": "rays/s",
+                "h2d_bytes_per_step": None, "d2h_bytes_per_step": 0,
+                "note": "wall clock of the serving loop: host update phases, scene "
+                        "uploads, batched launches; frames stay on the device"},
+        "clocks": ck,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
 
 
 def run_batch(args, wl, rank, world, dist, local):
@@ -379,6 +476,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
+    if wl.get("serve"):
+        run_serve(args, wl, rank, world, dist, local)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     if wl.get("batch"):
         run_batch(args, wl, rank, world, dist, local)
         if dist is not None:

@@ -24,6 +24,7 @@ SCN_ANIM = 2
 SCN_PT = 3
 GEN_IDS = 1 << 0
 GEN_TARRAY = 1 << 3      # animated scene keeps RT_OPTS_TARRAY on
+GEN_SPIN = 1 << 4        # plain scene whose quadrics spin
 
 # runtime options (csrc/format.h): -1 selects the default (FULL minus the
 # scene's opt-outs)
@@ -213,6 +214,11 @@ class Context:
         rc = lib().qr_scene_update(self.h, sid, ctypes.byref(desc))
         if rc != QR_OK:
             raise RuntimeError("qr_scene_update: %d %s" % (rc, self.error()))
+
+    def release(self, sid):
+        rc = lib().qr_scene_release(self.h, sid)
+        if rc != QR_OK:
+            raise RuntimeError("qr_scene_release: %d %s" % (rc, self.error()))
 
     def render_host(self, sid, params):
         out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)

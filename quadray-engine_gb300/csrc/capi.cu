@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -30,7 +31,11 @@ struct qr_ctx
 {
     int          device;
     char         err[256];
-    std::vector<qr_scene_slot> scenes;
+    /* scene table: slots live on the heap (their addresses stay valid),
+     * the table and the error text are guarded by mu so that scenes can be
+     * uploaded and updated from several host threads */
+    std::vector<qr_scene_slot *> scenes;
+    std::mutex   mu;
     uint32_t    *dframe;    /* frame buffer for qr_render_host */
     size_t       dframe_px;
     float       *dacc;      /* path-tracer running sums (3 floats a pixel) */
@@ -42,6 +47,7 @@ static int fail(qr_ctx *ctx, int code, const char *what, cudaError_t e)
 {
     if (ctx != NULL)
     {
+        std::lock_guard<std::mutex> lock(ctx->mu);
         snprintf(ctx->err, sizeof(ctx->err), "%s: %s", what,
                  e == cudaSuccess ? "error" : cudaGetErrorString(e));
     }
@@ -79,7 +85,11 @@ extern "C" int qr_ctx_destroy(qr_ctx *ctx)
     cudaSetDevice(ctx->device);
     for (size_t i = 0; i < ctx->scenes.size(); i++)
     {
-        if (ctx->scenes[i].used) cudaFree(ctx->scenes[i].block);
+        if (ctx->scenes[i] != NULL)
+        {
+            cudaFree(ctx->scenes[i]->block);
+            delete ctx->scenes[i];
+        }
     }
     if (ctx->dframe) cudaFree(ctx->dframe);
     if (ctx->dacc) cudaFree(ctx->dacc);
@@ -251,14 +261,21 @@ extern "C" int qr_scene_upload(qr_ctx *ctx, const qr_scene_desc *desc, int *scen
     if (ctx == NULL || scene_id == NULL) return QR_ERR_ARG;
     int rc = check_desc(desc);
     if (rc != QR_OK) return rc;
-    qr_scene_slot sl;
-    memset(&sl, 0, sizeof(sl));
-    rc = upload(ctx, sl, desc, true);
-    if (rc != QR_OK) return rc;
-    sl.used = 1;
+    qr_scene_slot *sl = new (std::nothrow) qr_scene_slot();
+    if (sl == NULL) return QR_ERR_OOM;
+    memset(sl, 0, sizeof(*sl));
+    rc = upload(ctx, *sl, desc, true);
+    if (rc != QR_OK)
+    {
+        if (sl->block) cudaFree(sl->block);
+        delete sl;
+        return rc;
+    }
+    sl->used = 1;
+    std::lock_guard<std::mutex> lock(ctx->mu);
     for (size_t i = 0; i < ctx->scenes.size(); i++)
     {
-        if (!ctx->scenes[i].used)
+        if (ctx->scenes[i] == NULL)
         {
             ctx->scenes[i] = sl;
             *scene_id = (int)i;
@@ -272,9 +289,10 @@ extern "C" int qr_scene_upload(qr_ctx *ctx, const qr_scene_desc *desc, int *scen
 
 static qr_scene_slot *slot(qr_ctx *ctx, int id)
 {
-    if (ctx == NULL || id < 0 || id >= (int)ctx->scenes.size()) return NULL;
-    if (!ctx->scenes[id].used) return NULL;
-    return &ctx->scenes[id];
+    if (ctx == NULL) return NULL;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (id < 0 || id >= (int)ctx->scenes.size()) return NULL;
+    return ctx->scenes[id];
 }
 
 extern "C" int qr_scene_update(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc)
@@ -288,11 +306,18 @@ extern "C" int qr_scene_update(qr_ctx *ctx, int scene_id, const qr_scene_desc *d
 
 extern "C" int qr_scene_release(qr_ctx *ctx, int scene_id)
 {
-    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (ctx == NULL) return QR_ERR_ARG;
+    qr_scene_slot *sl = NULL;
+    {
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        if (scene_id < 0 || scene_id >= (int)ctx->scenes.size()) return QR_ERR_NOSCENE;
+        sl = ctx->scenes[scene_id];
+        ctx->scenes[scene_id] = NULL;
+    }
     if (sl == NULL) return QR_ERR_NOSCENE;
     cudaSetDevice(ctx->device);
     cudaFree(sl->block);
-    memset(sl, 0, sizeof(*sl));
+    delete sl;
     return QR_OK;
 }
 
@@ -474,5 +499,7 @@ int qr_internal_fail(qr_ctx *ctx, int code, const char *what, cudaError_t e)
 
 void qr_internal_message(qr_ctx *ctx, const char *msg)
 {
-    if (ctx != NULL) snprintf(ctx->err, sizeof(ctx->err), "%s", msg);
+    if (ctx == NULL) return;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    snprintf(ctx->err, sizeof(ctx->err), "%s", msg);
 }

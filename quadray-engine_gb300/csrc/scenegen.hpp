@@ -22,6 +22,8 @@
  *   QR_SCN_PT      a closed box of 5 planes with N quadrics inside, 60%
  *                  Lambertian / 25% mirror / 15% dielectric, a LIGHT-material
  *                  emitter with a light cluster, for the path tracer
+ * Flag QR_GEN_SPIN makes the quadrics of QR_SCN_PLAIN spin (the animated
+ * scenes of the serving workload).
  * Flag QR_GEN_IDS replaces every material with a LIGHT material whose colour
  * encodes (surface index, side), so the rendered frame is a hit-ID buffer.
  */
@@ -47,6 +49,7 @@
 #define QR_GEN_NOSPEC   (1 << 1)   /* debug: no specular */
 #define QR_GEN_ONELIGHT (1 << 2)   /* debug: a single light */
 #define QR_GEN_TARRAY   (1 << 3)   /* QR_SCN_ANIM: keep RT_OPTS_TARRAY on */
+#define QR_GEN_SPIN     (1 << 4)   /* QR_SCN_PLAIN: the quadrics spin (anim_spin) */
 
 namespace qr_gen
 {
@@ -396,6 +399,7 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
         float px = r.uf(-10, 10), py = r.uf(-10, 10), pz = r.uf(0.5, 5);
         float rx = r.uf(-180, 180), ry = r.uf(-180, 180), rz = r.uf(-180, 180);
         Scene::trm_set(&q.trm, 1, 1, 1, rx, ry, rz, px, py, pz);
+        if (sc.flags & QR_GEN_SPIN) q.f_anim = anim_spin;
         root.push_back(q);
     }
     rt_OBJECT ro = sc.array(root);

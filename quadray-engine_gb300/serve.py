@@ -1,0 +1,229 @@
+"""Frame server: continuous batching of frame requests on device-resident
+scenes.
+
+The reference renders one frame per rt_Scene::render call on a CPU thread
+pool (core/engine/engine.cpp:3014) and has no server.  This module serves
+many clients from one GPU:
+
+* scenes stay resident; each request names a scene, an animation time, a
+  frame size and a sampling (Whitted: 1 sample or the reference's 4x AA;
+  path tracer: pt_on samples);
+* admission: a request is admitted when its device memory (frame, path-
+  tracer sums, its version of the scene) fits the HBM budget; otherwise it
+  waits;
+* admitted requests are prepared on host threads: the scene's update phases
+  at the request's time (animators, transforms, lists, the hierarchy) and an
+  in-place upload into a pooled device copy of that scene;
+* continuous batching: prepared requests go into the next batched launch
+  (qr_batch_*), two batches in flight so the GPU never waits for the host;
+  requests that arrive while a batch runs join the following one;
+* every frame equals the frame of the same request rendered alone.
+
+Latency is arrival to completion (the batch's end, seen by polling).
+"""
+import collections
+import ctypes
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+
+class Request:
+    """One frame request."""
+
+    __slots__ = ("rid", "scene", "time", "w", "h", "spp", "arrival", "done",
+                 "frame", "acc", "slot", "bytes", "fp", "flat_key")
+
+    def __init__(self, rid, scene, time_ms, w, h, spp, arrival):
+        self.rid, self.scene, self.time = rid, scene, time_ms
+        self.w, self.h, self.spp = w, h, spp
+        self.arrival = arrival
+        self.done = None
+        self.frame = self.acc = None
+        self.slot = None
+        self.bytes = 0
+        self.fp = None
+        self.flat_key = None
+
+
+class Server:
+    """Continuous-batching frame server over one context."""
+
+    def __init__(self, qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
+                 max_batch_pixels=24 << 20, prep_threads=4):
+        """scenes: list of dicts with keys gen (a GenScene), pt (path-traced
+        scene) and depth"""
+        import torch
+        self.qr, self.ctx, self.torch = qr, ctx, torch
+        self.scenes = scenes
+        self.budget = budget_bytes
+        self.used = 0
+        self.max_batch = max_batch
+        self.max_batch_pixels = max_batch_pixels
+        self.pool = ThreadPoolExecutor(max_workers=prep_threads)
+        self.locks = [threading.Lock() for _ in scenes]
+        self.flats = {}                 # (scene, w, h, fsaa) -> Flat
+        self.slots = [collections.deque() for _ in scenes]   # free scene copies
+        self.slot_bytes = {}
+        self.stream = torch.cuda.Stream()
+        self.batches = [qr.Batch(ctx, max_batch), qr.Batch(ctx, max_batch)]
+        self.free_batches = collections.deque(self.batches)
+        self.waiting = collections.deque()      # arrived, not admitted
+        self.preparing = []                      # futures
+        self.ready = collections.deque()         # prepared, not launched
+        self.inflight = collections.deque()      # (batch, [requests])
+        self.completed = []
+
+    # ---- preparation --------------------------------------------------
+    def _fsaa(self, req):
+        return 0 if (self.scenes[req.scene]["pt"] or req.spp <= 1) else 2
+
+    def _prepare(self, req):
+        """update phases at the request's time, upload into a scene copy"""
+        qr = self.qr
+        sc = self.scenes[req.scene]
+        fsaa = self._fsaa(req)
+        key = (req.scene, req.w, req.h, fsaa)
+        with self.locks[req.scene]:
+            flat = self.flats.get(key)
+            if flat is None:
+                flat = qr.Flat(sc["gen"], req.w, req.h, fsaa)
+                self.flats[key] = flat
+            desc, params = flat.update(req.time, sc["depth"])
+            fp = qr.QrFrameParams.from_buffer_copy(params)
+            if req.slot is None:
+                req.slot = self.ctx.upload(desc)
+            else:
+                self.ctx.update(req.slot, desc)
+        if sc["pt"]:
+            fp.pt_on, fp.pts_c, fp.seed, fp.frame_idx = req.spp, 0.0, 0x5E, req.rid
+        req.fp = fp
+        return req
+
+    def need_bytes(self, req):
+        """device memory a request holds while in flight: frame, path-tracer
+        sums, and (an allowance of 1 MiB for) its version of the scene"""
+        pt = self.scenes[req.scene]["pt"]
+        return req.w * req.h * 4 * (4 if pt else 1) + (1 << 20)
+
+    def _admit(self):
+        torch = self.torch
+        while self.waiting:
+            req = self.waiting[0]
+            pt = self.scenes[req.scene]["pt"]
+            need = self.need_bytes(req)
+            if self.used + need > self.budget:
+                break
+            self.waiting.popleft()
+            self.used += need
+            req.bytes = need
+            req.frame = torch.empty((req.h, req.w), dtype=torch.int32, device="cuda")
+            if pt:
+                req.acc = torch.empty((req.h, req.w, 3), dtype=torch.float32, device="cuda")
+            if self.slots[req.scene]:
+                req.slot = self.slots[req.scene].popleft()
+            self.preparing.append(self.pool.submit(self._prepare, req))
+
+    def _collect_prepared(self):
+        keep = []
+        for f in self.preparing:
+            if f.done():
+                self.ready.append(f.result())
+            else:
+                keep.append(f)
+        self.preparing = keep
+
+    # ---- batches ------------------------------------------------------
+    def _launch(self):
+        qr = self.qr
+        while self.ready and self.free_batches:
+            reqs, px = [], 0
+            while self.ready and len(reqs) < self.max_batch:
+                r = self.ready[0]
+                if reqs and px + r.w * r.h > self.max_batch_pixels:
+                    break
+                self.ready.popleft()
+                reqs.append(r)
+                px += r.w * r.h
+            table = []
+            for r in reqs:
+                q = qr.QrRequest()
+                q.scene_id = r.slot
+                q.fp = r.fp
+                q.fp.x_row = r.w
+                q.dev_frame = r.frame.data_ptr()
+                q.dev_acc = r.acc.data_ptr() if r.acc is not None else None
+                table.append(q)
+            b = self.free_batches.popleft()
+            b.set(table)
+            b.launch(self.stream.cuda_stream)
+            self.inflight.append((b, reqs))
+
+    def _complete(self, now_fn):
+        while self.inflight and self.inflight[0][0].poll():
+            b, reqs = self.inflight.popleft()
+            t = now_fn()
+            for r in reqs:
+                r.done = t
+                self.used -= r.bytes
+                self.slots[r.scene].append(r.slot)
+                self.completed.append(r)
+            self.free_batches.append(b)
+
+    def step(self, now_fn):
+        self._complete(now_fn)
+        self._admit()
+        self._collect_prepared()
+        self._launch()
+
+    def busy(self):
+        return bool(self.waiting or self.preparing or self.ready or self.inflight)
+
+    def run(self, arrivals, keep_frames=False):
+        """serve a list of Requests (their arrival in seconds from the
+        start); returns the completed requests"""
+        for r in arrivals:
+            if self.need_bytes(r) > self.budget:
+                raise ValueError("request %d needs %d bytes, more than the budget"
+                                 % (r.rid, self.need_bytes(r)))
+        pending = collections.deque(sorted(arrivals, key=lambda r: r.arrival))
+        t0 = time.perf_counter()
+
+        def now():
+            return time.perf_counter() - t0
+
+        while pending or self.busy():
+            t = now()
+            while pending and pending[0].arrival <= t:
+                self.waiting.append(pending.popleft())
+            self.step(now)
+            if not keep_frames:
+                for r in self.completed:
+                    r.frame = r.acc = None
+        done, self.completed = self.completed, []
+        return done, now()
+
+    def close(self):
+        for b in self.batches:
+            b.close()
+        self.pool.shutdown()
+
+
+def poisson_requests(n_scenes, rate, duration, sizes, spp_max, seed, pt_scenes=()):
+    """Poisson arrivals at `rate` per second over `duration` seconds; each
+    request picks a scene, the scene's next animation frame (16 ms apart), a
+    size and a sampling uniformly"""
+    rng = np.random.default_rng(seed)
+    t, out, nxt = 0.0, [], [0] * n_scenes
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        s = int(rng.integers(0, n_scenes))
+        w, h = sizes[int(rng.integers(0, len(sizes)))]
+        spp = int(rng.integers(1, spp_max + 1))
+        out.append(Request(len(out), s, 16 * nxt[s], w, h, spp, t))
+        nxt[s] += 1
+    return out
