@@ -90,6 +90,16 @@ __device__ __forceinline__ float fxor(float a, uint32_t m) { return u2f(f2u(a) ^
 __device__ __forceinline__ uint32_t sgnbit(float a) { return f2u(a) & SIGN_BIT; }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+/* 128-bit read-only loads of the 16-byte groups of the records (qr_srf,
+ * qr_elem, qr_bitem, qr_bnode are laid out in such groups) */
+__device__ __forceinline__ float4 ldf4(const float *p)
+{
+    return __ldg(reinterpret_cast<const float4 *>(p));
+}
+__device__ __forceinline__ int4 ldi4(const int32_t *p)
+{
+    return __ldg(reinterpret_cast<const int4 *>(p));
+}
 /* full-precision rsqrt of the reference's compat mode: 1 / sqrt(x) */
 __device__ __forceinline__ float rsq(float x) { return __fdiv_rn(1.0f, __fsqrt_rn(x)); }
 
@@ -98,17 +108,18 @@ __device__ __forceinline__ void xform(const qr_srf *__restrict__ t,
                                       const float v[3], float o[3])
 {
     const int am = __ldg(&t->amap[3]);
-    float x = __ldg(&t->tci[0]) * v[0];
-    float y = __ldg(&t->tcj[1]) * v[1];
-    float z = __ldg(&t->tck[2]) * v[2];
+    const float4 a = ldf4(t->tci), b = ldf4(t->tcj), c = ldf4(t->tck);
+    float x = a.x * v[0];
+    float y = b.y * v[1];
+    float z = c.z * v[2];
     if (am != 1)
     {
-        x = x + __ldg(&t->tci[1]) * v[1];
-        x = x + __ldg(&t->tci[2]) * v[2];
-        y = y + __ldg(&t->tcj[0]) * v[0];
-        y = y + __ldg(&t->tcj[2]) * v[2];
-        z = z + __ldg(&t->tck[0]) * v[0];
-        z = z + __ldg(&t->tck[1]) * v[1];
+        x = x + a.y * v[1];
+        x = x + a.z * v[2];
+        y = y + b.x * v[0];
+        y = y + b.z * v[2];
+        z = z + c.x * v[0];
+        z = z + c.y * v[1];
     }
     o[0] = x; o[1] = y; o[2] = z;
 }
@@ -136,8 +147,10 @@ __device__ int clip_root(const qr_dscene &S, const Ray &r, int si, float t,
     }
     else
     {
+        const float4 ps = ldf4(s->pos);
+        const float pp[3] = {ps.x, ps.y, ps.z};
         #pragma unroll
-        for (int k = 0; k < 3; k++) loc[k] = hit[k] - __ldg(&s->pos[k]);
+        for (int k = 0; k < 3; k++) loc[k] = hit[k] - pp[k];
     }
 
     const int conic = __ldg(&s->conic);
@@ -181,12 +194,14 @@ __device__ int clip_root(const qr_dscene &S, const Ray &r, int si, float t,
     }
 
     /* axis clippers (2963-3014) */
-    const int mint = __ldg(&s->mint), maxt = __ldg(&s->maxt);
+    const float4 bn = ldf4(s->bmin), bx = ldf4(s->bmax);
+    const int mint = __float_as_int(bn.w), maxt = __float_as_int(bx.w);
+    const float bl[3] = {bn.x, bn.y, bn.z}, bh[3] = {bx.x, bx.y, bx.z};
     #pragma unroll
     for (int k = 0; k < 3; k++)
     {
-        if ((mint >> k) & 1) valid = valid && (__ldg(&s->bmin[k]) <= loc[k]);
-        if ((maxt >> k) & 1) valid = valid && (__ldg(&s->bmax[k]) >= loc[k]);
+        if ((mint >> k) & 1) valid = valid && (bl[k] <= loc[k]);
+        if ((maxt >> k) & 1) valid = valid && (bh[k] >= loc[k]);
     }
 
     /* custom clippers with boolean accumulator segments (3020-3240) */
@@ -391,11 +406,13 @@ __device__ __forceinline__ void solve_surface(const qr_dscene &S, const Ray &r, 
     else if (solver == 2)
     {
         /* quadric coefficients (5722-5783) */
+        const float4 ci = ldf4(s->sci), cj = ldf4(s->scj);
+        const float sciv[3] = {ci.x, ci.y, ci.z}, scjv[3] = {cj.x, cj.y, cj.z};
         float a = 0.0f, b = 0.0f, c = 0.0f;
         #pragma unroll
         for (int k = 0; k < 3; k++)
         {
-            const float sci = __ldg(&s->sci[k]), scj = __ldg(&s->scj[k]);
+            const float sci = sciv[k], scj = scjv[k];
             const float sri = sci * lray[k];
             float sdi = sci * ldff[k];
             sdi = sdi - scj;
@@ -406,7 +423,7 @@ __device__ __forceinline__ void solve_surface(const qr_dscene &S, const Ray &r, 
             if (k == 0) { a = ax; b = bx; c = cx; }
             else { a = a + ax; b = b + bx; c = c + cx; }
         }
-        c = c - __ldg(&s->sci[3]);
+        c = c - ci.w;
         const float d = b * b - c * a;
         CNT(QR_STAT_TEST_QUADRIC);
         root_pair(S, r, w, si, p, ldff, lray, a, b, c, d, st);
@@ -430,27 +447,12 @@ __device__ __forceinline__ void solve_surface(const qr_dscene &S, const Ray &r, 
     }
 }
 
-/* the surface's local ray without the walk's per-node cache: through
- * transform node xf (>= 0), the surface's own transform, or a translation
- * (2518-2645) */
+/* the surface's local ray outside a transform node's group: through the
+ * surface's own transform or a translation (2518-2645) */
 __device__ __forceinline__ void local_ray(const qr_dscene &S, const Ray &r, int si,
-                                          int xf, float ldff[3], float lray[3], StP st)
+                                          float ldff[3], float lray[3], StP st)
 {
     const qr_srf *__restrict__ s = &S.srf[si];
-    if (xf >= 0)
-    {
-        const qr_srf *__restrict__ t = &S.srf[xf];
-        float d[3], cdff[3];
-        #pragma unroll
-        for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&t->pos[k]);
-        CNT(QR_STAT_XFORM);
-        xform(t, d, cdff);
-        xform(t, r.dir, lray);
-        #pragma unroll
-        for (int k = 0; k < 3; k++)
-            ldff[k] = r.from == si ? r.phit[k] : cdff[k] - __ldg(&s->pos[k]);
-        return;
-    }
     const int am3 = __ldg(&s->amap[3]);
     if (r.from == si)
     {
@@ -465,8 +467,10 @@ __device__ __forceinline__ void local_ray(const qr_dscene &S, const Ray &r, int 
         return;
     }
     float d[3];
-    #pragma unroll
-    for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&s->pos[k]);
+    const float4 ps = ldf4(s->pos);
+    d[0] = r.org[0] - ps.x;
+    d[1] = r.org[1] - ps.y;
+    d[2] = r.org[2] - ps.z;
     if (am3 != 0) { CNT(QR_STAT_XFORM); xform(s, d, ldff); xform(s, r.dir, lray); }
     else
     {
@@ -480,10 +484,12 @@ __device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray
                                        const float inv[3], float tmax, float &tn)
 {
     float t0 = -FLT_MAX, t1 = FLT_MAX;
+    const float4 l4 = ldf4(n->lo), h4 = ldf4(n->hi);
+    const float los[3] = {l4.x, l4.y, l4.z}, his[3] = {h4.x, h4.y, h4.z};
     #pragma unroll
     for (int k = 0; k < 3; k++)
     {
-        const float lo = __ldg(&n->lo[k]), hi = __ldg(&n->hi[k]);
+        const float lo = los[k], hi = his[k];
         if (r.dir[k] == 0.0f)
         {
             if (r.org[k] < lo || r.org[k] > hi) return 0;
@@ -516,8 +522,9 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
                         dx * dx + dy * dy + dz * dz <= S.ray_r2 &&
                         ((off == S.cam_off && num == S.cam_num) ||
                          (off == S.shd_off && num == S.shd_num));
-    /* list source */
-    int e = 0, cache_last = -1;
+    /* list source (cache_last) and hierarchy source (cxf): the transform
+     * node whose transformed ray cdff / cray holds */
+    int e = 0, cache_last = -1, cxf = -1;
     float cdff[3] = {0.0f, 0.0f, 0.0f}, cray[3] = {0.0f, 0.0f, 0.0f};
     /* hierarchy source */
     int ai = 0, ia = 0, ib = 0, sp = 0;
@@ -548,21 +555,20 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
             while (e < num)
             {
                 const int ei = off + e;
-                const qr_elem *__restrict__ el = &S.elems[ei];
-                const int kind = __ldg(&el->kind);
-                const int ref = __ldg(&el->ref);
+                const int4 el = ldi4(&S.elems[ei].kind);   /* kind, ref, last, rel */
+                const int kind = el.x;
+                const int ref = el.y;
                 e++;
                 if (kind == QR_ELM_TRNODE)
                 {
                     const qr_srf *__restrict__ t = &S.srf[ref];
-                    float d[3];
-                    #pragma unroll
-                    for (int k = 0; k < 3; k++) d[k] = r.org[k] - __ldg(&t->pos[k]);
                     if (__ldg(&t->amap[3]) == 0) continue;
+                    const float4 tp = ldf4(t->pos);
+                    const float d[3] = {r.org[0] - tp.x, r.org[1] - tp.y, r.org[2] - tp.z};
                     CNT(QR_STAT_XFORM);
                     xform(t, d, cdff);
                     xform(t, r.dir, cray);
-                    cache_last = __ldg(&el->last);
+                    cache_last = el.z;
                     continue;
                 }
                 si = ref;
@@ -616,25 +622,41 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
                 if (ia >= ib) break;
                 it = &S.items[ia++];
             }
-            si = __ldg(&it->srf);
-            p = __ldg(&it->pos);
-            xf = __ldg(&it->xf);
+            const int4 iv = ldi4(&it->pos);              /* pos, srf, xf, pad */
+            si = iv.y;
+            p = iv.x;
+            xf = iv.z;
+            if (xf >= 0)
+            {
+                if (xf != cxf)
+                {
+                    const qr_srf *__restrict__ t = &S.srf[xf];
+                    const float4 tp = ldf4(t->pos);
+                    const float d[3] = {r.org[0] - tp.x, r.org[1] - tp.y, r.org[2] - tp.z};
+                    CNT(QR_STAT_XFORM);
+                    xform(t, d, cdff);
+                    xform(t, r.dir, cray);
+                    cxf = xf;
+                }
+                cached = 1;
+            }
         }
 
         float ldff[3], lray[3];
         if (cached)
         {
-            const qr_srf *__restrict__ s = &S.srf[si];
+            const float4 ps = ldf4(S.srf[si].pos);
+            const float pp[3] = {ps.x, ps.y, ps.z};
             #pragma unroll
             for (int k = 0; k < 3; k++)
             {
-                ldff[k] = r.from == si ? r.phit[k] : cdff[k] - __ldg(&s->pos[k]);
+                ldff[k] = r.from == si ? r.phit[k] : cdff[k] - pp[k];
                 lray[k] = cray[k];
             }
         }
         else
         {
-            local_ray(S, r, si, xf, ldff, lray, st);
+            local_ray(S, r, si, ldff, lray, st);
         }
         solve_surface(S, r, w, si, p, ldff, lray, st);
         if (w.shadow && w.occluded) return;
@@ -1410,6 +1432,26 @@ __device__ __forceinline__ uint32_t pack(const qr_frame_params &P, const float c
     return px;
 }
 
+/* pixels of a frame kernel's thread: each warp of a 32x4 block covers a
+ * tile of QR_TILE_W x (32 / QR_TILE_W) pixels, the block's four warps 2 x 2
+ * tiles, so neighbouring lanes trace neighbouring rays */
+#ifndef QR_TILE_W
+#define QR_TILE_W 16
+#endif
+#define QR_TILE_H (32 / QR_TILE_W)
+
+__device__ __forceinline__ int tile_x()
+{
+    return blockIdx.x * (2 * QR_TILE_W) + (threadIdx.y & 1) * QR_TILE_W +
+           threadIdx.x % QR_TILE_W;
+}
+
+__device__ __forceinline__ int tile_y()
+{
+    return blockIdx.y * (2 * QR_TILE_H) + (threadIdx.y >> 1) * QR_TILE_H +
+           threadIdx.x / QR_TILE_W;
+}
+
 /* blocks of 32x4 threads; QR_MIN_BLOCKS resident blocks per SM bound the
  * registers per thread (65536 / (128 * QR_MIN_BLOCKS)).  Measured on the
  * 1920x1080 4x AA animated frame: 1 (152 registers) 55.0 ms, unbounded (128)
@@ -1455,8 +1497,7 @@ __global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
 whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
                qr_dstats *gst)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int x = tile_x(), y = tile_y();
     if (x >= P.x_res || y >= P.y_res) return;
 #ifdef QR_STATS
     TCnt cnt;
@@ -1882,8 +1923,7 @@ __global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
 pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *frame,
           qr_dstats *gst)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int x = tile_x(), y = tile_y();
     if (x >= P.x_res || y >= P.y_res) return;
 #ifdef QR_STATS
     TCnt cnt;
@@ -2013,8 +2053,8 @@ cudaError_t qr_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *
 #endif
 {
     const dim3 block(32, 4);
-    const dim3 grid((fp.x_res + block.x - 1) / block.x,
-                    (fp.y_res + block.y - 1) / block.y);
+    const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
+                    (fp.y_res + 2 * QR_TILE_H - 1) / (2 * QR_TILE_H));
 #ifdef QR_STATS
     QR_NS::pt_kernel<<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, dstats);
 #else
@@ -2033,8 +2073,8 @@ cudaError_t qr_launch_whitted(const qr_dscene &sc, const qr_frame_params &fp,
 #endif
 {
     const dim3 block(32, 4);
-    const dim3 grid((fp.x_res + block.x - 1) / block.x,
-                    (fp.y_res + block.y - 1) / block.y);
+    const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
+                    (fp.y_res + 2 * QR_TILE_H - 1) / (2 * QR_TILE_H));
 #ifdef QR_STATS
     QR_NS::whitted_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, dstats);
 #else
