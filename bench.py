@@ -42,7 +42,8 @@ FLOPS = {
 }
 STAT_NAMES = ["ray_primary", "ray_shadow", "ray_secondary", "test_plane",
               "test_quadric", "test_twoplane", "xform", "clip_root",
-              "clip_custom", "shade", "light", "refract", "reflect"]
+              "clip_custom", "shade", "light", "refract", "reflect",
+              "box_test", "far_walk"]
 
 WORKLOADS = {
     # animated Whitted frame: 1920x1080, 4x AA, 64 quadrics cut by 1-2 planes
@@ -122,7 +123,7 @@ def run_serve(args, wl, rank, world, dist, local):
             sid = ctx.upload(desc)
             if sc["pt"]:
                 params.pt_on, params.pts_c = 1, 0.0
-            counts = (ctypes.c_uint64 * 13)()
+            counts = (ctypes.c_uint64 * len(STAT_NAMES))()
             host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
             rc = qr.lib().qr_render_stats(ctx.h, sid, ctypes.byref(params),
                                           host.ctypes.data_as(ctypes.c_void_p), counts)
@@ -203,7 +204,7 @@ def run_batch(args, wl, rank, world, dist, local):
         keep.append((g, f))
         bufs.append((fr, acc))
         reqs.append(r)
-        counts = (ctypes.c_uint64 * 13)()
+        counts = (ctypes.c_uint64 * len(STAT_NAMES))()
         host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
         rc = qr.lib().qr_render_stats(ctx.h, sid, ctypes.byref(r.fp),
                                       host.ctypes.data_as(ctypes.c_void_p), counts)
@@ -511,7 +512,7 @@ def main():
     stats = dict((k, 0) for k in STAT_NAMES)
     frame_rays = []
     for i in range(args.steps if wl["anim"] else 1):
-        counts = (ctypes.c_uint64 * 13)()
+        counts = (ctypes.c_uint64 * len(STAT_NAMES))()
         rc = qr.lib().qr_render_stats(ctx.h, sid_of(args.warmup + i), ctypes.byref(params),
                                       host.ctypes.data_as(ctypes.c_void_p), counts)
         assert rc == 0, ctx.error()

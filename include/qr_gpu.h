@@ -238,7 +238,10 @@ int qr_sync(qr_ctx *ctx, void *stream);
 #define QR_STAT_LIGHT           10
 #define QR_STAT_REFRACT         11
 #define QR_STAT_REFLECT         12
-#define QR_STAT_COUNT           13
+#define QR_STAT_BOX_TEST        13      /* bounding-volume box tests */
+#define QR_STAT_FAR_WALK        14      /* full-list walks of rays starting
+                                           beyond the hierarchy's radius */
+#define QR_STAT_COUNT           15
 int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                     uint32_t *host_frame, uint64_t *counts);
 

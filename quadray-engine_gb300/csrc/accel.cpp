@@ -427,7 +427,7 @@ int build_node(std::vector<Prim> &p, int lo, int hi, int depth, qr_accel_host *o
 
 } /* namespace */
 
-int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out)
+int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level)
 {
     out->nodes.clear();
     out->items.clear();
@@ -480,8 +480,9 @@ int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out)
     }
     rs = sqrt(rs);
     /* rays starting within ray_r of the centre use the hierarchy; their
-     * local coordinates stay below D */
-    const double ray_r = 6.0 * rs + 8.0;
+     * local coordinates stay below D.  Each level covers 8 times the radius
+     * of the previous one, with boxes widened for the larger rounding */
+    const double ray_r = (6.0 * rs + 8.0) * pow(8.0, (double)level);
     const double D = gain * (ray_r + 2.0 * rs + 1.0) + 1.0;
     out->ray_r2 = (float)(ray_r * ray_r);
 
@@ -568,4 +569,44 @@ int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out)
     }
     if (!prims.empty()) build_node(prims, 0, (int)prims.size(), 1, out);
     return 0;
+}
+
+void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
+                           int root[QR_BVH_LEVELS], int aoff[QR_BVH_LEVELS],
+                           int anum[QR_BVH_LEVELS], float r2[QR_BVH_LEVELS])
+{
+    out->nodes.clear();
+    out->items.clear();
+    out->always.clear();
+    out->depth = 0;
+    for (int l = 0; l < QR_BVH_LEVELS; l++)
+    {
+        qr_accel_host lv;
+        qr_accel_build(d, &lv, l);
+        const int n0 = (int)out->nodes.size(), i0 = (int)out->items.size();
+        root[l] = n0;
+        aoff[l] = (int)out->always.size();
+        anum[l] = (int)lv.always.size();
+        /* the outer levels' boxes are wide; for short lists a walk in list
+         * order is cheaper than traversing them */
+        const bool used = l == 0 || d->cam_num >= QR_BVH_OUTER_MIN;
+        r2[l] = (used && lv.depth < QR_BVH_STACK - 2 && !lv.nodes.empty()) ? lv.ray_r2 : -1.0f;
+        if (l == 0)
+        {
+            for (int k = 0; k < 3; k++) out->ray_c[k] = lv.ray_c[k];
+            out->ray_r2 = lv.ray_r2;
+            out->boxes = lv.boxes;
+            out->bounded = lv.bounded;
+        }
+        out->depth = std::max(out->depth, lv.depth);
+        for (size_t k = 0; k < lv.nodes.size(); k++)
+        {
+            qr_bnode nd = lv.nodes[k];
+            if (nd.count > 0) nd.a += i0;
+            else { nd.a += n0; nd.b += n0; }
+            out->nodes.push_back(nd);
+        }
+        out->items.insert(out->items.end(), lv.items.begin(), lv.items.end());
+        out->always.insert(out->always.end(), lv.always.begin(), lv.always.end());
+    }
 }

@@ -60,9 +60,23 @@ struct qr_accel_host
     float ray_c[3], ray_r2;
 };
 
-/* build the hierarchy over the camera list of `d` (which the flattening
- * also uses, in the same order, for shadow and secondary rays); returns 0 */
-int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out);
+/* build the hierarchy of one level over the camera list of `d` (which the
+ * flattening also uses, in the same order, for shadow and secondary rays):
+ * level l serves rays starting within 8^l times the base radius of the
+ * scene's centre, its boxes allowing for their rounding; returns 0 */
+int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level);
+
+/* hierarchy levels built per scene; levels past the first only for lists of
+ * at least QR_BVH_OUTER_MIN elements */
+#define QR_BVH_LEVELS 3
+#define QR_BVH_OUTER_MIN 64
+
+/* all levels concatenated into `out` (node indices and item ranges shifted
+ * by the preceding levels); per level its root node, its unbounded surfaces
+ * always[aoff, aoff + anum) and the squared radius it serves (-1: none) */
+void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
+                           int root[QR_BVH_LEVELS], int aoff[QR_BVH_LEVELS],
+                           int anum[QR_BVH_LEVELS], float r2[QR_BVH_LEVELS]);
 
 /* deepest traversal stack the tracer supports */
 #define QR_BVH_STACK 48

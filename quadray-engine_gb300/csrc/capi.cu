@@ -185,14 +185,10 @@ static void shadow_list(const qr_scene_desc *d, int *off, int *num)
 static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool fresh)
 {
     qr_accel_host acc;
-    qr_accel_build(d, &acc);
-    const bool use_bvh = acc.depth < QR_BVH_STACK - 2;
-    if (!use_bvh)
-    {
-        acc.nodes.clear();
-        acc.items.clear();
-    }
-
+    int lvl_root[QR_BVH_LEVELS], lvl_aoff[QR_BVH_LEVELS], lvl_anum[QR_BVH_LEVELS];
+    float lvl_r2[QR_BVH_LEVELS];
+    qr_accel_build_levels(d, &acc, lvl_root, lvl_aoff, lvl_anum, lvl_r2);
+    const bool use_bvh = !acc.nodes.empty();
     size_t o_srf = 0;
     size_t o_mat = o_srf + al16(sizeof(qr_srf) * d->nsrf);
     size_t o_lgt = o_mat + al16(sizeof(qr_mat) * d->nmat);
@@ -251,7 +247,13 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     sl.d.nalways = (int32_t)acc.always.size();
     shadow_list(d, &sl.d.shd_off, &sl.d.shd_num);
     for (int k = 0; k < 3; k++) sl.d.ray_c[k] = acc.ray_c[k];
-    sl.d.ray_r2 = acc.ray_r2;
+    for (int l = 0; l < QR_BVH_LEVELS; l++)
+    {
+        sl.d.lvl_root[l] = lvl_root[l];
+        sl.d.lvl_aoff[l] = lvl_aoff[l];
+        sl.d.lvl_anum[l] = lvl_anum[l];
+        sl.d.lvl_r2[l] = lvl_r2[l];
+    }
     sl.shape = *d;
     return QR_OK;
 }

@@ -481,8 +481,9 @@ __device__ __forceinline__ void local_ray(const qr_dscene &S, const Ray &r, int 
 
 /* ray / box slab test against the node's box, for t in (t_min, tmax] */
 __device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray &r,
-                                       const float inv[3], float tmax, float &tn)
+                                       const float inv[3], float tmax, float &tn, StP st)
 {
+    CNT(QR_STAT_BOX_TEST);
     float t0 = -FLT_MAX, t1 = FLT_MAX;
     const float4 l4 = ldf4(n->lo), h4 = ldf4(n->hi);
     const float los[3] = {l4.x, l4.y, l4.z}, his[3] = {h4.x, h4.y, h4.z};
@@ -518,10 +519,16 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
 {
     const float dx = r.org[0] - S.ray_c[0], dy = r.org[1] - S.ray_c[1],
                 dz = r.org[2] - S.ray_c[2];
-    const int use_bvh = S.nnodes >= 0 && !(P.flags & QR_FP_LINEAR_WALK) &&
-                        dx * dx + dy * dy + dz * dz <= S.ray_r2 &&
-                        ((off == S.cam_off && num == S.cam_num) ||
-                         (off == S.shd_off && num == S.shd_num));
+    const int full = (off == S.cam_off && num == S.cam_num) ||
+                     (off == S.shd_off && num == S.shd_num);
+    /* the smallest hierarchy level that covers the ray's origin */
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    int lvl = -1;
+    #pragma unroll
+    for (int l = QR_BVH_LEVELS - 1; l >= 0; l--)
+        if (d2 <= S.lvl_r2[l]) lvl = l;
+    const int use_bvh = S.nnodes >= 0 && !(P.flags & QR_FP_LINEAR_WALK) && lvl >= 0 && full;
+    if (S.nnodes >= 0 && full && lvl < 0) CNT(QR_STAT_FAR_WALK);
     /* list source (cache_last) and hierarchy source (cxf): the transform
      * node whose transformed ray cdff / cray holds */
     int e = 0, cache_last = -1, cxf = -1;
@@ -531,14 +538,18 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
     int stk[QR_BVH_STACK];
     float stt[QR_BVH_STACK];
     float inv[3];
+    int aend = 0;
     if (use_bvh)
     {
         #pragma unroll
         for (int k = 0; k < 3; k++) inv[k] = r.dir[k] != 0.0f ? fdiv(1.0f, r.dir[k]) : 0.0f;
+        ai = S.lvl_aoff[lvl];
+        aend = ai + S.lvl_anum[lvl];
+        const int root = S.lvl_root[lvl];
         float tn;
-        if (S.nnodes > 0 && box_hit(&S.nodes[0], r, inv, w.tbuf, tn))
+        if (box_hit(&S.nodes[root], r, inv, w.tbuf, tn, st))
         {
-            stk[0] = 0;
+            stk[0] = root;
             stt[0] = tn;
             sp = 1;
         }
@@ -586,7 +597,7 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
         else
         {
             const qr_bitem *__restrict__ it;
-            if (ai < S.nalways)
+            if (ai < aend)
             {
                 it = &S.always[ai++];
             }
@@ -608,8 +619,8 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
                     }
                     const int b = __ldg(&n->b);
                     float ta, tb;
-                    const int ha = box_hit(&S.nodes[a], r, inv, w.tbuf, ta);
-                    const int hb = box_hit(&S.nodes[b], r, inv, w.tbuf, tb);
+                    const int ha = box_hit(&S.nodes[a], r, inv, w.tbuf, ta, st);
+                    const int hb = box_hit(&S.nodes[b], r, inv, w.tbuf, tb, st);
                     if (ha && hb)
                     {
                         const int near_a = ta <= tb;

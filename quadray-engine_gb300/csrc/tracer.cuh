@@ -27,13 +27,17 @@ struct qr_dscene
     /* bounding-volume hierarchy over the camera list (accel.h); nnodes < 0
      * when the scene has none.  The shadow list [shd_off, shd_off + shd_num)
      * holds the same surfaces, so shadow rays use it too */
-    const qr_bnode *nodes;
+    const qr_bnode *nodes;          /* all levels, concatenated */
     const qr_bitem *items;
     const qr_bitem *always;
     int32_t nnodes, nitems, nalways;
     int32_t shd_off, shd_num;
-    /* rays starting within sqrt(ray_r2) of ray_c use the hierarchy */
-    float   ray_c[3], ray_r2;
+    /* level l: root node, unbounded surfaces always[aoff, aoff + anum),
+     * and the rays it serves: origin within sqrt(r2) of ray_c (r2 < 0: the
+     * level is missing) */
+    int32_t lvl_root[QR_BVH_LEVELS], lvl_aoff[QR_BVH_LEVELS], lvl_anum[QR_BVH_LEVELS];
+    float   lvl_r2[QR_BVH_LEVELS];
+    float   ray_c[3];
 };
 
 /* per-launch counters (instrumented runs only) */
