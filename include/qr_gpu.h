@@ -44,6 +44,19 @@ extern "C" {
 #define QR_ERR_NOSCENE      6   /* unknown scene id */
 #define QR_ERR_LIMIT        7   /* request exceeds a compiled-in limit */
 #define QR_ERR_BUSY         8   /* launched work still running (poll) */
+#define QR_ERR_TRACE        9   /* a pixel's ray tree or hierarchy walk ran
+                                   past its bound (corrupt scene data); see
+                                   qr_fault */
+
+/* bounds of the per-pixel loops; a pixel that runs past one is rendered
+ * black and recorded in the context's fault word (qr_fault):
+ *   QR_FAULT_TREE   more traced segments than a ray tree of the frame's
+ *                   depth can hold (Whitted: (2^(depth+1) - 1) * (1 + lights)
+ *                   per camera ray; path tracer: (3^(depth+1) - 1) / 2 per
+ *                   sample)
+ *   QR_FAULT_STACK  the hierarchy walk's node stack (48 entries) is full */
+#define QR_FAULT_TREE       1
+#define QR_FAULT_STACK      2
 
 /* ---- material / context property bits (tracer.h:66-77) ----------------- */
 #define QR_PROP_LIGHT       0x00000010
@@ -219,6 +232,14 @@ int qr_render_pt_noalloc(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
 int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                    uint32_t *host_frame);
 int qr_sync(qr_ctx *ctx, void *stream);
+
+/* read and clear the context's fault word: out[0] = QR_FAULT_* bits seen
+ * since the last call (0: none), out[1], out[2] = x, y of the first pixel
+ * that recorded one, out[3] = how many pixels did.  Renders on a caller's
+ * stream must have finished (qr_sync) before the call.  Returns QR_OK, or
+ * QR_ERR_TRACE when a bit was set.  qr_render_host checks the word itself
+ * and returns QR_ERR_TRACE */
+int qr_fault(qr_ctx *ctx, int32_t out[4]);
 
 /* instrumented render: counts the work of one frame (traced segments by
  * kind, solver tests, clip evaluations, shaded hits, light evaluations) into

@@ -75,6 +75,8 @@ class QrRequest(ctypes.Structure):
 
 
 QR_ERR_BUSY = 8
+QR_ERR_TRACE = 9
+FAULT_TREE, FAULT_STACK = 1, 2
 
 _lib = None
 
@@ -129,6 +131,7 @@ def lib():
         L.qr_batch_poll.argtypes = [vp]
         L.qr_batch_wait.argtypes = [vp]
         L.qr_sync.argtypes = [vp, vp]
+        L.qr_fault.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
         L.qr_render_stats.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp,
                                       ctypes.POINTER(ctypes.c_uint64)]
         _lib = L
@@ -246,6 +249,16 @@ class Context:
         rc = lib().qr_sync(self.h, ctypes.c_void_p(stream))
         if rc != QR_OK:
             raise RuntimeError("qr_sync: %d %s" % (rc, self.error()))
+
+    def fault(self):
+        """read and clear the fault word: (QR_FAULT_* bits, x, y of the first
+        pixel, count of pixels); (0, 0, 0, 0) when no loop ran past its
+        bound"""
+        out = (ctypes.c_int32 * 4)()
+        rc = lib().qr_fault(self.h, out)
+        if rc not in (QR_OK, QR_ERR_TRACE):
+            raise RuntimeError("qr_fault: %d %s" % (rc, self.error()))
+        return tuple(out)
 
     def close(self):
         if self.h:

@@ -40,6 +40,7 @@ struct qr_ctx
     size_t       dframe_px;
     float       *dacc;      /* path-tracer running sums (3 floats a pixel) */
     size_t       dacc_px;
+    uint32_t    *dfault;    /* fault word of the context's scenes (qr_fault) */
     cudaStream_t stream;
 };
 
@@ -66,12 +67,18 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
     ctx->dframe_px = 0;
     ctx->dacc = NULL;
     ctx->dacc_px = 0;
+    ctx->dfault = NULL;
     ctx->stream = 0;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->dfault, 4 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dfault, 0, 4 * sizeof(uint32_t), ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess)
     {
         fprintf(stderr, "qr_ctx_create: %s\n", cudaGetErrorString(e));
+        if (ctx->dfault) cudaFree(ctx->dfault);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return QR_ERR_CUDA;
     }
@@ -93,6 +100,7 @@ extern "C" int qr_ctx_destroy(qr_ctx *ctx)
     }
     if (ctx->dframe) cudaFree(ctx->dframe);
     if (ctx->dacc) cudaFree(ctx->dacc);
+    if (ctx->dfault) cudaFree(ctx->dfault);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return QR_OK;
@@ -254,6 +262,7 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
         sl.d.lvl_anum[l] = lvl_anum[l];
         sl.d.lvl_r2[l] = lvl_r2[l];
     }
+    sl.d.fault = ctx->dfault;
     sl.shape = *d;
     return QR_OK;
 }
@@ -421,7 +430,8 @@ extern "C" int qr_render_host(qr_ctx *ctx, int scene_id, const qr_frame_params *
                             cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "render host", e);
-    return QR_OK;
+    int32_t f[4];
+    return qr_fault(ctx, f);
 }
 
 extern "C" int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
@@ -463,6 +473,29 @@ extern "C" int qr_render_stats(qr_ctx *ctx, int scene_id, const qr_frame_params 
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "render stats", e);
     for (int k = 0; k < QR_STAT_COUNT; k++) counts[k] = hst.c[k];
     return QR_OK;
+}
+
+extern "C" int qr_fault(qr_ctx *ctx, int32_t out[4])
+{
+    if (ctx == NULL || out == NULL) return QR_ERR_ARG;
+    uint32_t h[4];
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h, ctx->dfault, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "fault word", e);
+    for (int k = 0; k < 4; k++) out[k] = (int32_t)h[k];
+    if (h[0] == 0) return QR_OK;
+    e = cudaMemsetAsync(ctx->dfault, 0, sizeof(h), ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "fault word", e);
+    {
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        snprintf(ctx->err, sizeof(ctx->err),
+                 "%u pixel(s) ran past a loop bound (faults 0x%x, first at %u, %u)",
+                 h[3], h[0], h[1], h[2]);
+    }
+    return QR_ERR_TRACE;
 }
 
 extern "C" int qr_sync(qr_ctx *ctx, void *stream)

@@ -82,6 +82,7 @@ struct Walk
     float tbuf;
     int   bestp;        /* list position of the nearest hit (-1: none) */
     Hit   best;
+    int   fault;        /* QR_FAULT_STACK when the walk gave up */
 };
 
 __device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
@@ -606,6 +607,8 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
                 #pragma unroll 1
                 while (ia >= ib && sp > 0)
                 {
+                    /* the pop below and up to two pushes */
+                    if (sp >= QR_BVH_STACK) { w.fault = QR_FAULT_STACK; return; }
                     --sp;
                     if (stt[sp] > w.tbuf) continue;
                     const qr_bnode *__restrict__ n = &S.nodes[stk[sp]];
@@ -1215,6 +1218,18 @@ __device__ __forceinline__ void child_ray(Ray &cr, const float hit[3], const flo
     cr.depth = depth;
 }
 
+/* record a pixel that ran past a loop bound in the context's fault word */
+__device__ __noinline__ void note_fault(const qr_dscene &S, int bit, int x, int y)
+{
+    if (S.fault == NULL) return;
+    if (atomicOr(&S.fault[0], (uint32_t)bit) == 0u)
+    {
+        S.fault[1] = (uint32_t)x;
+        S.fault[2] = (uint32_t)y;
+    }
+    atomicAdd(&S.fault[3], 1u);
+}
+
 /*
  * The Whitted ray tree of one camera ray as one loop with a single list walk.
  * Each turn of the loop traces one segment: a camera or secondary ray
@@ -1224,25 +1239,43 @@ __device__ __forceinline__ void child_ray(Ray &cr, const float hit[3], const flo
  * shaded hit that spawns a child is parked on a small per-thread stack and
  * combined when the child's colour is known, in the reference's order:
  * colour = rc * c_rfl + (tc * c_trn + local).
+ * The tree holds at most 2^(depth+1) - 1 rays, each with one shadow ray a
+ * light; a pixel that traces more segments (or whose walk gives up) is
+ * recorded in the fault word and rendered black.
  */
 __device__ void trace_tree(const qr_dscene &S, const qr_frame_params &P, Ray r,
-                           int off, int num, float col[3], StP st)
+                           int x, int y, float col[3], StP st)
 {
     Pend stk[QR_MAX_DEPTH];
-    int sp = 0;
+    int sp = 0, off = S.cam_off, num = S.cam_num;
     float ret[3];
     Shade sh;
     int shadow = 0, li = 0;
+    const int seg_lim = ((2 << P.depth) - 1) * (1 + S.nlgt);
+    int seg = 0;
     #pragma unroll 1
     for (;;)
     {
+        if (++seg > seg_lim)
+        {
+            note_fault(S, QR_FAULT_TREE, x, y);
+            col[0] = col[1] = col[2] = 0.0f;
+            return;
+        }
         Walk w;
+        w.fault = 0;
         w.shadow = shadow;
         w.occluded = 0;
         w.tbuf = r.t_max;
         w.bestp = -1;
         w.best.srf = -1;
         walk(S, P, r, off, num, w, st);
+        if (w.fault)
+        {
+            note_fault(S, w.fault, x, y);
+            col[0] = col[1] = col[2] = 0.0f;
+            return;
+        }
 
         int finish = 0;         /* the shading of sh is complete */
         if (shadow)
@@ -1399,11 +1432,11 @@ __constant__ float c_aa4_h[4] = {-0.08f - 0.25f, -0.08f + 0.25f,
 __constant__ float c_aa4_v[4] = {+0.08f - 0.25f, -0.08f - 0.25f,
                                  +0.08f + 0.25f, -0.08f + 0.25f};
 
-__device__ __forceinline__ void primary(const qr_dscene &S, const qr_frame_params &P,
-                                        float hs, float vs, float col[3],
-                                        StP st)
+/* camera ray through image position (hs, vs): dir = hor * hs + ver * vs +
+ * dir, from the camera position (engine.cpp:3530-3610) */
+__device__ __forceinline__ void camera_ray(const qr_frame_params &P, float hs, float vs,
+                                           Ray &r)
 {
-    Ray r;
     #pragma unroll
     for (int k = 0; k < 3; k++)
     {
@@ -1419,8 +1452,17 @@ __device__ __forceinline__ void primary(const qr_dscene &S, const qr_frame_param
     r.from = -1;
     r.flags = 0;
     r.depth = P.depth;
+}
+
+/* the colour of the camera ray through (hs, vs) of pixel (x, y) */
+__device__ __forceinline__ void primary(const qr_dscene &S, const qr_frame_params &P,
+                                        int x, int y, float hs, float vs, float col[3],
+                                        StP st)
+{
+    Ray r;
+    camera_ray(P, hs, vs, r);
     CNT(QR_STAT_RAY_PRIMARY);
-    trace_tree(S, P, r, S.cam_off, S.cam_num, col, st);
+    trace_tree(S, P, r, x, y, col, st);
 }
 
 __device__ __forceinline__ float clamp1(float v) { return v < 1.0f ? v : 1.0f; }
@@ -1483,7 +1525,7 @@ __device__ __forceinline__ void whitted_pixel(const qr_dscene &S, const qr_frame
         #pragma unroll 1
         for (int s = 0; s < 4; s++)
         {
-            primary(S, P, (float)x + c_aa4_h[s], (float)y + c_aa4_v[s], cs[s], st);
+            primary(S, P, x, y, (float)x + c_aa4_h[s], (float)y + c_aa4_v[s], cs[s], st);
             #pragma unroll
             for (int k = 0; k < 3; k++) cs[s][k] = clamp1(cs[s][k]);
         }
@@ -1497,7 +1539,7 @@ __device__ __forceinline__ void whitted_pixel(const qr_dscene &S, const qr_frame
     }
     else
     {
-        primary(S, P, (float)x, (float)y, col, st);
+        primary(S, P, x, y, (float)x, (float)y, col, st);
         #pragma unroll
         for (int k = 0; k < 3; k++) col[k] = clamp1(col[k]);
     }
@@ -1823,23 +1865,41 @@ __device__ int pt_advance(const qr_dscene &S, PtPend &p, float ret[3], Ray &r,
     return 0;
 }
 
-/* one path-tracer sample: the ray tree as one loop over traced segments */
+/* one path-tracer sample: the ray tree as one loop over traced segments.
+ * Every node has at most three children (diffuse, transmitted, reflected),
+ * so the tree holds at most (3^(depth+1) - 1) / 2 rays; a pixel that traces
+ * more (or whose walk gives up) is recorded in the fault word and the
+ * sample is black */
 __device__ void trace_pt(const qr_dscene &S, const qr_frame_params &P, Ray r,
-                         Pcg &g, float col[3], StP st)
+                         int x, int y, int seg_lim, Pcg &g, float col[3], StP st)
 {
     PtPend stk[QR_MAX_DEPTH + 1];
     int sp = 0, off = S.cam_off, num = S.cam_num;
     float ret[3];
+    int seg = 0;
     #pragma unroll 1
     for (;;)
     {
+        if (++seg > seg_lim)
+        {
+            note_fault(S, QR_FAULT_TREE, x, y);
+            col[0] = col[1] = col[2] = 0.0f;
+            return;
+        }
         Walk w;
+        w.fault = 0;
         w.shadow = 0;
         w.occluded = 0;
         w.tbuf = r.t_max;
         w.bestp = -1;
         w.best.srf = -1;
         walk(S, P, r, off, num, w, st);
+        if (w.fault)
+        {
+            note_fault(S, w.fault, x, y);
+            col[0] = col[1] = col[2] = 0.0f;
+            return;
+        }
         if (w.best.srf < 0)
         {
             ret[0] = ret[1] = ret[2] = 0.0f;
@@ -1888,33 +1948,24 @@ __device__ __forceinline__ void pt_pixel(const qr_dscene &S, const qr_frame_para
     pcg_seed(g, P.seed, P.frame_idx, (unsigned long long)y * P.x_res + x);
     const int spp = P.pt_on;
     const int n0 = (int)P.pts_c;
+    int seg_lim = 1;
+    #pragma unroll 1
+    for (int d = 0; d <= P.depth; d++) seg_lim *= 3;
+    seg_lim = (seg_lim - 1) / 2;
     float sum[3] = {0.0f, 0.0f, 0.0f};
     #pragma unroll 1
     for (int n = 0; n < spp; n++)
     {
+        /* tent-jittered position in the pixel (two draws) */
         float hs = pt_tent(pcg_unit(g));
         float vs = pt_tent(pcg_unit(g));
         hs = (float)x + hs;
         vs = (float)y + vs;
         Ray r;
-        #pragma unroll
-        for (int k = 0; k < 3; k++)
-        {
-            float hx = P.hor[k] * hs;
-            const float vx = P.ver[k] * vs;
-            hx = hx + vx;
-            r.dir[k] = hx + P.dir[k];
-            r.org[k] = P.org[k];
-            r.phit[k] = 0.0f;
-        }
-        r.t_min = P.t_min;
-        r.t_max = P.t_max;
-        r.from = -1;
-        r.flags = 0;
-        r.depth = P.depth;
+        camera_ray(P, hs, vs, r);
         CNT(QR_STAT_RAY_PRIMARY);
         float col[3];
-        trace_pt(S, P, r, g, col, st);
+        trace_pt(S, P, r, x, y, seg_lim, g, col, st);
         #pragma unroll
         for (int k = 0; k < 3; k++) sum[k] = sum[k] + col[k];
     }

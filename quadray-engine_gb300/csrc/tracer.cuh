@@ -38,6 +38,9 @@ struct qr_dscene
     int32_t lvl_root[QR_BVH_LEVELS], lvl_aoff[QR_BVH_LEVELS], lvl_anum[QR_BVH_LEVELS];
     float   lvl_r2[QR_BVH_LEVELS];
     float   ray_c[3];
+    /* the owning context's fault word: QR_FAULT_* bits, x, y of the first
+     * pixel that set one, count of such pixels (NULL: not recorded) */
+    uint32_t *fault;
 };
 
 /* per-launch counters (instrumented runs only) */

@@ -159,3 +159,28 @@ def test_bvh_equals_linear_walk(qr, ctx, kind, seed, nq, w, h, fsaa, t, depth):
     lin.flags = qr.FP_LINEAR_WALK
     b = ctx.render_host(sid, lin)
     assert (a != b).sum() == 0
+
+
+def test_fault_word_clear_after_renders(qr, ctx):
+    """Valid scenes never run past the per-pixel loop bounds: after device
+    renders of every kind (Whitted at depth 10 with 4x AA, the animated scene,
+    the path tracer at depth 10) the context's fault word holds zeros."""
+    import torch
+    stream = torch.cuda.current_stream().cuda_stream
+    for kind, seed, nq, w, h, fsaa, depth, spp in [
+            (1, 2, 40, 160, 96, 2, 10, 0), (2, 3, 64, 192, 108, 2, 10, 0),
+            (3, 4, 32, 96, 54, 0, 10, 8)]:
+        g = qr.GenScene(kind, seed, nq, 0)
+        f = qr.Flat(g, w, h, fsaa)
+        desc, params = f.update(0, depth)
+        sid = ctx.upload(desc)
+        frame = torch.zeros((params.y_res, params.x_row), dtype=torch.int32, device="cuda")
+        if spp:
+            params.pt_on, params.pts_c, params.seed = spp, 0.0, 5
+            acc = torch.zeros((params.y_res, params.x_row, 3), dtype=torch.float32,
+                              device="cuda")
+            ctx.render_pt(sid, params, acc.data_ptr(), frame.data_ptr(), stream)
+        else:
+            ctx.render_device(sid, params, frame.data_ptr(), stream)
+        torch.cuda.synchronize()
+        assert ctx.fault() == (0, 0, 0, 0), (kind, seed)
