@@ -185,6 +185,10 @@ typedef struct qr_frame_params
 #define QR_FP_LINEAR_WALK   1   /* walk every surface list in order instead of
                                    the scene's bounding-volume hierarchy (the
                                    frame is the same; for tests) */
+#define QR_FP_PIXEL_THREADS 2   /* 4x AA: one thread traces all four
+                                   sub-samples of its pixel instead of one
+                                   thread a sub-sample (the frame is the
+                                   same; for tests) */
 
 typedef struct qr_ctx qr_ctx;
 

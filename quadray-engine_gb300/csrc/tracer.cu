@@ -1576,6 +1576,62 @@ whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
 }
 
 
+/*
+ * 4x AA frames with one thread per sub-sample.  The four sub-samples of a
+ * pixel are neighbouring lanes (lane = 4 * pixel + sub-sample), a warp
+ * covers 4 x 2 pixels and a block of 32 x 4 threads 8 x 4 pixels, so the
+ * lanes of a warp trace rays a fraction of a pixel apart and mostly take
+ * the same branches and nodes.  The AA average is formed with shuffles in
+ * the reference's pairing: p01 = c0 / 2 + c1 / 2 between lanes 0 and 1,
+ * p23 likewise, then p01 / 2 + p23 / 2 (the two operands of each sum are the
+ * same in both lanes and the sum commutes, so every lane holds the same
+ * bits).
+ */
+__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
+whitted_aa_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
+                  qr_dstats *gst)
+{
+    const int lane = threadIdx.x;
+    const int sub = lane & 3, pix = lane >> 2;
+    const int x = blockIdx.x * 8 + (threadIdx.y & 1) * 4 + (pix & 3);
+    const int y = blockIdx.y * 4 + (threadIdx.y >> 1) * 2 + (pix >> 2);
+    const int inside = x < P.x_res && y < P.y_res;
+#ifdef QR_STATS
+    TCnt cnt;
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
+    StP st = &cnt;
+#else
+    StP st = NULL;
+    (void)gst;
+#endif
+    float c[3] = {0.0f, 0.0f, 0.0f};
+    if (inside)
+    {
+        primary(S, P, x, y, (float)x + c_aa4_h[sub], (float)y + c_aa4_v[sub], c, st);
+        #pragma unroll
+        for (int k = 0; k < 3; k++) c[k] = clamp1(c[k]);
+    }
+    float col[3];
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        const float h = c[k] * 0.5f;
+        const float pr = h + __shfl_xor_sync(0xFFFFFFFFu, h, 1);
+        const float q = pr * 0.5f;
+        col[k] = q + __shfl_xor_sync(0xFFFFFFFFu, q, 2);
+    }
+    if (inside && sub == 0) frame[(size_t)y * P.x_row + x] = pack(P, col);
+#ifdef QR_STATS
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++)
+    {
+        const unsigned v = __reduce_add_sync(0xFFFFFFFFu, cnt.c[k]);
+        if (lane == 0 && v != 0) atomicAdd(&gst->c[k], (unsigned long long)v);
+    }
+#endif
+}
+
 /* ==== path tracer (the reference's RT_FEAT_PT estimator) ====================
  *
  * Per sample: a camera ray with a tent-filter jitter of +-0.5 pixel
@@ -2135,12 +2191,17 @@ cudaError_t qr_launch_whitted(const qr_dscene &sc, const qr_frame_params &fp,
 #endif
 {
     const dim3 block(32, 4);
+#ifndef QR_STATS
+    qr_dstats *dstats = NULL;
+#endif
+    if (fp.fsaa == 2 && !(fp.flags & QR_FP_PIXEL_THREADS))
+    {
+        const dim3 grid((fp.x_res + 7) / 8, (fp.y_res + 3) / 4);
+        QR_NS::whitted_aa_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, dstats);
+        return cudaGetLastError();
+    }
     const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
                     (fp.y_res + 2 * QR_TILE_H - 1) / (2 * QR_TILE_H));
-#ifdef QR_STATS
     QR_NS::whitted_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, dstats);
-#else
-    QR_NS::whitted_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, NULL);
-#endif
     return cudaGetLastError();
 }

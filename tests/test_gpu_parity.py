@@ -184,3 +184,19 @@ def test_fault_word_clear_after_renders(qr, ctx):
             ctx.render_device(sid, params, frame.data_ptr(), stream)
         torch.cuda.synchronize()
         assert ctx.fault() == (0, 0, 0, 0), (kind, seed)
+
+
+@pytest.mark.parametrize("kind,seed,nq,w,h,depth", [
+    (2, 4, 64, 203, 117, 4), (1, 6, 40, 161, 93, 10), (2, 5, 32, 7, 3, 10)])
+def test_aa_subsample_threads_equal_pixel_threads(qr, ctx, kind, seed, nq, w, h, depth):
+    """4x AA with a thread per sub-sample (shuffle average) gives the frame
+    of a thread per pixel, on ragged sizes too"""
+    g = qr.GenScene(kind, seed, nq, 0)
+    f = qr.Flat(g, w, h, 2)
+    desc, params = f.update(16, depth)
+    sid = ctx.upload(desc)
+    a = ctx.render_host(sid, params).copy()
+    pp = qr.QrFrameParams.from_buffer_copy(params)
+    pp.flags = qr.FP_PIXEL_THREADS
+    b = ctx.render_host(sid, pp)
+    assert (a != b).sum() == 0
