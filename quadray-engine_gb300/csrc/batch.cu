@@ -126,8 +126,12 @@ static int upload_jobs(qr_batch *b)
             j.P = r.fp;
             j.frame = r.dev_frame;
             j.acc = r.dev_acc;
-            j.tiles_x = (r.fp.x_res + b->tw - 1) / b->tw;
-            const int ty = (r.fp.y_res + b->th - 1) / b->th;
+            /* 4x AA Whitted requests: tiles of 4 x 2 pixels, a thread per
+             * sub-sample; otherwise tiles of tw x th pixels */
+            const int aa = !pt && r.fp.fsaa == 2 && !(r.fp.flags & QR_FP_PIXEL_THREADS);
+            const int tw = aa ? 4 : b->tw, th = aa ? 2 : b->th;
+            j.tiles_x = (r.fp.x_res + tw - 1) / tw;
+            const int ty = (r.fp.y_res + th - 1) / th;
             j.tile0 = tile;
             tile += j.tiles_x * ty;
             jobs.push_back(j);

@@ -1587,24 +1587,10 @@ whitted_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
  * same in both lanes and the sum commutes, so every lane holds the same
  * bits).
  */
-__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
-whitted_aa_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
-                  qr_dstats *gst)
+__device__ __forceinline__ void aa_subsample(const qr_dscene &S, const qr_frame_params &P,
+                                             int x, int y, int sub, uint32_t *frame, StP st)
 {
-    const int lane = threadIdx.x;
-    const int sub = lane & 3, pix = lane >> 2;
-    const int x = blockIdx.x * 8 + (threadIdx.y & 1) * 4 + (pix & 3);
-    const int y = blockIdx.y * 4 + (threadIdx.y >> 1) * 2 + (pix >> 2);
     const int inside = x < P.x_res && y < P.y_res;
-#ifdef QR_STATS
-    TCnt cnt;
-    #pragma unroll
-    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
-    StP st = &cnt;
-#else
-    StP st = NULL;
-    (void)gst;
-#endif
     float c[3] = {0.0f, 0.0f, 0.0f};
     if (inside)
     {
@@ -1622,6 +1608,26 @@ whitted_aa_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
         col[k] = q + __shfl_xor_sync(0xFFFFFFFFu, q, 2);
     }
     if (inside && sub == 0) frame[(size_t)y * P.x_row + x] = pack(P, col);
+}
+
+__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
+whitted_aa_kernel(const qr_dscene S, const qr_frame_params P, uint32_t *frame,
+                  qr_dstats *gst)
+{
+    const int lane = threadIdx.x;
+    const int sub = lane & 3, pix = lane >> 2;
+    const int x = blockIdx.x * 8 + (threadIdx.y & 1) * 4 + (pix & 3);
+    const int y = blockIdx.y * 4 + (threadIdx.y >> 1) * 2 + (pix >> 2);
+#ifdef QR_STATS
+    TCnt cnt;
+    #pragma unroll
+    for (int k = 0; k < QR_STAT_COUNT; k++) cnt.c[k] = 0;
+    StP st = &cnt;
+#else
+    StP st = NULL;
+    (void)gst;
+#endif
+    aa_subsample(S, P, x, y, sub, frame, st);
 #ifdef QR_STATS
     #pragma unroll
     for (int k = 0; k < QR_STAT_COUNT; k++)
@@ -2119,6 +2125,15 @@ batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter
             const qr_job *__restrict__ J = &jobs[lo];
             const int local = t - __ldg(&J->tile0);
             const int tx = __ldg(&J->tiles_x);
+            if (MODE == 0 && sP[wid].fsaa == 2 && !(sP[wid].flags & QR_FP_PIXEL_THREADS))
+            {
+                /* 4x AA: a tile is 4 x 2 pixels, a thread a sub-sample (the
+                 * whole warp takes part in the shuffle average) */
+                const int pix = lane >> 2;
+                aa_subsample(sS[wid], sP[wid], (local % tx) * 4 + (pix & 3),
+                             (local / tx) * 2 + (pix >> 2), lane & 3, J->frame, NULL);
+                continue;
+            }
             const int x = (local % tx) * tw + lane % tw;
             const int y = (local / tx) * th + lane / tw;
             if (x < sP[wid].x_res && y < sP[wid].y_res)
