@@ -34,13 +34,14 @@ class Request:
     """One frame request."""
 
     __slots__ = ("rid", "scene", "time", "w", "h", "spp", "arrival", "done",
-                 "frame", "acc", "slot", "bytes", "fp", "flat_key")
+                 "frame", "acc", "slot", "bytes", "fp", "flat_key", "prepared")
 
     def __init__(self, rid, scene, time_ms, w, h, spp, arrival):
         self.rid, self.scene, self.time = rid, scene, time_ms
         self.w, self.h, self.spp = w, h, spp
         self.arrival = arrival
         self.done = None
+        self.prepared = None
         self.frame = self.acc = None
         self.slot = None
         self.bytes = 0
@@ -75,6 +76,7 @@ class Server:
         self.ready = collections.deque()         # prepared, not launched
         self.inflight = collections.deque()      # (batch, [requests])
         self.completed = []
+        self.idle_sleep = 100e-6
 
     # ---- preparation --------------------------------------------------
     def _fsaa(self, req):
@@ -126,11 +128,13 @@ class Server:
                 req.slot = self.slots[req.scene].popleft()
             self.preparing.append(self.pool.submit(self._prepare, req))
 
-    def _collect_prepared(self):
+    def _collect_prepared(self, now_fn):
         keep = []
         for f in self.preparing:
             if f.done():
-                self.ready.append(f.result())
+                r = f.result()
+                r.prepared = now_fn()
+                self.ready.append(r)
             else:
                 keep.append(f)
         self.preparing = keep
@@ -173,10 +177,13 @@ class Server:
             self.free_batches.append(b)
 
     def step(self, now_fn):
+        """one turn of the loop; returns whether anything moved"""
+        n = len(self.completed) + len(self.waiting) + len(self.ready) + len(self.inflight)
         self._complete(now_fn)
         self._admit()
-        self._collect_prepared()
+        self._collect_prepared(now_fn)
         self._launch()
+        return n != len(self.completed) + len(self.waiting) + len(self.ready) + len(self.inflight)
 
     def busy(self):
         return bool(self.waiting or self.preparing or self.ready or self.inflight)
@@ -198,10 +205,18 @@ class Server:
             t = now()
             while pending and pending[0].arrival <= t:
                 self.waiting.append(pending.popleft())
-            self.step(now)
+            moved = self.step(now)
             if not keep_frames:
                 for r in self.completed:
                     r.frame = r.acc = None
+            if not moved:
+                # idle turn: sleep briefly (up to the next arrival) so that the
+                # preparation threads get the interpreter lock at once instead
+                # of after the interpreter's switch interval
+                wait = self.idle_sleep
+                if pending:
+                    wait = min(wait, max(0.0, pending[0].arrival - now()))
+                time.sleep(wait)
         done, self.completed = self.completed, []
         return done, now()
 
