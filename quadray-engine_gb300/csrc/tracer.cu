@@ -1512,6 +1512,11 @@ __device__ __forceinline__ int tile_y()
 #ifndef QR_MIN_BLOCKS
 #define QR_MIN_BLOCKS 6
 #endif
+/* the path tracer's own bound: 6 (80 registers) 66.5 ms, 8 (64) 67.9 ms
+ * on the 1280x720 16-spp frame with 64-byte pending-node records */
+#ifndef QR_PT_MIN_BLOCKS
+#define QR_PT_MIN_BLOCKS 6
+#endif
 
 /* one pixel of a Whitted frame: the camera ray, or the 4 sub-samples of
  * 4x AA combined in the reference's tree order, then clamp and pack */
@@ -1761,13 +1766,29 @@ __device__ __forceinline__ float pt_tent(float u)
 /* a shaded path-tracer hit with its children: 0 awaits the bounce, 1 may
  * spawn the refracted child, 2 awaits it, 3 may spawn the reflected child,
  * 4 awaits it */
+/* a shaded node of a path-tracer ray tree waiting for its children, in
+ * 16-byte fields that are written only when a later stage reads them:
+ *   a   stage 0: tex, l_dff (the diffuse child's weight); from stage 1 on:
+ *       the node's colour so far
+ *   b   emission (stage 0 only), c_trn
+ *   h   hit point, c_rfl            (a refracted or reflected child to come)
+ *   l   local hit point, bits       (always: stage, flags, side, depth)
+ *   n   refracted direction, record (a refracted child to come)
+ *   m   reflected direction, record (a reflected child to come) */
 struct PtPend
 {
-    float c[3], tex[3], emit[3];
-    float l_dff, c_trn, c_rfl;
-    float hit[3], loc[3], nw[3], rw[3];
-    int   srf, side, depth, stage, trn, rfl;
+    float4 a, b, h, l, n, m;
 };
+
+#define PT_TRN   8
+#define PT_RFL   16
+#define PT_SIDE  32
+
+__device__ __forceinline__ int pt_bits(const PtPend &p) { return __float_as_int(p.l.w); }
+__device__ __forceinline__ void pt_set_stage(PtPend &p, int stage)
+{
+    p.l.w = __int_as_float((pt_bits(p) & ~7) | stage);
+}
 
 /* shade a hit: normal, texel, the random draws (roulette, bounce, split)
  * and the children's weights; returns whether the bounce is taken (its
@@ -1829,25 +1850,23 @@ __device__ int pt_begin(const qr_dscene &S, const qr_frame_params &P, const Ray 
         }
     }
 
-    #pragma unroll
-    for (int k = 0; k < 3; k++)
-    {
-        p.c[k] = 0.0f;
-        p.tex[k] = tex[k];
-        p.emit[k] = __ldg(&m->emit[k]);
-        p.hit[k] = h.hit[k];
-        p.loc[k] = h.loc[k];
-        p.nw[k] = o.nw[k];
-        p.rw[k] = o.rw[k];
-    }
-    p.l_dff = __ldg(&m->l_dff);
-    p.c_trn = o.c_trn;
-    p.c_rfl = o.c_rfl;
-    p.srf = h.srf;
-    p.side = side;
-    p.depth = r.depth;
-    p.trn = o.trn;
-    p.rfl = o.rfl;
+    /* stage 0 waits for the diffuse child; without one the node starts
+     * with its emission and stage 1 folds nothing */
+    const float4 emit = make_float4(__ldg(&m->emit[0]), __ldg(&m->emit[1]),
+                                    __ldg(&m->emit[2]), o.c_trn);
+    if (dif)
+        p.a = make_float4(tex[0], tex[1], tex[2], __ldg(&m->l_dff));
+    else
+        p.a = make_float4(0.0f + emit.x, 0.0f + emit.y, 0.0f + emit.z, 0.0f);
+    if (dif || o.trn) p.b = emit;
+    const int spawn = (o.trn || o.rfl) && r.depth != 0;
+    if (spawn || o.rfl) p.h = make_float4(h.hit[0], h.hit[1], h.hit[2], o.c_rfl);
+    p.l = make_float4(h.loc[0], h.loc[1], h.loc[2],
+                      __int_as_float((dif ? 0 : 1) | (o.trn ? PT_TRN : 0) |
+                                     (o.rfl ? PT_RFL : 0) | (side ? PT_SIDE : 0) |
+                                     (r.depth << 8)));
+    if (spawn && o.trn) p.n = make_float4(o.nw[0], o.nw[1], o.nw[2], __int_as_float(h.srf));
+    if (spawn && o.rfl) p.m = make_float4(o.rw[0], o.rw[1], o.rw[2], __int_as_float(h.srf));
     return dif;
 }
 
@@ -1857,73 +1876,85 @@ __device__ int pt_begin(const qr_dscene &S, const qr_frame_params &P, const Ray 
 __device__ int pt_advance(const qr_dscene &S, PtPend &p, float ret[3], Ray &r,
                           int &off, int &num, StP st)
 {
-    const qr_srf *__restrict__ s = &S.srf[p.srf];
-    if (p.stage == 0)
+    const int bits = pt_bits(p);
+    int stage = bits & 7;
+    const int side = (bits & PT_SIDE) ? 1 : 0, depth = bits >> 8;
+    float4 c = p.a;
+    if (stage == 0)
     {
-        #pragma unroll
-        for (int k = 0; k < 3; k++)
-        {
-            float c = ret[k] * p.l_dff;
-            c = c * p.tex[k];
-            p.c[k] = c + p.emit[k];
-        }
-        p.stage = 1;
+        const float4 e = p.b;
+        float t;
+        t = ret[0] * c.w; c.x = t * c.x; c.x = c.x + e.x;
+        t = ret[1] * c.w; c.y = t * c.y; c.y = c.y + e.y;
+        t = ret[2] * c.w; c.z = t * c.z; c.z = c.z + e.z;
+        stage = 1;
     }
-    if (p.stage == 1)
+    if (stage == 1)
     {
-        if (p.trn)
+        if (bits & PT_TRN)
         {
-            if (p.depth != 0)
+            if (depth != 0)
             {
+                const float4 hh = p.h, n = p.n;
+                const int srf = __float_as_int(n.w);
+                const qr_srf *__restrict__ s = &S.srf[srf];
+                const float hit[3] = {hh.x, hh.y, hh.z}, dir[3] = {n.x, n.y, n.z};
+                const float4 l = p.l;
+                const float loc[3] = {l.x, l.y, l.z};
                 CNT(QR_STAT_RAY_SECONDARY);
-                child_ray(r, p.hit, p.nw, p.loc, p.srf, p.side | FLAG_PASS, p.depth - 1);
-                off = __ldg(&s->sec_off[1 - p.side]);
-                num = __ldg(&s->sec_num[1 - p.side]);
-                p.stage = 2;
+                child_ray(r, hit, dir, loc, srf, side | FLAG_PASS, depth - 1);
+                off = __ldg(&s->sec_off[1 - side]);
+                num = __ldg(&s->sec_num[1 - side]);
+                c.w = 0.0f;
+                p.a = c;
+                pt_set_stage(p, 2);
                 return 1;
             }
-            #pragma unroll
-            for (int k = 0; k < 3; k++) p.c[k] = 0.0f + p.c[k];
+            c.x = 0.0f + c.x; c.y = 0.0f + c.y; c.z = 0.0f + c.z;
         }
-        p.stage = 3;
+        stage = 3;
     }
-    else if (p.stage == 2)
+    else if (stage == 2)
     {
-        #pragma unroll
-        for (int k = 0; k < 3; k++)
-        {
-            const float tc = ret[k] * p.c_trn;
-            p.c[k] = tc + p.c[k];
-        }
-        p.stage = 3;
+        const float ct = p.b.w;
+        float t;
+        t = ret[0] * ct; c.x = t + c.x;
+        t = ret[1] * ct; c.y = t + c.y;
+        t = ret[2] * ct; c.z = t + c.z;
+        stage = 3;
     }
-    if (p.stage == 3)
+    if (stage == 3)
     {
-        if (p.rfl)
+        if (bits & PT_RFL)
         {
-            if (p.depth != 0)
+            if (depth != 0)
             {
+                const float4 hh = p.h, m = p.m;
+                const int srf = __float_as_int(m.w);
+                const qr_srf *__restrict__ s = &S.srf[srf];
+                const float hit[3] = {hh.x, hh.y, hh.z}, dir[3] = {m.x, m.y, m.z};
+                const float4 l = p.l;
+                const float loc[3] = {l.x, l.y, l.z};
                 CNT(QR_STAT_RAY_SECONDARY);
-                child_ray(r, p.hit, p.rw, p.loc, p.srf, p.side, p.depth - 1);
-                off = __ldg(&s->sec_off[p.side]);
-                num = __ldg(&s->sec_num[p.side]);
-                p.stage = 4;
+                child_ray(r, hit, dir, loc, srf, side, depth - 1);
+                off = __ldg(&s->sec_off[side]);
+                num = __ldg(&s->sec_num[side]);
+                c.w = 0.0f;
+                p.a = c;
+                pt_set_stage(p, 4);
                 return 1;
             }
-            #pragma unroll
-            for (int k = 0; k < 3; k++) p.c[k] = 0.0f + p.c[k];
+            c.x = 0.0f + c.x; c.y = 0.0f + c.y; c.z = 0.0f + c.z;
         }
-        #pragma unroll
-        for (int k = 0; k < 3; k++) ret[k] = p.c[k];
+        ret[0] = c.x; ret[1] = c.y; ret[2] = c.z;
         return 0;
     }
-    #pragma unroll
-    for (int k = 0; k < 3; k++)
-    {
-        const float rc = ret[k] * p.c_rfl;
-        p.c[k] = rc + p.c[k];
-        ret[k] = p.c[k];
-    }
+    /* stage 4: the reflected child's colour */
+    const float cr = p.h.w;
+    float t;
+    t = ret[0] * cr; ret[0] = t + c.x;
+    t = ret[1] * cr; ret[1] = t + c.y;
+    t = ret[2] * cr; ret[2] = t + c.z;
     return 0;
 }
 
@@ -1971,21 +2002,16 @@ __device__ void trace_pt(const qr_dscene &S, const qr_frame_params &P, Ray r,
             CNT(QR_STAT_SHADE);
             PtPend &p = stk[sp++];
             float ddir[3];
-            if (pt_begin(S, P, r, w.best, p, g, ddir, st))
+            const Hit hb = w.best;
+            if (pt_begin(S, P, r, hb, p, g, ddir, st))
             {
-                const qr_srf *__restrict__ s = &S.srf[p.srf];
-                p.stage = 0;
+                const qr_srf *__restrict__ s = &S.srf[hb.srf];
                 CNT(QR_STAT_RAY_SECONDARY);
-                child_ray(r, p.hit, ddir, p.loc, p.srf, p.side, p.depth - 1);
-                off = __ldg(&s->sec_off[p.side]);
-                num = __ldg(&s->sec_num[p.side]);
+                child_ray(r, hb.hit, ddir, hb.loc, hb.srf, hb.side, r.depth - 1);
+                off = __ldg(&s->sec_off[hb.side]);
+                num = __ldg(&s->sec_num[hb.side]);
                 continue;
             }
-            /* no bounce: the node starts with its emission, and stage 1
-             * folds nothing */
-            #pragma unroll
-            for (int k = 0; k < 3; k++) p.c[k] = p.c[k] + p.emit[k];
-            p.stage = 1;
         }
 
         int spawned = 0;
@@ -2043,7 +2069,7 @@ __device__ __forceinline__ void pt_pixel(const qr_dscene &S, const qr_frame_para
     frame[(size_t)y * P.x_row + x] = pack(P, mean);
 }
 
-__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
+__global__ void __launch_bounds__(128, QR_PT_MIN_BLOCKS)
 pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *frame,
           qr_dstats *gst)
 {
@@ -2083,7 +2109,7 @@ pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *fram
  * path tracer), so each keeps only its own code.
  */
 template <int MODE>
-__global__ void __launch_bounds__(128, QR_MIN_BLOCKS)
+__global__ void __launch_bounds__(128, MODE == 0 ? QR_MIN_BLOCKS : QR_PT_MIN_BLOCKS)
 batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter,
              int tw, int th, int grab)
 {
