@@ -413,6 +413,11 @@ int build_node(std::vector<Prim> &p, int lo, int hi, int depth, qr_accel_host *o
         nd.a = (int)out->items.size();
         nd.count = n;
         for (int i = lo; i < hi; i++) out->items.push_back(p[i].it);
+        /* items under one transform node next to each other, so the walk
+         * transforms the ray once for them (ties between hits are decided
+         * by list position, not by the order of the items) */
+        std::stable_sort(out->items.begin() + nd.a, out->items.end(),
+                         [](const qr_bitem &u, const qr_bitem &v) { return u.xf < v.xf; });
         out->nodes[idx] = nd;
         return idx;
     }

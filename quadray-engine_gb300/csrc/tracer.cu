@@ -536,8 +536,8 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
     float cdff[3] = {0.0f, 0.0f, 0.0f}, cray[3] = {0.0f, 0.0f, 0.0f};
     /* hierarchy source */
     int ai = 0, ia = 0, ib = 0, sp = 0;
-    int stk[QR_BVH_STACK];
-    float stt[QR_BVH_STACK];
+    int2 stk[QR_BVH_STACK];         /* node, entry distance (float bits) */
+    int cur = -1;                   /* node to visit next without a pop */
     float inv[3];
     int aend = 0;
     if (use_bvh)
@@ -550,9 +550,8 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
         float tn;
         if (box_hit(&S.nodes[root], r, inv, w.tbuf, tn, st))
         {
-            stk[0] = root;
-            stt[0] = tn;
-            sp = 1;
+            (void)tn;
+            cur = root;
         }
     }
 
@@ -604,14 +603,25 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
             }
             else
             {
+                /* near child first: it is visited at once, the far one
+                 * pushed with its entry distance and skipped on the pop
+                 * if a hit nearer than that has been found meanwhile */
                 #pragma unroll 1
-                while (ia >= ib && sp > 0)
+                while (ia >= ib)
                 {
-                    /* the pop below and up to two pushes */
-                    if (sp >= QR_BVH_STACK) { w.fault = QR_FAULT_STACK; return; }
-                    --sp;
-                    if (stt[sp] > w.tbuf) continue;
-                    const qr_bnode *__restrict__ n = &S.nodes[stk[sp]];
+                    int node = cur;
+                    if (node >= 0)
+                    {
+                        cur = -1;
+                    }
+                    else
+                    {
+                        if (sp <= 0) break;
+                        const int2 e = stk[--sp];
+                        if (__int_as_float(e.y) > w.tbuf) continue;
+                        node = e.x;
+                    }
+                    const qr_bnode *__restrict__ n = &S.nodes[node];
                     const int cnt = __ldg(&n->count);
                     const int a = __ldg(&n->a);
                     if (cnt > 0)
@@ -626,12 +636,13 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
                     const int hb = box_hit(&S.nodes[b], r, inv, w.tbuf, tb, st);
                     if (ha && hb)
                     {
+                        if (sp >= QR_BVH_STACK) { w.fault = QR_FAULT_STACK; return; }
                         const int near_a = ta <= tb;
-                        stk[sp] = near_a ? b : a; stt[sp] = near_a ? tb : ta; sp++;
-                        stk[sp] = near_a ? a : b; stt[sp] = near_a ? ta : tb; sp++;
+                        stk[sp++] = make_int2(near_a ? b : a, __float_as_int(near_a ? tb : ta));
+                        cur = near_a ? a : b;
                     }
-                    else if (ha) { stk[sp] = a; stt[sp] = ta; sp++; }
-                    else if (hb) { stk[sp] = b; stt[sp] = tb; sp++; }
+                    else if (ha) cur = a;
+                    else if (hb) cur = b;
                 }
                 if (ia >= ib) break;
                 it = &S.items[ia++];
