@@ -188,6 +188,7 @@ def run_batch(args, wl, rank, world, dist, local):
     spec = batch_requests(wl["batch"], wl["seed"])
     keep, reqs, bufs = [], [], []
     rays = 0
+    req_rays = []
     for i, rq in enumerate(spec):
         g = qr.GenScene(rq["kind"], rq["seed"], rq["nq"], 0)
         f = qr.Flat(g, rq["w"], rq["h"], 0)
@@ -210,7 +211,8 @@ def run_batch(args, wl, rank, world, dist, local):
         rc = qr.lib().qr_render_stats(ctx.h, sid, ctypes.byref(r.fp),
                                       host.ctypes.data_as(ctypes.c_void_p), counts)
         assert rc == 0, ctx.error()
-        rays += int(counts[0]) + int(counts[1]) + int(counts[2])
+        req_rays.append(int(counts[0]) + int(counts[1]) + int(counts[2]))
+        rays += req_rays[-1]
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
 
@@ -252,6 +254,36 @@ def run_batch(args, wl, rank, world, dist, local):
     ms = [a.elapsed_time(c) for a, c in ev]
     value, t_total = whole_job(rays, args.steps, sum(ms) / 1000.0, dist, "cuda")
 
+    # each class alone (Whitted requests, path-traced requests): one batch
+    # against one launch per request, device time of one pass after a warm-up
+    classes = {}
+    for name, pick in (("whitted", lambda r: not r.fp.pt_on), ("path_traced", lambda r: r.fp.pt_on)):
+        idx = [i for i, r in enumerate(reqs) if pick(r)]
+        sub = [reqs[i] for i in idx]
+        bc = qr.Batch(ctx, len(sub))
+        bc.config(tw, grab)
+        bc.set(sub)
+        bc.launch(sp)
+        torch.cuda.synchronize()
+        c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        c0.record(stream)
+        bc.launch(sp)
+        c1.record(stream)
+        for i in idx:
+            r, (fr, acc) = reqs[i], bufs[i]
+            if r.fp.pt_on:
+                ctx.render_pt(r.scene_id, r.fp, acc.data_ptr(), fr.data_ptr(), sp)
+            else:
+                ctx.render_device(r.scene_id, r.fp, fr.data_ptr(), sp)
+        c2.record(stream)
+        torch.cuda.synchronize()
+        bc.close()
+        crays = sum(req_rays[i] for i in idx)
+        tb, tf = c0.elapsed_time(c1) / 1000.0, c1.elapsed_time(c2) / 1000.0
+        classes[name] = {"requests": len(idx), "rays": crays,
+                         "batch_rays_per_s": crays / tb, "per_frame_rays_per_s": crays / tf,
+                         "batch_over_per_frame": tf / tb}
+
     # end to end: request table in, batch, every frame out to pinned memory
     hosts = [torch.empty(fr.shape, dtype=torch.int32, pin_memory=True) for fr, _ in bufs]
     d2h = sum(h.numel() * 4 for h in hosts)
@@ -274,6 +306,7 @@ def run_batch(args, wl, rank, world, dist, local):
         "ms_per_step": 1000.0 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
+        "classes": classes,
         "config": {"workload": "batch", "requests": len(reqs),
                    "whitted": sum(1 for q in spec if not q["spp"]),
                    "path_traced": sum(1 for q in spec if q["spp"]),
