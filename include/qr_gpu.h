@@ -306,6 +306,14 @@ int qr_batch_launch(qr_batch *b, void *stream);
 /* QR_OK once the last launch finished, QR_ERR_BUSY while it runs */
 int qr_batch_poll(qr_batch *b);
 int qr_batch_wait(qr_batch *b);
+/* per-request completion of the last launch: *flags points at one word per
+ * request (in qr_batch_set order) in host memory that the device writes;
+ * a word turns 1 once that request's frame is complete in device memory,
+ * while the rest of the batch may still run.  qr_batch_launch clears the
+ * words, so when they are read, launch again only after the previous launch
+ * finished (qr_batch_poll / qr_batch_wait); read them as volatile.  No
+ * counterpart in the reference (it renders one frame per call) */
+int qr_batch_done(qr_batch *b, const volatile uint32_t **flags);
 
 #ifdef __cplusplus
 }

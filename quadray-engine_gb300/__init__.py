@@ -130,6 +130,7 @@ def lib():
                                     ctypes.POINTER(ctypes.c_float)]
         L.qr_batch_launch.argtypes = [vp, vp]
         L.qr_batch_poll.argtypes = [vp]
+        L.qr_batch_done.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p)]
         L.qr_batch_wait.argtypes = [vp]
         L.qr_sync.argtypes = [vp, vp]
         L.qr_fault.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
@@ -306,6 +307,14 @@ class Batch:
 
     def wait(self):
         self._check(lib().qr_batch_wait(self.h), "qr_batch_wait")
+
+    def done_flags(self, n):
+        """the per-request completion words of the last launch (n of them,
+        1 = that request's frame is complete); a live view of host memory
+        the device writes"""
+        p = ctypes.c_void_p()
+        self._check(lib().qr_batch_done(self.h, ctypes.byref(p)), "qr_batch_done")
+        return (ctypes.c_uint32 * n).from_address(p.value)
 
     def close(self):
         if self.h:

@@ -11,6 +11,11 @@
  * launch until the requests or the tile configuration change.  The tile
  * shape and the tiles a warp claims at once come from qr_batch_tune, which
  * times each configuration on the batch itself and keeps the fastest.
+ *
+ * Completion per request: the warp that finishes a request's last tile sets
+ * the request's flag in host memory mapped into the device
+ * (qr_batch_done), so a caller can take each frame as soon as it is ready
+ * instead of when the whole batch is.
  */
 #include <cuda_runtime.h>
 #include <stdio.h>
@@ -34,6 +39,10 @@ struct qr_batch
     int          max;
     qr_job      *djobs;         /* Whitted jobs, then path-tracer jobs */
     int         *dcount;        /* claim counters of the two kernels */
+    int         *dtiles;        /* finished tiles per job */
+    uint32_t    *hdone;         /* per request: 1 once its frame is done
+                                   (mapped host memory) */
+    uint32_t    *ddone;         /* its device address */
     std::vector<qr_request> reqs;
     int          nw, np;        /* jobs per mode */
     int          tiles[2];      /* tiles per mode */
@@ -67,6 +76,12 @@ extern "C" int qr_batch_create(qr_ctx *ctx, int max_requests, qr_batch **out)
     cudaError_t e = cudaSetDevice(b->device);
     if (e == cudaSuccess) e = cudaMalloc(&b->djobs, sizeof(qr_job) * (size_t)max_requests);
     if (e == cudaSuccess) e = cudaMalloc(&b->dcount, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dtiles, sizeof(int) * (size_t)max_requests);
+    if (e == cudaSuccess)
+        e = cudaHostAlloc((void **)&b->hdone, sizeof(uint32_t) * (size_t)max_requests,
+                          cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&b->ddone, b->hdone, 0);
+    if (e == cudaSuccess) memset(b->hdone, 0, sizeof(uint32_t) * (size_t)max_requests);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
@@ -95,6 +110,8 @@ extern "C" int qr_batch_destroy(qr_batch *b)
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->djobs) cudaFree(b->djobs);
     if (b->dcount) cudaFree(b->dcount);
+    if (b->dtiles) cudaFree(b->dtiles);
+    if (b->hdone) cudaFreeHost(b->hdone);
     if (b->main) cudaStreamDestroy(b->main);
     if (b->side) cudaStreamDestroy(b->side);
     if (b->fork) cudaEventDestroy(b->fork);
@@ -133,7 +150,9 @@ static int upload_jobs(qr_batch *b)
             j.tiles_x = (r.fp.x_res + tw - 1) / tw;
             const int ty = (r.fp.y_res + th - 1) / th;
             j.tile0 = tile;
-            tile += j.tiles_x * ty;
+            j.ntiles = j.tiles_x * ty;
+            j.req = (int)i;
+            tile += j.ntiles;
             jobs.push_back(j);
         }
         b->tiles[pass] = tile;
@@ -193,14 +212,17 @@ extern "C" int qr_batch_config(qr_batch *b, int tile_w, int grab)
 static cudaError_t enqueue(qr_batch *b)
 {
     cudaError_t e = cudaMemsetAsync(b->dcount, 0, 2 * sizeof(int), b->main);
+    if (e == cudaSuccess && b->nw + b->np > 0)
+        e = cudaMemsetAsync(b->dtiles, 0, sizeof(int) * (size_t)(b->nw + b->np), b->main);
     if (e == cudaSuccess) e = cudaEventRecord(b->fork, b->main);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork, 0);
     if (e == cudaSuccess)
         e = qr_launch_batch(0, b->djobs, b->nw, b->tiles[0], b->dcount, b->tw, b->th,
-                            b->grab, b->blocks[0], b->main);
+                            b->grab, b->blocks[0], b->dtiles, b->ddone, b->main);
     if (e == cudaSuccess)
         e = qr_launch_batch(1, b->djobs + b->nw, b->np, b->tiles[1], b->dcount + 1,
-                            b->tw, b->th, b->grab, b->blocks[1], b->side);
+                            b->tw, b->th, b->grab, b->blocks[1], b->dtiles + b->nw,
+                            b->ddone, b->side);
     if (e == cudaSuccess) e = cudaEventRecord(b->join, b->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->main, b->join, 0);
     return e;
@@ -226,6 +248,9 @@ extern "C" int qr_batch_launch(qr_batch *b, void *stream)
         if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch graph capture", e);
         b->graph_ok = 1;
     }
+    /* the previous launch has finished (the caller polled or waited): clear
+     * the completion flags before the graph can set them */
+    memset(b->hdone, 0, sizeof(uint32_t) * b->reqs.size());
     e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
     if (e == cudaSuccess) e = cudaEventRecord(b->done, (cudaStream_t)stream);
     if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch graph launch", e);
@@ -241,6 +266,13 @@ extern "C" int qr_batch_poll(qr_batch *b)
     if (e == cudaSuccess) return QR_OK;
     if (e == cudaErrorNotReady) return QR_ERR_BUSY;
     return bfail(b, QR_ERR_CUDA, "batch poll", e);
+}
+
+extern "C" int qr_batch_done(qr_batch *b, const volatile uint32_t **flags)
+{
+    if (b == NULL || flags == NULL) return QR_ERR_ARG;
+    *flags = b->hdone;
+    return QR_OK;
 }
 
 extern "C" int qr_batch_wait(qr_batch *b)

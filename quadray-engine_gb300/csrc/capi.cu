@@ -226,11 +226,15 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaSetDevice", e);
     if (fresh || sl.bytes < total)
     {
+        /* a quarter of headroom: the hierarchy of an animated scene changes
+         * size from frame to frame, and replacing the block (cudaFree waits
+         * for all work on the device) would stall in-place updates */
+        const size_t cap = (total + total / 4 + 65535) & ~(size_t)65535;
         if (!fresh && sl.block) cudaFree(sl.block);
         sl.block = NULL;
-        e = cudaMalloc(&sl.block, total);
+        e = cudaMalloc(&sl.block, cap);
         if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaMalloc scene", e);
-        sl.bytes = total;
+        sl.bytes = cap;
     }
     e = cudaMemcpyAsync(sl.block, h.data(), total, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);

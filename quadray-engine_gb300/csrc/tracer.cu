@@ -2122,7 +2122,7 @@ pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *fram
 template <int MODE>
 __global__ void __launch_bounds__(128, MODE == 0 ? QR_MIN_BLOCKS : QR_PT_MIN_BLOCKS)
 batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter,
-             int tw, int th, int grab)
+             int tw, int th, int grab, int *tiles_done, uint32_t *done)
 {
     __shared__ qr_dscene sS[4];
     __shared__ qr_frame_params sP[4];
@@ -2169,16 +2169,32 @@ batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter
                 const int pix = lane >> 2;
                 aa_subsample(sS[wid], sP[wid], (local % tx) * 4 + (pix & 3),
                              (local / tx) * 2 + (pix >> 2), lane & 3, J->frame, NULL);
-                continue;
             }
-            const int x = (local % tx) * tw + lane % tw;
-            const int y = (local / tx) * th + lane / tw;
-            if (x < sP[wid].x_res && y < sP[wid].y_res)
+            else
             {
-                if (MODE == 0)
-                    whitted_pixel(sS[wid], sP[wid], x, y, J->frame, NULL);
-                else
-                    pt_pixel(sS[wid], sP[wid], x, y, J->acc, J->frame, NULL);
+                const int x = (local % tx) * tw + lane % tw;
+                const int y = (local / tx) * th + lane / tw;
+                if (x < sP[wid].x_res && y < sP[wid].y_res)
+                {
+                    if (MODE == 0)
+                        whitted_pixel(sS[wid], sP[wid], x, y, J->frame, NULL);
+                    else
+                        pt_pixel(sS[wid], sP[wid], x, y, J->acc, J->frame, NULL);
+                }
+            }
+            /* the tile's pixels are written (the warp barrier orders the
+             * lanes' stores before lane 0's fence): count the tile; the
+             * warp with the request's last tile publishes its completion */
+            __syncwarp();
+            if (lane == 0)
+            {
+                __threadfence();
+                const int d = atomicAdd(&tiles_done[lo], 1) + 1;
+                if (d == __ldg(&J->ntiles))
+                {
+                    __threadfence_system();
+                    *(volatile uint32_t *)&done[__ldg(&J->req)] = 1u;
+                }
             }
         }
     }
@@ -2190,16 +2206,18 @@ batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter
 #ifndef QR_STATS
 cudaError_t qr_launch_batch(int mode, const qr_job *jobs, int njobs, int total_tiles,
                             int *counter, int tw, int th, int grab, int blocks,
-                            cudaStream_t stream)
+                            int *tiles_done, uint32_t *done, cudaStream_t stream)
 {
     if (njobs <= 0 || total_tiles <= 0) return cudaSuccess;
     const dim3 block(32, 4);
     if (mode == 0)
         QR_NS::batch_kernel<0><<<blocks, block, 0, stream>>>(jobs, njobs, total_tiles,
-                                                            counter, tw, th, grab);
+                                                            counter, tw, th, grab,
+                                                            tiles_done, done);
     else
         QR_NS::batch_kernel<1><<<blocks, block, 0, stream>>>(jobs, njobs, total_tiles,
-                                                            counter, tw, th, grab);
+                                                            counter, tw, th, grab,
+                                                            tiles_done, done);
     return cudaGetLastError();
 }
 

@@ -76,14 +76,18 @@ struct qr_job
     qr_frame_params P;
     uint32_t       *frame;
     float          *acc;
-    int32_t         tile0, tiles_x, pad[2];
+    int32_t         tile0, tiles_x;
+    int32_t         ntiles;         /* tiles of the request */
+    int32_t         req;            /* its index in the batch */
 };
 
 /* persistent launch over the tiles of njobs requests of one mode (0
- * Whitted, 1 path tracer); *counter must hold 0 */
+ * Whitted, 1 path tracer); *counter and tiles_done[0, njobs) must hold 0.
+ * The warp that finishes a request's last tile sets done[req] to 1 (done
+ * may be host memory mapped into the device) */
 cudaError_t qr_launch_batch(int mode, const qr_job *jobs, int njobs, int total_tiles,
                             int *counter, int tw, int th, int grab, int blocks,
-                            cudaStream_t stream);
+                            int *tiles_done, uint32_t *done, cudaStream_t stream);
 /* resident blocks of 128 threads per SM of the batch kernel of a mode */
 int qr_batch_blocks_per_sm(int mode);
 

@@ -17,9 +17,12 @@ many clients from one GPU:
 * continuous batching: prepared requests go into the next batched launch
   (qr_batch_*), two batches in flight so the GPU never waits for the host;
   requests that arrive while a batch runs join the following one;
+* a request completes when its own frame does (the batch's per-request
+  completion words), not when its whole batch does;
 * every frame equals the frame of the same request rendered alone.
 
-Latency is arrival to completion (the batch's end, seen by polling).
+Latency is arrival to completion (the request's completion word, seen by
+polling).
 """
 import collections
 import ctypes
@@ -53,9 +56,11 @@ class Server:
     """Continuous-batching frame server over one context."""
 
     def __init__(self, qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
-                 max_batch_pixels=24 << 20, prep_threads=4):
+                 max_batch_pixels=24 << 20, prep_threads=4, per_request=True):
         """scenes: list of dicts with keys gen (a GenScene), pt (path-traced
-        scene) and depth"""
+        scene) and depth; per_request: complete each request when its frame
+        is done (else when its batch is)"""
+        self.per_request = per_request
         import torch
         self.qr, self.ctx, self.torch = qr, ctx, torch
         self.scenes = scenes
@@ -163,17 +168,32 @@ class Server:
             b = self.free_batches.popleft()
             b.set(table)
             b.launch(self.stream.cuda_stream)
-            self.inflight.append((b, reqs))
+            flags = np.frombuffer(b.done_flags(len(reqs)), dtype=np.uint32)
+            self.inflight.append((b, reqs, flags))
+
+    def _finish(self, r, t):
+        r.done = t
+        self.used -= r.bytes
+        self.slots[r.scene].append(r.slot)
+        self.completed.append(r)
 
     def _complete(self, now_fn):
+        # each request completes when its own frame is done (the batch's
+        # per-request completion words), its batch is recycled when all are
+        t = None
+        for b, reqs, flags in (self.inflight if self.per_request else ()):
+            for i in np.flatnonzero(flags.copy()):    # a snapshot: the device
+                                                      # writes the words live
+                r = reqs[i]
+                if r.done is None:
+                    if t is None:
+                        t = now_fn()
+                    self._finish(r, t)
         while self.inflight and self.inflight[0][0].poll():
-            b, reqs = self.inflight.popleft()
-            t = now_fn()
+            b, reqs, flags = self.inflight.popleft()
             for r in reqs:
-                r.done = t
-                self.used -= r.bytes
-                self.slots[r.scene].append(r.slot)
-                self.completed.append(r)
+                if r.done is None:
+                    self._finish(r, now_fn())
             self.free_batches.append(b)
 
     def step(self, now_fn):

@@ -90,3 +90,56 @@ def test_batch_rejects_bad_requests(qr):
         b.set([r, r, r])
     b.close()
     ctx.close()
+
+
+def test_request_completion_flags(qr):
+    """A request's completion word turns 1 once its frame is complete, while
+    the rest of the batch may still run: the first request (a small Whitted
+    frame) is read back as soon as its word is set, on another stream than
+    the batch's, and must equal the frame rendered alone; after the batch
+    every word is 1 and every frame equals its frame alone."""
+    import time
+    import torch
+    ctx = qr.Context(0)
+    cases = [(1, 21, 16, 64, 48, 0, 4, 0)] + [(3, 22 + i, 32, 320, 240, 0, 8, 64)
+                                             for i in range(3)]
+    reqs, keep, bufs = [], [], []
+    for i, (kind, seed, nq, w, h, fsaa, depth, spp) in enumerate(cases):
+        g = qr.GenScene(kind, seed, nq, 0)
+        f = qr.Flat(g, w, h, fsaa)
+        desc, params = f.update(0, depth)
+        sid = ctx.upload(desc)
+        keep.append((g, f))
+        r = qr.QrRequest()
+        r.scene_id = sid
+        r.fp = params
+        r.fp.pt_on, r.fp.pts_c, r.fp.seed, r.fp.frame_idx = spp, 0.0, 300 + i, 0
+        fr = torch.zeros((h, params.x_row), dtype=torch.int32, device="cuda")
+        acc = torch.zeros((h, params.x_row, 3), dtype=torch.float32, device="cuda")
+        r.dev_frame = fr.data_ptr()
+        r.dev_acc = acc.data_ptr() if spp else None
+        bufs.append((fr, acc))
+        reqs.append(r)
+    alone = [ctx.render_host(r.scene_id, r.fp).copy() for r in reqs]
+    torch.cuda.synchronize()
+    b = qr.Batch(ctx, len(reqs))
+    b.set(reqs)
+    side = torch.cuda.Stream()
+    b.launch(side.cuda_stream)
+    flags = b.done_flags(len(reqs))
+    t_end = time.monotonic() + 120.0
+    while flags[0] != 1 and time.monotonic() < t_end:
+        time.sleep(0.0002)
+    assert flags[0] == 1
+    other = torch.cuda.Stream()
+    with torch.cuda.stream(other):
+        early = bufs[0][0].to("cpu", non_blocking=False)
+    got = early.numpy().view(np.uint32)[:, :reqs[0].fp.x_res]
+    assert (got != alone[0]).sum() == 0
+    b.wait()
+    assert list(flags) == [1] * len(reqs)
+    for i, (fr, _) in enumerate(bufs):
+        got = fr.cpu().numpy().view(np.uint32)[:, :reqs[i].fp.x_res]
+        assert (got != alone[i]).sum() == 0, i
+    b.close()
+    ctx.close()
