@@ -188,7 +188,8 @@ typedef struct qr_frame_params
 #define QR_FP_PIXEL_THREADS 2   /* 4x AA: one thread traces all four
                                    sub-samples of its pixel instead of one
                                    thread a sub-sample (the frame is the
-                                   same; for tests) */
+                                   same; for tests; single-frame renders
+                                   only, batches ignore it) */
 
 typedef struct qr_ctx qr_ctx;
 

@@ -145,7 +145,7 @@ static int upload_jobs(qr_batch *b)
             j.acc = r.dev_acc;
             /* 4x AA Whitted requests: tiles of 4 x 2 pixels, a thread per
              * sub-sample; otherwise tiles of tw x th pixels */
-            const int aa = !pt && r.fp.fsaa == 2 && !(r.fp.flags & QR_FP_PIXEL_THREADS);
+            const int aa = !pt && r.fp.fsaa == 2;
             const int tw = aa ? 4 : b->tw, th = aa ? 2 : b->th;
             j.tiles_x = (r.fp.x_res + tw - 1) / tw;
             const int ty = (r.fp.y_res + th - 1) / th;

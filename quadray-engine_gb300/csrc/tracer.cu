@@ -2162,25 +2162,48 @@ batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter
             const qr_job *__restrict__ J = &jobs[lo];
             const int local = t - __ldg(&J->tile0);
             const int tx = __ldg(&J->tiles_x);
-            if (MODE == 0 && sP[wid].fsaa == 2 && !(sP[wid].flags & QR_FP_PIXEL_THREADS))
+            /* 4x AA requests: a tile is 4 x 2 pixels and a thread a
+             * sub-sample (the whole warp takes part in the shuffle
+             * average); otherwise a tile is tw x th pixels, a thread a
+             * pixel.  One camera-ray call site serves both. */
+            const int aa = MODE == 0 && sP[wid].fsaa == 2;
+            const int pix = lane >> 2, sub = lane & 3;
+            const int x = aa ? (local % tx) * 4 + (pix & 3) : (local % tx) * tw + lane % tw;
+            const int y = aa ? (local / tx) * 2 + (pix >> 2) : (local / tx) * th + lane / tw;
+            const int inside = x < sP[wid].x_res && y < sP[wid].y_res;
+            if (MODE == 0)
             {
-                /* 4x AA: a tile is 4 x 2 pixels, a thread a sub-sample (the
-                 * whole warp takes part in the shuffle average) */
-                const int pix = lane >> 2;
-                aa_subsample(sS[wid], sP[wid], (local % tx) * 4 + (pix & 3),
-                             (local / tx) * 2 + (pix >> 2), lane & 3, J->frame, NULL);
-            }
-            else
-            {
-                const int x = (local % tx) * tw + lane % tw;
-                const int y = (local / tx) * th + lane / tw;
-                if (x < sP[wid].x_res && y < sP[wid].y_res)
+                float c[3] = {0.0f, 0.0f, 0.0f};
+                if (inside)
                 {
-                    if (MODE == 0)
-                        whitted_pixel(sS[wid], sP[wid], x, y, J->frame, NULL);
-                    else
-                        pt_pixel(sS[wid], sP[wid], x, y, J->acc, J->frame, NULL);
+                    const float hs = aa ? (float)x + c_aa4_h[sub] : (float)x;
+                    const float vs = aa ? (float)y + c_aa4_v[sub] : (float)y;
+                    primary(sS[wid], sP[wid], x, y, hs, vs, c, NULL);
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++) c[k] = clamp1(c[k]);
                 }
+                if (aa)
+                {
+                    float col[3];
+                    #pragma unroll
+                    for (int k = 0; k < 3; k++)
+                    {
+                        const float h = c[k] * 0.5f;
+                        const float pr = h + __shfl_xor_sync(0xFFFFFFFFu, h, 1);
+                        const float q = pr * 0.5f;
+                        col[k] = q + __shfl_xor_sync(0xFFFFFFFFu, q, 2);
+                    }
+                    if (inside && sub == 0)
+                        J->frame[(size_t)y * sP[wid].x_row + x] = pack(sP[wid], col);
+                }
+                else if (inside)
+                {
+                    J->frame[(size_t)y * sP[wid].x_row + x] = pack(sP[wid], c);
+                }
+            }
+            else if (inside)
+            {
+                pt_pixel(sS[wid], sP[wid], x, y, J->acc, J->frame, NULL);
             }
             /* the tile's pixels are written (the warp barrier orders the
              * lanes' stores before lane 0's fence): count the tile; the
