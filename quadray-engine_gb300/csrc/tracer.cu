@@ -1534,30 +1534,34 @@ __device__ __forceinline__ int tile_y()
 __device__ __forceinline__ void whitted_pixel(const qr_dscene &S, const qr_frame_params &P,
                                               int x, int y, uint32_t *frame, StP st)
 {
-    float col[3];
-    if (P.fsaa == 2)
+    /* one camera-ray call site for both forms; the 4x AA average keeps the
+     * reference's pairing, every term halved before it is added */
+    const int ns = P.fsaa == 2 ? 4 : 1;
+    float col[3], half[3], p01[3];
+    #pragma unroll 1
+    for (int s = 0; s < ns; s++)
     {
-        float cs[4][3];
-        #pragma unroll 1
-        for (int s = 0; s < 4; s++)
-        {
-            primary(S, P, x, y, (float)x + c_aa4_h[s], (float)y + c_aa4_v[s], cs[s], st);
-            #pragma unroll
-            for (int k = 0; k < 3; k++) cs[s][k] = clamp1(cs[s][k]);
-        }
+        const float hs = ns == 4 ? (float)x + c_aa4_h[s] : (float)x;
+        const float vs = ns == 4 ? (float)y + c_aa4_v[s] : (float)y;
+        float c[3];
+        primary(S, P, x, y, hs, vs, c, st);
         #pragma unroll
         for (int k = 0; k < 3; k++)
         {
-            const float p01 = cs[0][k] * 0.5f + cs[1][k] * 0.5f;
-            const float p23 = cs[2][k] * 0.5f + cs[3][k] * 0.5f;
-            col[k] = p01 * 0.5f + p23 * 0.5f;
+            c[k] = clamp1(c[k]);
+            if (ns == 1) { col[k] = c[k]; continue; }
+            const float hv = c[k] * 0.5f;
+            if (s & 1)
+            {
+                const float pv = half[k] + hv;
+                if (s == 1) p01[k] = pv;
+                else        col[k] = p01[k] * 0.5f + pv * 0.5f;
+            }
+            else
+            {
+                half[k] = hv;
+            }
         }
-    }
-    else
-    {
-        primary(S, P, x, y, (float)x, (float)y, col, st);
-        #pragma unroll
-        for (int k = 0; k < 3; k++) col[k] = clamp1(col[k]);
     }
     frame[(size_t)y * P.x_row + x] = pack(P, col);
 }
