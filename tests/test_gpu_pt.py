@@ -6,8 +6,9 @@ C ABI.
   over two accumulating launches.
 * Against the FP64 oracle (the same source in double, the same streams):
   per-pixel means clamped to [0, 1] within RMSE 0.05 at 64 samples a pixel
-  and below 15% of the RMSE between two independent FP64 renders; mean bias
-  below 0.002.
+  and below 15% of the RMSE between two independent FP64 renders, mean bias
+  below 0.002; at 4096 samples a pixel within RMSE 0.01 and 15% of the
+  independent-render RMSE, mean bias below 0.001.
 * Against the reference's own CPU path tracer (tests/golden, 256 samples a
   pixel, its own LCG streams): statistically the same image.
 """
@@ -154,3 +155,33 @@ def test_engine_pt_refused_when_prohibited(qr):
     eng = qr.Engine(g, 32, 24)
     assert eng.set_pton(4) == 0
     eng.close()
+
+
+def test_pt_vs_fp64_oracle_4096spp(qr, ctx, oracle64):
+    """High-sample comparison with the FP64 oracle (the same source in double,
+    the same PCG32 streams): at 4096 samples a pixel the clamped per-pixel
+    means of the fp32 GPU path tracer lie within RMSE 0.01 of the oracle's
+    and below 15% of the RMSE between two independent FP64 renders
+    (different seeds), with a mean bias below 0.001 (the float oracle, which
+    the GPU matches bit for bit, measures 0.0045 against a noise of 0.056
+    and a bias of 3e-5 here)."""
+    g, f, desc, params = pt_scene(qr, 3, 48, 27)
+    sid = ctx.upload(desc)
+    p = qr.QrFrameParams.from_buffer_copy(params)
+    p.pt_on, p.pts_c, p.seed, p.frame_idx = 4096, 0.0, 4242, 0
+    gm = np.minimum(gpu_means(qr, ctx, sid, p), 1.0)
+    acc = np.zeros((p.y_res, p.x_row, 3), dtype=np.float64)
+    oracle_pt(oracle64, desc, p, acc)
+    om = np.minimum(acc[:, :p.x_res] / p.pt_on, 1.0)
+    p2 = qr.QrFrameParams.from_buffer_copy(p)
+    p2.seed = 4243
+    acc2 = np.zeros_like(acc)
+    oracle_pt(oracle64, desc, p2, acc2)
+    om2 = np.minimum(acc2[:, :p.x_res] / p.pt_on, 1.0)
+    rmse = float(np.sqrt(((gm - om) ** 2).mean()))
+    noise = float(np.sqrt(((om - om2) ** 2).mean()))
+    bias = float((gm - om).mean())
+    print("4096 spp: rmse %.5f noise %.5f bias %.6f" % (rmse, noise, bias))
+    assert rmse < 0.01, rmse
+    assert rmse < 0.15 * noise, (rmse, noise)
+    assert abs(bias) < 0.001, bias
