@@ -61,8 +61,7 @@ class Server:
         scene) and depth; per_request: complete each request when its frame
         is done (else when its batch is)"""
         self.per_request = per_request
-        import torch
-        self.qr, self.ctx, self.torch = qr, ctx, torch
+        self.qr, self.ctx = qr, ctx
         self.scenes = scenes
         self.budget = budget_bytes
         self.used = 0
@@ -73,7 +72,7 @@ class Server:
         self.flats = {}                 # (scene, w, h, fsaa) -> Flat
         self.slots = [collections.deque() for _ in scenes]   # free scene copies
         self.slot_bytes = {}
-        self.stream = torch.cuda.Stream()
+        self.stream = self._new_stream()
         self.batches = [qr.Batch(ctx, max_batch), qr.Batch(ctx, max_batch)]
         self.free_batches = collections.deque(self.batches)
         self.waiting = collections.deque()      # arrived, not admitted
@@ -82,6 +81,18 @@ class Server:
         self.inflight = collections.deque()      # (batch, [requests])
         self.completed = []
         self.idle_sleep = 100e-6
+
+    # ---- device memory ------------------------------------------------
+    def _new_stream(self):
+        import torch
+        return torch.cuda.Stream()
+
+    def _alloc(self, req, pt):
+        """the request's frame (and path-tracer sums) in device memory"""
+        import torch
+        req.frame = torch.empty((req.h, req.w), dtype=torch.int32, device="cuda")
+        if pt:
+            req.acc = torch.empty((req.h, req.w, 3), dtype=torch.float32, device="cuda")
 
     # ---- preparation --------------------------------------------------
     def _fsaa(self, req):
@@ -116,7 +127,6 @@ class Server:
         return req.w * req.h * 4 * (4 if pt else 1) + (1 << 20)
 
     def _admit(self):
-        torch = self.torch
         while self.waiting:
             req = self.waiting[0]
             pt = self.scenes[req.scene]["pt"]
@@ -126,9 +136,7 @@ class Server:
             self.waiting.popleft()
             self.used += need
             req.bytes = need
-            req.frame = torch.empty((req.h, req.w), dtype=torch.int32, device="cuda")
-            if pt:
-                req.acc = torch.empty((req.h, req.w, 3), dtype=torch.float32, device="cuda")
+            self._alloc(req, pt)
             if self.slots[req.scene]:
                 req.slot = self.slots[req.scene].popleft()
             self.preparing.append(self.pool.submit(self._prepare, req))
