@@ -26,6 +26,14 @@
  * scenes of the serving workload).
  * Flag QR_GEN_IDS replaces every material with a LIGHT material whose colour
  * encodes (surface index, side), so the rendered frame is a hit-ID buffer.
+ * Flag QR_GEN_TEX binds XRGB texel arrays (power-of-two sizes, as
+ * RT_TEX_BIND does) to the ground of QR_SCN_PLAIN and adds three textured
+ * finite planes (scaled and rotated, some by non-right angles), with
+ * per-side texture scales (either sign), rotations and offsets.  Only planes
+ * are textured: the reference computes texture coordinates for planes alone
+ * (tracer.cpp:5647-5667) and reads stale context fields for quadrics.  Flag
+ * QR_GEN_GAMMA turns the reference's gamma mode on (scene opts).  Both draw
+ * from their own random stream, so the rest of the scene is unchanged.
  */
 #ifndef QR_SCENEGEN_HPP
 #define QR_SCENEGEN_HPP
@@ -50,6 +58,8 @@
 #define QR_GEN_ONELIGHT (1 << 2)   /* debug: a single light */
 #define QR_GEN_TARRAY   (1 << 3)   /* QR_SCN_ANIM: keep RT_OPTS_TARRAY on */
 #define QR_GEN_SPIN     (1 << 4)   /* QR_SCN_PLAIN: the quadrics spin (anim_spin) */
+#define QR_GEN_TEX      (1 << 5)   /* QR_SCN_PLAIN: textured ground and quadrics */
+#define QR_GEN_GAMMA    (1 << 6)   /* opt out of RT_OPTS_GAMMA: gamma on */
 
 namespace qr_gen
 {
@@ -156,6 +166,7 @@ struct Scene
     std::deque<std::vector<rt_OBJECT> > arrays;
     std::deque<std::vector<rt_RELATION> > rels;
     std::deque<rt_MATERIAL> mats;
+    std::deque<std::vector<rt_ui32> > texs;
     std::deque<rt_CAMERA>   cams;
     std::deque<rt_LIGHT>    lgts;
     std::deque<rt_PLANE>    planes;
@@ -183,6 +194,19 @@ struct Scene
         m.lgt[0] = dff; m.lgt[1] = spc; m.lgt[2] = pw; m.lgt[3] = 0.0f;
         m.prp[0] = rfl; m.prp[1] = trn; m.prp[2] = rfr; m.prp[3] = ext;
         mats.push_back(m);
+        return &mats.back();
+    }
+
+    /* material m with an XRGB texel array of xd x yd (powers of two) bound
+     * in place of its plain colour */
+    rt_MATERIAL *textured(const rt_MATERIAL *m, const rt_ui32 *tx, int xd, int yd)
+    {
+        rt_MATERIAL t = *m;
+        t.tex.col.val = 0;
+        t.tex.ptex = (rt_void *)tx;
+        t.tex.x_dim = xd;
+        t.tex.y_dim = yd;
+        mats.push_back(t);
         return &mats.back();
     }
 
@@ -374,9 +398,61 @@ static rt_OBJECT look_camera(Scene &sc, float px, float py, float pz,
     return sc.camera(px, py, pz, (float)ang, 0.0f, 0.0f, pov, 0xFFFFFF, 0.1f);
 }
 
+/* texture set of QR_GEN_TEX: a checker of two colours with a distinct low
+ * nibble per texel, so a wrong texel index changes the colour */
+static void make_textures(Scene &sc, Rng &r)
+{
+    static const int dims[3][2] = {{16, 16}, {32, 8}, {8, 64}};
+    for (int k = 0; k < 3; k++)
+    {
+        const rt_ui32 a = rand_rgb(r, 0.2, 1.0), b = rand_rgb(r, 0.2, 1.0);
+        std::vector<rt_ui32> t((size_t)dims[k][0] * dims[k][1]);
+        for (int y = 0; y < dims[k][1]; y++)
+            for (int x = 0; x < dims[k][0]; x++)
+            {
+                const rt_ui32 n = (rt_ui32)((x * 7 + y * 13) & 0x0F);
+                t[(size_t)y * dims[k][0] + x] = (((x ^ y) & 1) ? a : b) ^ (n * 0x010101u);
+            }
+        sc.texs.push_back(t);
+    }
+}
+
+static float r_half(Rng &r) { return r.uf(1.5, 3.0); }
+
+/* bind texture k of the set to both sides of surface s with side
+ * transforms drawn from r (scale, right-angle or other rotation, offset) */
+static void texture_sides(Scene &sc, Rng &r, rt_SURFACE *s, int k)
+{
+    static const int dims[3][2] = {{16, 16}, {32, 8}, {8, 64}};
+    static const float rots[5] = {0.0f, 90.0f, -90.0f, 180.0f, 30.0f};
+    const rt_ui32 *tx = sc.texs[k].data();
+    rt_SIDE *sd[2] = {&s->side_outer, &s->side_inner};
+    for (int i = 0; i < 2; i++)
+    {
+        float v[5];
+        v[0] = r.uf(0.5, 2.0);
+        v[0] = r.ui(0, 3) == 0 ? -v[0] : v[0];
+        v[1] = r.uf(0.5, 2.0);
+        v[1] = r.ui(0, 3) == 0 ? -v[1] : v[1];
+        v[2] = rots[r.ui(0, 4)];
+        v[3] = r.uf(-1.0, 1.0);
+        v[4] = r.uf(-1.0, 1.0);
+        /* hit-ID scenes keep their ID materials (same draws, same scene) */
+        if (sc.flags & QR_GEN_IDS) continue;
+        sd[i]->pmat = sc.textured(sd[i]->pmat, tx, dims[k][0], dims[k][1]);
+        sd[i]->scl[0] = v[0];
+        sd[i]->scl[1] = v[1];
+        sd[i]->rot = v[2];
+        sd[i]->pos[0] = v[3];
+        sd[i]->pos[1] = v[4];
+    }
+}
+
 /* QR_SCN_PLAIN: ground plane + nq quadrics + 2 lights */
 static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
 {
+    Rng rt(seed ^ 0x7E57C0DE5EEDull);
+    if (sc.flags & QR_GEN_TEX) make_textures(sc, rt);
     Rng r(seed);
     std::vector<rt_OBJECT> root;
     root.push_back(look_camera(sc, 0.0f, -25.0f, 8.0f, 60.0f));
@@ -391,6 +467,8 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
                                   (sc.flags & QR_GEN_NOSPEC) ? 0.0f : 0.2f, 16.0f,
                                   0.0f, 0.0f, 1.0f, 0.0f);
     root.push_back(sc.plane(gm, gm));
+    if (sc.flags & QR_GEN_TEX)
+        texture_sides(sc, rt, &((rt_PLANE *)root.back().obj.pobj)->srf, 0);
     for (int i = 0; i < nq; i++)
     {
         rt_MATERIAL *m = random_plain(sc, r);
@@ -402,9 +480,29 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
         if (sc.flags & QR_GEN_SPIN) q.f_anim = anim_spin;
         root.push_back(q);
     }
+    if (sc.flags & QR_GEN_TEX)
+    {
+        /* three textured walls: finite planes, scaled, turned about two
+         * axes (right angles or not), facing the camera's side */
+        static const float turns[4] = {90.0f, -90.0f, 60.0f, 105.0f};
+        for (int k = 0; k < 3; k++)
+        {
+            rt_MATERIAL *m = random_plain(sc, rt);
+            rt_OBJECT w = sc.plane(m, m);
+            rt_PLANE *pl = (rt_PLANE *)w.obj.pobj;
+            pl->srf.min[RT_I] = -r_half(rt); pl->srf.max[RT_I] = +r_half(rt);
+            pl->srf.min[RT_J] = -r_half(rt); pl->srf.max[RT_J] = +r_half(rt);
+            const float sx = rt.uf(0.6, 1.6), sy = rt.uf(0.6, 1.6);
+            const float rx = turns[rt.ui(0, 3)], rz = rt.uf(-40, 40);
+            const float px = rt.uf(-8, 8), py = rt.uf(-4, 8), pz = rt.uf(1.5, 4);
+            Scene::trm_set(&w.trm, sx, sy, 1, rx, 0, rz, px, py, pz);
+            texture_sides(sc, rt, &pl->srf, k);
+            root.push_back(w);
+        }
+    }
     rt_OBJECT ro = sc.array(root);
     sc.scn.root = ro.obj;
-    sc.scn.opts = 0;
+    sc.scn.opts = (sc.flags & QR_GEN_GAMMA) ? RT_OPTS_GAMMA : 0;
     sc.scn.lock = RT_NULL;
 }
 

@@ -10,6 +10,7 @@ CPU restatement in oracle/qr_oracle.c (tests/test_oracle_golden.py) and the
 CUDA path (tests/test_gpu_parity.py) without the reference being present.
 
     python tests/golden/make_golden.py            # (re)write all fixtures
+    python tests/golden/make_golden.py NAME ...   # (re)write the named ones
 
 The reference is compiled with its SSE4 128-bit target (4 lanes), so the
 frames carry the SIMD-group effects of that target (see the oracle header).
@@ -30,7 +31,9 @@ DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 #   kind 1 = plain Whitted scene, 2 = animated scene (clippers, booleans,
 #   3-level spinning hierarchy, reflection/refraction with Fresnel; frames
 #   at t = 0, 16, 32 ms); flags 1 = hit-ID materials, 8 = animated scene
-#   that keeps RT_OPTS_TARRAY on (see test_oracle_golden.py); fsaa 2 = 4x;
+#   that keeps RT_OPTS_TARRAY on (see test_oracle_golden.py), 32 = textured
+#   ground and walls (bound texel arrays, side scales, rotations, offsets),
+#   64 = gamma on; fsaa 2 = 4x;
 #   opts "none" renders the reference without its list optimisations
 CASES = {
     "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
@@ -43,6 +46,9 @@ CASES = {
     "plain_s2_aa4_128x80":  (1, 2, 16, 128, 80, 2, 1, 0, "full"),
     "plain_s8_q32_200x120": (1, 8, 32, 200, 120, 0, 1, 0, "full"),
     "plain_s9_ragged_37x23": (1, 9, 16, 37, 23, 0, 1, 0, "full"),
+    "plain_s7_tex_160x96":  (1, 7, 16, 160, 96, 0, 1, 32, "full"),
+    "plain_s9_gamma_160x96": (1, 9, 16, 160, 96, 0, 1, 64, "full"),
+    "plain_s10_tex_gamma_aa4_128x80": (1, 10, 16, 128, 80, 2, 1, 96, "full"),
     "anim_s1_none_160x90_d4":     (2, 1, 64, 160, 90, 0, 2, 0, "none", 4),
     "anim_s2_none_aa4_128x72_d4": (2, 2, 64, 128, 72, 2, 2, 0, "none", 4),
     "anim_s4_none_96x54_d10":     (2, 4, 64, 96, 54, 0, 1, 0, "none", 10),
@@ -85,7 +91,9 @@ def run_case(name, case):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("oracle/_ref/ref_driver is missing: run `make -C oracle ref`")
-    for name, case in CASES.items():
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        case = CASES[name]
         data = run_case(name, case)
         print("%-24s %s nonzero=%d" % (name, data.shape, int((data != 0).sum())))
 

@@ -48,6 +48,16 @@ def test_plain_aa4_bit_exact(qr, oracle, ctx):
     assert (gpu != cpu).sum() == 0
 
 
+@pytest.mark.parametrize("seed,fsaa,flags", [(7, 0, 32), (11, 2, 32), (9, 0, 64), (10, 2, 96)])
+def test_textured_and_gamma_bit_exact(qr, oracle, ctx, seed, fsaa, flags):
+    """bound texel arrays on the ground and on scaled, rotated walls (side
+    scales of either sign, rotations, offsets), and the reference's gamma
+    mode (texels squared, square root before packing)"""
+    gpu, cpu = _render_both(qr, oracle, ctx, qr.SCN_PLAIN, seed, 16, 320, 192,
+                            fsaa=fsaa, flags=flags)
+    assert (gpu != cpu).sum() == 0
+
+
 def test_plain_full_size(qr, oracle, ctx):
     gpu, cpu = _render_both(qr, oracle, ctx, qr.SCN_PLAIN, 1, 16, 800, 480)
     assert (gpu != cpu).sum() == 0
