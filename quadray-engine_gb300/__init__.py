@@ -27,6 +27,7 @@ GEN_TARRAY = 1 << 3      # animated scene keeps RT_OPTS_TARRAY on
 GEN_SPIN = 1 << 4        # plain scene whose quadrics spin
 GEN_TEX = 1 << 5         # plain scene with textured ground and quadrics
 GEN_GAMMA = 1 << 6       # the reference's gamma mode on
+GEN_SHAPES = 1 << 7      # plain scene with the other quadric kinds too
 
 # runtime options (csrc/format.h): -1 selects the default (FULL minus the
 # scene's opt-outs)

@@ -32,8 +32,13 @@
  * per-side texture scales (either sign), rotations and offsets.  Only planes
  * are textured: the reference computes texture coordinates for planes alone
  * (tracer.cpp:5647-5667) and reads stale context fields for quadrics.  Flag
- * QR_GEN_GAMMA turns the reference's gamma mode on (scene opts).  Both draw
- * from their own random stream, so the rest of the scene is unchanged.
+ * QR_GEN_GAMMA turns the reference's gamma mode on (scene opts).  Flag
+ * QR_GEN_SHAPES adds the quadric kinds the plain mix leaves out: a
+ * paracylinder, a hypercylinder, a hypercylinder of zero hyp (two planes,
+ * the two-plane solver), a hyperboloid of zero hyp (a double cone, the
+ * apex adjustment) and a hyperbolic paraboloid, each cut to a finite
+ * extent, at right-angle or other rotations.  These flags draw from their
+ * own random stream, so the rest of the scene is unchanged.
  */
 #ifndef QR_SCENEGEN_HPP
 #define QR_SCENEGEN_HPP
@@ -60,6 +65,7 @@
 #define QR_GEN_SPIN     (1 << 4)   /* QR_SCN_PLAIN: the quadrics spin (anim_spin) */
 #define QR_GEN_TEX      (1 << 5)   /* QR_SCN_PLAIN: textured ground and quadrics */
 #define QR_GEN_GAMMA    (1 << 6)   /* opt out of RT_OPTS_GAMMA: gamma on */
+#define QR_GEN_SHAPES   (1 << 7)   /* QR_SCN_PLAIN: the other quadric kinds too */
 
 namespace qr_gen
 {
@@ -479,6 +485,38 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
         Scene::trm_set(&q.trm, 1, 1, 1, rx, ry, rz, px, py, pz);
         if (sc.flags & QR_GEN_SPIN) q.f_anim = anim_spin;
         root.push_back(q);
+    }
+    if (sc.flags & QR_GEN_SHAPES)
+    {
+        Rng rs(seed ^ 0x5A4E5EC0DE11ull);
+        static const int tags[5] = {RT_TAG_PARACYLINDER, RT_TAG_HYPERCYLINDER,
+                                    RT_TAG_HYPERCYLINDER, RT_TAG_HYPERBOLOID,
+                                    RT_TAG_HYPERPARABOLOID};
+        for (int k = 0; k < 5; k++)
+        {
+            rt_MATERIAL *m = random_plain(sc, rs);
+            float a = rs.uf(0.4, 1.2), b = 0.0f;
+            if (k == 1) b = rs.uf(0.25, 1.0);           /* hypercylinder */
+            if (k == 4) b = rs.uf(0.5, 2.0);            /* saddle: pr2 */
+            const float ke = rs.uf(0.8, 2.0);
+            rt_OBJECT q = sc.quadric(tags[k], a, b, k == 4 ? -RT_INF : -ke,
+                                     k == 4 ? +RT_INF : +ke, m, m);
+            rt_SURFACE *sf = (rt_SURFACE *)q.obj.pobj;
+            if (k == 0 || k == 4)
+            {
+                /* open in I (paracylinder) or I and J (saddle): cut */
+                const float ie = rs.uf(1.0, 2.5), je = rs.uf(1.0, 2.5);
+                sf->min[RT_I] = -ie; sf->max[RT_I] = +ie;
+                if (k == 4) { sf->min[RT_J] = -je; sf->max[RT_J] = +je; }
+            }
+            const int right = rs.ui(0, 1);
+            float rx = right ? 90.0f * (float)rs.ui(-2, 2) : rs.uf(-180, 180);
+            float ry = right ? 90.0f * (float)rs.ui(-2, 2) : rs.uf(-180, 180);
+            float rz = right ? 90.0f * (float)rs.ui(-2, 2) : rs.uf(-180, 180);
+            const float px = rs.uf(-8, 8), py = rs.uf(-4, 8), pz = rs.uf(1.0, 4.0);
+            Scene::trm_set(&q.trm, 1, 1, 1, rx, ry, rz, px, py, pz);
+            root.push_back(q);
+        }
     }
     if (sc.flags & QR_GEN_TEX)
     {

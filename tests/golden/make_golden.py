@@ -33,7 +33,8 @@ DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 #   at t = 0, 16, 32 ms); flags 1 = hit-ID materials, 8 = animated scene
 #   that keeps RT_OPTS_TARRAY on (see test_oracle_golden.py), 32 = textured
 #   ground and walls (bound texel arrays, side scales, rotations, offsets),
-#   64 = gamma on; fsaa 2 = 4x;
+#   64 = gamma on, 128 = paracylinder, hypercylinder, two-plane, double
+#   cone and hyperbolic paraboloid added; fsaa 2 = 4x;
 #   opts "none" renders the reference without its list optimisations
 CASES = {
     "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
@@ -49,6 +50,9 @@ CASES = {
     "plain_s7_tex_160x96":  (1, 7, 16, 160, 96, 0, 1, 32, "full"),
     "plain_s9_gamma_160x96": (1, 9, 16, 160, 96, 0, 1, 64, "full"),
     "plain_s10_tex_gamma_aa4_128x80": (1, 10, 16, 128, 80, 2, 1, 96, "full"),
+    "plain_s12_shapes_160x96": (1, 12, 8, 160, 96, 0, 1, 128, "full"),
+    "plain_s15_shapes_ids_160x96": (1, 15, 8, 160, 96, 0, 1, 129, "full"),
+    "plain_s13_shapes_aa4_128x80": (1, 13, 8, 128, 80, 2, 1, 128, "full"),
     "anim_s1_none_160x90_d4":     (2, 1, 64, 160, 90, 0, 2, 0, "none", 4),
     "anim_s2_none_aa4_128x72_d4": (2, 2, 64, 128, 72, 2, 2, 0, "none", 4),
     "anim_s4_none_96x54_d10":     (2, 4, 64, 96, 54, 0, 1, 0, "none", 10),

@@ -58,6 +58,17 @@ def test_textured_and_gamma_bit_exact(qr, oracle, ctx, seed, fsaa, flags):
     assert (gpu != cpu).sum() == 0
 
 
+@pytest.mark.parametrize("seed,fsaa,flags", [(12, 0, 128), (13, 2, 128), (15, 0, 129),
+                                             (16, 0, 128 | 32)])
+def test_other_quadric_kinds_bit_exact(qr, oracle, ctx, seed, fsaa, flags):
+    """paracylinder, hypercylinder, two planes (the two-plane solver), double
+    cone (apex adjustment) and hyperbolic paraboloid, at right-angle and other
+    rotations; colour and hit IDs"""
+    gpu, cpu = _render_both(qr, oracle, ctx, qr.SCN_PLAIN, seed, 8, 320, 192,
+                            fsaa=fsaa, flags=flags)
+    assert (gpu != cpu).sum() == 0
+
+
 def test_plain_full_size(qr, oracle, ctx):
     gpu, cpu = _render_both(qr, oracle, ctx, qr.SCN_PLAIN, 1, 16, 800, 480)
     assert (gpu != cpu).sum() == 0
