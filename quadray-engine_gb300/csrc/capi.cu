@@ -160,9 +160,16 @@ static int check_desc(const qr_scene_desc *d)
     for (int i = 0; i < d->nmat; i++)
     {
         const qr_mat &m = d->mat[i];
-        long span = (long)(m.xmask + 1) * (long)((m.ymask + 1) << m.yshft);
         if (m.tex_off < 0 || m.tex_off >= d->ntex) return QR_ERR_ARG;
-        if ((m.props & QR_PROP_TEXTURE) && m.tex_off + span > d->ntex) return QR_ERR_ARG;
+        if (m.props & QR_PROP_TEXTURE)
+        {
+            /* the texel index is (x & xmask) + ((y & ymask) << yshft) */
+            if (m.xmask < 0 || m.ymask < 0 || m.yshft < 0 || m.yshft > 30) return QR_ERR_ARG;
+            if (m.tmap[0] < 0 || m.tmap[0] > 1 || m.tmap[1] < 0 || m.tmap[1] > 1)
+                return QR_ERR_ARG;
+            const long long top = (long long)m.xmask + ((long long)m.ymask << m.yshft);
+            if ((long long)m.tex_off + top >= (long long)d->ntex) return QR_ERR_ARG;
+        }
     }
     return QR_OK;
 }
