@@ -37,8 +37,10 @@
  * paracylinder, a hypercylinder, a hypercylinder of zero hyp (two planes,
  * the two-plane solver), a hyperboloid of zero hyp (a double cone, the
  * apex adjustment) and a hyperbolic paraboloid, each cut to a finite
- * extent, at right-angle or other rotations.  These flags draw from their
- * own random stream, so the rest of the scene is unchanged.
+ * extent, at right-angle or other rotations.  Flag QR_GEN_ATTN gives the
+ * lights an ambient share and constant, linear and quadratic attenuation.
+ * These flags draw from their own random stream, so the rest of the scene
+ * is unchanged.
  */
 #ifndef QR_SCENEGEN_HPP
 #define QR_SCENEGEN_HPP
@@ -66,6 +68,7 @@
 #define QR_GEN_TEX      (1 << 5)   /* QR_SCN_PLAIN: textured ground and quadrics */
 #define QR_GEN_GAMMA    (1 << 6)   /* opt out of RT_OPTS_GAMMA: gamma on */
 #define QR_GEN_SHAPES   (1 << 7)   /* QR_SCN_PLAIN: the other quadric kinds too */
+#define QR_GEN_ATTN     (1 << 8)   /* QR_SCN_PLAIN: light ambient and attenuation */
 
 namespace qr_gen
 {
@@ -459,6 +462,7 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
 {
     Rng rt(seed ^ 0x7E57C0DE5EEDull);
     if (sc.flags & QR_GEN_TEX) make_textures(sc, rt);
+    Rng ra(seed ^ 0xA77E0A7E0ull);
     Rng r(seed);
     std::vector<rt_OBJECT> root;
     root.push_back(look_camera(sc, 0.0f, -25.0f, 8.0f, 60.0f));
@@ -467,7 +471,16 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
         float px = r.uf(-15, 15), py = r.uf(-15, 15), pz = r.uf(8, 15);
         rt_ui32 col = rand_rgb(r, 0.3, 1.0);
         if ((sc.flags & QR_GEN_ONELIGHT) && i > 0) continue;
-        root.push_back(sc.light(px, py, pz, col, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f));
+        float lamb = 0.0f, lsrc = 1.0f, ac = 0.0f, al = 0.0f, aq = 0.0f;
+        if (sc.flags & QR_GEN_ATTN)
+        {
+            lamb = ra.uf(0.0, 0.3);
+            lsrc = ra.uf(2.0, 6.0);
+            ac = ra.uf(0.5, 1.5);
+            al = ra.uf(0.0, 0.1);
+            aq = ra.uf(0.0, 0.02);
+        }
+        root.push_back(sc.light(px, py, pz, col, lamb, lsrc, ac, al, aq));
     }
     rt_MATERIAL *gm = sc.material(RT_MAT_PLAIN, 0xB0B0A8, 0.8f,
                                   (sc.flags & QR_GEN_NOSPEC) ? 0.0f : 0.2f, 16.0f,

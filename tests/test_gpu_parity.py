@@ -48,11 +48,13 @@ def test_plain_aa4_bit_exact(qr, oracle, ctx):
     assert (gpu != cpu).sum() == 0
 
 
-@pytest.mark.parametrize("seed,fsaa,flags", [(7, 0, 32), (11, 2, 32), (9, 0, 64), (10, 2, 96)])
+@pytest.mark.parametrize("seed,fsaa,flags", [(7, 0, 32), (11, 2, 32), (9, 0, 64), (10, 2, 96),
+                                             (17, 0, 256), (19, 2, 480)])
 def test_textured_and_gamma_bit_exact(qr, oracle, ctx, seed, fsaa, flags):
     """bound texel arrays on the ground and on scaled, rotated walls (side
-    scales of either sign, rotations, offsets), and the reference's gamma
-    mode (texels squared, square root before packing)"""
+    scales of either sign, rotations, offsets), the reference's gamma mode
+    (texels squared, square root before packing), and lights with an
+    ambient share and constant, linear and quadratic attenuation"""
     gpu, cpu = _render_both(qr, oracle, ctx, qr.SCN_PLAIN, seed, 16, 320, 192,
                             fsaa=fsaa, flags=flags)
     assert (gpu != cpu).sum() == 0
