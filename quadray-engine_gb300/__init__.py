@@ -29,6 +29,7 @@ GEN_TEX = 1 << 5         # plain scene with textured ground and quadrics
 GEN_GAMMA = 1 << 6       # the reference's gamma mode on
 GEN_SHAPES = 1 << 7      # plain scene with the other quadric kinds too
 GEN_ATTN = 1 << 8        # plain scene whose lights have ambient and attenuation
+GEN_NOFRESNEL = 1 << 9   # animated scene without Fresnel terms (the default)
 
 # runtime options (csrc/format.h): -1 selects the default (FULL minus the
 # scene's opt-outs)

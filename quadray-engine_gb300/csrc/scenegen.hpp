@@ -69,6 +69,7 @@
 #define QR_GEN_GAMMA    (1 << 6)   /* opt out of RT_OPTS_GAMMA: gamma on */
 #define QR_GEN_SHAPES   (1 << 7)   /* QR_SCN_PLAIN: the other quadric kinds too */
 #define QR_GEN_ATTN     (1 << 8)   /* QR_SCN_PLAIN: light ambient and attenuation */
+#define QR_GEN_NOFRESNEL (1 << 9)  /* QR_SCN_ANIM: keep the default, Fresnel off */
 
 namespace qr_gen
 {
@@ -707,8 +708,9 @@ static void build_anim(Scene &sc, uint64_t seed, int nq)
      * on, and no array-level transform nodes (RT_OPTS_TARRAY), under which
      * the reference's per-surface shadow and secondary-ray lists of this
      * spinning hierarchy lose occluders and candidates (its frame then
-     * departs from its own unculled render); QR_GEN_TARRAY keeps it on */
-    sc.scn.opts = RT_OPTS_FRESNEL;
+     * departs from its own unculled render); QR_GEN_TARRAY keeps it on,
+     * QR_GEN_NOFRESNEL the reference's default (no Fresnel terms) */
+    sc.scn.opts = (sc.flags & QR_GEN_NOFRESNEL) ? 0 : RT_OPTS_FRESNEL;
     if ((sc.flags & QR_GEN_TARRAY) == 0) sc.scn.opts |= RT_OPTS_TARRAY;
     sc.scn.lock = RT_NULL;
 }

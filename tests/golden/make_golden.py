@@ -35,7 +35,8 @@ DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 #   ground and walls (bound texel arrays, side scales, rotations, offsets),
 #   64 = gamma on, 128 = paracylinder, hypercylinder, two-plane, double
 #   cone and hyperbolic paraboloid added, 256 = lights with an ambient share
-#   and attenuation; fsaa 2 = 4x;
+#   and attenuation, 512 = animated scene without Fresnel terms (the
+#   reference's default); fsaa 2 = 4x;
 #   opts "none" renders the reference without its list optimisations
 CASES = {
     "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
@@ -64,6 +65,8 @@ CASES = {
     "anim_s3_full_aa4_128x72_d4": (2, 3, 64, 128, 72, 2, 1, 0, "full", 4),
     "anim_s1_tarray_160x90_d4":   (2, 1, 64, 160, 90, 0, 1, 8, "full", 4),
     "anim_s1_tarray_none_160x90_d4": (2, 1, 64, 160, 90, 0, 1, 8, "none", 4),
+    "anim_s6_nofresnel_160x90_d4": (2, 6, 64, 160, 90, 0, 2, 512, "full", 4),
+    "anim_s8_nofresnel_96x54_d10": (2, 8, 64, 96, 54, 0, 1, 512, "none", 10),
     # path tracer (kind 3): the reference's running mean after 256 frames of
     # one sample each (its own random streams); only the last frame is kept
     "pt_s1_ref256_80x45_d8":      (3, 1, 32, 80, 45, 0, 256, 0, "full", 8, "last"),

@@ -96,9 +96,11 @@ def test_tiny_and_ragged_frames(qr, oracle, ctx):
 
 # ---- animated scene: clippers, booleans, spinning hierarchy, secondary rays
 
-@pytest.mark.parametrize("seed,fsaa", [(1, 0), (2, 2), (3, 0)])
-def test_anim_bit_exact_over_frames(qr, oracle, ctx, seed, fsaa):
-    g = qr.GenScene(qr.SCN_ANIM, seed, 64, 0)
+@pytest.mark.parametrize("seed,fsaa,flags", [(1, 0, 0), (2, 2, 0), (3, 0, 0), (6, 2, 512)])
+def test_anim_bit_exact_over_frames(qr, oracle, ctx, seed, fsaa, flags):
+    """animated frames; flags 512 keeps the reference's default of no
+    Fresnel terms"""
+    g = qr.GenScene(qr.SCN_ANIM, seed, 64, flags)
     f = qr.Flat(g, 192, 108, fsaa)
     for k in range(3):
         desc, params = f.update(16 * k, 4)
