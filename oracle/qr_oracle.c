@@ -1077,6 +1077,12 @@ static const real aa4_h[4] = {-0.08f - 0.25f, -0.08f + 0.25f,
                                +0.08f - 0.25f, +0.08f + 0.25f};
 static const real aa4_v[4] = {+0.08f - 0.25f, -0.08f - 0.25f,
                                +0.08f + 0.25f, -0.08f + 0.25f};
+/* 2x alternating (engine.cpp:3536-3570): the pair of offsets depends on
+ * the parity of the pixel's column */
+static const real aa2_h[2][2] = {{-0.08f + 0.25f, +0.08f - 0.25f},
+                                 {+0.08f - 0.25f, -0.08f + 0.25f}};
+static const real aa2_v[2][2] = {{+0.08f + 0.25f, -0.08f - 0.25f},
+                                 {+0.08f + 0.25f, -0.08f - 0.25f}};
 
 static void primary(scene_t *sc, const qr_scene_desc *d,
                     const qr_frame_params *fp, real hs, real vs,
@@ -1160,6 +1166,18 @@ int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
                     real p23 = cs[2][k] * 0.5f + cs[3][k] * 0.5f;
                     col[k] = p01 * 0.5f + p23 * 0.5f;
                 }
+            }
+            else if (fp->fsaa == 1)
+            {
+                real cs[2][3];
+                int s;
+                for (s = 0; s < 2; s++)
+                {
+                    primary(&sc, d, fp, (real)x + aa2_h[x & 1][s],
+                            (real)y + aa2_v[x & 1][s], cs[s]);
+                    for (k = 0; k < 3; k++) cs[s][k] = clamp1(cs[s][k]);
+                }
+                for (k = 0; k < 3; k++) col[k] = cs[0][k] * 0.5f + cs[1][k] * 0.5f;
             }
             else
             {

@@ -348,7 +348,7 @@ static int check_fp(const qr_frame_params *fp)
     if (fp == NULL) return QR_ERR_ARG;
     if (fp->x_res <= 0 || fp->y_res <= 0 || fp->x_row < fp->x_res) return QR_ERR_ARG;
     if (fp->x_res > 16384 || fp->y_res > 16384) return QR_ERR_LIMIT;
-    if (fp->fsaa != 0 && fp->fsaa != 2) return QR_ERR_ARG;
+    if (fp->fsaa < 0 || fp->fsaa > 2) return QR_ERR_ARG;   /* none, 2x, 4x */
     if (fp->depth < 0 || fp->depth > QR_MAX_DEPTH) return QR_ERR_LIMIT;
     if (fp->pt_on < 0 || fp->pt_on > QR_MAX_PT_SAMPLES) return QR_ERR_LIMIT;
     if (!(fp->pts_c >= 0.0f) || fp->pts_c > 16777216.0f) return QR_ERR_ARG;

@@ -51,9 +51,9 @@ rt_si32 rt_Platform::set_thnum(rt_si32 n) { thnum = n > 0 ? n : 1; return thnum;
 rt_si32 rt_Platform::set_simd(rt_si32 simd) { (void)simd; return 103; }
 rt_si32 rt_Platform::set_fsaa(rt_si32 f)
 {
-    /* 4x rotated grid and none; 2x falls back to none like an 8x request
-     * on the reference's targets without it */
-    fsaa = (f == RT_FSAA_4X) ? RT_FSAA_4X : RT_FSAA_NO;
+    /* none, 2x alternating, 4x rotated grid; as the reference, modes above
+     * the maximum fall back to it (engine.cpp:662-672) */
+    fsaa = f > RT_FSAA_4X ? RT_FSAA_4X : (f < RT_FSAA_NO ? RT_FSAA_NO : f);
     return fsaa;
 }
 rt_si32 rt_Platform::get_fsaa_max() { return RT_FSAA_4X; }

@@ -1442,6 +1442,12 @@ __constant__ float c_aa4_h[4] = {-0.08f - 0.25f, -0.08f + 0.25f,
                                  +0.08f - 0.25f, +0.08f + 0.25f};
 __constant__ float c_aa4_v[4] = {+0.08f - 0.25f, -0.08f - 0.25f,
                                  +0.08f + 0.25f, -0.08f + 0.25f};
+/* 2x alternating (engine.cpp:3536-3570): the pair of offsets depends on the
+ * parity of the pixel's column */
+__constant__ float c_aa2_h[2][2] = {{-0.08f + 0.25f, +0.08f - 0.25f},
+                                    {+0.08f - 0.25f, -0.08f + 0.25f}};
+__constant__ float c_aa2_v[2][2] = {{+0.08f + 0.25f, -0.08f - 0.25f},
+                                    {+0.08f + 0.25f, -0.08f - 0.25f}};
 
 /* camera ray through image position (hs, vs): dir = hor * hs + ver * vs +
  * dir, from the camera position (engine.cpp:3530-3610) */
@@ -1534,15 +1540,17 @@ __device__ __forceinline__ int tile_y()
 __device__ __forceinline__ void whitted_pixel(const qr_dscene &S, const qr_frame_params &P,
                                               int x, int y, uint32_t *frame, StP st)
 {
-    /* one camera-ray call site for both forms; the 4x AA average keeps the
-     * reference's pairing, every term halved before it is added */
-    const int ns = P.fsaa == 2 ? 4 : 1;
+    /* one camera-ray call site for all forms (1 ray, 2x alternating, 4x
+     * rotated grid); the AA average keeps the reference's pairing, every
+     * term halved before it is added (7047-7135) */
+    const int ns = P.fsaa == 2 ? 4 : P.fsaa == 1 ? 2 : 1;
     float col[3], half[3], p01[3];
     #pragma unroll 1
     for (int s = 0; s < ns; s++)
     {
-        const float hs = ns == 4 ? (float)x + c_aa4_h[s] : (float)x;
-        const float vs = ns == 4 ? (float)y + c_aa4_v[s] : (float)y;
+        float hs = (float)x, vs = (float)y;
+        if (ns == 4) { hs = hs + c_aa4_h[s]; vs = vs + c_aa4_v[s]; }
+        if (ns == 2) { hs = hs + c_aa2_h[x & 1][s]; vs = vs + c_aa2_v[x & 1][s]; }
         float c[3];
         primary(S, P, x, y, hs, vs, c, st);
         #pragma unroll
@@ -1554,8 +1562,9 @@ __device__ __forceinline__ void whitted_pixel(const qr_dscene &S, const qr_frame
             if (s & 1)
             {
                 const float pv = half[k] + hv;
-                if (s == 1) p01[k] = pv;
-                else        col[k] = p01[k] * 0.5f + pv * 0.5f;
+                if (ns == 2)     col[k] = pv;
+                else if (s == 1) p01[k] = pv;
+                else             col[k] = p01[k] * 0.5f + pv * 0.5f;
             }
             else
             {
@@ -2177,14 +2186,25 @@ batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter
             const int inside = x < sP[wid].x_res && y < sP[wid].y_res;
             if (MODE == 0)
             {
-                float c[3] = {0.0f, 0.0f, 0.0f};
-                if (inside)
+                /* a thread's samples: one, or its pixel's two of 2x AA */
+                const int n2 = (!aa && sP[wid].fsaa == 1) ? 2 : 1;
+                float c[3] = {0.0f, 0.0f, 0.0f}, h0[3];
+                #pragma unroll 1
+                for (int s = 0; s < n2 && inside; s++)
                 {
-                    const float hs = aa ? (float)x + c_aa4_h[sub] : (float)x;
-                    const float vs = aa ? (float)y + c_aa4_v[sub] : (float)y;
-                    primary(sS[wid], sP[wid], x, y, hs, vs, c, NULL);
+                    float hs = (float)x, vs = (float)y;
+                    if (aa) { hs = hs + c_aa4_h[sub]; vs = vs + c_aa4_v[sub]; }
+                    if (n2 == 2) { hs = hs + c_aa2_h[x & 1][s]; vs = vs + c_aa2_v[x & 1][s]; }
+                    float cc[3];
+                    primary(sS[wid], sP[wid], x, y, hs, vs, cc, NULL);
                     #pragma unroll
-                    for (int k = 0; k < 3; k++) c[k] = clamp1(c[k]);
+                    for (int k = 0; k < 3; k++)
+                    {
+                        cc[k] = clamp1(cc[k]);
+                        if (n2 == 1)     c[k] = cc[k];
+                        else if (s == 0) h0[k] = cc[k] * 0.5f;
+                        else             c[k] = h0[k] + cc[k] * 0.5f;
+                    }
                 }
                 if (aa)
                 {

@@ -36,7 +36,7 @@ DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 #   64 = gamma on, 128 = paracylinder, hypercylinder, two-plane, double
 #   cone and hyperbolic paraboloid added, 256 = lights with an ambient share
 #   and attenuation, 512 = animated scene without Fresnel terms (the
-#   reference's default); fsaa 2 = 4x;
+#   reference's default); fsaa 1 = 2x alternating, 2 = 4x rotated grid;
 #   opts "none" renders the reference without its list optimisations
 CASES = {
     "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
@@ -57,6 +57,8 @@ CASES = {
     "plain_s13_shapes_aa4_128x80": (1, 13, 8, 128, 80, 2, 1, 128, "full"),
     "plain_s17_attn_160x96": (1, 17, 16, 160, 96, 0, 1, 256, "full"),
     "plain_s19_all_160x96": (1, 19, 8, 160, 96, 0, 1, 480, "full"),
+    "plain_s21_aa2_160x96": (1, 21, 16, 160, 96, 1, 1, 0, "full"),
+    "anim_s9_none_aa2_128x72_d4": (2, 9, 64, 128, 72, 1, 2, 0, "none", 4),
     "anim_s1_none_160x90_d4":     (2, 1, 64, 160, 90, 0, 2, 0, "none", 4),
     "anim_s2_none_aa4_128x72_d4": (2, 2, 64, 128, 72, 2, 2, 0, "none", 4),
     "anim_s4_none_96x54_d10":     (2, 4, 64, 96, 54, 0, 1, 0, "none", 10),

@@ -11,6 +11,7 @@ CASES = [  # kind, seed, nq, w, h, fsaa, depth, spp
     (1, 11, 8, 64, 48, 0, 3, 0), (1, 12, 40, 100, 75, 2, 6, 0),
     (2, 13, 64, 96, 54, 0, 4, 0), (3, 14, 16, 80, 45, 0, 8, 4),
     (3, 15, 32, 48, 36, 0, 8, 12), (1, 16, 120, 33, 17, 0, 1, 0),
+    (2, 17, 64, 50, 30, 1, 4, 0),
 ]
 
 

@@ -43,8 +43,11 @@ def test_plain_ids_bit_exact(qr, oracle, ctx, seed):
     assert (gpu != cpu).sum() == 0
 
 
-def test_plain_aa4_bit_exact(qr, oracle, ctx):
-    gpu, cpu = _render_both(qr, oracle, ctx, qr.SCN_PLAIN, 3, 16, 200, 120, fsaa=2)
+@pytest.mark.parametrize("fsaa,w,h", [(2, 200, 120), (1, 200, 120), (1, 37, 23)])
+def test_plain_aa_bit_exact(qr, oracle, ctx, fsaa, w, h):
+    """4x rotated grid (fsaa 2) and 2x alternating (fsaa 1), on an odd
+    width too (the 2x offsets follow the column's parity)"""
+    gpu, cpu = _render_both(qr, oracle, ctx, qr.SCN_PLAIN, 3, 16, w, h, fsaa=fsaa)
     assert (gpu != cpu).sum() == 0
 
 
@@ -96,7 +99,8 @@ def test_tiny_and_ragged_frames(qr, oracle, ctx):
 
 # ---- animated scene: clippers, booleans, spinning hierarchy, secondary rays
 
-@pytest.mark.parametrize("seed,fsaa,flags", [(1, 0, 0), (2, 2, 0), (3, 0, 0), (6, 2, 512)])
+@pytest.mark.parametrize("seed,fsaa,flags", [(1, 0, 0), (2, 2, 0), (3, 0, 0), (6, 2, 512),
+                                             (9, 1, 0)])
 def test_anim_bit_exact_over_frames(qr, oracle, ctx, seed, fsaa, flags):
     """animated frames; flags 512 keeps the reference's default of no
     Fresnel terms"""
