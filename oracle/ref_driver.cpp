@@ -245,8 +245,23 @@ int main(int argc, char **argv)
         if (kind == QR_SCN_PT) scene->set_pton(1);
         scene->depth = depth;
 
+        /* QR_ACTIONS="a,b,...": camera action a_k (object.h:47-62) through
+         * rt_Scene::update before frame k + 1, at that frame's time */
+        std::vector<int> actions;
+        if (getenv("QR_ACTIONS") != NULL)
+        {
+            const char *p = getenv("QR_ACTIONS");
+            while (*p)
+            {
+                actions.push_back(atoi(p));
+                while (*p && *p != ',') p++;
+                if (*p == ',') p++;
+            }
+        }
         for (int f = 0; f < frames; f++)
         {
+            if (f > 0 && !actions.empty())
+                scene->update((rt_time)f * 16, actions[(f - 1) % actions.size()]);
             double t0 = now_ms();
             scene->render((rt_time)f * 16);
             tsum += now_ms() - t0;

@@ -30,6 +30,10 @@ GEN_GAMMA = 1 << 6       # the reference's gamma mode on
 GEN_SHAPES = 1 << 7      # plain scene with the other quadric kinds too
 GEN_ATTN = 1 << 8        # plain scene whose lights have ambient and attenuation
 GEN_NOFRESNEL = 1 << 9   # animated scene without Fresnel terms (the default)
+# camera actions (rt_Scene::update; codes of core/engine/object.h:47-63)
+CAMERA_MOVE_DOWN, CAMERA_MOVE_UP, CAMERA_MOVE_LEFT, CAMERA_MOVE_RIGHT = 2, 3, 4, 5
+CAMERA_MOVE_BACK, CAMERA_MOVE_FORWARD = 6, 7
+CAMERA_ROTATE_DOWN, CAMERA_ROTATE_UP, CAMERA_ROTATE_LEFT, CAMERA_ROTATE_RIGHT = 10, 11, 12, 13
 
 # runtime options (csrc/format.h): -1 selects the default (FULL minus the
 # scene's opt-outs)
@@ -104,6 +108,10 @@ def lib():
         L.qrpy_flat_new.restype = vp
         L.qrpy_flat_new.argtypes = [vp, i32, i32, i32, i32]
         L.qrpy_flat_update.argtypes = [vp, i64, i32]
+        L.qrpy_flat_action.argtypes = [vp, i64, i32]
+        L.qrpy_flat_action.restype = None
+        L.qrpy_scene_update.argtypes = [vp, i64, i32]
+        L.qrpy_scene_update.restype = None
         L.qrpy_flat_desc.argtypes = [vp, ctypes.POINTER(QrSceneDesc),
                                      ctypes.POINTER(QrFrameParams)]
         L.qrpy_flat_free.argtypes = [vp]
@@ -187,6 +195,11 @@ class Flat:
             raise RuntimeError("update failed: %d" % rc)
         lib().qrpy_flat_desc(self.h, ctypes.byref(self.desc), ctypes.byref(self.params))
         return self.desc, self.params
+
+    def action(self, time, action):
+        """camera movement before the next update (rt_Scene::update(time,
+        action); CAMERA_* codes)"""
+        lib().qrpy_flat_action(self.h, int(time), int(action))
 
     def close(self):
         if self.h:
@@ -337,6 +350,10 @@ class Engine:
         if not self.h:
             raise RuntimeError("rt_Scene construction failed")
         self.pton = lib().qrpy_scene_set_pton(self.h, pton) if pton else 0
+
+    def update(self, time, action):
+        """camera movement from user input (rt_Scene::update(time, action))"""
+        lib().qrpy_scene_update(self.h, int(time), int(action))
 
     def set_pton(self, pton):
         """Path-tracer samples per render (rt_Scene::set_pton); returns the

@@ -145,50 +145,8 @@ rt_Scene::~rt_Scene()
 
 rt_void rt_Scene::update(rt_time time, rt_si32 action)
 {
-    /* camera movement from user input (rt_Camera::update_action,
-     * object.cpp:495-573) */
-    qr::Node *cn = fl->cameras[fl->cam_idx];
-    rt_CAMERA *cam = (rt_CAMERA *)cn->obj->obj.pobj;
-    rt_TRANSFORM3D *trm = cn->trm;
-    rt_real t = (time - cn->obj->time) / 50.0f;
-    rt_real hs = (rt_real)sinf((float)((double)trm->rot[RT_Z] * RT_PI / 180.0));
-    rt_real hc = (rt_real)cosf((float)((double)trm->rot[RT_Z] * RT_PI / 180.0));
-    switch (action)
-    {
-    case RT_CAMERA_MOVE_UP:     trm->pos[RT_Z] += cam->dps[RT_K] * t; break;
-    case RT_CAMERA_MOVE_DOWN:   trm->pos[RT_Z] -= cam->dps[RT_K] * t; break;
-    case RT_CAMERA_MOVE_LEFT:
-        trm->pos[RT_X] -= cam->dps[RT_I] * t * hc;
-        trm->pos[RT_Y] -= cam->dps[RT_I] * t * hs; break;
-    case RT_CAMERA_MOVE_RIGHT:
-        trm->pos[RT_X] += cam->dps[RT_I] * t * hc;
-        trm->pos[RT_Y] += cam->dps[RT_I] * t * hs; break;
-    case RT_CAMERA_MOVE_BACK:
-        trm->pos[RT_X] += cam->dps[RT_J] * t * hs;
-        trm->pos[RT_Y] -= cam->dps[RT_J] * t * hc; break;
-    case RT_CAMERA_MOVE_FORWARD:
-        trm->pos[RT_X] -= cam->dps[RT_J] * t * hs;
-        trm->pos[RT_Y] += cam->dps[RT_J] * t * hc; break;
-    case RT_CAMERA_ROTATE_LEFT:
-        trm->rot[RT_Z] += cam->drt[RT_I] * t;
-        if (trm->rot[RT_Z] >= +180.0f) trm->rot[RT_Z] -= +360.0f; break;
-    case RT_CAMERA_ROTATE_RIGHT:
-        trm->rot[RT_Z] -= cam->drt[RT_I] * t;
-        if (trm->rot[RT_Z] <= -180.0f) trm->rot[RT_Z] += +360.0f; break;
-    case RT_CAMERA_ROTATE_UP:
-        if (trm->rot[RT_X] < 0.0f)
-        {
-            trm->rot[RT_X] += cam->drt[RT_J] * t;
-            if (trm->rot[RT_X] > 0.0f) trm->rot[RT_X] = 0.0f;
-        } break;
-    case RT_CAMERA_ROTATE_DOWN:
-        if (trm->rot[RT_X] > -180.0f)
-        {
-            trm->rot[RT_X] -= cam->drt[RT_J] * t;
-            if (trm->rot[RT_X] < -180.0f) trm->rot[RT_X] = -180.0f;
-        } break;
-    default: break;
-    }
+    /* camera movement from user input (rt_Scene::update, engine.cpp:3006) */
+    fl->camera_action(time, action);
 }
 
 rt_void rt_Scene::prepare(rt_time time)

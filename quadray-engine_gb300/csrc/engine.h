@@ -16,6 +16,7 @@
 #include "format.h"
 #include "rt_exception.h"
 #include "qr_gpu.h"
+#include "flatten.h"
 
 #define RT_FSAA_NO              0
 #define RT_FSAA_2X              1
@@ -24,22 +25,6 @@
 
 #define RT_TILE_W               8
 #define RT_TILE_H               8
-
-/* camera actions (codes of core/engine/object.h:47-63) */
-#define RT_CAMERA_CROUCH            0
-#define RT_CAMERA_JUMP              1
-#define RT_CAMERA_MOVE_DOWN         2
-#define RT_CAMERA_MOVE_UP           3
-#define RT_CAMERA_MOVE_LEFT         4
-#define RT_CAMERA_MOVE_RIGHT        5
-#define RT_CAMERA_MOVE_BACK         6
-#define RT_CAMERA_MOVE_FORWARD      7
-#define RT_CAMERA_LEAN_LEFT         8
-#define RT_CAMERA_LEAN_RIGHT        9
-#define RT_CAMERA_ROTATE_DOWN       10
-#define RT_CAMERA_ROTATE_UP         11
-#define RT_CAMERA_ROTATE_LEFT       12
-#define RT_CAMERA_ROTATE_RIGHT      13
 
 class rt_Platform;
 class rt_Scene;

@@ -70,6 +70,9 @@ static float cosa_(float a)
     return cosf((float)((double)a * RT_PI / 180.0));
 }
 
+float sina(float deg) { return sina_(deg); }
+float cosa(float deg) { return cosa_(deg); }
+
 /* ---- 4x4 column-major matrices (core/engine/rtgeom.cpp:59-228) ---------- */
 
 static void mat_mul_vec(float vp[4], float (*m1)[4], const float v1[4])
@@ -155,7 +158,8 @@ static void col_hdr(rt_COL *col)
 
 Flat::Flat(rt_SCENE *scn, int opts_, int x_res_, int y_res_, int fsaa_)
     : opts(opts_), x_res(x_res_), y_res(y_res_), fsaa(fsaa_),
-      depth(10), cam_idx(0), cam_off(0), cam_num(0), root(0)
+      depth(10), cam_idx(0), hor_sin(0.0f), hor_cos(1.0f), cam_off(0), cam_num(0),
+      root(0)
 {
     if (scn == RT_NULL || scn->root.tag != RT_TAG_ARRAY)
     {
@@ -1328,6 +1332,52 @@ void Flat::update(rt_time time)
     }
     emit_records();
     emit_lists();
+    hor_sin = sina_(cameras[cam_idx]->trm->rot[RT_Z]);
+    hor_cos = cosa_(cameras[cam_idx]->trm->rot[RT_Z]);
+}
+
+void Flat::camera_action(rt_time time, int action)
+{
+    Node *cn = cameras[cam_idx];
+    rt_CAMERA *cam = (rt_CAMERA *)cn->obj->obj.pobj;
+    rt_TRANSFORM3D *trm = cn->trm;
+    const rt_real t = (time - cn->obj->time) / 50.0f;
+    switch (action)
+    {
+    case RT_CAMERA_MOVE_UP:     trm->pos[RT_Z] += cam->dps[RT_K] * t; break;
+    case RT_CAMERA_MOVE_DOWN:   trm->pos[RT_Z] -= cam->dps[RT_K] * t; break;
+    case RT_CAMERA_MOVE_LEFT:
+        trm->pos[RT_X] -= cam->dps[RT_I] * t * hor_cos;
+        trm->pos[RT_Y] -= cam->dps[RT_I] * t * hor_sin; break;
+    case RT_CAMERA_MOVE_RIGHT:
+        trm->pos[RT_X] += cam->dps[RT_I] * t * hor_cos;
+        trm->pos[RT_Y] += cam->dps[RT_I] * t * hor_sin; break;
+    case RT_CAMERA_MOVE_BACK:
+        trm->pos[RT_X] += cam->dps[RT_J] * t * hor_sin;
+        trm->pos[RT_Y] -= cam->dps[RT_J] * t * hor_cos; break;
+    case RT_CAMERA_MOVE_FORWARD:
+        trm->pos[RT_X] -= cam->dps[RT_J] * t * hor_sin;
+        trm->pos[RT_Y] += cam->dps[RT_J] * t * hor_cos; break;
+    case RT_CAMERA_ROTATE_LEFT:
+        trm->rot[RT_Z] += cam->drt[RT_I] * t;
+        if (trm->rot[RT_Z] >= +180.0f) trm->rot[RT_Z] -= +360.0f; break;
+    case RT_CAMERA_ROTATE_RIGHT:
+        trm->rot[RT_Z] -= cam->drt[RT_I] * t;
+        if (trm->rot[RT_Z] <= -180.0f) trm->rot[RT_Z] += +360.0f; break;
+    case RT_CAMERA_ROTATE_UP:
+        if (trm->rot[RT_X] < 0.0f)
+        {
+            trm->rot[RT_X] += cam->drt[RT_J] * t;
+            if (trm->rot[RT_X] > 0.0f) trm->rot[RT_X] = 0.0f;
+        } break;
+    case RT_CAMERA_ROTATE_DOWN:
+        if (trm->rot[RT_X] > -180.0f)
+        {
+            trm->rot[RT_X] -= cam->drt[RT_J] * t;
+            if (trm->rot[RT_X] < -180.0f) trm->rot[RT_X] = -180.0f;
+        } break;
+    default: break;
+    }
 }
 
 void Flat::emit_records()

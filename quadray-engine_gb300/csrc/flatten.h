@@ -28,8 +28,31 @@
 #include "format.h"
 #include "qr_gpu.h"
 
+#ifndef RT_CAMERA_CROUCH
+/* camera actions (codes of core/engine/object.h:47-63) */
+#define RT_CAMERA_CROUCH            0
+#define RT_CAMERA_JUMP              1
+#define RT_CAMERA_MOVE_DOWN         2
+#define RT_CAMERA_MOVE_UP           3
+#define RT_CAMERA_MOVE_LEFT         4
+#define RT_CAMERA_MOVE_RIGHT        5
+#define RT_CAMERA_MOVE_BACK         6
+#define RT_CAMERA_MOVE_FORWARD      7
+#define RT_CAMERA_LEAN_LEFT         8
+#define RT_CAMERA_LEAN_RIGHT        9
+#define RT_CAMERA_ROTATE_DOWN       10
+#define RT_CAMERA_ROTATE_UP         11
+#define RT_CAMERA_ROTATE_LEFT       12
+#define RT_CAMERA_ROTATE_RIGHT      13
+#endif
+
 namespace qr
 {
+
+/* sine / cosine of an angle in degrees, exact at multiples of 90 degrees
+ * (RT_SINA / RT_COSA, core/config/rtbase.h:858-875) */
+float sina(float deg);
+float cosa(float deg);
 
 struct Node;
 
@@ -104,6 +127,9 @@ public:
 
     /* run the update phases for `time` and rebuild the flat arrays */
     void update(rt_time time);
+    /* camera movement from user input before the next update
+     * (rt_Camera::update_action, object.cpp:495-573) */
+    void camera_action(rt_time time, int action);
     /* ambient/camera parameters for the current camera */
     void frame_params(qr_frame_params *fp) const;
     /* descriptor pointing into this object's arrays */
@@ -114,6 +140,8 @@ public:
     int  depth;
     int  cam_idx;
     float factor, aspect;
+    float hor_sin, hor_cos;     /* current camera's heading as of the last
+                                   update (object.cpp:485-486) */
 
     std::vector<Node*>  nodes;      /* all nodes, creation order */
     std::vector<Node*>  surfaces;   /* creation order */

@@ -66,6 +66,11 @@ int qrpy_flat_update(void *f, long long time, int depth)
     return QR_OK;
 }
 
+void qrpy_flat_action(void *f, long long time, int action)
+{
+    ((qr::Flat *)f)->camera_action((rt_time)time, action);
+}
+
 int qrpy_flat_desc(void *f, qr_scene_desc *d, qr_frame_params *fp)
 {
     qr::Flat *fl = (qr::Flat *)f;
@@ -147,6 +152,11 @@ int qrpy_scene_render_device(void *h, long long time, unsigned int *dev_frame,
         return QR_ERR_CUDA;
     }
     return QR_OK;
+}
+
+void qrpy_scene_update(void *h, long long time, int action)
+{
+    ((qrpy_engine *)h)->scn->update((rt_time)time, action);
 }
 
 void *qrpy_scene_ctx(void *h)

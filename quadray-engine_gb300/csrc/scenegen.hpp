@@ -274,6 +274,10 @@ struct Scene
         c.col.val = amb_col;
         c.lum[0] = amb_lum;
         c.vpt[0] = pov;
+        /* movement and rotation steps per unit of time (50 ms) for the
+         * camera actions of rt_Scene::update */
+        c.dps[0] = 0.6f; c.dps[1] = 0.8f; c.dps[2] = 0.4f;
+        c.drt[0] = 3.0f; c.drt[1] = 2.0f; c.drt[2] = 0.0f;
         cams.push_back(c);
         rt_OBJECT o = obj(RT_TAG_CAMERA, &cams.back(), 1);
         trm_set(&o.trm, 1, 1, 1, rx, ry, rz, px, py, pz);

@@ -59,6 +59,8 @@ CASES = {
     "plain_s19_all_160x96": (1, 19, 8, 160, 96, 0, 1, 480, "full"),
     "plain_s21_aa2_160x96": (1, 21, 16, 160, 96, 1, 1, 0, "full"),
     "anim_s9_none_aa2_128x72_d4": (2, 9, 64, 128, 72, 1, 2, 0, "none", 4),
+    "plain_s24_actions_160x96": (1, 24, 16, 160, 96, 0, 4, 0, "full"),
+    "anim_s10_actions_128x72_d4": (2, 10, 64, 128, 72, 0, 3, 0, "none", 4),
     "anim_s1_none_160x90_d4":     (2, 1, 64, 160, 90, 0, 2, 0, "none", 4),
     "anim_s2_none_aa4_128x72_d4": (2, 2, 64, 128, 72, 2, 2, 0, "none", 4),
     "anim_s4_none_96x54_d10":     (2, 4, 64, 96, 54, 0, 1, 0, "none", 10),
@@ -76,6 +78,15 @@ CASES = {
 }
 
 
+# camera actions (rt_Scene::update(time, action), codes of
+# core/engine/object.h:47-63) applied before frames 1, 2, ... in turn:
+# forward, rotate left, up; rotate right, back
+ACTIONS = {
+    "plain_s24_actions_160x96": "7,12,3",
+    "anim_s10_actions_128x72_d4": "13,6",
+}
+
+
 def run_case(name, case):
     kind, seed, nq, w, h, fsaa, frames, flags, opts = case[:9]
     depth = case[9] if len(case) > 9 else 10
@@ -86,11 +97,17 @@ def run_case(name, case):
         cmd = [DRIVER, str(kind), str(seed), str(nq), str(w), str(h),
                str(fsaa), str(frames), str(flags), opts, out,
                str(min(8, os.cpu_count() or 1)), str(depth)]
+        env = dict(os.environ)
+        env.pop("QR_ACTIONS", None)
+        if name in ACTIONS:
+            env["QR_ACTIONS"] = ACTIONS[name]
         subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL,
-                       stderr=subprocess.DEVNULL)
+                       stderr=subprocess.DEVNULL, env=env)
         data = np.fromfile(out, dtype="<u4").reshape(frames, h, w)
     meta = dict(kind=kind, seed=seed, nq=nq, w=w, h=h, fsaa=fsaa,
                 frames=frames, flags=flags, opts=opts, depth=depth)
+    if name in ACTIONS:
+        meta["actions"] = ACTIONS[name]
     if last_only:
         data = data[-1:]
         meta["samples"] = frames

@@ -53,10 +53,15 @@ def flatten_case(qr, meta, time=0):
 
 
 def frames_of(qr, meta):
-    """Flatten every frame of a fixture (t = 16 ms per frame) in order."""
+    """Flatten every frame of a fixture (t = 16 ms per frame) in order,
+    applying the fixture's camera actions (rt_Scene::update) before frames
+    1, 2, ... as the reference's driver did."""
     g, f, desc, params = flatten_case(qr, meta, 0)
     yield desc, params
+    acts = [int(a) for a in meta.get("actions", "").split(",") if a]
     for k in range(1, meta["frames"]):
+        if acts:
+            f.action(16 * k, acts[(k - 1) % len(acts)])
         desc, params = f.update(16 * k, meta.get("depth", 10))
         yield desc, params
 
