@@ -180,17 +180,14 @@ def test_anim_full_size_frame_properties(qr, ctx):
 # ---- the reference's own frames (tests/golden), through the GPU
 
 def test_gpu_matches_reference_goldens(qr, ctx):
-    from test_oracle_golden import EXACT, load_golden, check_against_golden
+    from test_oracle_golden import EXACT, load_golden, check_against_golden, frames_of
     for path in EXACT:
         frames, meta = load_golden(path)
-        g = qr.GenScene(meta["kind"], meta["seed"], meta["nq"], meta["flags"])
-        opts = qr.OPTS_NONE if meta["opts"] == "none" else qr.OPTS_DEFAULT
-        f = qr.Flat(g, meta["w"], meta["h"], meta["fsaa"], opts)
-        for k in range(meta["frames"]):
-            desc, params = f.update(16 * k, meta.get("depth", 10))
+        for k, (desc, params) in enumerate(frames_of(qr, meta)):
             sid = ctx.upload(desc)
             img = ctx.render_host(sid, params)
             check_against_golden(img, frames[k], meta)
+            ctx.release(sid)
 
 
 # ---- bounding-volume hierarchy: the same frames as the in-order list walk
