@@ -373,16 +373,25 @@ int build_node(std::vector<Prim> &p, int lo, int hi, int depth, qr_accel_host *o
                 bin[q] = cnt[q] ? merge(bin[q], p[i].b) : p[i].b;
                 cnt[q]++;
             }
+            /* boxes and counts right of every split in one sweep from the
+             * right, then the left ones in one sweep from the left */
+            Box rb[NB];
+            int rn[NB + 1];
+            rn[NB] = 0;
+            for (int q = NB - 1; q >= 0; q--)
+            {
+                rn[q] = rn[q + 1] + cnt[q];
+                if (cnt[q]) rb[q] = rn[q + 1] ? merge(rb[q + 1], bin[q]) : bin[q];
+                else if (rn[q + 1]) rb[q] = rb[q + 1];
+            }
+            Box l;
+            int nl = 0;
             for (int s = 1; s < NB; s++)
             {
-                Box l, r;
-                int nl = 0, nr = 0;
-                for (int q = 0; q < s; q++)
-                    if (cnt[q]) { l = nl ? merge(l, bin[q]) : bin[q]; nl += cnt[q]; }
-                for (int q = s; q < NB; q++)
-                    if (cnt[q]) { r = nr ? merge(r, bin[q]) : bin[q]; nr += cnt[q]; }
+                if (cnt[s - 1]) { l = nl ? merge(l, bin[s - 1]) : bin[s - 1]; nl += cnt[s - 1]; }
+                const int nr = rn[s];
                 if (nl == 0 || nr == 0) continue;
-                const double cost = 0.5 * area(bb) + area(l) * nl + area(r) * nr;
+                const double cost = 0.5 * area(bb) + area(l) * nl + area(rb[s]) * nr;
                 if (cost < best) { best = cost; bax = ax; bsplit = s; }
             }
         }
@@ -432,7 +441,54 @@ int build_node(std::vector<Prim> &p, int lo, int hi, int depth, qr_accel_host *o
 
 } /* namespace */
 
+/* node boxes of a tree whose items' boxes changed, bottom-up: nodes are
+ * stored parent before children (build_node), so a reverse sweep sees
+ * children first */
+static void refit(qr_accel_host *out)
+{
+    for (int i = (int)out->nodes.size() - 1; i >= 0; i--)
+    {
+        qr_bnode &nd = out->nodes[i];
+        float lo[3] = {HUGE_VALF, HUGE_VALF, HUGE_VALF};
+        float hi[3] = {-HUGE_VALF, -HUGE_VALF, -HUGE_VALF};
+        if (nd.count > 0)
+        {
+            for (int j = nd.a; j < nd.a + nd.count; j++)
+            {
+                const float *b = &out->boxes[6 * (size_t)out->items[j].srf];
+                for (int k = 0; k < 3; k++)
+                {
+                    lo[k] = std::min(lo[k], b[k]);
+                    hi[k] = std::max(hi[k], b[3 + k]);
+                }
+            }
+        }
+        else
+        {
+            const qr_bnode &a = out->nodes[nd.a], &b = out->nodes[nd.b];
+            for (int k = 0; k < 3; k++)
+            {
+                lo[k] = std::min(a.lo[k], b.lo[k]);
+                hi[k] = std::max(a.hi[k], b.hi[k]);
+            }
+        }
+        for (int k = 0; k < 3; k++) { nd.lo[k] = lo[k]; nd.hi[k] = hi[k]; }
+    }
+}
+
+static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
+                       const qr_accel_host *topo);
+
 int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level)
+{
+    return accel_build(d, out, level, NULL);
+}
+
+/* level `level` of the hierarchy; with `topo` (the tree of another level
+ * over the same bounded surfaces) its topology is kept and only the boxes
+ * are refitted, the tree shape does not change the frame */
+static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
+                       const qr_accel_host *topo)
 {
     out->nodes.clear();
     out->items.clear();
@@ -572,6 +628,14 @@ int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level)
         p.it.pad = 0;
         prims.push_back(p);
     }
+    if (topo != NULL && topo->bounded == out->bounded && topo->always.size() == out->always.size())
+    {
+        out->nodes = topo->nodes;
+        out->items = topo->items;
+        out->depth = topo->depth;
+        refit(out);
+        return 0;
+    }
     if (!prims.empty()) build_node(prims, 0, (int)prims.size(), 1, out);
     return 0;
 }
@@ -584,18 +648,23 @@ void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
     out->items.clear();
     out->always.clear();
     out->depth = 0;
+    qr_accel_host lv0;
     for (int l = 0; l < QR_BVH_LEVELS; l++)
     {
-        qr_accel_host lv;
-        qr_accel_build(d, &lv, l);
-        const int n0 = (int)out->nodes.size(), i0 = (int)out->items.size();
+        const int n0 = (int)out->nodes.size();
         root[l] = n0;
         aoff[l] = (int)out->always.size();
-        anum[l] = (int)lv.always.size();
+        anum[l] = 0;
+        r2[l] = -1.0f;
         /* the outer levels' boxes are wide; for short lists a walk in list
-         * order is cheaper than traversing them */
+         * order is cheaper than traversing them, and they are not built */
         const bool used = l == 0 || d->cam_num >= QR_BVH_OUTER_MIN;
-        r2[l] = (used && lv.depth < QR_BVH_STACK - 2 && !lv.nodes.empty()) ? lv.ray_r2 : -1.0f;
+        if (!used) continue;
+        qr_accel_host lv;
+        accel_build(d, &lv, l, l == 0 ? NULL : &lv0);
+        const int i0 = (int)out->items.size();
+        anum[l] = (int)lv.always.size();
+        r2[l] = (lv.depth < QR_BVH_STACK - 2 && !lv.nodes.empty()) ? lv.ray_r2 : -1.0f;
         if (l == 0)
         {
             for (int k = 0; k < 3; k++) out->ray_c[k] = lv.ray_c[k];
@@ -613,5 +682,6 @@ void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
         }
         out->items.insert(out->items.end(), lv.items.begin(), lv.items.end());
         out->always.insert(out->always.end(), lv.always.begin(), lv.always.end());
+        if (l == 0) lv0 = lv;
     }
 }
