@@ -588,14 +588,13 @@ def main():
     # end to end through the engine API with a host frame buffer
     eng = qr.Engine(qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0), wl["w"], wl["h"],
                     fsaa=wl["fsaa"], depth=wl["depth"], pton=spp)
-    hbuf = np.zeros((wl["h"], wl["w"]), dtype=np.uint32)
     step_t = (lambda j: 16 * j) if wl["anim"] else (lambda j: 0)
     for j in range(args.warmup):
-        eng.render(step_t(j), hbuf)
+        eng.render(step_t(j))
     lat = []
     for i in range(args.steps):
         t0 = time.perf_counter()
-        eng.render(step_t(args.warmup + i), hbuf)
+        eng.render(step_t(args.warmup + i))     # into the caller-owned host frame
         lat.append(time.perf_counter() - t0)
     e2e_t = sum(lat)
     h2d = scene_bytes

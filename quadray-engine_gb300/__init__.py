@@ -116,7 +116,7 @@ def lib():
                                      ctypes.POINTER(QrFrameParams)]
         L.qrpy_flat_free.argtypes = [vp]
         L.qrpy_scene_new.restype = vp
-        L.qrpy_scene_new.argtypes = [vp, i32, i32, i32, i32, i32]
+        L.qrpy_scene_new.argtypes = [vp, i32, i32, i32, i32, i32, vp]
         L.qrpy_scene_render.argtypes = [vp, i64, vp]
         L.qrpy_scene_render_device.argtypes = [vp, i64, vp, vp]
         L.qrpy_scene_ctx.restype = vp
@@ -346,7 +346,11 @@ class Engine:
     def __init__(self, gen, x_res, y_res, fsaa=0, opts=OPTS_DEFAULT, depth=10, pton=0):
         self.gen = gen
         self.x_res, self.y_res = x_res, y_res
-        self.h = lib().qrpy_scene_new(gen.h, x_res, y_res, fsaa, opts, depth)
+        # the frame buffer the scene renders into (rt_Scene's caller-owned
+        # frame): render() returns it without a copy
+        self.frame = np.zeros((y_res, x_res), dtype=np.uint32)
+        self.h = lib().qrpy_scene_new(gen.h, x_res, y_res, fsaa, opts, depth,
+                                      self.frame.ctypes.data_as(ctypes.c_void_p))
         if not self.h:
             raise RuntimeError("rt_Scene construction failed")
         self.pton = lib().qrpy_scene_set_pton(self.h, pton) if pton else 0
@@ -362,11 +366,14 @@ class Engine:
         return self.pton
 
     def render(self, time=0, out=None):
-        if out is None:
-            out = np.zeros((self.y_res, self.x_res), dtype=np.uint32)
-        rc = lib().qrpy_scene_render(self.h, int(time), out.ctypes.data_as(ctypes.c_void_p))
+        """render frame `time` into the scene's frame buffer and return it
+        (the next render overwrites it); with `out`, a copy goes there"""
+        rc = lib().qrpy_scene_render(self.h, int(time), None)
         if rc != QR_OK:
             raise RuntimeError("render failed: %d" % rc)
+        if out is None:
+            return self.frame
+        np.copyto(out, self.frame)
         return out
 
     def render_device(self, time, dev_ptr, stream=0):

@@ -92,7 +92,8 @@ struct qrpy_engine
     rt_Scene    *scn;
 };
 
-void *qrpy_scene_new(void *g, int x_res, int y_res, int fsaa, int opts, int depth)
+void *qrpy_scene_new(void *g, int x_res, int y_res, int fsaa, int opts, int depth,
+                     unsigned int *frame)
 {
     qr_gen::Scene *sc = (qr_gen::Scene *)g;
     qrpy_engine *e = new qrpy_engine();
@@ -102,7 +103,10 @@ void *qrpy_scene_new(void *g, int x_res, int y_res, int fsaa, int opts, int dept
     {
         e->pfm = new rt_Platform(NULL, NULL);
         e->pfm->set_fsaa(fsaa);
-        e->scn = new(e->pfm) rt_Scene(&sc->scn, x_res, y_res, x_res, NULL, e->pfm);
+        /* frame: caller-owned x_res x y_res buffer, or NULL for the scene's
+         * own (rt_Scene's frame argument) */
+        e->scn = new(e->pfm) rt_Scene(&sc->scn, x_res, y_res, x_res, (rt_ui32 *)frame,
+                                      e->pfm);
         if (opts >= 0) e->scn->set_opts(opts);
         e->scn->set_depth(depth);
     }
