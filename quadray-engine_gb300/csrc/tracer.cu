@@ -480,9 +480,14 @@ __device__ __forceinline__ void local_ray(const qr_dscene &S, const Ray &r, int 
     }
 }
 
-/* ray / box slab test against the node's box, for t in (t_min, tmax] */
+/* ray / box slab test against the node's box, for t in (t_min, tmax]; the
+ * slab distances are (lo - org) / dir formed as lo * inv - org * inv with a
+ * fused multiply-add (oinv = org * inv per ray).  The test only prunes
+ * nodes and every box carries a margin far above this rounding, so which
+ * surfaces are tested, and the frame, do not depend on it. */
 __device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray &r,
-                                       const float inv[3], float tmax, float &tn, StP st)
+                                       const float inv[3], const float oinv[3], float tmax,
+                                       float &tn, StP st)
 {
     CNT(QR_STAT_BOX_TEST);
     float t0 = -FLT_MAX, t1 = FLT_MAX;
@@ -497,7 +502,8 @@ __device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray
             if (r.org[k] < lo || r.org[k] > hi) return 0;
             continue;
         }
-        const float a = (lo - r.org[k]) * inv[k], b = (hi - r.org[k]) * inv[k];
+        const float a = __fmaf_rn(lo, inv[k], -oinv[k]);
+        const float b = __fmaf_rn(hi, inv[k], -oinv[k]);
         t0 = fmaxf(t0, fminf(a, b));
         t1 = fminf(t1, fmaxf(a, b));
     }
@@ -538,17 +544,21 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
     int ai = 0, ia = 0, ib = 0, sp = 0;
     int2 stk[QR_BVH_STACK];         /* node, entry distance (float bits) */
     int cur = -1;                   /* node to visit next without a pop */
-    float inv[3];
+    float inv[3], oinv[3];
     int aend = 0;
     if (use_bvh)
     {
         #pragma unroll
-        for (int k = 0; k < 3; k++) inv[k] = r.dir[k] != 0.0f ? fdiv(1.0f, r.dir[k]) : 0.0f;
+        for (int k = 0; k < 3; k++)
+        {
+            inv[k] = r.dir[k] != 0.0f ? fdiv(1.0f, r.dir[k]) : 0.0f;
+            oinv[k] = r.org[k] * inv[k];
+        }
         ai = S.lvl_aoff[lvl];
         aend = ai + S.lvl_anum[lvl];
         const int root = S.lvl_root[lvl];
         float tn;
-        if (box_hit(&S.nodes[root], r, inv, w.tbuf, tn, st))
+        if (box_hit(&S.nodes[root], r, inv, oinv, w.tbuf, tn, st))
         {
             (void)tn;
             cur = root;
@@ -632,8 +642,8 @@ __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
                     }
                     const int b = __ldg(&n->b);
                     float ta, tb;
-                    const int ha = box_hit(&S.nodes[a], r, inv, w.tbuf, ta, st);
-                    const int hb = box_hit(&S.nodes[b], r, inv, w.tbuf, tb, st);
+                    const int ha = box_hit(&S.nodes[a], r, inv, oinv, w.tbuf, ta, st);
+                    const int hb = box_hit(&S.nodes[b], r, inv, oinv, w.tbuf, tb, st);
                     if (ha && hb)
                     {
                         if (sp >= QR_BVH_STACK) { w.fault = QR_FAULT_STACK; return; }

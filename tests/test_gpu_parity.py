@@ -247,3 +247,42 @@ def test_aa_subsample_threads_equal_pixel_threads(qr, ctx, kind, seed, nq, w, h,
     pp.flags = qr.FP_PIXEL_THREADS
     b = ctx.render_host(sid, pp)
     assert (a != b).sum() == 0
+
+
+def test_upload_rejects_out_of_range_indices(qr, ctx):
+    """qr_scene_upload checks every index the kernels follow before any copy:
+    descriptors with an element, material, texel or list index out of range
+    are refused with QR_ERR_ARG (no kernel ever sees them); the intact
+    descriptor is accepted"""
+    import ctypes
+    g = qr.GenScene(qr.SCN_PLAIN, 7, 16, qr.GEN_TEX)
+    f = qr.Flat(g, 64, 48, 0)
+    desc, params = f.update(0, 10)
+    elems = np.ctypeslib.as_array(ctypes.cast(desc.elems, ctypes.POINTER(ctypes.c_int32)),
+                                  shape=(desc.nelem * 4,)).copy()
+    mats = np.ctypeslib.as_array(ctypes.cast(desc.mat, ctypes.POINTER(ctypes.c_int32)),
+                                 shape=(desc.nmat * 28,)).copy()   # qr_mat: 112 bytes
+
+    def upload(el, mt, **fields):
+        d = qr.QrSceneDesc.from_buffer_copy(desc)
+        d.elems = el.ctypes.data
+        d.mat = mt.ctypes.data
+        for k, v in fields.items():
+            setattr(d, k, v)
+        sid = ctypes.c_int(-1)
+        rc = qr.lib().qr_scene_upload(ctx.h, ctypes.byref(d), ctypes.byref(sid))
+        if rc == 0:
+            ctx.release(sid.value)
+        return rc
+
+    assert upload(elems, mats) == 0
+    bad = elems.copy()
+    bad[1] = desc.nsrf + 5                      # element 0 refers past the records
+    assert upload(bad, mats) == 1
+    tex = [i for i in range(desc.nmat) if mats[28 * i + 3] & 0x800]   # QR_PROP_TEXTURE
+    assert tex
+    badm = mats.copy()
+    badm[28 * tex[0] + 19] = desc.ntex - 1       # tex_off: the texture runs past the texels
+    assert upload(elems, badm) == 1
+    assert upload(elems, mats, cam_num=desc.nelem + 1) == 1
+    assert upload(elems, mats, nmat=-1) == 1
