@@ -220,6 +220,16 @@ int main(int argc, char **argv)
         return 2;
     }
 
+    /* file-named textures: written where the reference's load_image looks
+     * (RT_PATH "data/textures/", RT_PATH = "../" in this build) */
+    if (flags & QR_GEN_TEXFILE)
+    {
+        if (qr_gen::write_texture_files(seed, "../data/textures") != 0)
+        {
+            fprintf(stderr, "cannot write ../data/textures/qr_tex*.bmp\n");
+            return 1;
+        }
+    }
     qr_gen::Scene *sc = qr_gen::build(kind, seed, nq, flags);
 
     rt_Platform *pfm;

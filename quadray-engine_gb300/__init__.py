@@ -30,6 +30,7 @@ GEN_GAMMA = 1 << 6       # the reference's gamma mode on
 GEN_SHAPES = 1 << 7      # plain scene with the other quadric kinds too
 GEN_ATTN = 1 << 8        # plain scene whose lights have ambient and attenuation
 GEN_NOFRESNEL = 1 << 9   # animated scene without Fresnel terms (the default)
+GEN_TEXFILE = 1 << 10    # with GEN_TEX: textures named as BMP files (write_textures)
 # camera actions (rt_Scene::update; codes of core/engine/object.h:47-63)
 CAMERA_MOVE_DOWN, CAMERA_MOVE_UP, CAMERA_MOVE_LEFT, CAMERA_MOVE_RIGHT = 2, 3, 4, 5
 CAMERA_MOVE_BACK, CAMERA_MOVE_FORWARD = 6, 7
@@ -109,6 +110,7 @@ def lib():
         L.qrpy_flat_new.argtypes = [vp, i32, i32, i32, i32]
         L.qrpy_flat_update.argtypes = [vp, i64, i32]
         L.qrpy_flat_action.argtypes = [vp, i64, i32]
+        L.qrpy_gen_write_textures.argtypes = [ctypes.c_ulonglong, ctypes.c_char_p]
         L.qrpy_flat_action.restype = None
         L.qrpy_scene_update.argtypes = [vp, i64, i32]
         L.qrpy_scene_update.restype = None
@@ -176,6 +178,14 @@ class GenScene:
             self.close()
         except Exception:
             pass
+
+
+def write_textures(seed, directory):
+    """write the BMP files qr_tex0-2.bmp that GEN_TEXFILE scenes of `seed`
+    name into `directory` (the engine reads them from $QR_PATH_TEXTURES,
+    default data/textures/)"""
+    if lib().qrpy_gen_write_textures(int(seed), os.fsencode(directory)) != 0:
+        raise RuntimeError("cannot write textures into %s" % directory)
 
 
 class Flat:

@@ -8,6 +8,7 @@
 #include <math.h>
 #include <string.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <algorithm>
 
 #include "flatten.h"
@@ -188,6 +189,49 @@ Flat::~Flat()
 }
 
 /* resolve a material (rt_Material ctor, object.cpp:4038-4180) */
+/* a 24-bit uncompressed BMP as the reference's load_image reads it
+ * (rtimag.cpp:47-186): signature, data offset, width, height, one plane,
+ * 24 bits, no compression; texels in file order (rows are not flipped),
+ * each row padded to 4 bytes, texel = B | G << 8 | R << 16 */
+static bool load_bmp(const char *path, std::vector<rt_ui32> &out, int &xd, int &yd)
+{
+    FILE *f = fopen(path, "rb");
+    if (f == NULL) return false;
+    unsigned char h[34];
+    bool ok = fread(h, 1, sizeof(h), f) == sizeof(h);
+    const unsigned sig = h[0] | (h[1] << 8);
+    const unsigned off = h[10] | (h[11] << 8) | (h[12] << 16) | ((unsigned)h[13] << 24);
+    const int w = (int)(h[18] | (h[19] << 8) | (h[20] << 16) | ((unsigned)h[21] << 24));
+    const int hh = (int)(h[22] | (h[23] << 8) | (h[24] << 16) | ((unsigned)h[25] << 24));
+    const unsigned planes = h[26] | (h[27] << 8), depth = h[28] | (h[29] << 8);
+    const unsigned comp = h[30] | (h[31] << 8) | (h[32] << 16) | ((unsigned)h[33] << 24);
+    ok = ok && sig == 0x4D42 && planes == 1 && depth == 24 && comp == 0 && w != 0 && hh != 0;
+    if (ok)
+    {
+        xd = w < 0 ? -w : w;
+        yd = hh < 0 ? -hh : hh;
+        ok = xd <= 65536 && yd <= 65536 && fseek(f, (long)off, SEEK_SET) == 0;
+    }
+    if (ok)
+    {
+        const int pad = ((xd * 3 + 3) / 4) * 4 - xd * 3;
+        out.assign((size_t)xd * yd, 0u);
+        unsigned char px[3], skip[3];
+        for (int y = 0; y < yd && ok; y++)
+        {
+            for (int x = 0; x < xd && ok; x++)
+            {
+                ok = fread(px, 1, 3, f) == 3;
+                out[(size_t)y * xd + x] = (rt_ui32)px[0] | ((rt_ui32)px[1] << 8) |
+                                          ((rt_ui32)px[2] << 16);
+            }
+            if (ok && pad) ok = fread(skip, 1, (size_t)pad, f) == (size_t)pad;
+        }
+    }
+    fclose(f);
+    return ok;
+}
+
 int Flat::material(rt_SIDE *sd, rt_MATERIAL *mt)
 {
     if (mt == RT_NULL)
@@ -211,7 +255,29 @@ int Flat::material(rt_SIDE *sd, rt_MATERIAL *mt)
     }
     if (x_dim == 0 && y_dim == 0 && ptex != RT_NULL)
     {
-        throw rt_Exception("texture loading from files is not supported");
+        /* a file name: the texture loads once per scene (rt_Texture,
+         * object.cpp:3990-4011; rtimag.cpp:47-186) */
+        const std::string name((const char *)tx->ptex);
+        size_t k = 0;
+        while (k < file_tex_name.size() && file_tex_name[k] != name) k++;
+        if (k == file_tex_name.size())
+        {
+            const char *pfx = getenv("QR_PATH_TEXTURES");
+            const std::string path = std::string(pfx ? pfx : "data/textures/") + name;
+            std::vector<rt_ui32> t;
+            int xd = 0, yd = 0;
+            if (!load_bmp(path.c_str(), t, xd, yd))
+            {
+                throw rt_Exception("failed to load image");
+            }
+            file_tex.push_back(t);
+            file_tex_name.push_back(name);
+            file_tex_dim.push_back(xd);
+            file_tex_dim.push_back(yd);
+        }
+        ptex = file_tex[k].data();
+        x_dim = file_tex_dim[2 * k];
+        y_dim = file_tex_dim[2 * k + 1];
     }
     M.texels = ptex;
     M.x_dim = x_dim;

@@ -24,6 +24,8 @@
 #ifndef QR_FLATTEN_H
 #define QR_FLATTEN_H
 
+#include <deque>
+#include <string>
 #include <vector>
 #include "format.h"
 #include "qr_gpu.h"
@@ -149,6 +151,11 @@ public:
     std::vector<Node*>  lights;     /* creation order */
     std::vector<Node*>  cameras;    /* creation order */
     std::vector<Material> mats;
+    /* textures loaded from files, by name (rt_Texture registry,
+     * object.cpp:3990-4011) */
+    std::deque<std::vector<rt_ui32> > file_tex;
+    std::vector<std::string> file_tex_name;
+    std::vector<int> file_tex_dim;
 
     std::vector<qr_srf>   srf;
     std::vector<qr_mat>   mat;

@@ -33,6 +33,11 @@ int qrpy_gen_nsurf(void *g)
     return ((qr_gen::Scene *)g)->nsurf;
 }
 
+int qrpy_gen_write_textures(unsigned long long seed, const char *dir)
+{
+    return qr_gen::write_texture_files(seed, dir);
+}
+
 void *qrpy_flat_new(void *g, int opts, int x_res, int y_res, int fsaa)
 {
     qr_gen::Scene *sc = (qr_gen::Scene *)g;

@@ -39,6 +39,9 @@
  * apex adjustment) and a hyperbolic paraboloid, each cut to a finite
  * extent, at right-angle or other rotations.  Flag QR_GEN_ATTN gives the
  * lights an ambient share and constant, linear and quadratic attenuation.
+ * Flag QR_GEN_TEXFILE (with QR_GEN_TEX) names the textures as files
+ * (qr_tex0-2.bmp, written by write_texture_files) instead of binding arrays,
+ * so the renderer loads them the way the reference's load_image does.
  * These flags draw from their own random stream, so the rest of the scene
  * is unchanged.
  */
@@ -46,6 +49,7 @@
 #define QR_SCENEGEN_HPP
 
 #include <stdint.h>
+#include <stdio.h>
 #include <math.h>
 #include <string.h>
 #include <vector>
@@ -70,6 +74,7 @@
 #define QR_GEN_SHAPES   (1 << 7)   /* QR_SCN_PLAIN: the other quadric kinds too */
 #define QR_GEN_ATTN     (1 << 8)   /* QR_SCN_PLAIN: light ambient and attenuation */
 #define QR_GEN_NOFRESNEL (1 << 9)  /* QR_SCN_ANIM: keep the default, Fresnel off */
+#define QR_GEN_TEXFILE  (1 << 10)  /* with QR_GEN_TEX: textures named as BMP files */
 
 namespace qr_gen
 {
@@ -216,6 +221,19 @@ struct Scene
         t.tex.ptex = (rt_void *)tx;
         t.tex.x_dim = xd;
         t.tex.y_dim = yd;
+        mats.push_back(t);
+        return &mats.back();
+    }
+
+    /* material m with a texture named as a file (RT_TEX with a name in
+     * ptex and no dimensions: the engine loads it) */
+    rt_MATERIAL *textured_file(const rt_MATERIAL *m, const char *name)
+    {
+        rt_MATERIAL t = *m;
+        t.tex.col.val = 0;
+        t.tex.ptex = (rt_void *)name;
+        t.tex.x_dim = 0;
+        t.tex.y_dim = 0;
         mats.push_back(t);
         return &mats.back();
     }
@@ -433,6 +451,50 @@ static void make_textures(Scene &sc, Rng &r)
 
 static float r_half(Rng &r) { return r.uf(1.5, 3.0); }
 
+/* the texture set of a seed as 24-bit BMP files qr_tex0-2.bmp in dir (rows
+ * in array order, so loading them gives the arrays back): returns 0, or -1
+ * when a file cannot be written */
+static int write_texture_files(uint64_t seed, const char *dir)
+{
+    static const int dims[3][2] = {{16, 16}, {32, 8}, {8, 64}};
+    Scene sc;
+    Rng rt(seed ^ 0x7E57C0DE5EEDull);
+    make_textures(sc, rt);
+    for (int k = 0; k < 3; k++)
+    {
+        char path[4096];
+        snprintf(path, sizeof(path), "%s/qr_tex%d.bmp", dir, k);
+        FILE *f = fopen(path, "wb");
+        if (f == NULL) return -1;
+        const int w = dims[k][0], h = dims[k][1], row = (w * 3 + 3) & ~3;
+        const unsigned size = 54u + (unsigned)(row * h), img = (unsigned)(row * h);
+        unsigned char hd[54];
+        memset(hd, 0, sizeof(hd));
+        const unsigned v[6] = {size, 0u, 54u, 40u, (unsigned)w, (unsigned)h};
+        const int at[6] = {2, 6, 10, 14, 18, 22};
+        hd[0] = 'B'; hd[1] = 'M';
+        for (int i = 0; i < 6; i++)
+            for (int b = 0; b < 4; b++) hd[at[i] + b] = (unsigned char)(v[i] >> (8 * b));
+        hd[26] = 1; hd[28] = 24;
+        for (int b = 0; b < 4; b++) hd[34 + b] = (unsigned char)(img >> (8 * b));
+        fwrite(hd, 1, 54, f);
+        std::vector<unsigned char> line((size_t)row, 0);
+        for (int y = 0; y < h; y++)
+        {
+            for (int x = 0; x < w; x++)
+            {
+                const rt_ui32 p = sc.texs[k][(size_t)y * w + x];
+                line[x * 3 + 0] = (unsigned char)(p & 0xFF);
+                line[x * 3 + 1] = (unsigned char)((p >> 8) & 0xFF);
+                line[x * 3 + 2] = (unsigned char)((p >> 16) & 0xFF);
+            }
+            fwrite(line.data(), 1, line.size(), f);
+        }
+        if (fclose(f) != 0) return -1;
+    }
+    return 0;
+}
+
 /* bind texture k of the set to both sides of surface s with side
  * transforms drawn from r (scale, right-angle or other rotation, offset) */
 static void texture_sides(Scene &sc, Rng &r, rt_SURFACE *s, int k)
@@ -453,7 +515,10 @@ static void texture_sides(Scene &sc, Rng &r, rt_SURFACE *s, int k)
         v[4] = r.uf(-1.0, 1.0);
         /* hit-ID scenes keep their ID materials (same draws, same scene) */
         if (sc.flags & QR_GEN_IDS) continue;
-        sd[i]->pmat = sc.textured(sd[i]->pmat, tx, dims[k][0], dims[k][1]);
+        static const char *const files[3] = {"qr_tex0.bmp", "qr_tex1.bmp", "qr_tex2.bmp"};
+        sd[i]->pmat = (sc.flags & QR_GEN_TEXFILE) ? sc.textured_file(sd[i]->pmat, files[k])
+                                                  : sc.textured(sd[i]->pmat, tx, dims[k][0],
+                                                                dims[k][1]);
         sd[i]->scl[0] = v[0];
         sd[i]->scl[1] = v[1];
         sd[i]->rot = v[2];

@@ -36,7 +36,10 @@ DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 #   64 = gamma on, 128 = paracylinder, hypercylinder, two-plane, double
 #   cone and hyperbolic paraboloid added, 256 = lights with an ambient share
 #   and attenuation, 512 = animated scene without Fresnel terms (the
-#   reference's default); fsaa 1 = 2x alternating, 2 = 4x rotated grid;
+#   reference's default), 1024 = the textures named as BMP files that the
+#   reference's load_image reads (the driver writes them to
+#   ../data/textures/ of its working directory); fsaa 1 = 2x alternating,
+#   2 = 4x rotated grid;
 #   opts "none" renders the reference without its list optimisations
 CASES = {
     "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
@@ -61,6 +64,7 @@ CASES = {
     "anim_s9_none_aa2_128x72_d4": (2, 9, 64, 128, 72, 1, 2, 0, "none", 4),
     "plain_s24_actions_160x96": (1, 24, 16, 160, 96, 0, 4, 0, "full"),
     "anim_s10_actions_128x72_d4": (2, 10, 64, 128, 72, 0, 3, 0, "none", 4),
+    "plain_s7_texfile_aa4_128x80": (1, 7, 16, 128, 80, 2, 1, 32 | 1024, "full"),
     "anim_s1_none_160x90_d4":     (2, 1, 64, 160, 90, 0, 2, 0, "none", 4),
     "anim_s2_none_aa4_128x72_d4": (2, 2, 64, 128, 72, 2, 2, 0, "none", 4),
     "anim_s4_none_96x54_d10":     (2, 4, 64, 96, 54, 0, 1, 0, "none", 10),
@@ -93,6 +97,9 @@ def run_case(name, case):
     last_only = len(case) > 10 and case[10] == "last"
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "frame.bin")
+        run = os.path.join(td, "run")
+        os.makedirs(run)
+        os.makedirs(os.path.join(td, "data", "textures"))
         # the frame does not depend on the worker count (rows are independent)
         cmd = [DRIVER, str(kind), str(seed), str(nq), str(w), str(h),
                str(fsaa), str(frames), str(flags), opts, out,
@@ -102,7 +109,7 @@ def run_case(name, case):
         if name in ACTIONS:
             env["QR_ACTIONS"] = ACTIONS[name]
         subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL,
-                       stderr=subprocess.DEVNULL, env=env)
+                       stderr=subprocess.DEVNULL, env=env, cwd=run)
         data = np.fromfile(out, dtype="<u4").reshape(frames, h, w)
     meta = dict(kind=kind, seed=seed, nq=nq, w=w, h=h, fsaa=fsaa,
                 frames=frames, flags=flags, opts=opts, depth=depth)

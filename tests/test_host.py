@@ -169,3 +169,28 @@ def test_frame_params_camera(qr):
     assert abs(np.dot(hor, ver)) < 1e-6
     assert np.allclose(p.org, [0.0, -25.0, 8.0])
     assert abs(p.t_min - 0.5 / np.tan(np.radians(30.0))) < 1e-5
+
+
+def test_bmp_textures_load_like_the_reference(qr, tmp_path, monkeypatch):
+    """Textures named as files load as the reference's load_image reads
+    them: 24-bit uncompressed BMPs, texels in file order; a file of another
+    depth, or a missing file, fails the scene's construction"""
+    qr.write_textures(7, str(tmp_path))
+    monkeypatch.setenv("QR_PATH_TEXTURES", str(tmp_path) + "/")
+    ref = qr.Flat(qr.GenScene(qr.SCN_PLAIN, 7, 16, qr.GEN_TEX), 64, 48)
+    d_ref, _ = ref.update(0, 10)
+    f = qr.Flat(qr.GenScene(qr.SCN_PLAIN, 7, 16, qr.GEN_TEX | qr.GEN_TEXFILE), 64, 48)
+    d, _ = f.update(0, 10)
+    import ctypes
+    a = np.ctypeslib.as_array(ctypes.cast(d.texels, ctypes.POINTER(ctypes.c_uint32)), (d.ntex,))
+    b = np.ctypeslib.as_array(ctypes.cast(d_ref.texels, ctypes.POINTER(ctypes.c_uint32)),
+                              (d_ref.ntex,))
+    assert d.ntex == d_ref.ntex and (a == b).all()
+    raw = bytearray((tmp_path / "qr_tex1.bmp").read_bytes())
+    raw[28] = 32                                    # bits per pixel
+    (tmp_path / "qr_tex1.bmp").write_bytes(bytes(raw))
+    with pytest.raises(RuntimeError):
+        qr.Flat(qr.GenScene(qr.SCN_PLAIN, 7, 16, qr.GEN_TEX | qr.GEN_TEXFILE), 64, 48)
+    (tmp_path / "qr_tex1.bmp").unlink()
+    with pytest.raises(RuntimeError):
+        qr.Flat(qr.GenScene(qr.SCN_PLAIN, 7, 16, qr.GEN_TEX | qr.GEN_TEXFILE), 64, 48)

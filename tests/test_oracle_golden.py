@@ -44,7 +44,22 @@ def load_golden(path):
     return z["frames"], json.loads(str(z["meta"]))
 
 
+_TEXDIRS = {}
+
+
+def texture_dir(qr, seed):
+    """a directory holding the BMP textures of GEN_TEXFILE scenes of `seed`"""
+    if seed not in _TEXDIRS:
+        import tempfile
+        d = tempfile.mkdtemp(prefix="qr_tex_")
+        qr.write_textures(seed, d)
+        _TEXDIRS[seed] = d
+    return _TEXDIRS[seed]
+
+
 def flatten_case(qr, meta, time=0):
+    if meta["flags"] & qr.GEN_TEXFILE:
+        os.environ["QR_PATH_TEXTURES"] = texture_dir(qr, meta["seed"]) + os.sep
     g = qr.GenScene(meta["kind"], meta["seed"], meta["nq"], meta["flags"])
     opts = qr.OPTS_NONE if meta["opts"] == "none" else qr.OPTS_DEFAULT
     f = qr.Flat(g, meta["w"], meta["h"], meta["fsaa"], opts)
