@@ -268,8 +268,22 @@ int main(int argc, char **argv)
                 if (*p == ',') p++;
             }
         }
+        /* QR_NEXTCAM="k,...": rt_Scene::next_cam before frame k */
+        std::vector<int> nextcam;
+        if (getenv("QR_NEXTCAM") != NULL)
+        {
+            const char *p = getenv("QR_NEXTCAM");
+            while (*p)
+            {
+                nextcam.push_back(atoi(p));
+                while (*p && *p != ',') p++;
+                if (*p == ',') p++;
+            }
+        }
         for (int f = 0; f < frames; f++)
         {
+            for (size_t c = 0; c < nextcam.size(); c++)
+                if (nextcam[c] == f) scene->next_cam();
             if (f > 0 && !actions.empty())
                 scene->update((rt_time)f * 16, actions[(f - 1) % actions.size()]);
             double t0 = now_ms();

@@ -31,6 +31,7 @@ GEN_SHAPES = 1 << 7      # plain scene with the other quadric kinds too
 GEN_ATTN = 1 << 8        # plain scene whose lights have ambient and attenuation
 GEN_NOFRESNEL = 1 << 9   # animated scene without Fresnel terms (the default)
 GEN_TEXFILE = 1 << 10    # with GEN_TEX: textures named as BMP files (write_textures)
+GEN_CAMERAS = 1 << 11    # plain scene with a second camera (next_cam)
 # camera actions (rt_Scene::update; codes of core/engine/object.h:47-63)
 CAMERA_MOVE_DOWN, CAMERA_MOVE_UP, CAMERA_MOVE_LEFT, CAMERA_MOVE_RIGHT = 2, 3, 4, 5
 CAMERA_MOVE_BACK, CAMERA_MOVE_FORWARD = 6, 7
@@ -110,6 +111,8 @@ def lib():
         L.qrpy_flat_new.argtypes = [vp, i32, i32, i32, i32]
         L.qrpy_flat_update.argtypes = [vp, i64, i32]
         L.qrpy_flat_action.argtypes = [vp, i64, i32]
+        L.qrpy_flat_next_cam.argtypes = [vp]
+        L.qrpy_scene_next_cam.argtypes = [vp]
         L.qrpy_gen_write_textures.argtypes = [ctypes.c_ulonglong, ctypes.c_char_p]
         L.qrpy_flat_action.restype = None
         L.qrpy_scene_update.argtypes = [vp, i64, i32]
@@ -205,6 +208,11 @@ class Flat:
             raise RuntimeError("update failed: %d" % rc)
         lib().qrpy_flat_desc(self.h, ctypes.byref(self.desc), ctypes.byref(self.params))
         return self.desc, self.params
+
+    def next_cam(self):
+        """switch to the next camera (rt_Scene::next_cam); returns its index
+        in the reference's camera list"""
+        return lib().qrpy_flat_next_cam(self.h)
 
     def action(self, time, action):
         """camera movement before the next update (rt_Scene::update(time,
@@ -364,6 +372,10 @@ class Engine:
         if not self.h:
             raise RuntimeError("rt_Scene construction failed")
         self.pton = lib().qrpy_scene_set_pton(self.h, pton) if pton else 0
+
+    def next_cam(self):
+        """rt_Scene::next_cam"""
+        return lib().qrpy_scene_next_cam(self.h)
 
     def update(self, time, action):
         """camera movement from user input (rt_Scene::update(time, action))"""

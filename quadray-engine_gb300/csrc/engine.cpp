@@ -229,7 +229,8 @@ rt_si32 rt_Scene::set_opts(rt_si32 o)
     int keep_cam = fl->cam_idx;
     delete fl;
     fl = new qr::Flat(scn, opts, x_res, y_res, pfm->fsaa);
-    fl->cam_idx = keep_cam < (int)fl->cameras.size() ? keep_cam : 0;
+    fl->cam_idx = keep_cam < (int)fl->cameras.size() ? keep_cam
+                                                      : (int)fl->cameras.size() - 1;
     if (scene_id >= 0)
     {
         qr_scene_release(pfm->get_ctx(), scene_id);
@@ -251,11 +252,12 @@ rt_si32 rt_Scene::set_pton(rt_si32 pton)
     }
     return pt_on;
 }
-rt_si32 rt_Scene::get_cam_idx() { return fl->cam_idx; }
+/* the index in the reference's camera list: the camera created last is 0
+ * (engine.cpp:3828-3850) */
+rt_si32 rt_Scene::get_cam_idx() { return (rt_si32)fl->cameras.size() - 1 - fl->cam_idx; }
 rt_si32 rt_Scene::next_cam()
 {
-    fl->cam_idx = (fl->cam_idx + 1) % (int)fl->cameras.size();
-    return fl->cam_idx;
+    return fl->next_cam();
 }
 rt_ui32 *rt_Scene::get_frame() { return frame; }
 rt_Platform *rt_Scene::get_platform() { return pfm; }

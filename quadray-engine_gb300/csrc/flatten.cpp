@@ -181,6 +181,10 @@ Flat::Flat(rt_SCENE *scn, int opts_, int x_res_, int y_res_, int fsaa_)
     {
         throw rt_Exception("scene doesn't contain camera");
     }
+    /* the reference keeps its cameras in a list each new one is pushed in
+     * front of (object.cpp:429-431, object.h:178) and starts with its head
+     * (engine.cpp:2956-2961): the camera created last */
+    cam_idx = (int)cameras.size() - 1;
 }
 
 Flat::~Flat()
@@ -1400,6 +1404,15 @@ void Flat::update(rt_time time)
     emit_lists();
     hor_sin = sina_(cameras[cam_idx]->trm->rot[RT_Z]);
     hor_cos = cosa_(cameras[cam_idx]->trm->rot[RT_Z]);
+}
+
+int Flat::next_cam()
+{
+    const int n = (int)cameras.size();
+    int r = n - 1 - cam_idx;
+    r = r + 1 < n ? r + 1 : 0;
+    cam_idx = n - 1 - r;
+    return r;
 }
 
 void Flat::camera_action(rt_time time, int action)

@@ -132,6 +132,9 @@ public:
     /* camera movement from user input before the next update
      * (rt_Camera::update_action, object.cpp:495-573) */
     void camera_action(rt_time time, int action);
+    /* the next camera of the reference's list (rt_Scene::next_cam,
+     * engine.cpp:3836-3850); returns its index in that list */
+    int next_cam();
     /* ambient/camera parameters for the current camera */
     void frame_params(qr_frame_params *fp) const;
     /* descriptor pointing into this object's arrays */
@@ -140,7 +143,8 @@ public:
     int  opts;
     int  x_res, y_res, fsaa;
     int  depth;
-    int  cam_idx;
+    int  cam_idx;               /* current camera in `cameras`; the
+                                   reference's list runs the other way */
     float factor, aspect;
     float hor_sin, hor_cos;     /* current camera's heading as of the last
                                    update (object.cpp:485-486) */

@@ -71,6 +71,11 @@ int qrpy_flat_update(void *f, long long time, int depth)
     return QR_OK;
 }
 
+int qrpy_flat_next_cam(void *f)
+{
+    return ((qr::Flat *)f)->next_cam();
+}
+
 void qrpy_flat_action(void *f, long long time, int action)
 {
     ((qr::Flat *)f)->camera_action((rt_time)time, action);
@@ -161,6 +166,11 @@ int qrpy_scene_render_device(void *h, long long time, unsigned int *dev_frame,
         return QR_ERR_CUDA;
     }
     return QR_OK;
+}
+
+int qrpy_scene_next_cam(void *h)
+{
+    return ((qrpy_engine *)h)->scn->next_cam();
 }
 
 void qrpy_scene_update(void *h, long long time, int action)

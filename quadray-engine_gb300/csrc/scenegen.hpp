@@ -39,6 +39,8 @@
  * apex adjustment) and a hyperbolic paraboloid, each cut to a finite
  * extent, at right-angle or other rotations.  Flag QR_GEN_ATTN gives the
  * lights an ambient share and constant, linear and quadratic attenuation.
+ * Flag QR_GEN_CAMERAS adds a second camera (created last, so the
+ * reference starts with it) to QR_SCN_PLAIN; rt_Scene::next_cam switches.
  * Flag QR_GEN_TEXFILE (with QR_GEN_TEX) names the textures as files
  * (qr_tex0-2.bmp, written by write_texture_files) instead of binding arrays,
  * so the renderer loads them the way the reference's load_image does.
@@ -75,6 +77,7 @@
 #define QR_GEN_ATTN     (1 << 8)   /* QR_SCN_PLAIN: light ambient and attenuation */
 #define QR_GEN_NOFRESNEL (1 << 9)  /* QR_SCN_ANIM: keep the default, Fresnel off */
 #define QR_GEN_TEXFILE  (1 << 10)  /* with QR_GEN_TEX: textures named as BMP files */
+#define QR_GEN_CAMERAS  (1 << 11)  /* QR_SCN_PLAIN: a second camera */
 
 namespace qr_gen
 {
@@ -621,6 +624,9 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
             root.push_back(w);
         }
     }
+    if (sc.flags & QR_GEN_CAMERAS)
+        root.push_back(sc.camera(14.0f, -18.0f, 6.0f, -72.0f, 0.0f, 38.0f, 0.7f,
+                                 0xE0E8FF, 0.15f));
     rt_OBJECT ro = sc.array(root);
     sc.scn.root = ro.obj;
     sc.scn.opts = (sc.flags & QR_GEN_GAMMA) ? RT_OPTS_GAMMA : 0;

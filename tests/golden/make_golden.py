@@ -39,7 +39,8 @@ DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 #   reference's default), 1024 = the textures named as BMP files that the
 #   reference's load_image reads (the driver writes them to
 #   ../data/textures/ of its working directory); fsaa 1 = 2x alternating,
-#   2 = 4x rotated grid;
+#   2 = 4x rotated grid; 2048 = a second camera (next_cam before the frames
+#   listed in NEXTCAM);
 #   opts "none" renders the reference without its list optimisations
 CASES = {
     "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
@@ -65,6 +66,7 @@ CASES = {
     "plain_s24_actions_160x96": (1, 24, 16, 160, 96, 0, 4, 0, "full"),
     "anim_s10_actions_128x72_d4": (2, 10, 64, 128, 72, 0, 3, 0, "none", 4),
     "plain_s7_texfile_aa4_128x80": (1, 7, 16, 128, 80, 2, 1, 32 | 1024, "full"),
+    "plain_s25_cameras_160x96": (1, 25, 16, 160, 96, 0, 3, 2048, "full"),
     "anim_s1_none_160x90_d4":     (2, 1, 64, 160, 90, 0, 2, 0, "none", 4),
     "anim_s2_none_aa4_128x72_d4": (2, 2, 64, 128, 72, 2, 2, 0, "none", 4),
     "anim_s4_none_96x54_d10":     (2, 4, 64, 96, 54, 0, 1, 0, "none", 10),
@@ -89,6 +91,10 @@ ACTIONS = {
     "plain_s24_actions_160x96": "7,12,3",
     "anim_s10_actions_128x72_d4": "13,6",
 }
+# rt_Scene::next_cam before the listed frames
+NEXTCAM = {
+    "plain_s25_cameras_160x96": "1,2",
+}
 
 
 def run_case(name, case):
@@ -106,8 +112,11 @@ def run_case(name, case):
                str(min(8, os.cpu_count() or 1)), str(depth)]
         env = dict(os.environ)
         env.pop("QR_ACTIONS", None)
+        env.pop("QR_NEXTCAM", None)
         if name in ACTIONS:
             env["QR_ACTIONS"] = ACTIONS[name]
+        if name in NEXTCAM:
+            env["QR_NEXTCAM"] = NEXTCAM[name]
         subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL,
                        stderr=subprocess.DEVNULL, env=env, cwd=run)
         data = np.fromfile(out, dtype="<u4").reshape(frames, h, w)
@@ -115,6 +124,8 @@ def run_case(name, case):
                 frames=frames, flags=flags, opts=opts, depth=depth)
     if name in ACTIONS:
         meta["actions"] = ACTIONS[name]
+    if name in NEXTCAM:
+        meta["nextcam"] = NEXTCAM[name]
     if last_only:
         data = data[-1:]
         meta["samples"] = frames

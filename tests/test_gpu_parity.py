@@ -91,11 +91,13 @@ def test_engine_api_matches_c_abi(qr, oracle):
     assert (a != cpu).sum() == 0
 
 
-@pytest.mark.parametrize("name", ["plain_s24_actions_160x96", "anim_s10_actions_128x72_d4"])
+@pytest.mark.parametrize("name", ["plain_s24_actions_160x96", "anim_s10_actions_128x72_d4",
+                                  "plain_s25_cameras_160x96"])
 def test_engine_camera_actions_match_reference(qr, name):
-    """rt_Scene::update(time, action) then render(time), frame after frame,
-    through the drop-in rt_Scene: the reference's own frames under the same
-    camera actions (forward, rotate, up / rotate, back)"""
+    """rt_Scene::update(time, action) and next_cam, then render(time), frame
+    after frame, through the drop-in rt_Scene: the reference's own frames
+    under the same camera actions (forward, rotate, up / rotate, back) and
+    camera switches"""
     import os
     from test_oracle_golden import check_against_golden, load_golden
     frames, meta = load_golden(os.path.join(os.path.dirname(os.path.abspath(__file__)),
@@ -103,9 +105,13 @@ def test_engine_camera_actions_match_reference(qr, name):
     g = qr.GenScene(meta["kind"], meta["seed"], meta["nq"], meta["flags"])
     opts = qr.OPTS_NONE if meta["opts"] == "none" else qr.OPTS_DEFAULT
     eng = qr.Engine(g, meta["w"], meta["h"], fsaa=meta["fsaa"], opts=opts, depth=meta["depth"])
-    acts = [int(x) for x in meta["actions"].split(",")]
+    acts = [int(x) for x in meta.get("actions", "").split(",") if x]
+    cams = [int(x) for x in meta.get("nextcam", "").split(",") if x]
     for k in range(meta["frames"]):
-        if k > 0:
+        for c in cams:
+            if c == k:
+                eng.next_cam()
+        if k > 0 and acts:
             eng.update(16 * k, acts[(k - 1) % len(acts)])
         img = eng.render(16 * k).copy()
         check_against_golden(img, frames[k], meta)

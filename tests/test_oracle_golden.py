@@ -74,7 +74,11 @@ def frames_of(qr, meta):
     g, f, desc, params = flatten_case(qr, meta, 0)
     yield desc, params
     acts = [int(a) for a in meta.get("actions", "").split(",") if a]
+    cams = [int(a) for a in meta.get("nextcam", "").split(",") if a]
     for k in range(1, meta["frames"]):
+        for c in cams:
+            if c == k:
+                f.next_cam()
         if acts:
             f.action(16 * k, acts[(k - 1) % len(acts)])
         desc, params = f.update(16 * k, meta.get("depth", 10))
