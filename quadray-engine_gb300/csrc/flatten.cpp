@@ -12,6 +12,7 @@
 #include <algorithm>
 
 #include "flatten.h"
+#include "xform.h"
 #include "rt_exception.h"
 
 namespace qr
@@ -76,72 +77,15 @@ float cosa(float deg) { return cosa_(deg); }
 
 /* ---- 4x4 column-major matrices (core/engine/rtgeom.cpp:59-228) ---------- */
 
-static void mat_mul_vec(float vp[4], float (*m1)[4], const float v1[4])
-{
-    for (int i = 0; i < 4; i++)
-    {
-        vp[i] = m1[0][i] * v1[0] +
-                m1[1][i] * v1[1] +
-                m1[2][i] * v1[2] +
-                m1[3][i] * v1[3];
-    }
-}
-
-static void mat_mul_mat(float (*mp)[4], float (*m1)[4], float (*m2)[4])
-{
-    for (int i = 0; i < 4; i++)
-    {
-        mat_mul_vec(mp[i], m1, m2[i]);
-    }
-}
-
-/* T * Rz * Ry * Rx * S (rtgeom.cpp:102-164) */
+/* T * Rz * Ry * Rx * S (rtgeom.cpp:102-164), scale only with `as` */
 static void mat_from_transform(float (*mp)[4], const rt_TRANSFORM3D *t, int as)
 {
-    float mt[4][4];
-    float sx = as ? t->scl[RT_X] : 1.0f;
-    float sy = as ? t->scl[RT_Y] : 1.0f;
-    float sz = as ? t->scl[RT_Z] : 1.0f;
-    float sc[4][4] = {{sx, 0, 0, 0}, {0, sy, 0, 0}, {0, 0, sz, 0}, {0, 0, 0, 1}};
-
-    float s, c;
-    s = sina_(t->rot[RT_X]); c = cosa_(t->rot[RT_X]);
-    float rx[4][4] = {{1, 0, 0, 0}, {0, +c, +s, 0}, {0, -s, +c, 0}, {0, 0, 0, 1}};
-    s = sina_(t->rot[RT_Y]); c = cosa_(t->rot[RT_Y]);
-    float ry[4][4] = {{+c, 0, -s, 0}, {0, 1, 0, 0}, {+s, 0, +c, 0}, {0, 0, 0, 1}};
-    s = sina_(t->rot[RT_Z]); c = cosa_(t->rot[RT_Z]);
-    float rz[4][4] = {{+c, +s, 0, 0}, {-s, +c, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
-    float ps[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0},
-                      {t->pos[RT_X], t->pos[RT_Y], t->pos[RT_Z], 1}};
-
-    mat_mul_mat(mt, rx, sc);
-    mat_mul_mat(mp, ry, mt);
-    mat_mul_mat(mt, rz, mp);
-    mat_mul_mat(mp, ps, mt);
-}
-
-/* 3x3 inverse by cofactors (rtgeom.cpp:167-195) */
-static void mat_inverse(float (*mp)[4], float (*m1)[4])
-{
-    memset(mp, 0, sizeof(float) * 16);
-
-    float a = m1[1][1] * m1[2][2] - m1[2][1] * m1[1][2];
-    float b = m1[2][1] * m1[0][2] - m1[0][1] * m1[2][2];
-    float c = m1[0][1] * m1[1][2] - m1[1][1] * m1[0][2];
-
-    float d = m1[2][0] * m1[1][2] - m1[1][0] * m1[2][2];
-    float e = m1[0][0] * m1[2][2] - m1[2][0] * m1[0][2];
-    float f = m1[0][2] * m1[1][0] - m1[0][0] * m1[1][2];
-
-    float g = m1[1][0] * m1[2][1] - m1[2][0] * m1[1][1];
-    float h = m1[2][0] * m1[0][1] - m1[0][0] * m1[2][1];
-    float l = m1[0][0] * m1[1][1] - m1[1][0] * m1[0][1];
-
-    float q = 1.0f / (m1[0][0] * a + m1[1][0] * b + m1[2][0] * c);
-
-    mp[0][0] = a * q; mp[0][1] = b * q; mp[0][2] = c * q;
-    mp[1][0] = d * q; mp[1][1] = e * q; mp[1][2] = f * q;
-    mp[2][0] = g * q; mp[2][1] = h * q; mp[2][2] = l * q;
+    const float scl[3] = {as ? t->scl[RT_X] : 1.0f, as ? t->scl[RT_Y] : 1.0f,
+                          as ? t->scl[RT_Z] : 1.0f};
+    const float s3[3] = {sina_(t->rot[RT_X]), sina_(t->rot[RT_Y]), sina_(t->rot[RT_Z])};
+    const float c3[3] = {cosa_(t->rot[RT_X]), cosa_(t->rot[RT_Y]), cosa_(t->rot[RT_Z])};
+    const float pos[3] = {t->pos[RT_X], t->pos[RT_Y], t->pos[RT_Z]};
+    mat_from_sc(mp, s3, c3, pos, scl);
 }
 
 /* packed XRGB to [0,1] colour (object.cpp:435-440, 599-604) */
