@@ -204,6 +204,75 @@ int qr_scene_upload(qr_ctx *ctx, const qr_scene_desc *desc, int *scene_id);
 int qr_scene_update(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc);
 int qr_scene_release(qr_ctx *ctx, int scene_id);
 
+/*
+ * Device-side update phases for animated scenes.  The reference runs the
+ * update phases on the host for every frame (rt_Scene::render,
+ * core/engine/engine.cpp:3350-3501: animators and transforms in
+ * rt_Object::update_status / update_matrix, object.cpp:175-389; inverse
+ * matrices in rt_Node::update_fields, object.cpp:826-857).  Here the host
+ * runs only the animators and hands over each animated transform's sines,
+ * cosines and position; one kernel launch per frame then forms the
+ * transform chain, the inverse matrices and positions of the records that
+ * move, the world boxes of the surfaces that move and the hierarchy's node
+ * boxes, and the frame equals the frame of a full host update.
+ *
+ * The table (qr_anim_node, one entry per record or light whose transform
+ * changes when animators run, parents before children) says how each
+ * entry's matrix M follows from its parent entry's matrix T and fixed
+ * matrices P, R (rt_Object::update_matrix, object.cpp:221-389):
+ *   QR_ANIM_OWN     M = P R            (own rotation, no transform node)
+ *   QR_ANIM_UNDER   M = (T P) R        (own rotation under a transform node)
+ *   QR_ANIM_NODE    M = T P            (becomes a transform node)
+ * where R is the entry's own rotation: T(pos) Rz Ry Rx from animated
+ * transform `param`, or the fixed matrix r when param < 0.
+ */
+#define QR_ANIM_OWN     0
+#define QR_ANIM_UNDER   1
+#define QR_ANIM_NODE    2
+
+typedef struct qr_anim_node
+{
+    int32_t kind;       /* QR_ANIM_* */
+    int32_t parent;     /* entry of T (QR_ANIM_UNDER, QR_ANIM_NODE), else -1 */
+    int32_t param;      /* animated transform forming R, -1: R = r */
+    int32_t rec;        /* record whose tci/tcj/tck/pos M gives, -1: none */
+    int32_t light;      /* light whose pos M gives, -1: none */
+    int32_t pad[3];
+    float   p[16];      /* P, column-major (m[column][row]) */
+    float   r[16];      /* R when param < 0 */
+} qr_anim_node;
+
+/* one animated transform for a frame: sines and cosines of its rotation
+ * about x, y, z in degrees as the reference computes them (RT_SINA /
+ * RT_COSA, core/config/rtbase.h:858-875) and its position */
+typedef struct qr_anim_param
+{
+    float   sin[3];
+    float   cos[3];
+    float   pos[3];
+    float   pad[3];
+} qr_anim_param;
+
+/* Upload `desc` into scene `scene_id` in place (as qr_scene_update) with
+ * the hierarchy sized for the motion bound (lo[3], hi[3], NULL: the
+ * scene's extent widened by half its radius on each side) and prepare the
+ * device update of the n entries of `nodes` (records and lights in range,
+ * parents earlier).  A later qr_scene_update drops the preparation. */
+int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc,
+                       const qr_anim_node *nodes, int n, const float *bound);
+/* one frame's update on `stream` (asynchronous; NULL: the context's own
+ * stream, which qr_render_host and the uploads use; `params` is copied
+ * before the call returns): params[i] for every animated transform i named
+ * by the table.  When a moved record or surface leaves the motion bound the
+ * hierarchy's boxes are opened to the whole space for that frame (the frame
+ * stays exact, rays walk every surface) and the miss is counted */
+int qr_scene_anim_update(qr_ctx *ctx, int scene_id, const qr_anim_param *params,
+                         int nparams, void *stream);
+/* out[0] = frames updated on the device, out[1] = frames whose update left
+ * the motion bound (opened boxes); updates on other streams must have
+ * finished */
+int qr_scene_anim_status(qr_ctx *ctx, int scene_id, int32_t out[2]);
+
 /* render one frame into a device frame buffer (uint32 XRGB, x_row stride),
  * asynchronously on `stream` (a cudaStream_t, 0 = default stream).
  * With fp->pt_on > 0 the frame is path traced: pt_on samples per pixel are

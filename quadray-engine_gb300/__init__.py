@@ -86,6 +86,26 @@ class QrRequest(ctypes.Structure):
     ]
 
 
+class QrAnimNode(ctypes.Structure):
+    """qr_anim_node of include/qr_gpu.h (one entry of a device update table)."""
+    _fields_ = [
+        ("kind", ctypes.c_int32), ("parent", ctypes.c_int32),
+        ("param", ctypes.c_int32), ("rec", ctypes.c_int32),
+        ("light", ctypes.c_int32), ("pad", ctypes.c_int32 * 3),
+        ("p", ctypes.c_float * 16), ("r", ctypes.c_float * 16),
+    ]
+
+
+class QrAnimParam(ctypes.Structure):
+    """qr_anim_param of include/qr_gpu.h (one animated transform)."""
+    _fields_ = [
+        ("sin", ctypes.c_float * 3), ("cos", ctypes.c_float * 3),
+        ("pos", ctypes.c_float * 3), ("pad", ctypes.c_float * 3),
+    ]
+
+
+ANIM_OWN, ANIM_UNDER, ANIM_NODE = 0, 1, 2
+QR_ERR_STATE = 5
 QR_ERR_BUSY = 8
 QR_ERR_TRACE = 9
 FAULT_TREE, FAULT_STACK = 1, 2
@@ -120,6 +140,17 @@ def lib():
         L.qrpy_flat_desc.argtypes = [vp, ctypes.POINTER(QrSceneDesc),
                                      ctypes.POINTER(QrFrameParams)]
         L.qrpy_flat_free.argtypes = [vp]
+        L.qrpy_flat_anim_table.argtypes = [vp, ctypes.POINTER(QrAnimNode), i32,
+                                           ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, i32]
+        L.qrpy_flat_anim_params.argtypes = [vp, i64, ctypes.POINTER(QrAnimParam), i32,
+                                            ctypes.POINTER(ctypes.c_int)]
+        L.qrpy_anim_check.argtypes = [vp, ctypes.POINTER(QrAnimNode), i32,
+                                      ctypes.POINTER(QrAnimParam)]
+        L.qr_scene_anim_init.argtypes = [vp, i32, ctypes.POINTER(QrSceneDesc),
+                                         ctypes.POINTER(QrAnimNode), i32,
+                                         ctypes.POINTER(ctypes.c_float)]
+        L.qr_scene_anim_update.argtypes = [vp, i32, ctypes.POINTER(QrAnimParam), i32, vp]
+        L.qr_scene_anim_status.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int32)]
         L.qrpy_scene_new.restype = vp
         L.qrpy_scene_new.argtypes = [vp, i32, i32, i32, i32, i32, vp]
         L.qrpy_scene_render.argtypes = [vp, i64, vp]
@@ -219,6 +250,42 @@ class Flat:
         action); CAMERA_* codes)"""
         lib().qrpy_flat_action(self.h, int(time), int(action))
 
+    def anim_table(self):
+        """the device update table after the last update: a QrAnimNode
+        array; raises ValueError (with the reason) when the scene cannot be
+        updated on the device"""
+        n = ctypes.c_int(0)
+        why = ctypes.create_string_buffer(160)
+        rc = lib().qrpy_flat_anim_table(self.h, None, 0, ctypes.byref(n), why, 160)
+        if rc == QR_ERR_STATE:
+            raise ValueError(why.value.decode())
+        arr = (QrAnimNode * n.value)()
+        rc = lib().qrpy_flat_anim_table(self.h, arr, n.value, ctypes.byref(n), why, 160)
+        if rc != QR_OK:
+            raise ValueError(why.value.decode() or "anim table: %d" % rc)
+        return arr
+
+    def anim_params(self, time):
+        """run the animators for `time`; returns (status, QrAnimParam array):
+        status 0, or 1 / 2 when an animated transform lost its free rotation
+        or changed scale (the frame then needs update() and a new table)"""
+        n = ctypes.c_int(0)
+        cap = getattr(self, "_anim_n", 0)
+        buf = (QrAnimParam * cap)()
+        rc = lib().qrpy_flat_anim_params(self.h, int(time), buf, cap, ctypes.byref(n))
+        if rc == -1:
+            # the animators ran; a second call at the same time only reads
+            buf = (QrAnimParam * n.value)()
+            rc = lib().qrpy_flat_anim_params(self.h, int(time), buf, n.value, ctypes.byref(n))
+        self._anim_n = n.value
+        return rc, buf
+
+    def anim_check(self, table, params):
+        """entries of `table` whose records or lights, formed from `params`
+        by the device update's matrix steps on the host, differ from this
+        scene's last update (0: all equal bit for bit)"""
+        return lib().qrpy_anim_check(self.h, table, len(table), params)
+
     def close(self):
         if self.h:
             lib().qrpy_flat_free(self.h)
@@ -255,6 +322,29 @@ class Context:
         rc = lib().qr_scene_update(self.h, sid, ctypes.byref(desc))
         if rc != QR_OK:
             raise RuntimeError("qr_scene_update: %d %s" % (rc, self.error()))
+
+    def anim_init(self, sid, desc, table, bound=None):
+        """upload desc into scene sid with its device update table (and a
+        motion bound lo[3] + hi[3], default: the scene's extent widened)"""
+        b = (ctypes.c_float * 6)(*bound) if bound is not None else None
+        rc = lib().qr_scene_anim_init(self.h, sid, ctypes.byref(desc), table, len(table), b)
+        if rc != QR_OK:
+            raise RuntimeError("qr_scene_anim_init: %d %s" % (rc, self.error()))
+
+    def anim_update(self, sid, params, stream=0):
+        """one frame's device update of scene sid on `stream`"""
+        rc = lib().qr_scene_anim_update(self.h, sid, params, len(params), ctypes.c_void_p(stream))
+        if rc != QR_OK:
+            raise RuntimeError("qr_scene_anim_update: %d %s" % (rc, self.error()))
+
+    def anim_status(self, sid):
+        """(frames updated on the device, frames whose update left the
+        motion bound)"""
+        out = (ctypes.c_int32 * 2)()
+        rc = lib().qr_scene_anim_status(self.h, sid, out)
+        if rc != QR_OK:
+            raise RuntimeError("qr_scene_anim_status: %d %s" % (rc, self.error()))
+        return tuple(out)
 
     def release(self, sid):
         rc = lib().qr_scene_release(self.h, sid)

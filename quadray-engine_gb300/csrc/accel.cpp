@@ -476,48 +476,35 @@ static void refit(qr_accel_host *out)
     }
 }
 
-static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
-                       const qr_accel_host *topo);
-
-int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level)
+/* the scene's extent, from which every level's radius and rounding
+ * allowance follow: boxes without rounding allowance and record positions,
+ * joined with the motion bound `bound` (lo[3], hi[3]; NULL: none) */
+struct Extent
 {
-    return accel_build(d, out, level, NULL);
-}
+    std::vector<int> xf;        /* transform node per camera-list element */
+    std::vector<int> srf_xf;    /* per record (-2: not in the camera list) */
+    double clo[3], chi[3], rs, gain;
+};
 
-/* level `level` of the hierarchy; with `topo` (the tree of another level
- * over the same bounded surfaces) its topology is kept and only the boxes
- * are refitted, the tree shape does not change the frame */
-static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
-                       const qr_accel_host *topo)
+static void scene_extent(const qr_scene_desc *d, const float *bound, Extent &x)
 {
-    out->nodes.clear();
-    out->items.clear();
-    out->always.clear();
-    out->depth = 0;
-    out->boxes.assign((size_t)d->nsrf * 6, 0.0f);
-    out->bounded.assign(d->nsrf, 0);
-
-    /* transform node of each surface in the camera list */
-    std::vector<int> xf;
-    list_groups(d, d->cam_off, d->cam_num, xf);
-    std::vector<int> srf_xf(d->nsrf, -2);
+    list_groups(d, d->cam_off, d->cam_num, x.xf);
+    x.srf_xf.assign(d->nsrf, -2);
     for (int e = 0; e < d->cam_num; e++)
     {
         const qr_elem &el = d->elems[d->cam_off + e];
-        if (el.kind == QR_ELM_SURFACE) srf_xf[el.ref] = xf[e];
+        if (el.kind == QR_ELM_SURFACE) x.srf_xf[el.ref] = x.xf[e];
     }
-
-    /* the scene's extent: boxes without rounding allowance, and the gain
-     * from world distances to local coordinates */
-    double gain = 1.0;
-    for (int i = 0; i < d->nsrf; i++) gain = std::max(gain, record_gain(d->srf[i]));
-    double clo[3] = {INF, INF, INF}, chi[3] = {-INF, -INF, -INF};
+    x.gain = 1.0;
+    for (int i = 0; i < d->nsrf; i++) x.gain = std::max(x.gain, record_gain(d->srf[i]));
+    double *clo = x.clo, *chi = x.chi;
+    for (int k = 0; k < 3; k++) { clo[k] = INF; chi[k] = -INF; }
     for (int i = 0; i < d->nsrf; i++)
     {
         const qr_srf &s = d->srf[i];
-        if (s.is_node || srf_xf[i] == -2) continue;
+        if (s.is_node || x.srf_xf[i] == -2) continue;
         Box u = local_surface_box(s, 0.0), w;
-        if (u.empty() || !world_box(d, s, srf_xf[i], false, u, w) || !w.finite()) continue;
+        if (u.empty() || !world_box(d, s, x.srf_xf[i], false, u, w) || !w.finite()) continue;
         for (int k = 0; k < 3; k++)
         {
             clo[k] = std::min(clo[k], w.lo[k]);
@@ -532,19 +519,63 @@ static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
             clo[k] = std::min(clo[k], (double)d->srf[i].pos[k]);
             chi[k] = std::max(chi[k], (double)d->srf[i].pos[k]);
         }
+    if (bound != NULL)
+        for (int k = 0; k < 3; k++)
+        {
+            clo[k] = std::min(clo[k], (double)bound[k]);
+            chi[k] = std::max(chi[k], (double)bound[3 + k]);
+        }
     double rs = 0.0;
     for (int k = 0; k < 3; k++)
     {
         if (!(clo[k] <= chi[k])) { clo[k] = chi[k] = 0.0; }
-        out->ray_c[k] = (float)(0.5 * (clo[k] + chi[k]));
         rs += 0.25 * (chi[k] - clo[k]) * (chi[k] - clo[k]);
     }
-    rs = sqrt(rs);
-    /* rays starting within ray_r of the centre use the hierarchy; their
-     * local coordinates stay below D.  Each level covers 8 times the radius
-     * of the previous one, with boxes widened for the larger rounding */
-    const double ray_r = (6.0 * rs + 8.0) * pow(8.0, (double)level);
-    const double D = gain * (ray_r + 2.0 * rs + 1.0) + 1.0;
+    x.rs = sqrt(rs);
+}
+
+/* rays starting within ray_r of the extent's centre use level `level`;
+ * their local coordinates stay below D.  Each level covers 8 times the
+ * radius of the previous one, with boxes widened for the larger rounding */
+static void level_radius(const Extent &x, int level, double *ray_r, double *D)
+{
+    *ray_r = (6.0 * x.rs + 8.0) * pow(8.0, (double)level);
+    *D = x.gain * (*ray_r + 2.0 * x.rs + 1.0) + 1.0;
+}
+
+static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
+                       const qr_accel_host *topo, const float *bound);
+
+int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level)
+{
+    return accel_build(d, out, level, NULL, NULL);
+}
+
+/* level `level` of the hierarchy; with `topo` (the tree of another level
+ * over the same bounded surfaces) its topology is kept and only the boxes
+ * are refitted, the tree shape does not change the frame */
+static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
+                       const qr_accel_host *topo, const float *bound)
+{
+    out->nodes.clear();
+    out->items.clear();
+    out->always.clear();
+    out->depth = 0;
+    out->boxes.assign((size_t)d->nsrf * 6, 0.0f);
+    out->bounded.assign(d->nsrf, 0);
+
+    Extent x;
+    scene_extent(d, bound, x);
+    const std::vector<int> &xf = x.xf, &srf_xf = x.srf_xf;
+    for (int k = 0; k < 3; k++)
+    {
+        out->ray_c[k] = (float)(0.5 * (x.clo[k] + x.chi[k]));
+        out->ext[k] = x.clo[k];
+        out->ext[3 + k] = x.chi[k];
+    }
+    out->gain = x.gain;
+    double ray_r, D;
+    level_radius(x, level, &ray_r, &D);
     out->ray_r2 = (float)(ray_r * ray_r);
 
     /* world boxes of the surfaces (unclipped by custom clippers) */
@@ -642,7 +673,8 @@ static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
 
 void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
                            int root[QR_BVH_LEVELS], int aoff[QR_BVH_LEVELS],
-                           int anum[QR_BVH_LEVELS], float r2[QR_BVH_LEVELS])
+                           int anum[QR_BVH_LEVELS], float r2[QR_BVH_LEVELS],
+                           const float *bound)
 {
     out->nodes.clear();
     out->items.clear();
@@ -659,15 +691,21 @@ void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
         /* the outer levels' boxes are wide; for short lists a walk in list
          * order is cheaper than traversing them, and they are not built */
         const bool used = l == 0 || d->cam_num >= QR_BVH_OUTER_MIN;
+        out->lboxes[l].clear();
+        out->lbounded[l].clear();
         if (!used) continue;
         qr_accel_host lv;
-        accel_build(d, &lv, l, l == 0 ? NULL : &lv0);
+        accel_build(d, &lv, l, l == 0 ? NULL : &lv0, bound);
+        out->lboxes[l] = lv.boxes;
+        out->lbounded[l] = lv.bounded;
         const int i0 = (int)out->items.size();
         anum[l] = (int)lv.always.size();
         r2[l] = (lv.depth < QR_BVH_STACK - 2 && !lv.nodes.empty()) ? lv.ray_r2 : -1.0f;
         if (l == 0)
         {
             for (int k = 0; k < 3; k++) out->ray_c[k] = lv.ray_c[k];
+            for (int k = 0; k < 6; k++) out->ext[k] = lv.ext[k];
+            out->gain = lv.gain;
             out->ray_r2 = lv.ray_r2;
             out->boxes = lv.boxes;
             out->bounded = lv.bounded;
@@ -684,4 +722,106 @@ void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
         out->always.insert(out->always.end(), lv.always.begin(), lv.always.end());
         if (l == 0) lv0 = lv;
     }
+}
+
+void qr_accel_extent(const qr_scene_desc *d, double ext[6])
+{
+    Extent x;
+    scene_extent(d, NULL, x);
+    for (int k = 0; k < 3; k++)
+    {
+        ext[k] = x.clo[k];
+        ext[3 + k] = x.chi[k];
+    }
+}
+
+/* ---- terms of the world boxes that animated records move ------------------ */
+
+static void term_local(qr_anim_term &t, int l, const Box &u)
+{
+    for (int k = 0; k < 3; k++)
+    {
+        t.u[l][k] = u.lo[k];
+        t.u[l][3 + k] = u.hi[k];
+    }
+}
+
+/* the world_box form for record s in the frame of transform node xf */
+static int term_mode(const qr_scene_desc *d, const qr_srf &s, int xf, bool node_only)
+{
+    if (xf >= 0 && (node_only || d->srf[xf].amap[3] != 0))
+        return d->srf[xf].amap[3] != 0 ? QR_TERM_NODE : QR_TERM_NODE_SHIFT;
+    return s.amap[3] != 0 ? QR_TERM_OWN : QR_TERM_OWN_SHIFT;
+}
+
+int qr_accel_anim_terms(const qr_scene_desc *d, const qr_accel_host *acc,
+                        const float *bound, const std::vector<char> &dyn,
+                        std::vector<qr_anim_term> &terms,
+                        std::vector<qr_anim_target> &targets)
+{
+    terms.clear();
+    targets.clear();
+    Extent x;
+    scene_extent(d, bound, x);
+    double Dl[QR_BVH_LEVELS];
+    for (int l = 0; l < QR_BVH_LEVELS; l++)
+    {
+        double r;
+        level_radius(x, l, &r, &Dl[l]);
+    }
+    for (int i = 0; i < d->nsrf; i++)
+    {
+        const qr_srf &s = d->srf[i];
+        if (s.is_node || x.srf_xf[i] == -2) continue;
+        int lv = 0;
+        for (int l = 0; l < QR_BVH_LEVELS; l++)
+            if (!acc->lbounded[l].empty() && acc->lbounded[l][i]) lv |= 1 << l;
+        if (lv == 0) continue;
+        const int sx = x.srf_xf[i];
+        bool moved = dyn[i] || (sx >= 0 && dyn[sx]);
+        qr_anim_target tg;
+        tg.srf = i;
+        tg.t0 = (int)terms.size();
+        tg.levels = lv;
+
+        /* the surface itself */
+        qr_anim_term t;
+        memset(&t, 0, sizeof(t));
+        t.srf = i;
+        t.xf = sx;
+        t.mode = term_mode(d, s, sx, false);
+        for (int l = 0; l < QR_BVH_LEVELS; l++) term_local(t, l, local_surface_box(s, Dl[l]));
+        term_local(t, QR_BVH_LEVELS, local_surface_box(s, 0.0));
+        terms.push_back(t);
+
+        /* clippers that keep only its inside (as in accel_build) */
+        if (s.clip_num > 0)
+        {
+            std::vector<int> cxf;
+            list_groups(d, s.clip_off, s.clip_num, cxf);
+            int accm = 0;
+            for (int e = 0; e < s.clip_num; e++)
+            {
+                const qr_elem &el = d->elems[s.clip_off + e];
+                if (el.kind == QR_ELM_ACC_ENTER) { accm = 1; continue; }
+                if (el.kind == QR_ELM_ACC_LEAVE) { accm = 0; continue; }
+                if (el.kind != QR_ELM_SURFACE || accm || el.rel <= 0) continue;
+                const qr_srf &c = d->srf[el.ref];
+                qr_anim_term ct;
+                memset(&ct, 0, sizeof(ct));
+                ct.srf = el.ref;
+                ct.xf = cxf[e];
+                ct.mode = term_mode(d, c, cxf[e], true);
+                for (int l = 0; l < QR_BVH_LEVELS; l++)
+                    term_local(ct, l, local_clip_region(c, Dl[l]));
+                for (int k = 0; k < 6; k++) ct.u[QR_BVH_LEVELS][k] = 0.0;
+                terms.push_back(ct);
+                moved = moved || dyn[el.ref] || (cxf[e] >= 0 && dyn[cxf[e]]);
+            }
+        }
+        tg.tn = (int)terms.size() - tg.t0;
+        if (moved) targets.push_back(tg);
+        else terms.resize(tg.t0);
+    }
+    return 0;
 }

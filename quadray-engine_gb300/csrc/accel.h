@@ -24,6 +24,11 @@
 #include <vector>
 #include "qr_gpu.h"
 
+/* hierarchy levels built per scene; levels past the first only for lists of
+ * at least QR_BVH_OUTER_MIN elements */
+#define QR_BVH_LEVELS 3
+#define QR_BVH_OUTER_MIN 64
+
 /* BVH node: inner nodes have count == 0 and children a, b; leaves hold
  * items [a, a + count) */
 struct qr_bnode
@@ -52,12 +57,19 @@ struct qr_accel_host
     std::vector<qr_bnode> nodes;        /* nodes[0] is the root */
     std::vector<qr_bitem> items;        /* leaf items (BVH order) */
     std::vector<qr_bitem> always;       /* unbounded surfaces (list order) */
-    std::vector<float>    boxes;        /* per record: lo[3], hi[3] (debug) */
-    std::vector<int32_t>  bounded;      /* per record */
+    std::vector<float>    boxes;        /* per record: lo[3], hi[3] (level 0) */
+    std::vector<int32_t>  bounded;      /* per record (level 0) */
+    /* the same per level (qr_accel_build_levels; empty for levels not built) */
+    std::vector<float>    lboxes[QR_BVH_LEVELS];
+    std::vector<int32_t>  lbounded[QR_BVH_LEVELS];
     int depth;
     /* rays whose origin lies within sqrt(ray_r2) of ray_c may use the
      * hierarchy (the boxes allow for their rounding); others walk the list */
     float ray_c[3], ray_r2;
+    /* the extent the levels' radii and rounding allowances follow from
+     * (lo[3], hi[3]), and the largest gain from world distances to local
+     * coordinates */
+    double ext[6], gain;
 };
 
 /* build the hierarchy of one level over the camera list of `d` (which the
@@ -66,17 +78,51 @@ struct qr_accel_host
  * scene's centre, its boxes allowing for their rounding; returns 0 */
 int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level);
 
-/* hierarchy levels built per scene; levels past the first only for lists of
- * at least QR_BVH_OUTER_MIN elements */
-#define QR_BVH_LEVELS 3
-#define QR_BVH_OUTER_MIN 64
-
 /* all levels concatenated into `out` (node indices and item ranges shifted
  * by the preceding levels); per level its root node, its unbounded surfaces
  * always[aoff, aoff + anum) and the squared radius it serves (-1: none) */
 void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
                            int root[QR_BVH_LEVELS], int aoff[QR_BVH_LEVELS],
-                           int anum[QR_BVH_LEVELS], float r2[QR_BVH_LEVELS]);
+                           int anum[QR_BVH_LEVELS], float r2[QR_BVH_LEVELS],
+                           const float *bound);
+
+/* the extent of the scene's surfaces and records (lo[3], hi[3]) that the
+ * levels' radii follow from when there is no motion bound */
+void qr_accel_extent(const qr_scene_desc *d, double ext[6]);
+
+/* one term of a surface's world box: record srf's local box u[l] at level l
+ * (u[QR_BVH_LEVELS]: the surface's box without rounding allowance, for the
+ * extent check) mapped to world space by the frame `mode`:
+ *   QR_TERM_NODE        h = M_T^-1 (u + srf.pos) + T.pos, T = record xf
+ *   QR_TERM_NODE_SHIFT  h = u + srf.pos + T.pos
+ *   QR_TERM_OWN         h = M_s^-1 u + srf.pos
+ *   QR_TERM_OWN_SHIFT   h = u + srf.pos
+ * (world_box in accel.cpp) */
+#define QR_TERM_NODE        0
+#define QR_TERM_NODE_SHIFT  1
+#define QR_TERM_OWN         2
+#define QR_TERM_OWN_SHIFT   3
+
+struct qr_anim_term
+{
+    int32_t srf, xf, mode, pad;
+    double  u[QR_BVH_LEVELS + 1][6];
+};
+
+/* a surface whose box is the meet of terms [t0, t0 + tn), the first its
+ * own; bit l of levels: the surface is bounded at level l */
+struct qr_anim_target
+{
+    int32_t srf, t0, tn, levels;
+};
+
+/* the terms of every bounded surface whose box depends on a record marked
+ * in dyn (its own, its transform node's, a bounding clipper's or that
+ * clipper's node); acc is the hierarchy built with the same bound */
+int qr_accel_anim_terms(const qr_scene_desc *d, const qr_accel_host *acc,
+                        const float *bound, const std::vector<char> &dyn,
+                        std::vector<qr_anim_term> &terms,
+                        std::vector<qr_anim_target> &targets);
 
 /* deepest traversal stack the tracer supports */
 #define QR_BVH_STACK 48

@@ -1,0 +1,318 @@
+/*
+ * anim.cu: device-side update phases of an animated scene, one block per
+ * update (the work is a few hundred matrices and boxes; one block keeps the
+ * ordering between its stages to block barriers and the whole update to
+ * one launch).
+ *
+ * Stage 1  transform chain, generation by generation: the matrices of
+ *          rt_Object::update_matrix (core/engine/object.cpp:221-389) with
+ *          the shared matrix steps of xform.h, so the records equal those
+ *          of the host update bit for bit (no FMA contraction, IEEE
+ *          division: the library's device flags).
+ * Stage 2  records: inverse matrix rows tci/tcj/tck and position
+ *          (rt_Node::update_fields, object.cpp:826-857), light positions
+ *          (the light's pos in rt_Light::update_fields, object.cpp:649-667).
+ * Stage 3  world boxes of the surfaces that move, in double precision, as
+ *          accel.cpp forms them (world_box, affine_image, pad), and the
+ *          check that every moved record and surface stays inside the
+ *          motion bound the boxes' rounding allowance was sized for.
+ * Stage 4  hierarchy node boxes bottom-up by depth band; when the check
+ *          failed, every node box is opened instead, so every ray walks
+ *          every surface and the frame stays exact.
+ */
+#include <float.h>
+#include <math.h>
+#include "anim.cuh"
+#include "xform.h"
+
+namespace
+{
+
+__device__ void load16(float (*m)[4], const float *p)
+{
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) m[i][j] = p[4 * i + j];
+}
+
+__device__ void store16(float *p, const float (*m)[4])
+{
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) p[4 * i + j] = m[i][j];
+}
+
+/* a record's 3x3 transform as the tracer applies it (diagonal only when
+ * amap[3] == 1, "scaling only"), accel.cpp record_matrix */
+__device__ void record_matrix(const qr_srf &t, double m[3][3])
+{
+    const float *row[3] = {t.tci, t.tcj, t.tck};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            m[i][j] = (t.amap[3] == 1 && i != j) ? 0.0 : (double)row[i][j];
+}
+
+__device__ bool invert3(const double m[3][3], double r[3][3])
+{
+    const double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1];
+    const double c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2];
+    const double c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+    const double det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
+    if (!(fabs(det) > 1e-30)) return false;
+    const double id = 1.0 / det;
+    r[0][0] = c00 * id;
+    r[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+    r[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+    r[1][0] = c01 * id;
+    r[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+    r[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
+    r[2][0] = c02 * id;
+    r[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
+    r[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
+    return true;
+}
+
+/* world box of one term at level l (accel.h, QR_TERM_*); false when the
+ * record's transform is singular */
+__device__ bool term_box(const qr_anim_dev &A, const qr_anim_term &t, int l,
+                         double lo[3], double hi[3])
+{
+    const qr_srf &s = A.srf[t.srf];
+    double a[3][3] = {{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
+    double o[3], u[6];
+    for (int k = 0; k < 6; k++) u[k] = t.u[l][k];
+    if (t.mode == QR_TERM_NODE || t.mode == QR_TERM_NODE_SHIFT)
+    {
+        const qr_srf &T = A.srf[t.xf];
+        for (int k = 0; k < 3; k++)
+        {
+            u[k] += (double)s.pos[k];
+            u[3 + k] += (double)s.pos[k];
+            o[k] = (double)T.pos[k];
+        }
+        if (t.mode == QR_TERM_NODE)
+        {
+            double m[3][3];
+            record_matrix(T, m);
+            if (!invert3(m, a)) return false;
+        }
+    }
+    else
+    {
+        for (int k = 0; k < 3; k++) o[k] = (double)s.pos[k];
+        if (t.mode == QR_TERM_OWN)
+        {
+            double m[3][3];
+            record_matrix(s, m);
+            if (!invert3(m, a)) return false;
+        }
+    }
+    /* interval image of u under h = a u + o (accel.cpp affine_image) */
+    for (int i = 0; i < 3; i++)
+    {
+        double l0 = o[i], h0 = o[i];
+        for (int j = 0; j < 3; j++)
+        {
+            const double c = a[i][j];
+            if (c == 0.0) continue;
+            const double p = c * u[j], q = c * u[3 + j];
+            if (isnan(p) || isnan(q)) { l0 = -HUGE_VAL; h0 = HUGE_VAL; break; }
+            l0 += fmin(p, q);
+            h0 += fmax(p, q);
+        }
+        lo[i] = l0;
+        hi[i] = h0;
+    }
+    return true;
+}
+
+__device__ bool inside(const double ext[6], const double lo[3], const double hi[3])
+{
+    for (int k = 0; k < 3; k++)
+        if (!(lo[k] >= ext[k] && hi[k] <= ext[3 + k])) return false;
+    return true;
+}
+
+__global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev A)
+{
+    __shared__ int fail;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (tid == 0) fail = 0;
+    __syncthreads();
+
+    /* stage 1: matrices, parents before children */
+    for (int g = 0; g < A.ngen; g++)
+    {
+        for (int i = A.gen_off[g] + tid; i < A.gen_off[g + 1]; i += nt)
+        {
+            const int e = A.order[i];
+            const qr_anim_node &N = A.nodes[e];
+            float P[4][4], R[4][4], M[4][4], T[4][4], tmp[4][4];
+            load16(P, N.p);
+            if (N.kind != QR_ANIM_NODE)
+            {
+                if (N.param >= 0)
+                {
+                    const qr_anim_param &q = A.params[N.param];
+                    const float one[3] = {1.0f, 1.0f, 1.0f};
+                    qr::mat_from_sc(R, q.sin, q.cos, q.pos, one);
+                }
+                else
+                {
+                    load16(R, N.r);
+                }
+            }
+            if (N.kind != QR_ANIM_OWN) load16(T, A.mtx + 16 * (size_t)N.parent);
+            if (N.kind == QR_ANIM_OWN)
+            {
+                qr::mat_mul_mat(M, P, R);
+            }
+            else if (N.kind == QR_ANIM_UNDER)
+            {
+                qr::mat_mul_mat(tmp, T, P);
+                qr::mat_mul_mat(M, tmp, R);
+            }
+            else
+            {
+                qr::mat_mul_mat(M, T, P);
+            }
+            store16(A.mtx + 16 * (size_t)e, M);
+        }
+        __syncthreads();
+    }
+
+    /* stage 2: records and lights */
+    for (int e = tid; e < A.n; e += nt)
+    {
+        const qr_anim_node &N = A.nodes[e];
+        float M[4][4];
+        load16(M, A.mtx + 16 * (size_t)e);
+        if (N.rec >= 0)
+        {
+            float inv[4][4];
+            qr::mat_inverse(inv, M);
+            qr_srf &s = A.srf[N.rec];
+            for (int k = 0; k < 3; k++)
+            {
+                s.tci[k] = inv[k][0];
+                s.tcj[k] = inv[k][1];
+                s.tck[k] = inv[k][2];
+                s.pos[k] = M[3][k];
+            }
+            /* record positions bound the local coordinates the walk forms
+             * (light positions take no part, as in the host build) */
+            const double p[3] = {M[3][0], M[3][1], M[3][2]};
+            if (!inside(A.ext, p, p)) fail = 1;
+        }
+        if (N.light >= 0)
+        {
+            for (int k = 0; k < 3; k++) A.lgt[N.light].pos[k] = M[3][k];
+        }
+    }
+    __syncthreads();
+
+    /* stage 3: world boxes of the moved surfaces per level, and the extent
+     * check on their boxes without rounding allowance */
+    const int L = QR_BVH_LEVELS;
+    for (int w = tid; w < A.ntargets * (L + 1); w += nt)
+    {
+        const qr_anim_target tg = A.targets[w / (L + 1)];
+        const int l = w % (L + 1);
+        if (l < L && ((tg.levels >> l) & 1) == 0) continue;
+        double lo[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+        double hi[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL};
+        const int nterm = l == L ? 1 : tg.tn;
+        bool ok = true;
+        for (int j = 0; j < nterm && ok; j++)
+        {
+            double tl[3], th[3];
+            ok = term_box(A, A.terms[tg.t0 + j], l, tl, th);
+            for (int k = 0; k < 3 && ok; k++)
+            {
+                lo[k] = fmax(lo[k], tl[k]);
+                hi[k] = fmin(hi[k], th[k]);
+            }
+        }
+        if (l == L)
+        {
+            /* the extent holds the finite ones of these boxes (a quadric
+             * that only its clippers bound has none), as in the host build */
+            bool fin = ok;
+            for (int k = 0; k < 3; k++)
+                fin = fin && lo[k] > -HUGE_VAL && hi[k] < HUGE_VAL && lo[k] <= hi[k];
+            if (!ok || (fin && !inside(A.ext, lo, hi))) fail = 1;
+            continue;
+        }
+        for (int k = 0; k < 3 && ok; k++)
+            ok = lo[k] <= hi[k] && lo[k] > -HUGE_VAL && hi[k] < HUGE_VAL;
+        if (!ok) { fail = 1; continue; }
+        float *b = A.lboxes + ((size_t)l * A.nsrf + tg.srf) * 6;
+        for (int k = 0; k < 3; k++)
+        {
+            /* accel.cpp pad */
+            const double m = 1e-3 + 1e-4 * (fabs(lo[k]) + fabs(hi[k]));
+            b[k] = (float)(lo[k] - m);
+            b[3 + k] = (float)(hi[k] + m);
+        }
+    }
+    __syncthreads();
+
+    /* stage 4: node boxes */
+    if (fail)
+    {
+        for (int i = tid; i < A.nbvh; i += nt)
+        {
+            qr_bnode &nd = A.bvh[i];
+            for (int k = 0; k < 3; k++) { nd.lo[k] = -1e30f; nd.hi[k] = 1e30f; }
+        }
+    }
+    else
+    {
+        for (int band = 0; band < A.nbands; band++)
+        {
+            for (int i = A.depth_off[band] + tid; i < A.depth_off[band + 1]; i += nt)
+            {
+                const int ni = A.rorder[i];
+                qr_bnode &nd = A.bvh[ni];
+                float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+                float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                if (nd.count > 0)
+                {
+                    int l = 0;
+                    while (l < L - 1 && ni >= A.lvl_end[l]) l++;
+                    for (int j = nd.a; j < nd.a + nd.count; j++)
+                    {
+                        const float *b = A.lboxes + ((size_t)l * A.nsrf + A.items[j].srf) * 6;
+                        for (int k = 0; k < 3; k++)
+                        {
+                            lo[k] = fminf(lo[k], b[k]);
+                            hi[k] = fmaxf(hi[k], b[3 + k]);
+                        }
+                    }
+                }
+                else
+                {
+                    const qr_bnode &ca = A.bvh[nd.a], &cb = A.bvh[nd.b];
+                    for (int k = 0; k < 3; k++)
+                    {
+                        lo[k] = fminf(ca.lo[k], cb.lo[k]);
+                        hi[k] = fmaxf(ca.hi[k], cb.hi[k]);
+                    }
+                }
+                for (int k = 0; k < 3; k++) { nd.lo[k] = lo[k]; nd.hi[k] = hi[k]; }
+            }
+            __syncthreads();
+        }
+    }
+    if (tid == 0)
+    {
+        A.status[0] += 1;
+        if (fail) A.status[1] += 1;
+    }
+}
+
+} /* namespace */
+
+cudaError_t qr_launch_anim(const qr_anim_dev &a, cudaStream_t stream)
+{
+    anim_kernel<<<1, 512, 0, stream>>>(a);
+    return cudaGetLastError();
+}

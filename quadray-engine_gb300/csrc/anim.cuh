@@ -1,0 +1,41 @@
+/*
+ * anim.cuh: device-side update of an animated scene's records, surface
+ * boxes and hierarchy (qr_scene_anim_update in include/qr_gpu.h).
+ */
+#ifndef QR_ANIM_CUH
+#define QR_ANIM_CUH
+
+#include <cuda_runtime.h>
+#include "qr_gpu.h"
+#include "accel.h"
+
+/* everything one update launch reads and writes, in device memory (params
+ * in mapped host memory) */
+struct qr_anim_dev
+{
+    const qr_anim_node  *nodes;     /* the table */
+    const int32_t       *order;     /* entries by generation (parents first) */
+    const int32_t       *gen_off;   /* generation g: order[gen_off[g], gen_off[g+1]) */
+    int32_t              n, ngen;
+    const qr_anim_param *params;
+    float               *mtx;       /* per entry: M, 16 floats */
+    qr_srf              *srf;
+    qr_light            *lgt;
+    const qr_anim_term  *terms;
+    const qr_anim_target *targets;
+    int32_t              ntargets, nsrf;
+    float               *lboxes;    /* [QR_BVH_LEVELS][nsrf][6] surface boxes */
+    qr_bnode            *bvh;       /* hierarchy nodes, all levels */
+    const qr_bitem      *items;
+    const int32_t       *rorder;    /* nodes by depth, deepest first */
+    const int32_t       *depth_off; /* depth band b: rorder[depth_off[b], depth_off[b+1]) */
+    int32_t              nbvh, nbands;
+    int32_t              lvl_end[QR_BVH_LEVELS];   /* level l: nodes below lvl_end[l] */
+    double               ext[6];    /* motion bound the boxes allow for */
+    uint32_t            *status;    /* [0] frames updated, [1] frames out of bound */
+};
+
+/* one update on `stream`: a single block */
+cudaError_t qr_launch_anim(const qr_anim_dev &a, cudaStream_t stream);
+
+#endif /* QR_ANIM_CUH */

@@ -7,8 +7,10 @@
  * kept in the context's message buffer.
  */
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdio.h>
 #include <string.h>
+#include <algorithm>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -16,7 +18,23 @@
 #include "qr_gpu.h"
 #include "tracer.cuh"
 #include "accel.h"
+#include "anim.cuh"
 
+
+/* device update of an animated scene (qr_scene_anim_*) */
+#define QR_ANIM_RING 4
+struct qr_anim_state
+{
+    int          ok;        /* prepared for the scene's current upload */
+    void        *block;     /* device: table, matrices, terms, boxes, order */
+    size_t       bytes;
+    qr_anim_param *ring;    /* mapped host memory: QR_ANIM_RING param sets */
+    size_t       ring_n;    /* params a set holds */
+    cudaEvent_t  ev[QR_ANIM_RING];  /* the update that last read each set */
+    int          next;
+    int          nparams;
+    qr_anim_dev  dev;
+};
 
 struct qr_scene_slot
 {
@@ -25,7 +43,18 @@ struct qr_scene_slot
     size_t       bytes;
     qr_dscene    d;
     qr_scene_desc shape;    /* sizes of the uploaded arrays */
+    qr_anim_state *anim;    /* NULL until qr_scene_anim_init */
 };
+
+static void anim_free(qr_anim_state *a)
+{
+    if (a == NULL) return;
+    if (a->block) cudaFree(a->block);
+    if (a->ring) cudaFreeHost(a->ring);
+    for (int k = 0; k < QR_ANIM_RING; k++)
+        if (a->ev[k]) cudaEventDestroy(a->ev[k]);
+    delete a;
+}
 
 struct qr_ctx
 {
@@ -95,6 +124,7 @@ extern "C" int qr_ctx_destroy(qr_ctx *ctx)
         if (ctx->scenes[i] != NULL)
         {
             cudaFree(ctx->scenes[i]->block);
+            anim_free(ctx->scenes[i]->anim);
             delete ctx->scenes[i];
         }
     }
@@ -195,14 +225,18 @@ static void shadow_list(const qr_scene_desc *d, int *off, int *num)
     *num = sn;
 }
 
-/* copy a scene's arrays, and the hierarchy built over them, into one device
- * block (or into an existing one) */
-static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool fresh)
+/* copy a scene's arrays, and the hierarchy built over them (for the motion
+ * bound `bound`, NULL: none), into one device block (or into an existing
+ * one); the hierarchy is left in *accp when given */
+static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool fresh,
+                  const float *bound = NULL, qr_accel_host *accp = NULL)
 {
-    qr_accel_host acc;
+    qr_accel_host acc_local;
+    qr_accel_host &acc = accp != NULL ? *accp : acc_local;
     int lvl_root[QR_BVH_LEVELS], lvl_aoff[QR_BVH_LEVELS], lvl_anum[QR_BVH_LEVELS];
     float lvl_r2[QR_BVH_LEVELS];
-    qr_accel_build_levels(d, &acc, lvl_root, lvl_aoff, lvl_anum, lvl_r2);
+    qr_accel_build_levels(d, &acc, lvl_root, lvl_aoff, lvl_anum, lvl_r2, bound);
+    if (sl.anim != NULL) sl.anim->ok = 0;
     const bool use_bvh = !acc.nodes.empty();
     size_t o_srf = 0;
     size_t o_mat = o_srf + al16(sizeof(qr_srf) * d->nsrf);
@@ -278,6 +312,283 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     return QR_OK;
 }
 
+/* ---- device update of animated scenes ----------------------------------- */
+
+static qr_scene_slot *slot(qr_ctx *ctx, int id);
+
+static int check_anim_table(const qr_scene_desc *d, const qr_anim_node *nodes, int n,
+                            int *nparams)
+{
+    if (n < 0 || (n > 0 && nodes == NULL)) return QR_ERR_ARG;
+    std::vector<char> rec(d->nsrf, 0), lgt(d->nlgt, 0);
+    int np = 0;
+    for (int i = 0; i < n; i++)
+    {
+        const qr_anim_node &N = nodes[i];
+        if (N.kind < QR_ANIM_OWN || N.kind > QR_ANIM_NODE) return QR_ERR_ARG;
+        if (N.kind == QR_ANIM_OWN ? N.parent != -1 : (N.parent < 0 || N.parent >= i))
+            return QR_ERR_ARG;
+        if (N.param < -1 || (N.kind == QR_ANIM_NODE && N.param != -1)) return QR_ERR_ARG;
+        if (N.rec < -1 || N.rec >= d->nsrf || N.light < -1 || N.light >= d->nlgt)
+            return QR_ERR_ARG;
+        if (N.rec >= 0)
+        {
+            if (rec[N.rec]) return QR_ERR_ARG;
+            rec[N.rec] = 1;
+        }
+        if (N.light >= 0)
+        {
+            if (lgt[N.light]) return QR_ERR_ARG;
+            lgt[N.light] = 1;
+        }
+        if (N.param + 1 > np) np = N.param + 1;
+    }
+    *nparams = np;
+    return QR_OK;
+}
+
+extern "C" int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc,
+                                  const qr_anim_node *nodes, int n, const float *bound)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    int rc = check_desc(desc);
+    if (rc != QR_OK) return rc;
+    int nparams = 0;
+    rc = check_anim_table(desc, nodes, n, &nparams);
+    if (rc != QR_OK) return rc;
+
+    /* the motion bound: given, or the scene's extent widened by half its
+     * radius on each side */
+    float b[6];
+    if (bound != NULL)
+    {
+        for (int k = 0; k < 3; k++)
+            if (!(bound[k] <= bound[3 + k]) || !isfinite(bound[k]) || !isfinite(bound[3 + k]))
+                return QR_ERR_ARG;
+        memcpy(b, bound, sizeof(b));
+    }
+    else
+    {
+        double ext[6];
+        qr_accel_extent(desc, ext);
+        double r = 0.0;
+        for (int k = 0; k < 3; k++) r += 0.25 * (ext[3 + k] - ext[k]) * (ext[3 + k] - ext[k]);
+        r = 0.5 * sqrt(r) + 1.0;
+        for (int k = 0; k < 3; k++)
+        {
+            b[k] = (float)(ext[k] - r);
+            b[3 + k] = (float)(ext[3 + k] + r);
+        }
+    }
+
+    qr_accel_host acc;
+    rc = upload(ctx, *sl, desc, false, b, &acc);
+    if (rc != QR_OK) return rc;
+
+    /* entries by generation */
+    std::vector<int> gen(n, 0);
+    int ngen = n > 0 ? 1 : 0;
+    for (int i = 0; i < n; i++)
+    {
+        if (nodes[i].parent >= 0) gen[i] = gen[nodes[i].parent] + 1;
+        ngen = std::max(ngen, gen[i] + 1);
+    }
+    std::vector<int32_t> order, gen_off(ngen + 1, 0);
+    for (int g = 0; g < ngen; g++)
+    {
+        gen_off[g] = (int)order.size();
+        for (int i = 0; i < n; i++)
+            if (gen[i] == g) order.push_back(i);
+    }
+    gen_off[ngen] = (int)order.size();
+
+    /* surface boxes that move */
+    std::vector<char> dyn(desc->nsrf, 0);
+    for (int i = 0; i < n; i++)
+        if (nodes[i].rec >= 0) dyn[nodes[i].rec] = 1;
+    std::vector<qr_anim_term> terms;
+    std::vector<qr_anim_target> targets;
+    qr_accel_anim_terms(desc, &acc, b, dyn, terms, targets);
+
+    /* hierarchy nodes by depth, deepest first (nodes are stored parent
+     * before children within a level) */
+    const int nbvh = sl->d.nnodes > 0 ? sl->d.nnodes : 0;
+    std::vector<int> depth(nbvh, 0);
+    int maxd = 0;
+    for (int i = 0; i < nbvh; i++)
+    {
+        const qr_bnode &nd = acc.nodes[i];
+        if (nd.count == 0)
+        {
+            depth[nd.a] = depth[i] + 1;
+            depth[nd.b] = depth[i] + 1;
+            maxd = std::max(maxd, depth[i] + 1);
+        }
+    }
+    std::vector<int32_t> rorder, depth_off;
+    for (int dd = nbvh > 0 ? maxd : -1; dd >= 0; dd--)
+    {
+        depth_off.push_back((int)rorder.size());
+        for (int i = 0; i < nbvh; i++)
+            if (depth[i] == dd) rorder.push_back(i);
+    }
+    depth_off.push_back((int)rorder.size());
+    std::vector<float> lboxes((size_t)QR_BVH_LEVELS * desc->nsrf * 6, 0.0f);
+    for (int l = 0; l < QR_BVH_LEVELS; l++)
+        if (acc.lboxes[l].size() == (size_t)desc->nsrf * 6)
+            memcpy(&lboxes[(size_t)l * desc->nsrf * 6], acc.lboxes[l].data(),
+                   sizeof(float) * 6 * desc->nsrf);
+
+    /* one device block */
+    size_t o_nod = 0;
+    size_t o_ord = o_nod + al16(sizeof(qr_anim_node) * n);
+    size_t o_gof = o_ord + al16(sizeof(int32_t) * order.size());
+    size_t o_mtx = o_gof + al16(sizeof(int32_t) * gen_off.size());
+    size_t o_trm = o_mtx + al16(sizeof(float) * 16 * n);
+    size_t o_tgt = o_trm + al16(sizeof(qr_anim_term) * terms.size());
+    size_t o_lbx = o_tgt + al16(sizeof(qr_anim_target) * targets.size());
+    size_t o_ror = o_lbx + al16(sizeof(float) * lboxes.size());
+    size_t o_dof = o_ror + al16(sizeof(int32_t) * rorder.size());
+    size_t o_sta = o_dof + al16(sizeof(int32_t) * depth_off.size());
+    size_t total = o_sta + al16(sizeof(uint32_t) * 2);
+    std::vector<unsigned char> h(total, 0);
+    if (n) memcpy(&h[o_nod], nodes, sizeof(qr_anim_node) * n);
+    if (!order.empty()) memcpy(&h[o_ord], order.data(), sizeof(int32_t) * order.size());
+    memcpy(&h[o_gof], gen_off.data(), sizeof(int32_t) * gen_off.size());
+    if (!terms.empty()) memcpy(&h[o_trm], terms.data(), sizeof(qr_anim_term) * terms.size());
+    if (!targets.empty())
+        memcpy(&h[o_tgt], targets.data(), sizeof(qr_anim_target) * targets.size());
+    if (!lboxes.empty()) memcpy(&h[o_lbx], lboxes.data(), sizeof(float) * lboxes.size());
+    if (!rorder.empty()) memcpy(&h[o_ror], rorder.data(), sizeof(int32_t) * rorder.size());
+    memcpy(&h[o_dof], depth_off.data(), sizeof(int32_t) * depth_off.size());
+
+    qr_anim_state *a = sl->anim;
+    if (a == NULL)
+    {
+        a = new (std::nothrow) qr_anim_state();
+        if (a == NULL) return QR_ERR_OOM;
+        memset(a, 0, sizeof(*a));
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < QR_ANIM_RING && e == cudaSuccess; k++)
+            e = cudaEventCreateWithFlags(&a->ev[k], cudaEventDisableTiming);
+        if (e != cudaSuccess)
+        {
+            anim_free(a);
+            return fail(ctx, QR_ERR_CUDA, "cudaEventCreate", e);
+        }
+        sl->anim = a;
+    }
+    a->ok = 0;
+    cudaError_t e = cudaSuccess;
+    /* earlier updates may still read the old block and ring */
+    for (int k = 0; k < QR_ANIM_RING && e == cudaSuccess; k++) e = cudaEventSynchronize(a->ev[k]);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim wait", e);
+    if (a->bytes < total)
+    {
+        if (a->block) cudaFree(a->block);
+        a->block = NULL;
+        a->bytes = 0;
+        e = cudaMalloc(&a->block, total);
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaMalloc anim", e);
+        a->bytes = total;
+    }
+    const size_t ring_n = nparams > 0 ? (size_t)nparams : 1;
+    if (a->ring_n < ring_n)
+    {
+        if (a->ring) cudaFreeHost(a->ring);
+        a->ring = NULL;
+        a->ring_n = 0;
+        e = cudaHostAlloc((void **)&a->ring, sizeof(qr_anim_param) * ring_n * QR_ANIM_RING,
+                          cudaHostAllocMapped);
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaHostAlloc anim params", e);
+        a->ring_n = ring_n;
+    }
+    e = cudaMemcpyAsync(a->block, h.data(), total, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim copy", e);
+
+    unsigned char *blk = (unsigned char *)a->block;
+    qr_anim_dev &D = a->dev;
+    D.nodes = (const qr_anim_node *)(blk + o_nod);
+    D.order = (const int32_t *)(blk + o_ord);
+    D.gen_off = (const int32_t *)(blk + o_gof);
+    D.n = n;
+    D.ngen = ngen;
+    D.params = NULL;
+    D.mtx = (float *)(blk + o_mtx);
+    D.srf = const_cast<qr_srf *>(sl->d.srf);
+    D.lgt = const_cast<qr_light *>(sl->d.lgt);
+    D.terms = (const qr_anim_term *)(blk + o_trm);
+    D.targets = (const qr_anim_target *)(blk + o_tgt);
+    D.ntargets = (int32_t)targets.size();
+    D.nsrf = desc->nsrf;
+    D.lboxes = (float *)(blk + o_lbx);
+    D.bvh = const_cast<qr_bnode *>(sl->d.nodes);
+    D.items = sl->d.items;
+    D.rorder = (const int32_t *)(blk + o_ror);
+    D.depth_off = (const int32_t *)(blk + o_dof);
+    D.nbvh = nbvh;
+    D.nbands = (int32_t)depth_off.size() - 1;
+    for (int l = 0; l < QR_BVH_LEVELS; l++)
+        D.lvl_end[l] = l + 1 < QR_BVH_LEVELS ? sl->d.lvl_root[l + 1] : nbvh;
+    for (int k = 0; k < 6; k++) D.ext[k] = acc.ext[k];
+    D.status = (uint32_t *)(blk + o_sta);
+    a->nparams = nparams;
+    a->next = 0;
+    a->ok = 1;
+    return QR_OK;
+}
+
+extern "C" int qr_scene_anim_update(qr_ctx *ctx, int scene_id, const qr_anim_param *params,
+                                    int nparams, void *stream)
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    qr_anim_state *a = sl->anim;
+    if (a == NULL || !a->ok) return QR_ERR_STATE;
+    if (nparams != a->nparams || (nparams > 0 && params == NULL)) return QR_ERR_ARG;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaSetDevice", e);
+    /* the next parameter set of the ring, once the update that last read it
+     * has run */
+    const int k = a->next;
+    a->next = (k + 1) % QR_ANIM_RING;
+    e = cudaEventSynchronize(a->ev[k]);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim ring wait", e);
+    qr_anim_param *set = a->ring + (size_t)k * a->ring_n;
+    if (nparams > 0) memcpy(set, params, sizeof(qr_anim_param) * nparams);
+    qr_anim_param *dset = NULL;
+    e = cudaHostGetDevicePointer((void **)&dset, set, 0);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaHostGetDevicePointer", e);
+    qr_anim_dev D = a->dev;
+    D.params = dset;
+    cudaStream_t st = stream != NULL ? (cudaStream_t)stream : ctx->stream;
+    e = qr_launch_anim(D, st);
+    if (e == cudaSuccess) e = cudaEventRecord(a->ev[k], st);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim launch", e);
+    return QR_OK;
+}
+
+extern "C" int qr_scene_anim_status(qr_ctx *ctx, int scene_id, int32_t out[2])
+{
+    qr_scene_slot *sl = slot(ctx, scene_id);
+    if (sl == NULL) return QR_ERR_NOSCENE;
+    if (out == NULL) return QR_ERR_ARG;
+    qr_anim_state *a = sl->anim;
+    if (a == NULL || !a->ok) return QR_ERR_STATE;
+    uint32_t st[2];
+    cudaError_t e = cudaSetDevice(ctx->device);
+    for (int k = 0; k < QR_ANIM_RING && e == cudaSuccess; k++) e = cudaEventSynchronize(a->ev[k]);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(st, a->dev.status, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim status", e);
+    out[0] = (int32_t)st[0];
+    out[1] = (int32_t)st[1];
+    return QR_OK;
+}
+
 extern "C" int qr_scene_upload(qr_ctx *ctx, const qr_scene_desc *desc, int *scene_id)
 {
     if (ctx == NULL || scene_id == NULL) return QR_ERR_ARG;
@@ -339,6 +650,7 @@ extern "C" int qr_scene_release(qr_ctx *ctx, int scene_id)
     if (sl == NULL) return QR_ERR_NOSCENE;
     cudaSetDevice(ctx->device);
     cudaFree(sl->block);
+    anim_free(sl->anim);
     delete sl;
     return QR_OK;
 }

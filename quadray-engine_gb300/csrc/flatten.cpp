@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <algorithm>
+#include <unordered_map>
 
 #include "flatten.h"
 #include "xform.h"
@@ -1401,6 +1402,179 @@ void Flat::camera_action(rt_time time, int action)
         } break;
     default: break;
     }
+}
+
+/* ---- device-side update phases ------------------------------------------ */
+
+/* the rotation flag of rt_Object::update_matrix (object.cpp:236-247): set
+ * unless every angle is a multiple of 90 degrees */
+static int rot_flag(const rt_TRANSFORM3D *trm)
+{
+    const float frt[] = {-270.0f, -180.0f, -90.0f, 0.0f, +90.0f, +180.0f, +270.0f};
+    int c = 0;
+    for (int i = 0; i < 7; i++)
+    {
+        if (trm->rot[RT_X] == frt[i]) c++;
+        if (trm->rot[RT_Y] == frt[i]) c++;
+        if (trm->rot[RT_Z] == frt[i]) c++;
+    }
+    return c == 3 ? 0 : FLAG_ROT;
+}
+
+static void copy16(float *d, const float (*m)[4])
+{
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) d[4 * i + j] = m[i][j];
+}
+
+int Flat::anim_table(std::vector<qr_anim_node> &out, std::string *why)
+{
+    out.clear();
+    anim_nodes.clear();
+    anim_scl.clear();
+    std::vector<int> entry(nodes.size(), -1);
+    std::unordered_map<const Node*, int> at;
+    for (size_t i = 0; i < nodes.size(); i++) at[nodes[i]] = (int)i;
+    /* nodes are in creation order: every parent before its children */
+    for (size_t i = 0; i < nodes.size(); i++)
+    {
+        Node *n = nodes[i];
+        const bool animated = n->obj->f_anim != RT_NULL;
+        Node *t0 = n->parent != RT_NULL ? n->parent->trnode : RT_NULL;
+        const int t0e = t0 != RT_NULL ? entry[at[t0]] : -1;
+        const float (*pm)[4] = n->parent != RT_NULL ? (const float (*)[4])n->parent->pmtx : iden4;
+        const int rot = rot_flag(n->trm);
+        if (animated && !rot)
+        {
+            if (why) *why = "an animated object has no free rotation";
+            return 1;
+        }
+        if (n->kind == K_CAMERA && (animated || t0e >= 0))
+        {
+            if (why) *why = "a camera moves with an animated object";
+            return 2;
+        }
+        qr_anim_node e;
+        memset(&e, 0, sizeof(e));
+        e.parent = -1;
+        e.param = -1;
+        e.rec = -1;
+        e.light = -1;
+        float P[4][4], R[4][4];
+        bool dyn = false;
+        if (rot)
+        {
+            if (!animated && t0e < 0) continue;
+            dyn = true;
+            if (t0 == RT_NULL)
+            {
+                e.kind = QR_ANIM_OWN;
+                memcpy(P, pm, sizeof(P));
+            }
+            else if (t0e < 0)
+            {
+                e.kind = QR_ANIM_OWN;
+                mat_mul_mat(P, t0->mtx, pm);
+            }
+            else
+            {
+                e.kind = QR_ANIM_UNDER;
+                e.parent = t0e;
+                memcpy(P, pm, sizeof(P));
+            }
+            mat_from_transform(R, n->trm, 0);
+            if (animated)
+            {
+                e.param = (int)anim_nodes.size();
+                anim_nodes.push_back(n);
+                std::vector<float> sc(n->trm->scl, n->trm->scl + 3);
+                anim_scl.push_back(sc);
+            }
+        }
+        else
+        {
+            const bool clause = t0 != RT_NULL && t0 != n &&
+                                ((opts & RT_OPTS_TARRAY) == 0 || n->tag > RT_TAG_SURFACE_MAX);
+            if (!clause || t0e < 0) continue;
+            dyn = true;
+            e.kind = QR_ANIM_NODE;
+            e.parent = t0e;
+            float trm_mtx[4][4];
+            mat_from_transform(trm_mtx, n->trm, 1);
+            mat_mul_mat(P, pm, trm_mtx);
+            memset(R, 0, sizeof(R));
+        }
+        if (!dyn || n->trnode != n)
+        {
+            if (why) *why = "a moving object is not a transform node";
+            return 3;
+        }
+        copy16(e.p, P);
+        copy16(e.r, R);
+        if (n->kind == K_SURFACE || n->kind == K_ARRAY) e.rec = n->index;
+        if (n->kind == K_LIGHT)
+        {
+            for (size_t j = 0; j < lights.size(); j++)
+                if (lights[j] == n) e.light = (int)j;
+        }
+        entry[i] = (int)out.size();
+        out.push_back(e);
+    }
+
+    /* the recipes must give the matrices of the last update */
+    std::vector<float> M(16 * out.size());
+    for (size_t i = 0; i < nodes.size(); i++)
+    {
+        if (entry[i] < 0) continue;
+        const qr_anim_node &e = out[entry[i]];
+        float P[4][4], R[4][4], T[4][4], tmp[4][4], m[4][4];
+        memcpy(P, e.p, sizeof(P));
+        memcpy(R, e.r, sizeof(R));
+        if (e.param >= 0) mat_from_transform(R, nodes[i]->trm, 0);
+        if (e.parent >= 0) memcpy(T, &M[16 * e.parent], sizeof(T));
+        if (e.kind == QR_ANIM_OWN) mat_mul_mat(m, P, R);
+        else if (e.kind == QR_ANIM_UNDER) { mat_mul_mat(tmp, T, P); mat_mul_mat(m, tmp, R); }
+        else mat_mul_mat(m, T, P);
+        memcpy(&M[16 * entry[i]], m, sizeof(m));
+        if (memcmp(m, nodes[i]->mtx, sizeof(m)) != 0)
+        {
+            if (why) *why = "the update table does not reproduce a transform";
+            return 4;
+        }
+    }
+    return 0;
+}
+
+int Flat::anim_params(rt_time time, std::vector<qr_anim_param> &out)
+{
+    /* animators and time stamps as in update_status (object.cpp:175-216) */
+    for (size_t i = 0; i < nodes.size(); i++)
+    {
+        rt_OBJECT *obj = nodes[i]->obj;
+        if (obj->f_anim != RT_NULL && obj->time != time)
+        {
+            obj->f_anim(time, obj->time < 0 ? 0 : obj->time, nodes[i]->trm, RT_NULL);
+        }
+        obj->time = time;
+    }
+    out.resize(anim_nodes.size());
+    int rc = 0;
+    for (size_t i = 0; i < anim_nodes.size(); i++)
+    {
+        const rt_TRANSFORM3D *t = anim_nodes[i]->trm;
+        if (!rot_flag(t)) rc = 1;
+        for (int k = 0; k < 3; k++)
+            if (memcmp(&t->scl[k], &anim_scl[i][k], sizeof(float)) != 0) rc = 2;
+        qr_anim_param &q = out[i];
+        memset(&q, 0, sizeof(q));
+        for (int k = 0; k < 3; k++)
+        {
+            q.sin[k] = sina_(t->rot[k]);
+            q.cos[k] = cosa_(t->rot[k]);
+            q.pos[k] = t->pos[k];
+        }
+    }
+    return rc;
 }
 
 void Flat::emit_records()

@@ -139,6 +139,17 @@ public:
     void frame_params(qr_frame_params *fp) const;
     /* descriptor pointing into this object's arrays */
     void desc(qr_scene_desc *d) const;
+    /* the device update table (qr_anim_node, include/qr_gpu.h) of the
+     * records and lights that move when animators run, from the state of
+     * the last update(); nonzero (and the reason in *why) when the scene
+     * cannot be updated on the device: an animated object without a free
+     * rotation (all angles multiples of 90 degrees) or a camera under one */
+    int anim_table(std::vector<qr_anim_node> &out, std::string *why);
+    /* run the animators for `time` (as update() does, without the update
+     * phases) and give each animated transform of the table; nonzero when
+     * one lost its free rotation (1) or changed its scale (2): the frame
+     * then needs update() and a new table */
+    int anim_params(rt_time time, std::vector<qr_anim_param> &out);
 
     int  opts;
     int  x_res, y_res, fsaa;
@@ -171,6 +182,9 @@ public:
 
     Node *root;
     rt_OBJECT rootobj;
+    /* animated transforms of the update table and their scales */
+    std::vector<Node*> anim_nodes;
+    std::vector<std::vector<float> > anim_scl;
 
 private:
     Node *build(Node *parent, rt_OBJECT *obj);

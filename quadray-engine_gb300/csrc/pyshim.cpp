@@ -12,6 +12,7 @@
 
 #include "scenegen.hpp"
 #include "flatten.h"
+#include "xform.h"
 #include "engine.h"
 
 extern "C"
@@ -92,6 +93,84 @@ int qrpy_flat_desc(void *f, qr_scene_desc *d, qr_frame_params *fp)
 void qrpy_flat_free(void *f)
 {
     delete (qr::Flat *)f;
+}
+
+/* the device update table (Flat::anim_table) into out[cap]; *n receives its
+ * length; QR_ERR_LIMIT when cap is short, QR_ERR_STATE (reason in why) when
+ * the scene cannot be updated on the device */
+int qrpy_flat_anim_table(void *f, qr_anim_node *out, int cap, int *n, char *why, int why_len)
+{
+    std::vector<qr_anim_node> t;
+    std::string reason;
+    int rc = ((qr::Flat *)f)->anim_table(t, &reason);
+    *n = (int)t.size();
+    if (rc != 0)
+    {
+        if (why != NULL && why_len > 0) snprintf(why, (size_t)why_len, "%s", reason.c_str());
+        return QR_ERR_STATE;
+    }
+    if ((int)t.size() > cap) return QR_ERR_LIMIT;
+    if (!t.empty()) memcpy(out, t.data(), sizeof(qr_anim_node) * t.size());
+    return QR_OK;
+}
+
+/* animators for `time` and the table's transforms (Flat::anim_params) into
+ * out[cap]; returns Flat::anim_params' status, or -1 when cap is short */
+int qrpy_flat_anim_params(void *f, long long time, qr_anim_param *out, int cap, int *n)
+{
+    std::vector<qr_anim_param> p;
+    int rc = ((qr::Flat *)f)->anim_params((rt_time)time, p);
+    *n = (int)p.size();
+    if ((int)p.size() > cap) return -1;
+    if (!p.empty()) memcpy(out, p.data(), sizeof(qr_anim_param) * p.size());
+    return rc;
+}
+
+/* host restatement of the device update's transform stages (anim.cu stages
+ * 1-2, with the same matrix steps of xform.h) applied to table[n] and
+ * params, compared with the records and lights of Flat f after its own
+ * update; returns how many entries differ in any bit */
+int qrpy_anim_check(void *f, const qr_anim_node *table, int n, const qr_anim_param *params)
+{
+    qr::Flat *fl = (qr::Flat *)f;
+    std::vector<float> M(16 * (size_t)(n > 0 ? n : 1));
+    int bad = 0;
+    for (int e = 0; e < n; e++)
+    {
+        const qr_anim_node &N = table[e];
+        float P[4][4], R[4][4], T[4][4], tmp[4][4], m[4][4], inv[4][4];
+        memcpy(P, N.p, sizeof(P));
+        memcpy(R, N.r, sizeof(R));
+        if (N.param >= 0)
+        {
+            const float one[3] = {1.0f, 1.0f, 1.0f};
+            qr::mat_from_sc(R, params[N.param].sin, params[N.param].cos,
+                            params[N.param].pos, one);
+        }
+        if (N.parent >= 0) memcpy(T, &M[16 * (size_t)N.parent], sizeof(T));
+        if (N.kind == QR_ANIM_OWN) qr::mat_mul_mat(m, P, R);
+        else if (N.kind == QR_ANIM_UNDER) { qr::mat_mul_mat(tmp, T, P); qr::mat_mul_mat(m, tmp, R); }
+        else qr::mat_mul_mat(m, T, P);
+        memcpy(&M[16 * (size_t)e], m, sizeof(m));
+        bool diff = false;
+        if (N.rec >= 0)
+        {
+            qr::mat_inverse(inv, m);
+            const qr_srf &s = fl->srf[N.rec];
+            for (int k = 0; k < 3; k++)
+            {
+                diff |= memcmp(&s.tci[k], &inv[k][0], 4) != 0;
+                diff |= memcmp(&s.tcj[k], &inv[k][1], 4) != 0;
+                diff |= memcmp(&s.tck[k], &inv[k][2], 4) != 0;
+                diff |= memcmp(&s.pos[k], &m[3][k], 4) != 0;
+            }
+        }
+        if (N.light >= 0)
+            for (int k = 0; k < 3; k++)
+                diff |= memcmp(&fl->lgt[N.light].pos[k], &m[3][k], 4) != 0;
+        bad += diff ? 1 : 0;
+    }
+    return bad;
 }
 
 /* ---- engine API --------------------------------------------------------- */

@@ -1,0 +1,170 @@
+"""Device-side update phases (qr_scene_anim_*): a scene whose animators run
+on the host and whose transforms, inverse matrices, surface boxes and
+hierarchy are updated by the device gives, frame after frame, the same
+frame bit for bit as the same scene updated by the host phases and
+uploaded, as the in-order list walk over the device-updated records, and as
+the reference's own frames of the golden fixtures."""
+import ctypes
+
+import pytest
+
+from conftest import oracle_render
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(qr):
+    c = qr.Context(0)
+    yield c
+    c.close()
+
+
+def _copy(qr, params):
+    return qr.QrFrameParams.from_buffer_copy(params)
+
+
+def _device_scene(qr, ctx, kind, seed, nq, flags, w, h, fsaa, depth, bound=None):
+    g = qr.GenScene(kind, seed, nq, flags)
+    f = qr.Flat(g, w, h, fsaa)
+    desc, params = f.update(0, depth)
+    fp = _copy(qr, params)
+    sid = ctx.upload(desc)
+    ctx.anim_init(sid, desc, f.anim_table(), bound)
+    return g, f, sid, fp
+
+
+@pytest.mark.parametrize("kind,seed,nq,flags,fsaa", [
+    (2, 1, 64, 0, 0),           # spinning 3-level hierarchy, every surface a node
+    (2, 2, 64, 8, 2),           # array-level transform nodes (TARRAY), 4x AA
+    (2, 6, 64, 512, 0),         # the reference's default of no Fresnel terms
+    (2, 4, 256, 0, 0),          # 256 quadrics: outer hierarchy levels in use
+    (1, 3, 32, 16, 0),          # spinning quadrics of the plain scene
+])
+def test_device_update_equals_host_update(qr, oracle, ctx, kind, seed, nq, flags, fsaa):
+    w, h, depth = 192, 108, 4
+    g, f, sid, fp = _device_scene(qr, ctx, kind, seed, nq, flags, w, h, fsaa, depth)
+    g2 = qr.GenScene(kind, seed, nq, flags)
+    f2 = qr.Flat(g2, w, h, fsaa)
+    hid = None
+    times = [16, 32, 48, 16 * 40, 16 * 97]
+    for k, t in enumerate(times):
+        rc, p = f.anim_params(t)
+        assert rc == 0
+        ctx.anim_update(sid, p)
+        dev = ctx.render_host(sid, fp).copy()
+        desc2, params2 = f2.update(t, depth)
+        if hid is None:
+            hid = ctx.upload(desc2)
+        else:
+            ctx.update(hid, desc2)
+        host = ctx.render_host(hid, params2)
+        assert (dev != host).sum() == 0, (t, int((dev != host).sum()))
+        lin = _copy(qr, fp)
+        lin.flags |= qr.FP_LINEAR_WALK
+        walk = ctx.render_host(sid, lin)
+        assert (dev != walk).sum() == 0, t
+        if k == 1:
+            cpu, _ = oracle_render(oracle, desc2, params2)
+            assert (dev != cpu).sum() == 0, t
+    assert ctx.anim_status(sid) == (len(times), 0)
+    ctx.release(sid)
+    ctx.release(hid)
+
+
+def test_device_update_outside_bound_stays_exact(qr, ctx):
+    """a motion bound no larger than the first frame's extent: spinning
+    surfaces leave it, the update opens the hierarchy's boxes for those
+    frames (counted), and the frames still equal the host's"""
+    kind, seed, nq, flags, w, h, depth = 2, 3, 64, 0, 160, 90, 4
+    g, f, sid, fp = _device_scene(qr, ctx, kind, seed, nq, flags, w, h, 0, depth,
+                                  bound=[0.0] * 6)
+    g2 = qr.GenScene(kind, seed, nq, flags)
+    f2 = qr.Flat(g2, w, h, 0)
+    hid = None
+    times = [16 * 25 * k for k in range(1, 7)]
+    for t in times:
+        rc, p = f.anim_params(t)
+        assert rc == 0
+        ctx.anim_update(sid, p)
+        dev = ctx.render_host(sid, fp).copy()
+        desc2, params2 = f2.update(t, depth)
+        if hid is None:
+            hid = ctx.upload(desc2)
+        else:
+            ctx.update(hid, desc2)
+        host = ctx.render_host(hid, params2)
+        assert (dev != host).sum() == 0, t
+    frames, missed = ctx.anim_status(sid)
+    assert frames == len(times) and missed >= 1
+    ctx.release(sid)
+    ctx.release(hid)
+
+
+def test_device_update_matches_reference_frames(qr, ctx):
+    """the reference's own frames of the animated golden fixtures (no
+    camera actions), every frame after the first updated on the device"""
+    from test_oracle_golden import EXACT, load_golden, check_against_golden, flatten_case
+    import os
+    done = 0
+    for path in EXACT:
+        frames, meta = load_golden(path)
+        if meta["kind"] != qr.SCN_ANIM or meta.get("actions") or meta.get("nextcam"):
+            continue
+        g, f, desc, params = flatten_case(qr, meta, 0)
+        fp = _copy(qr, params)
+        sid = ctx.upload(desc)
+        ctx.anim_init(sid, desc, f.anim_table())
+        for k in range(meta["frames"]):
+            if k > 0:
+                rc, p = f.anim_params(16 * k)
+                assert rc == 0
+                ctx.anim_update(sid, p)
+            img = ctx.render_host(sid, fp)
+            check_against_golden(img, frames[k], meta)
+        ctx.release(sid)
+        done += 1
+    assert done >= 4, os.listdir(os.path.dirname(path))
+
+
+def test_device_update_on_a_stream_and_in_a_batch(qr, ctx):
+    """updates enqueued on a caller's stream ahead of a batched launch of
+    several device-updated scenes: each frame equals its host-updated one"""
+    import numpy as np
+    import torch
+    w, h, depth = 128, 72, 4
+    s = torch.cuda.Stream()
+    scenes = []
+    for seed in (1, 2, 3):
+        g, f, sid, fp = _device_scene(qr, ctx, qr.SCN_ANIM, seed, 64, 0, w, h, 0, depth)
+        scenes.append((g, f, sid, fp))
+    b = qr.Batch(ctx, len(scenes))
+    for t in (48, 160):
+        outs, reqs = [], []
+        for g, f, sid, fp in scenes:
+            rc, p = f.anim_params(t)
+            assert rc == 0
+            ctx.anim_update(sid, p, s.cuda_stream)
+            out = torch.empty((h, w), dtype=torch.int32, device="cuda")
+            q = qr.QrRequest()
+            q.scene_id = sid
+            q.fp = fp
+            q.dev_frame = out.data_ptr()
+            q.dev_acc = None
+            reqs.append(q)
+            outs.append(out)
+        b.set(reqs)
+        b.launch(s.cuda_stream)
+        s.synchronize()
+        for (g, f, sid, fp), out in zip(scenes, outs):
+            g2 = qr.GenScene(qr.SCN_ANIM, g.seed, 64, 0)
+            f2 = qr.Flat(g2, w, h, 0)
+            desc2, params2 = f2.update(t, depth)
+            hid = ctx.upload(desc2)
+            host = ctx.render_host(hid, params2)
+            dev = out.cpu().numpy().view(np.uint32)
+            assert (dev != host).sum() == 0, (g.seed, t)
+            ctx.release(hid)
+    b.close()
+    for g, f, sid, fp in scenes:
+        ctx.release(sid)

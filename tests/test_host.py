@@ -54,6 +54,9 @@ def test_null_arguments_rejected(qr):
     assert L.qr_ctx_create(0, None) != qr.QR_OK
     assert L.qr_render_host(None, 0, None, None) != qr.QR_OK
     assert L.qr_scene_upload(None, None, None) != qr.QR_OK
+    assert L.qr_scene_anim_init(None, 0, None, None, 0, None) != qr.QR_OK
+    assert L.qr_scene_anim_update(None, 0, None, 0, None) != qr.QR_OK
+    assert L.qr_scene_anim_status(None, 0, None) != qr.QR_OK
 
 
 def _c_layout():
@@ -72,6 +75,9 @@ int main(void) {
     P(qr_frame_params, x_res); P(qr_frame_params, seed); P(qr_frame_params, pts_c);
     P(qr_scene_desc, texels); P(qr_scene_desc, cam_num);
     P(qr_srf, sci); P(qr_srf, amap); P(qr_srf, trnode); P(qr_srf, id);
+    printf("qr_anim_node %zu\nqr_anim_param %zu\n", sizeof(qr_anim_node),
+           sizeof(qr_anim_param));
+    P(qr_anim_node, p); P(qr_anim_node, r); P(qr_anim_param, pos);
     return 0;
 }
 """
@@ -98,6 +104,11 @@ def test_struct_layouts_match_ctypes_mirror(qr):
     assert lay["qr_frame_params.pts_c"] == qr.QrFrameParams.pts_c.offset
     assert lay["qr_scene_desc.texels"] == qr.QrSceneDesc.texels.offset
     assert lay["qr_scene_desc.cam_num"] == qr.QrSceneDesc.cam_num.offset
+    assert lay["qr_anim_node"] == ctypes.sizeof(qr.QrAnimNode) == 160
+    assert lay["qr_anim_param"] == ctypes.sizeof(qr.QrAnimParam) == 48
+    assert lay["qr_anim_node.p"] == qr.QrAnimNode.p.offset
+    assert lay["qr_anim_node.r"] == qr.QrAnimNode.r.offset
+    assert lay["qr_anim_param.pos"] == qr.QrAnimParam.pos.offset
 
 
 def _desc_arrays(desc, mat_size=112):
@@ -194,3 +205,38 @@ def test_bmp_textures_load_like_the_reference(qr, tmp_path, monkeypatch):
     (tmp_path / "qr_tex1.bmp").unlink()
     with pytest.raises(RuntimeError):
         qr.Flat(qr.GenScene(qr.SCN_PLAIN, 7, 16, qr.GEN_TEX | qr.GEN_TEXFILE), 64, 48)
+
+
+@pytest.mark.parametrize("kind,seed,nq,flags,opts", [
+    (2, 1, 64, 0, -1),          # every surface under a spinning array a node
+    (2, 2, 64, 8, -1),          # array-level transform nodes (TARRAY)
+    (2, 5, 64, 0, (1 << 20) | (1 << 21) | (1 << 25)),   # the reference's NONE opts
+    (1, 3, 32, 16, -1),         # spinning quadrics, no hierarchy of arrays
+])
+def test_device_update_table_reproduces_host_update(qr, kind, seed, nq, flags, opts):
+    """the device update table taken at one frame, with the animators'
+    transforms of later frames, gives the records and lights of the host
+    update phases of those frames bit for bit (the device's matrix steps run
+    on the host here; the GPU tests compare the device's own output)"""
+    f = qr.Flat(qr.GenScene(kind, seed, nq, flags), 160, 96, 0, opts)
+    f.update(16, 4)
+    table = f.anim_table()
+    assert len(table) > 0
+    assert all(e.parent < i for i, e in enumerate(table))
+    nparam = max(e.param for e in table) + 1
+    for t in (32, 48, 16 * 55, 16 * 301):
+        rc, p = f.anim_params(t)
+        assert rc == 0 and len(p) == nparam
+        f.update(t, 4)
+        assert f.anim_check(table, p) == 0, t
+    # a stale table does not reproduce frames it was not given
+    rc, p = f.anim_params(16 * 302)
+    assert f.anim_check(table, p) > 0
+
+
+def test_static_scene_has_an_empty_update_table(qr):
+    f = qr.Flat(qr.GenScene(qr.SCN_PLAIN, 4, 16, 0), 64, 48)
+    f.update(0, 4)
+    assert len(f.anim_table()) == 0
+    rc, p = f.anim_params(16)
+    assert rc == 0 and len(p) == 0
