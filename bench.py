@@ -91,6 +91,50 @@ def batch_requests(n, seed0):
     return out
 
 
+def anim_update_time(qr, ctx, seed):
+    """device time of one update launch (qr_scene_anim_update) of a spinning
+    scene of 256 quadrics and of the 512-quadric animated hierarchy, CUDA
+    events around 200 launches on one stream; beside it the host update
+    phases, hierarchy build and upload it replaces (wall clock)"""
+    import time as _t
+    import torch
+    out = {}
+    for name, kind, nq, flags in (("plain_spin_256", qr.SCN_PLAIN, 256, qr.GEN_SPIN),
+                                  ("anim_512", qr.SCN_ANIM, 512, 0)):
+        g = qr.GenScene(kind, seed, nq, flags)
+        f = qr.Flat(g, 1920, 1080, 0)
+        desc, _ = f.update(0, 4)
+        sid = ctx.upload(desc)
+        table = f.anim_table()
+        ctx.anim_init(sid, desc, table)
+        s = torch.cuda.Stream()
+        params = [f.anim_params(16 * (k + 1))[1] for k in range(200)]
+        for p in params[:5]:
+            ctx.anim_update(sid, p, s.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(s)
+        for p in params:
+            ctx.anim_update(sid, p, s.cuda_stream)
+        e1.record(s)
+        e1.synchronize()
+        dev_us = 1000.0 * e0.elapsed_time(e1) / len(params)
+        t0 = _t.perf_counter()
+        for k in range(20):
+            d2, _ = f.update(16 * (300 + k), 4)
+            ctx.update(sid, d2)
+        host_us = 1e6 * (_t.perf_counter() - t0) / 20
+        t0 = _t.perf_counter()
+        for k in range(200):
+            rc, p = f.anim_params(16 * (400 + k))
+        anim_host_us = 1e6 * (_t.perf_counter() - t0) / 200
+        out[name] = {"entries": len(table), "device_update_us": dev_us,
+                     "animators_host_us": anim_host_us,
+                     "host_update_and_upload_us": host_us}
+        ctx.release(sid)
+    return out
+
+
 def run_serve(args, wl, rank, world, dist, local):
     """served stream: rays/s sustained and latency at each arrival rate"""
     import torch
@@ -104,7 +148,7 @@ def run_serve(args, wl, rank, world, dist, local):
     for i in range(32):
         nq = int(round(math.exp(rng.uniform(math.log(16), math.log(256)))))
         scenes.append(dict(gen=qr.GenScene(qr.SCN_PLAIN, wl["seed"] + i, nq, qr.GEN_SPIN),
-                           pt=False, depth=10, nq=nq, kind=1))
+                           pt=False, depth=10, nq=nq, kind=1, anim=True))
     # rays per request class from instrumented frames at t = 0
     rays_of = {}
 
@@ -130,7 +174,8 @@ def run_serve(args, wl, rank, world, dist, local):
         return rays_of[key] * (req.spp if sc["pt"] else 1)
 
     srv = serve.Server(qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
-                       prep_threads=min(8, os.cpu_count() or 1))
+                       prep_threads=min(8, os.cpu_count() or 1),
+                       device_anim=not args.serve_host_update)
     # warm-up: every scene once at every size
     warm = [serve.Request(i, s, 0, w, h, 1, 0.0)
             for i, (s, (w, h)) in enumerate((s, sz) for s in range(32) for sz in SERVE_SIZES)]
@@ -156,7 +201,9 @@ def run_serve(args, wl, rank, world, dist, local):
                         "whitted_1080p_ms_p99": float(np.percentile(big, 99)) if len(big) else None,
                         "prepared_ms_p99": float(np.percentile(prep, 99)) if len(prep) else None})
     ck = clocks.stop()
+    counts = {"device_updates": srv.device_updates, "host_updates": srv.host_updates}
     srv.close()
+    anim_us = anim_update_time(qr, ctx, wl["seed"])
     top = results[-1]
     line = {
         "metric": "rays_per_s", "value": top["rays_per_s"], "unit": "rays/s",
@@ -170,10 +217,14 @@ def run_serve(args, wl, rank, world, dist, local):
                    "budget_bytes": 120 << 30, "seconds_per_rate": wl["seconds"],
                    "parallelism": "replicas" if world > 1 else "single"},
         "rates": results,
+        "scene_updates": counts,
+        "anim_update": anim_us,
         "e2e": {"value": top["rays_per_s"], "unit": "rays/s",
                 "h2d_bytes_per_step": None, "d2h_bytes_per_step": 0,
-                "note": "wall clock of the serving loop: host update phases, scene "
-                        "uploads, batched launches; frames stay on the device"},
+                "note": "wall clock of the serving loop: animators on the host, "
+                        "update phases on the device (host update phases and "
+                        "uploads for a scene copy's first frame), batched "
+                        "launches; frames stay on the device"},
         "clocks": ck,
     }
     if rank == 0:
@@ -491,6 +542,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="anim", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-host-update", action="store_true",
+                    help="serve: update animated scenes on the host (update phases, "
+                         "hierarchy build and upload per request) instead of the device")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     wl = WORKLOADS[args.workload]

@@ -254,12 +254,18 @@ typedef struct qr_anim_param
 } qr_anim_param;
 
 /* Upload `desc` into scene `scene_id` in place (as qr_scene_update) with
- * the hierarchy sized for the motion bound (lo[3], hi[3], NULL: the
- * scene's extent widened by half its radius on each side) and prepare the
+ * the hierarchy sized for the motion bound (lo[3], hi[3]; NULL: where
+ * rotations of the animated transforms about their origins can take the
+ * moving records and surfaces, joined with the scene's extent) and prepare the
  * device update of the n entries of `nodes` (records and lights in range,
  * parents earlier).  A later qr_scene_update drops the preparation. */
 int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc,
                        const qr_anim_node *nodes, int n, const float *bound);
+/* the same into a new resident scene (qr_scene_upload then
+ * qr_scene_anim_init, with one upload); returns its id */
+int qr_scene_anim_upload(qr_ctx *ctx, const qr_scene_desc *desc,
+                         const qr_anim_node *nodes, int n, const float *bound,
+                         int *scene_id);
 /* one frame's update on `stream` (asynchronous; NULL: the context's own
  * stream, which qr_render_host and the uploads use; `params` is copied
  * before the call returns): params[i] for every animated transform i named
@@ -268,6 +274,18 @@ int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc,
  * stays exact, rays walk every surface) and the miss is counted */
 int qr_scene_anim_update(qr_ctx *ctx, int scene_id, const qr_anim_param *params,
                          int nparams, void *stream);
+/* the updates of n scenes (distinct, each prepared by qr_scene_anim_init)
+ * in one launch on `stream` (NULL: the context's stream), one block a
+ * scene: for a batch of frames of animated scenes, ahead of the batched
+ * render on the same stream */
+typedef struct qr_anim_request
+{
+    int32_t              scene_id;
+    int32_t              nparams;
+    const qr_anim_param *params;
+} qr_anim_request;
+int qr_scene_anim_update_many(qr_ctx *ctx, const qr_anim_request *reqs, int n,
+                              void *stream);
 /* out[0] = frames updated on the device, out[1] = frames whose update left
  * the motion bound (opened boxes); updates on other streams must have
  * finished */

@@ -104,6 +104,14 @@ class QrAnimParam(ctypes.Structure):
     ]
 
 
+class QrAnimRequest(ctypes.Structure):
+    """qr_anim_request of include/qr_gpu.h (one scene of a batched update)."""
+    _fields_ = [
+        ("scene_id", ctypes.c_int32), ("nparams", ctypes.c_int32),
+        ("params", ctypes.POINTER(QrAnimParam)),
+    ]
+
+
 ANIM_OWN, ANIM_UNDER, ANIM_NODE = 0, 1, 2
 QR_ERR_STATE = 5
 QR_ERR_BUSY = 8
@@ -150,7 +158,11 @@ def lib():
                                          ctypes.POINTER(QrAnimNode), i32,
                                          ctypes.POINTER(ctypes.c_float)]
         L.qr_scene_anim_update.argtypes = [vp, i32, ctypes.POINTER(QrAnimParam), i32, vp]
+        L.qr_scene_anim_upload.argtypes = [vp, ctypes.POINTER(QrSceneDesc),
+                                           ctypes.POINTER(QrAnimNode), i32,
+                                           ctypes.POINTER(ctypes.c_float), ctypes.POINTER(i32)]
         L.qr_scene_anim_status.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int32)]
+        L.qr_scene_anim_update_many.argtypes = [vp, ctypes.POINTER(QrAnimRequest), i32, vp]
         L.qrpy_scene_new.restype = vp
         L.qrpy_scene_new.argtypes = [vp, i32, i32, i32, i32, i32, vp]
         L.qrpy_scene_render.argtypes = [vp, i64, vp]
@@ -245,6 +257,12 @@ class Flat:
         in the reference's camera list"""
         return lib().qrpy_flat_next_cam(self.h)
 
+    def frame_params(self):
+        """the frame parameters of the last update (a copy)"""
+        d, fp = QrSceneDesc(), QrFrameParams()
+        lib().qrpy_flat_desc(self.h, ctypes.byref(d), ctypes.byref(fp))
+        return fp
+
     def action(self, time, action):
         """camera movement before the next update (rt_Scene::update(time,
         action); CAMERA_* codes)"""
@@ -331,11 +349,33 @@ class Context:
         if rc != QR_OK:
             raise RuntimeError("qr_scene_anim_init: %d %s" % (rc, self.error()))
 
+    def anim_upload(self, desc, table, bound=None):
+        """a new resident scene prepared for device updates; returns its id"""
+        b = (ctypes.c_float * 6)(*bound) if bound is not None else None
+        sid = ctypes.c_int32(-1)
+        rc = lib().qr_scene_anim_upload(self.h, ctypes.byref(desc), table, len(table), b,
+                                        ctypes.byref(sid))
+        if rc != QR_OK:
+            raise RuntimeError("qr_scene_anim_upload: %d %s" % (rc, self.error()))
+        return sid.value
+
     def anim_update(self, sid, params, stream=0):
         """one frame's device update of scene sid on `stream`"""
         rc = lib().qr_scene_anim_update(self.h, sid, params, len(params), ctypes.c_void_p(stream))
         if rc != QR_OK:
             raise RuntimeError("qr_scene_anim_update: %d %s" % (rc, self.error()))
+
+    def anim_update_many(self, updates, stream=0):
+        """the updates [(sid, params), ...] of distinct scenes in one launch
+        on `stream`"""
+        arr = (QrAnimRequest * len(updates))()
+        for q, (sid, params) in zip(arr, updates):
+            q.scene_id = sid
+            q.nparams = len(params)
+            q.params = ctypes.cast(params, ctypes.POINTER(QrAnimParam))
+        rc = lib().qr_scene_anim_update_many(self.h, arr, len(updates), ctypes.c_void_p(stream))
+        if rc != QR_OK:
+            raise RuntimeError("qr_scene_anim_update_many: %d %s" % (rc, self.error()))
 
     def anim_status(self, sid):
         """(frames updated on the device, frames whose update left the

@@ -737,13 +737,36 @@ void qr_accel_extent(const qr_scene_desc *d, double ext[6])
 
 /* ---- terms of the world boxes that animated records move ------------------ */
 
+/* float bounds that contain [lo, hi] */
+static float down(double v)
+{
+    float f = (float)v;
+    return (double)f > v ? nextafterf(f, -HUGE_VALF) : f;
+}
+
+static float up(double v)
+{
+    float f = (float)v;
+    return (double)f < v ? nextafterf(f, HUGE_VALF) : f;
+}
+
 static void term_local(qr_anim_term &t, int l, const Box &u)
 {
     for (int k = 0; k < 3; k++)
     {
-        t.u[l][k] = u.lo[k];
-        t.u[l][3 + k] = u.hi[k];
+        t.u[l][k] = down(u.lo[k]);
+        t.u[l][3 + k] = up(u.hi[k]);
     }
+}
+
+bool qr_accel_record_frame(const qr_srf &t, float a[9])
+{
+    double m[3][3], r[3][3];
+    record_matrix(t, m);
+    if (!invert3(m, r)) return false;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) a[3 * i + j] = (float)r[i][j];
+    return true;
 }
 
 /* the world_box form for record s in the frame of transform node xf */
@@ -814,7 +837,6 @@ int qr_accel_anim_terms(const qr_scene_desc *d, const qr_accel_host *acc,
                 ct.mode = term_mode(d, c, cxf[e], true);
                 for (int l = 0; l < QR_BVH_LEVELS; l++)
                     term_local(ct, l, local_clip_region(c, Dl[l]));
-                for (int k = 0; k < 6; k++) ct.u[QR_BVH_LEVELS][k] = 0.0;
                 terms.push_back(ct);
                 moved = moved || dyn[el.ref] || (cxf[e] >= 0 && dyn[cxf[e]]);
             }

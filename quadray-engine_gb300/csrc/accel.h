@@ -106,7 +106,7 @@ void qr_accel_extent(const qr_scene_desc *d, double ext[6]);
 struct qr_anim_term
 {
     int32_t srf, xf, mode, pad;
-    double  u[QR_BVH_LEVELS + 1][6];
+    float   u[QR_BVH_LEVELS + 1][6];    /* rounded outwards from double */
 };
 
 /* a surface whose box is the meet of terms [t0, t0 + tn), the first its
@@ -115,6 +115,11 @@ struct qr_anim_target
 {
     int32_t srf, t0, tn, levels;
 };
+
+/* world-from-local matrix of a record's frame as the box terms use it: the
+ * inverse of the record's transform rows (record_matrix), row-major, in
+ * float; false when singular */
+bool qr_accel_record_frame(const qr_srf &t, float a[9]);
 
 /* the terms of every bounded surface whose box depends on a record marked
  * in dyn (its own, its transform node's, a bounding clipper's or that

@@ -1,8 +1,9 @@
 /*
- * anim.cu: device-side update phases of an animated scene, one block per
- * update (the work is a few hundred matrices and boxes; one block keeps the
- * ordering between its stages to block barriers and the whole update to
- * one launch).
+ * anim.cu: device-side update phases of animated scenes, one block per
+ * scene and one launch for all the scenes of a batch (a scene's work is a
+ * few hundred matrices and boxes; one block keeps the ordering between its
+ * stages to block barriers, and the blocks of different scenes run side by
+ * side).
  *
  * Stage 1  transform chain, generation by generation: the matrices of
  *          rt_Object::update_matrix (core/engine/object.cpp:221-389) with
@@ -12,10 +13,12 @@
  * Stage 2  records: inverse matrix rows tci/tcj/tck and position
  *          (rt_Node::update_fields, object.cpp:826-857), light positions
  *          (the light's pos in rt_Light::update_fields, object.cpp:649-667).
- * Stage 3  world boxes of the surfaces that move, in double precision, as
- *          accel.cpp forms them (world_box, affine_image, pad), and the
- *          check that every moved record and surface stays inside the
- *          motion bound the boxes' rounding allowance was sized for.
+ * Stage 3  world boxes of the surfaces that move, as accel.cpp forms them
+ *          (world_box, affine_image, pad) but in float: the pad (1e-3 +
+ *          1e-4 of the coordinates) is far above float rounding, and the
+ *          local boxes are rounded outwards; and the check that every
+ *          moved record and surface stays inside the motion bound the
+ *          boxes' rounding allowance was sized for.
  * Stage 4  hierarchy node boxes bottom-up by depth band; when the check
  *          failed, every node box is opened instead, so every ray walks
  *          every surface and the frame stays exact.
@@ -40,83 +43,80 @@ __device__ void store16(float *p, const float (*m)[4])
         for (int j = 0; j < 4; j++) p[4 * i + j] = m[i][j];
 }
 
-/* a record's 3x3 transform as the tracer applies it (diagonal only when
- * amap[3] == 1, "scaling only"), accel.cpp record_matrix */
-__device__ void record_matrix(const qr_srf &t, double m[3][3])
+/* world-from-local matrix of a record's frame (accel.cpp
+ * qr_accel_record_frame, in float): the inverse of the transform rows as the
+ * tracer applies them (diagonal only when amap[3] == 1, "scaling only") */
+__device__ void record_frame(const qr_srf &t, float *f)
 {
+    float m[3][3];
     const float *row[3] = {t.tci, t.tcj, t.tck};
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
-            m[i][j] = (t.amap[3] == 1 && i != j) ? 0.0 : (double)row[i][j];
-}
-
-__device__ bool invert3(const double m[3][3], double r[3][3])
-{
-    const double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1];
-    const double c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2];
-    const double c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
-    const double det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
-    if (!(fabs(det) > 1e-30)) return false;
-    const double id = 1.0 / det;
-    r[0][0] = c00 * id;
-    r[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
-    r[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
-    r[1][0] = c01 * id;
-    r[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
-    r[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
-    r[2][0] = c02 * id;
-    r[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
-    r[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
-    return true;
+            m[i][j] = (t.amap[3] == 1 && i != j) ? 0.0f : row[i][j];
+    const float c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1];
+    const float c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2];
+    const float c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+    const float det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
+    if (!(fabsf(det) > 1e-30f))
+    {
+        f[9] = 1.0f;
+        return;
+    }
+    const float id = 1.0f / det;
+    f[0] = c00 * id;
+    f[1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+    f[2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+    f[3] = c01 * id;
+    f[4] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+    f[5] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
+    f[6] = c02 * id;
+    f[7] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
+    f[8] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
+    f[9] = 0.0f;
 }
 
 /* world box of one term at level l (accel.h, QR_TERM_*); false when the
- * record's transform is singular */
+ * frame's transform is singular */
 __device__ bool term_box(const qr_anim_dev &A, const qr_anim_term &t, int l,
-                         double lo[3], double hi[3])
+                         float lo[3], float hi[3])
 {
     const qr_srf &s = A.srf[t.srf];
-    double a[3][3] = {{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
-    double o[3], u[6];
+    const bool node = t.mode == QR_TERM_NODE || t.mode == QR_TERM_NODE_SHIFT;
+    const int fr = node ? t.xf : t.srf;
+    const qr_srf &F = A.srf[fr];
+    float u[6];
     for (int k = 0; k < 6; k++) u[k] = t.u[l][k];
-    if (t.mode == QR_TERM_NODE || t.mode == QR_TERM_NODE_SHIFT)
+    if (node)
     {
-        const qr_srf &T = A.srf[t.xf];
         for (int k = 0; k < 3; k++)
         {
-            u[k] += (double)s.pos[k];
-            u[3 + k] += (double)s.pos[k];
-            o[k] = (double)T.pos[k];
-        }
-        if (t.mode == QR_TERM_NODE)
-        {
-            double m[3][3];
-            record_matrix(T, m);
-            if (!invert3(m, a)) return false;
+            u[k] += s.pos[k];
+            u[3 + k] += s.pos[k];
         }
     }
-    else
+    if (t.mode == QR_TERM_NODE_SHIFT || t.mode == QR_TERM_OWN_SHIFT)
     {
-        for (int k = 0; k < 3; k++) o[k] = (double)s.pos[k];
-        if (t.mode == QR_TERM_OWN)
+        for (int k = 0; k < 3; k++)
         {
-            double m[3][3];
-            record_matrix(s, m);
-            if (!invert3(m, a)) return false;
+            lo[k] = u[k] + F.pos[k];
+            hi[k] = u[3 + k] + F.pos[k];
         }
+        return true;
     }
+    const float *a = A.frame + 10 * (size_t)fr;
+    if (a[9] != 0.0f) return false;
     /* interval image of u under h = a u + o (accel.cpp affine_image) */
     for (int i = 0; i < 3; i++)
     {
-        double l0 = o[i], h0 = o[i];
+        float l0 = F.pos[i], h0 = F.pos[i];
         for (int j = 0; j < 3; j++)
         {
-            const double c = a[i][j];
-            if (c == 0.0) continue;
-            const double p = c * u[j], q = c * u[3 + j];
-            if (isnan(p) || isnan(q)) { l0 = -HUGE_VAL; h0 = HUGE_VAL; break; }
-            l0 += fmin(p, q);
-            h0 += fmax(p, q);
+            const float c = a[3 * i + j];
+            if (c == 0.0f) continue;
+            const float p = c * u[j], q = c * u[3 + j];
+            if (isnan(p) || isnan(q)) { l0 = -HUGE_VALF; h0 = HUGE_VALF; break; }
+            l0 += fminf(p, q);
+            h0 += fmaxf(p, q);
         }
         lo[i] = l0;
         hi[i] = h0;
@@ -124,18 +124,23 @@ __device__ bool term_box(const qr_anim_dev &A, const qr_anim_term &t, int l,
     return true;
 }
 
-__device__ bool inside(const double ext[6], const double lo[3], const double hi[3])
+__device__ bool inside(const float ext[6], const float lo[3], const float hi[3])
 {
     for (int k = 0; k < 3; k++)
         if (!(lo[k] >= ext[k] && hi[k] <= ext[3 + k])) return false;
     return true;
 }
 
-__global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev A)
+__global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev *devs)
 {
     __shared__ int fail;
+    __shared__ qr_anim_dev A;
     const int tid = threadIdx.x, nt = blockDim.x;
-    if (tid == 0) fail = 0;
+    if (tid == 0)
+    {
+        fail = 0;
+        A = devs[blockIdx.x];
+    }
     __syncthreads();
 
     /* stage 1: matrices, parents before children */
@@ -197,9 +202,10 @@ __global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev A)
                 s.tck[k] = inv[k][2];
                 s.pos[k] = M[3][k];
             }
+            record_frame(s, A.frame + 10 * (size_t)N.rec);
             /* record positions bound the local coordinates the walk forms
              * (light positions take no part, as in the host build) */
-            const double p[3] = {M[3][0], M[3][1], M[3][2]};
+            const float p[3] = {M[3][0], M[3][1], M[3][2]};
             if (!inside(A.ext, p, p)) fail = 1;
         }
         if (N.light >= 0)
@@ -217,18 +223,18 @@ __global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev A)
         const qr_anim_target tg = A.targets[w / (L + 1)];
         const int l = w % (L + 1);
         if (l < L && ((tg.levels >> l) & 1) == 0) continue;
-        double lo[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
-        double hi[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL};
+        float lo[3] = {-HUGE_VALF, -HUGE_VALF, -HUGE_VALF};
+        float hi[3] = {HUGE_VALF, HUGE_VALF, HUGE_VALF};
         const int nterm = l == L ? 1 : tg.tn;
         bool ok = true;
         for (int j = 0; j < nterm && ok; j++)
         {
-            double tl[3], th[3];
+            float tl[3], th[3];
             ok = term_box(A, A.terms[tg.t0 + j], l, tl, th);
             for (int k = 0; k < 3 && ok; k++)
             {
-                lo[k] = fmax(lo[k], tl[k]);
-                hi[k] = fmin(hi[k], th[k]);
+                lo[k] = fmaxf(lo[k], tl[k]);
+                hi[k] = fminf(hi[k], th[k]);
             }
         }
         if (l == L)
@@ -237,20 +243,20 @@ __global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev A)
              * that only its clippers bound has none), as in the host build */
             bool fin = ok;
             for (int k = 0; k < 3; k++)
-                fin = fin && lo[k] > -HUGE_VAL && hi[k] < HUGE_VAL && lo[k] <= hi[k];
+                fin = fin && lo[k] > -HUGE_VALF && hi[k] < HUGE_VALF && lo[k] <= hi[k];
             if (!ok || (fin && !inside(A.ext, lo, hi))) fail = 1;
             continue;
         }
         for (int k = 0; k < 3 && ok; k++)
-            ok = lo[k] <= hi[k] && lo[k] > -HUGE_VAL && hi[k] < HUGE_VAL;
+            ok = lo[k] <= hi[k] && lo[k] > -HUGE_VALF && hi[k] < HUGE_VALF;
         if (!ok) { fail = 1; continue; }
         float *b = A.lboxes + ((size_t)l * A.nsrf + tg.srf) * 6;
         for (int k = 0; k < 3; k++)
         {
             /* accel.cpp pad */
-            const double m = 1e-3 + 1e-4 * (fabs(lo[k]) + fabs(hi[k]));
-            b[k] = (float)(lo[k] - m);
-            b[3 + k] = (float)(hi[k] + m);
+            const float m = 1e-3f + 1e-4f * (fabsf(lo[k]) + fabsf(hi[k]));
+            b[k] = lo[k] - m;
+            b[3 + k] = hi[k] + m;
         }
     }
     __syncthreads();
@@ -311,8 +317,9 @@ __global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev A)
 
 } /* namespace */
 
-cudaError_t qr_launch_anim(const qr_anim_dev &a, cudaStream_t stream)
+cudaError_t qr_launch_anim(const qr_anim_dev *devs, int n, cudaStream_t stream)
 {
-    anim_kernel<<<1, 512, 0, stream>>>(a);
+    if (n <= 0) return cudaSuccess;
+    anim_kernel<<<n, 512, 0, stream>>>(devs);
     return cudaGetLastError();
 }

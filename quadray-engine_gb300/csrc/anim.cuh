@@ -31,11 +31,15 @@ struct qr_anim_dev
     const int32_t       *depth_off; /* depth band b: rorder[depth_off[b], depth_off[b+1]) */
     int32_t              nbvh, nbands;
     int32_t              lvl_end[QR_BVH_LEVELS];   /* level l: nodes below lvl_end[l] */
-    double               ext[6];    /* motion bound the boxes allow for */
+    float               *frame;     /* per record: world-from-local 3x3
+                                       (row-major) and a singular flag, 10
+                                       floats (qr_accel_record_frame) */
+    float                ext[6];    /* motion bound the boxes allow for */
     uint32_t            *status;    /* [0] frames updated, [1] frames out of bound */
 };
 
-/* one update on `stream`: a single block */
-cudaError_t qr_launch_anim(const qr_anim_dev &a, cudaStream_t stream);
+/* updates of n scenes on `stream`, one block each; devs (n entries, in
+ * mapped host memory) must stay unchanged until the launch has run */
+cudaError_t qr_launch_anim(const qr_anim_dev *devs, int n, cudaStream_t stream);
 
 #endif /* QR_ANIM_CUH */

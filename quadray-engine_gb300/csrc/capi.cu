@@ -22,7 +22,7 @@
 
 
 /* device update of an animated scene (qr_scene_anim_*) */
-#define QR_ANIM_RING 4
+#define QR_ANIM_RING 4          /* parameter / launch sets in turn */
 struct qr_anim_state
 {
     int          ok;        /* prepared for the scene's current upload */
@@ -71,6 +71,14 @@ struct qr_ctx
     size_t       dacc_px;
     uint32_t    *dfault;    /* fault word of the context's scenes (qr_fault) */
     cudaStream_t stream;
+    /* scene updates (qr_scene_anim_update_many): per launch a set of
+     * qr_anim_dev in mapped host memory, QR_ANIM_RING sets in turn, each
+     * reused once the launch that read it has run */
+    std::mutex   amu;
+    qr_anim_dev *adevs;
+    size_t       adevs_n;
+    cudaEvent_t  aev[4];
+    int          anext;
 };
 
 static int fail(qr_ctx *ctx, int code, const char *what, cudaError_t e)
@@ -98,6 +106,10 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
     ctx->dacc_px = 0;
     ctx->dfault = NULL;
     ctx->stream = 0;
+    ctx->adevs = NULL;
+    ctx->adevs_n = 0;
+    ctx->anext = 0;
+    for (int k = 0; k < 4; k++) ctx->aev[k] = NULL;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->dfault, 4 * sizeof(uint32_t));
@@ -131,6 +143,9 @@ extern "C" int qr_ctx_destroy(qr_ctx *ctx)
     if (ctx->dframe) cudaFree(ctx->dframe);
     if (ctx->dacc) cudaFree(ctx->dacc);
     if (ctx->dfault) cudaFree(ctx->dfault);
+    if (ctx->adevs) cudaFreeHost(ctx->adevs);
+    for (int k = 0; k < 4; k++)
+        if (ctx->aev[k]) cudaEventDestroy(ctx->aev[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return QR_OK;
@@ -315,6 +330,7 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
 /* ---- device update of animated scenes ----------------------------------- */
 
 static qr_scene_slot *slot(qr_ctx *ctx, int id);
+static int add_slot(qr_ctx *ctx, qr_scene_slot *sl, int *scene_id);
 
 static int check_anim_table(const qr_scene_desc *d, const qr_anim_node *nodes, int n,
                             int *nparams)
@@ -347,19 +363,181 @@ static int check_anim_table(const qr_scene_desc *d, const qr_anim_node *nodes, i
     return QR_OK;
 }
 
+/* largest singular value of a 3x3 matrix (power iteration on A^T A) */
+static double sigma_max(const double a[3][3])
+{
+    double g[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            g[i][j] = a[0][i] * a[0][j] + a[1][i] * a[1][j] + a[2][i] * a[2][j];
+    double v[3] = {1.0, 0.7, 0.4}, lam = 0.0;
+    for (int it = 0; it < 64; it++)
+    {
+        double w[3];
+        for (int i = 0; i < 3; i++) w[i] = g[i][0] * v[0] + g[i][1] * v[1] + g[i][2] * v[2];
+        const double n = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        if (!(n > 0.0)) return 0.0;
+        for (int i = 0; i < 3; i++) v[i] = w[i] / n;
+        lam = n;
+    }
+    /* a little above the estimate: power iteration approaches from below */
+    return sqrt(lam) * (1.0 + 1e-6) + 1e-12;
+}
+
+/*
+ * The default motion bound: where moving records and surfaces can be if the
+ * animators rotate and never move their transforms' origins.  Along the
+ * table (parents first) every entry's origin stays in a ball (c, r) and its
+ * linear part has a singular value bound s: an entry of its own keeps its
+ * origin, s = |M|; under a parent T the origin is T's origin plus T's linear
+ * part applied to a fixed offset, r = r_T + s_T |offset|, s = s_T |P|.  A
+ * moving surface stays within its frame's ball widened by s_F times the
+ * largest corner of its local box.  The bound holds these balls and the
+ * scene's extent; an update that leaves it anyway (an animator that
+ * translates) is caught by the update's own check.
+ */
+static void rotation_bound(const qr_scene_desc *d, const qr_anim_node *nodes, int n,
+                           float out[6])
+{
+    double ext[6];
+    qr_accel_extent(d, ext);
+    double lo[3] = {ext[0], ext[1], ext[2]}, hi[3] = {ext[3], ext[4], ext[5]};
+    std::vector<double> c(3 * (size_t)n), r(n), sg(n);
+    std::vector<int> of_rec(d->nsrf, -1);
+    auto grow = [&](const double *cc, double rr) {
+        for (int k = 0; k < 3; k++)
+        {
+            lo[k] = std::min(lo[k], cc[k] - rr);
+            hi[k] = std::max(hi[k], cc[k] + rr);
+        }
+    };
+    for (int e = 0; e < n; e++)
+    {
+        const qr_anim_node &N = nodes[e];
+        double P[3][3];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) P[i][j] = N.p[4 * j + i];   /* column-major */
+        double o[3] = {0.0, 0.0, 0.0};
+        double M[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        if (N.rec >= 0)
+        {
+            const qr_srf &s = d->srf[N.rec];
+            float f[9];
+            if (qr_accel_record_frame(s, f))
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) M[i][j] = f[3 * i + j];
+            for (int k = 0; k < 3; k++) o[k] = s.pos[k];
+            of_rec[N.rec] = e;
+        }
+        else if (N.light >= 0)
+        {
+            for (int k = 0; k < 3; k++) o[k] = d->lgt[N.light].pos[k];
+        }
+        if (N.kind == QR_ANIM_OWN)
+        {
+            for (int k = 0; k < 3; k++) c[3 * e + k] = o[k];
+            r[e] = 0.0;
+            sg[e] = sigma_max(M);
+        }
+        else
+        {
+            const int t = N.parent;
+            const qr_srf &T = d->srf[nodes[t].rec >= 0 ? nodes[t].rec : 0];
+            /* the offset in T's frame: T's transform rows applied to the
+             * origins' difference */
+            double q = 0.0;
+            const float *row[3] = {T.tci, T.tcj, T.tck};
+            for (int i = 0; i < 3; i++)
+            {
+                double v = 0.0;
+                for (int k = 0; k < 3; k++) v += (double)row[i][k] * (o[k] - (double)T.pos[k]);
+                q += v * v;
+            }
+            for (int k = 0; k < 3; k++) c[3 * e + k] = c[3 * t + k];
+            r[e] = r[t] + sg[t] * sqrt(q) * (1.0 + 1e-5) + 1e-5;
+            sg[e] = sg[t] * sigma_max(P);
+        }
+        if (N.rec >= 0) grow(&c[3 * e], r[e]);
+    }
+    /* moving surfaces: their frame's ball and the reach of their local box */
+    std::vector<char> dyn(d->nsrf, 0);
+    for (int e = 0; e < n; e++)
+        if (nodes[e].rec >= 0) dyn[nodes[e].rec] = 1;
+    qr_accel_host none;
+    std::vector<qr_anim_term> terms;
+    std::vector<qr_anim_target> targets;
+    for (int l = 0; l < QR_BVH_LEVELS; l++) none.lbounded[l].assign(d->nsrf, 1);
+    qr_accel_anim_terms(d, &none, NULL, dyn, terms, targets);
+    for (size_t i = 0; i < targets.size(); i++)
+    {
+        const qr_anim_term &t = terms[targets[i].t0];
+        const bool node = t.mode == QR_TERM_NODE || t.mode == QR_TERM_NODE_SHIFT;
+        const int fr = node ? t.xf : t.srf;
+        if (fr < 0 || of_rec[fr] < 0) continue;
+        const int e = of_rec[fr];
+        const qr_srf &s = d->srf[t.srf];
+        double rho = 0.0;
+        bool fin = true;
+        for (int k = 0; k < 3; k++)
+        {
+            const double a = t.u[QR_BVH_LEVELS][k], b = t.u[QR_BVH_LEVELS][3 + k];
+            const double sh = node ? (double)s.pos[k] : 0.0;
+            if (!(a > -HUGE_VAL && b < HUGE_VAL && a <= b)) fin = false;
+            const double m = std::max(fabs(a + sh), fabs(b + sh));
+            rho += m * m;
+        }
+        if (!fin) continue;
+        grow(&c[3 * e], r[e] + sg[e] * sqrt(rho) * (1.0 + 1e-5) + 1e-5);
+    }
+    for (int k = 0; k < 3; k++)
+    {
+        out[k] = (float)lo[k];
+        out[3 + k] = (float)hi[k];
+    }
+}
+
+static int anim_prepare(qr_ctx *ctx, qr_scene_slot *sl, const qr_scene_desc *desc,
+                        const qr_anim_node *nodes, int n, const float *bound);
+
 extern "C" int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc *desc,
                                   const qr_anim_node *nodes, int n, const float *bound)
 {
     qr_scene_slot *sl = slot(ctx, scene_id);
     if (sl == NULL) return QR_ERR_NOSCENE;
+    return anim_prepare(ctx, sl, desc, nodes, n, bound);
+}
+
+extern "C" int qr_scene_anim_upload(qr_ctx *ctx, const qr_scene_desc *desc,
+                                    const qr_anim_node *nodes, int n, const float *bound,
+                                    int *scene_id)
+{
+    if (ctx == NULL || scene_id == NULL) return QR_ERR_ARG;
+    qr_scene_slot *sl = new (std::nothrow) qr_scene_slot();
+    if (sl == NULL) return QR_ERR_OOM;
+    memset(sl, 0, sizeof(*sl));
+    int rc = anim_prepare(ctx, sl, desc, nodes, n, bound);
+    if (rc != QR_OK)
+    {
+        if (sl->block) cudaFree(sl->block);
+        anim_free(sl->anim);
+        delete sl;
+        return rc;
+    }
+    return add_slot(ctx, sl, scene_id);
+}
+
+static int anim_prepare(qr_ctx *ctx, qr_scene_slot *sl, const qr_scene_desc *desc,
+                        const qr_anim_node *nodes, int n, const float *bound)
+{
+    if (ctx == NULL) return QR_ERR_ARG;
     int rc = check_desc(desc);
     if (rc != QR_OK) return rc;
     int nparams = 0;
     rc = check_anim_table(desc, nodes, n, &nparams);
     if (rc != QR_OK) return rc;
 
-    /* the motion bound: given, or the scene's extent widened by half its
-     * radius on each side */
+    /* the motion bound: given, or where rotations about fixed origins can
+     * take the moving records and surfaces */
     float b[6];
     if (bound != NULL)
     {
@@ -370,16 +548,7 @@ extern "C" int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc
     }
     else
     {
-        double ext[6];
-        qr_accel_extent(desc, ext);
-        double r = 0.0;
-        for (int k = 0; k < 3; k++) r += 0.25 * (ext[3 + k] - ext[k]) * (ext[3 + k] - ext[k]);
-        r = 0.5 * sqrt(r) + 1.0;
-        for (int k = 0; k < 3; k++)
-        {
-            b[k] = (float)(ext[k] - r);
-            b[3 + k] = (float)(ext[3 + k] + r);
-        }
+        rotation_bound(desc, nodes, n, b);
     }
 
     qr_accel_host acc;
@@ -434,6 +603,12 @@ extern "C" int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc
             if (depth[i] == dd) rorder.push_back(i);
     }
     depth_off.push_back((int)rorder.size());
+    /* world-from-local frames of the records (moving ones are redone by
+     * every update) */
+    std::vector<float> frames((size_t)desc->nsrf * 10, 0.0f);
+    for (int i = 0; i < desc->nsrf; i++)
+        if (!qr_accel_record_frame(desc->srf[i], &frames[10 * (size_t)i]))
+            frames[10 * (size_t)i + 9] = 1.0f;
     std::vector<float> lboxes((size_t)QR_BVH_LEVELS * desc->nsrf * 6, 0.0f);
     for (int l = 0; l < QR_BVH_LEVELS; l++)
         if (acc.lboxes[l].size() == (size_t)desc->nsrf * 6)
@@ -450,7 +625,8 @@ extern "C" int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc
     size_t o_lbx = o_tgt + al16(sizeof(qr_anim_target) * targets.size());
     size_t o_ror = o_lbx + al16(sizeof(float) * lboxes.size());
     size_t o_dof = o_ror + al16(sizeof(int32_t) * rorder.size());
-    size_t o_sta = o_dof + al16(sizeof(int32_t) * depth_off.size());
+    size_t o_frm = o_dof + al16(sizeof(int32_t) * depth_off.size());
+    size_t o_sta = o_frm + al16(sizeof(float) * frames.size());
     size_t total = o_sta + al16(sizeof(uint32_t) * 2);
     std::vector<unsigned char> h(total, 0);
     if (n) memcpy(&h[o_nod], nodes, sizeof(qr_anim_node) * n);
@@ -462,6 +638,7 @@ extern "C" int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc
     if (!lboxes.empty()) memcpy(&h[o_lbx], lboxes.data(), sizeof(float) * lboxes.size());
     if (!rorder.empty()) memcpy(&h[o_ror], rorder.data(), sizeof(int32_t) * rorder.size());
     memcpy(&h[o_dof], depth_off.data(), sizeof(int32_t) * depth_off.size());
+    if (!frames.empty()) memcpy(&h[o_frm], frames.data(), sizeof(float) * frames.size());
 
     qr_anim_state *a = sl->anim;
     if (a == NULL)
@@ -532,7 +709,16 @@ extern "C" int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc
     D.nbands = (int32_t)depth_off.size() - 1;
     for (int l = 0; l < QR_BVH_LEVELS; l++)
         D.lvl_end[l] = l + 1 < QR_BVH_LEVELS ? sl->d.lvl_root[l + 1] : nbvh;
-    for (int k = 0; k < 6; k++) D.ext[k] = acc.ext[k];
+    D.frame = (float *)(blk + o_frm);
+    for (int k = 0; k < 3; k++)
+    {
+        /* rounded inwards: a float box inside it is inside the double one */
+        float lo = (float)acc.ext[k], hi = (float)acc.ext[3 + k];
+        if ((double)lo < acc.ext[k]) lo = nextafterf(lo, HUGE_VALF);
+        if ((double)hi > acc.ext[3 + k]) hi = nextafterf(hi, -HUGE_VALF);
+        D.ext[k] = lo;
+        D.ext[3 + k] = hi;
+    }
     D.status = (uint32_t *)(blk + o_sta);
     a->nparams = nparams;
     a->next = 0;
@@ -540,34 +726,91 @@ extern "C" int qr_scene_anim_init(qr_ctx *ctx, int scene_id, const qr_scene_desc
     return QR_OK;
 }
 
+extern "C" int qr_scene_anim_update_many(qr_ctx *ctx, const qr_anim_request *reqs, int n,
+                                         void *stream)
+{
+    if (ctx == NULL || n < 0 || (n > 0 && reqs == NULL)) return QR_ERR_ARG;
+    if (n == 0) return QR_OK;
+    std::vector<qr_scene_slot *> sls(n);
+    for (int i = 0; i < n; i++)
+    {
+        qr_scene_slot *sl = slot(ctx, reqs[i].scene_id);
+        if (sl == NULL) return QR_ERR_NOSCENE;
+        const qr_anim_state *a = sl->anim;
+        if (a == NULL || !a->ok) return QR_ERR_STATE;
+        if (reqs[i].nparams != a->nparams || (a->nparams > 0 && reqs[i].params == NULL))
+            return QR_ERR_ARG;
+        sls[i] = sl;
+    }
+    {
+        /* two blocks must not update one scene */
+        std::vector<qr_scene_slot *> u(sls);
+        std::sort(u.begin(), u.end());
+        if (std::adjacent_find(u.begin(), u.end()) != u.end()) return QR_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lock(ctx->amu);
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaSetDevice", e);
+    for (int k = 0; k < QR_ANIM_RING && e == cudaSuccess; k++)
+        if (ctx->aev[k] == NULL) e = cudaEventCreateWithFlags(&ctx->aev[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaEventCreate", e);
+    if (ctx->adevs_n < (size_t)n)
+    {
+        for (int k = 0; k < QR_ANIM_RING && e == cudaSuccess; k++) e = cudaEventSynchronize(ctx->aev[k]);
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim wait", e);
+        if (ctx->adevs) cudaFreeHost(ctx->adevs);
+        ctx->adevs = NULL;
+        ctx->adevs_n = 0;
+        const size_t cap = std::max((size_t)n, (size_t)64);
+        e = cudaHostAlloc((void **)&ctx->adevs, sizeof(qr_anim_dev) * cap * QR_ANIM_RING,
+                          cudaHostAllocMapped);
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_OOM, "cudaHostAlloc anim launch", e);
+        ctx->adevs_n = cap;
+    }
+    /* the next launch set, once the launch that last read it has run */
+    const int k = ctx->anext;
+    ctx->anext = (k + 1) % QR_ANIM_RING;
+    e = cudaEventSynchronize(ctx->aev[k]);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim ring wait", e);
+    qr_anim_dev *set = ctx->adevs + (size_t)k * ctx->adevs_n;
+    std::vector<int> used(n);
+    for (int i = 0; i < n; i++)
+    {
+        /* each scene's next parameter set, likewise */
+        qr_anim_state *a = sls[i]->anim;
+        const int kk = a->next;
+        a->next = (kk + 1) % QR_ANIM_RING;
+        used[i] = kk;
+        e = cudaEventSynchronize(a->ev[kk]);
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim ring wait", e);
+        qr_anim_param *ps = a->ring + (size_t)kk * a->ring_n;
+        if (a->nparams > 0) memcpy(ps, reqs[i].params, sizeof(qr_anim_param) * a->nparams);
+        qr_anim_param *dps = NULL;
+        e = cudaHostGetDevicePointer((void **)&dps, ps, 0);
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaHostGetDevicePointer", e);
+        set[i] = a->dev;
+        set[i].params = dps;
+    }
+    qr_anim_dev *dset = NULL;
+    e = cudaHostGetDevicePointer((void **)&dset, set, 0);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaHostGetDevicePointer", e);
+    cudaStream_t st = stream != NULL ? (cudaStream_t)stream : ctx->stream;
+    e = qr_launch_anim(dset, n, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->aev[k], st);
+    for (int i = 0; i < n && e == cudaSuccess; i++)
+        e = cudaEventRecord(sls[i]->anim->ev[used[i]], st);
+    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim launch", e);
+    return QR_OK;
+}
+
 extern "C" int qr_scene_anim_update(qr_ctx *ctx, int scene_id, const qr_anim_param *params,
                                     int nparams, void *stream)
 {
-    qr_scene_slot *sl = slot(ctx, scene_id);
-    if (sl == NULL) return QR_ERR_NOSCENE;
-    qr_anim_state *a = sl->anim;
-    if (a == NULL || !a->ok) return QR_ERR_STATE;
-    if (nparams != a->nparams || (nparams > 0 && params == NULL)) return QR_ERR_ARG;
-    cudaError_t e = cudaSetDevice(ctx->device);
-    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaSetDevice", e);
-    /* the next parameter set of the ring, once the update that last read it
-     * has run */
-    const int k = a->next;
-    a->next = (k + 1) % QR_ANIM_RING;
-    e = cudaEventSynchronize(a->ev[k]);
-    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim ring wait", e);
-    qr_anim_param *set = a->ring + (size_t)k * a->ring_n;
-    if (nparams > 0) memcpy(set, params, sizeof(qr_anim_param) * nparams);
-    qr_anim_param *dset = NULL;
-    e = cudaHostGetDevicePointer((void **)&dset, set, 0);
-    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaHostGetDevicePointer", e);
-    qr_anim_dev D = a->dev;
-    D.params = dset;
-    cudaStream_t st = stream != NULL ? (cudaStream_t)stream : ctx->stream;
-    e = qr_launch_anim(D, st);
-    if (e == cudaSuccess) e = cudaEventRecord(a->ev[k], st);
-    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim launch", e);
-    return QR_OK;
+    qr_anim_request r;
+    r.scene_id = scene_id;
+    r.nparams = nparams;
+    r.params = params;
+    return qr_scene_anim_update_many(ctx, &r, 1, stream);
 }
 
 extern "C" int qr_scene_anim_status(qr_ctx *ctx, int scene_id, int32_t out[2])
@@ -589,6 +832,25 @@ extern "C" int qr_scene_anim_status(qr_ctx *ctx, int scene_id, int32_t out[2])
     return QR_OK;
 }
 
+/* enter a filled slot into the context's table */
+static int add_slot(qr_ctx *ctx, qr_scene_slot *sl, int *scene_id)
+{
+    sl->used = 1;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    for (size_t i = 0; i < ctx->scenes.size(); i++)
+    {
+        if (ctx->scenes[i] == NULL)
+        {
+            ctx->scenes[i] = sl;
+            *scene_id = (int)i;
+            return QR_OK;
+        }
+    }
+    ctx->scenes.push_back(sl);
+    *scene_id = (int)ctx->scenes.size() - 1;
+    return QR_OK;
+}
+
 extern "C" int qr_scene_upload(qr_ctx *ctx, const qr_scene_desc *desc, int *scene_id)
 {
     if (ctx == NULL || scene_id == NULL) return QR_ERR_ARG;
@@ -604,20 +866,7 @@ extern "C" int qr_scene_upload(qr_ctx *ctx, const qr_scene_desc *desc, int *scen
         delete sl;
         return rc;
     }
-    sl->used = 1;
-    std::lock_guard<std::mutex> lock(ctx->mu);
-    for (size_t i = 0; i < ctx->scenes.size(); i++)
-    {
-        if (ctx->scenes[i] == NULL)
-        {
-            ctx->scenes[i] = sl;
-            *scene_id = (int)i;
-            return QR_OK;
-        }
-    }
-    ctx->scenes.push_back(sl);
-    *scene_id = (int)ctx->scenes.size() - 1;
-    return QR_OK;
+    return add_slot(ctx, sl, scene_id);
 }
 
 static qr_scene_slot *slot(qr_ctx *ctx, int id)

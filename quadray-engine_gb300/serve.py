@@ -13,7 +13,11 @@ many clients from one GPU:
   waits;
 * admitted requests are prepared on host threads: the scene's update phases
   at the request's time (animators, transforms, lists, the hierarchy) and an
-  in-place upload into a pooled device copy of that scene;
+  in-place upload into a pooled device copy of that scene; or, for animated
+  scenes whose copy was prepared for it, only the animators on the host and
+  the rest of the update phases on the device (qr_scene_anim_update_many:
+  the scene updates of a batch in one launch on the serving stream, ahead
+  of the batch);
 * continuous batching: prepared requests go into the next batched launch
   (qr_batch_*), two batches in flight so the GPU never waits for the host;
   requests that arrive while a batch runs join the following one;
@@ -37,7 +41,7 @@ class Request:
     """One frame request."""
 
     __slots__ = ("rid", "scene", "time", "w", "h", "spp", "arrival", "done",
-                 "frame", "acc", "slot", "bytes", "fp", "flat_key", "prepared")
+                 "frame", "acc", "slot", "bytes", "fp", "flat_key", "prepared", "anim")
 
     def __init__(self, rid, scene, time_ms, w, h, spp, arrival):
         self.rid, self.scene, self.time = rid, scene, time_ms
@@ -50,17 +54,29 @@ class Request:
         self.bytes = 0
         self.fp = None
         self.flat_key = None
+        self.anim = None                # animators' transforms for a device update
 
 
 class Server:
     """Continuous-batching frame server over one context."""
 
     def __init__(self, qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
-                 max_batch_pixels=24 << 20, prep_threads=4, per_request=True):
+                 max_batch_pixels=24 << 20, prep_threads=4, per_request=True,
+                 device_anim=False, rebuild_every=32):
         """scenes: list of dicts with keys gen (a GenScene), pt (path-traced
-        scene) and depth; per_request: complete each request when its frame
-        is done (else when its batch is)"""
+        scene), depth and anim (animated); per_request: complete each request
+        when its frame is done (else when its batch is); device_anim: update
+        animated scenes on the device (qr_scene_anim_*) where they allow it"""
         self.per_request = per_request
+        self.device_anim = device_anim
+        self.tables = {}                # (scene, w, h, fsaa) -> update table or None
+        # scene copies prepared for device updates -> device updates since:
+        # the hierarchy keeps its first frame's tree and only refits its
+        # boxes, which loosens as animated subtrees move, so every
+        # rebuild_every updates the copy takes the host phases again
+        self.anim_slots = {}
+        self.rebuild_every = rebuild_every
+        self.device_updates = self.host_updates = 0
         self.qr, self.ctx = qr, ctx
         self.scenes = scenes
         self.budget = budget_bytes
@@ -99,22 +115,56 @@ class Server:
         return 0 if (self.scenes[req.scene]["pt"] or req.spp <= 1) else 2
 
     def _prepare(self, req):
-        """update phases at the request's time, upload into a scene copy"""
+        """the scene at the request's time in a device copy of its own: on
+        the device (the animators' transforms and one update launch on the
+        serving stream) when the copy was prepared for it, else by the host
+        update phases and an upload"""
         qr = self.qr
         sc = self.scenes[req.scene]
         fsaa = self._fsaa(req)
         key = (req.scene, req.w, req.h, fsaa)
+        dev = self.device_anim and sc.get("anim", False)
         with self.locks[req.scene]:
             flat = self.flats.get(key)
             if flat is None:
                 flat = qr.Flat(sc["gen"], req.w, req.h, fsaa)
                 self.flats[key] = flat
-            desc, params = flat.update(req.time, sc["depth"])
-            fp = qr.QrFrameParams.from_buffer_copy(params)
-            if req.slot is None:
-                req.slot = self.ctx.upload(desc)
-            else:
-                self.ctx.update(req.slot, desc)
+            fp = None
+            refresh = False
+            if dev and self.tables.get(key) is not None and req.slot in self.anim_slots \
+                    and self.anim_slots[req.slot] < self.rebuild_every:
+                rc, prm = flat.anim_params(req.time)
+                refresh = rc != 0       # the table no longer fits the scene
+                if rc == 0:
+                    # the update runs with the others of the request's batch
+                    req.anim = prm
+                    fp = qr.QrFrameParams.from_buffer_copy(flat.frame_params())
+                    self.device_updates += 1
+                    self.anim_slots[req.slot] += 1
+            if fp is None:
+                desc, params = flat.update(req.time, sc["depth"])
+                fp = qr.QrFrameParams.from_buffer_copy(params)
+                table = None
+                if dev:
+                    if key not in self.tables or refresh:
+                        try:
+                            self.tables[key] = flat.anim_table()
+                        except ValueError:
+                            self.tables[key] = None
+                    table = self.tables[key]
+                if table is not None:
+                    if req.slot is None:
+                        req.slot = self.ctx.anim_upload(desc, table)
+                    else:
+                        self.ctx.anim_init(req.slot, desc, table)
+                    self.anim_slots[req.slot] = 0
+                else:
+                    if req.slot is None:
+                        req.slot = self.ctx.upload(desc)
+                    else:
+                        self.ctx.update(req.slot, desc)
+                    self.anim_slots.pop(req.slot, None)
+                self.host_updates += 1
         if sc["pt"]:
             fp.pt_on, fp.pts_c, fp.seed, fp.frame_idx = req.spp, 0.0, 0x5E, req.rid
         req.fp = fp
@@ -175,6 +225,12 @@ class Server:
                 table.append(q)
             b = self.free_batches.popleft()
             b.set(table)
+            ups = [(r.slot, r.anim) for r in reqs if r.anim is not None]
+            if ups:
+                # the batch's scene updates: one launch ahead of the batch
+                self.ctx.anim_update_many(ups, self.stream.cuda_stream)
+                for r in reqs:
+                    r.anim = None
             b.launch(self.stream.cuda_stream)
             flags = np.frombuffer(b.done_flags(len(reqs)), dtype=np.uint32)
             self.inflight.append((b, reqs, flags))

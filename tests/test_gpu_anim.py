@@ -24,13 +24,19 @@ def _copy(qr, params):
     return qr.QrFrameParams.from_buffer_copy(params)
 
 
-def _device_scene(qr, ctx, kind, seed, nq, flags, w, h, fsaa, depth, bound=None):
+def _device_scene(qr, ctx, kind, seed, nq, flags, w, h, fsaa, depth, bound=None,
+                  fresh=False):
+    """fresh: a new scene prepared in one call (qr_scene_anim_upload), else a
+    resident scene prepared in place (qr_scene_anim_init)"""
     g = qr.GenScene(kind, seed, nq, flags)
     f = qr.Flat(g, w, h, fsaa)
     desc, params = f.update(0, depth)
     fp = _copy(qr, params)
-    sid = ctx.upload(desc)
-    ctx.anim_init(sid, desc, f.anim_table(), bound)
+    if fresh:
+        sid = ctx.anim_upload(desc, f.anim_table(), bound)
+    else:
+        sid = ctx.upload(desc)
+        ctx.anim_init(sid, desc, f.anim_table(), bound)
     return g, f, sid, fp
 
 
@@ -128,23 +134,27 @@ def test_device_update_matches_reference_frames(qr, ctx):
 
 
 def test_device_update_on_a_stream_and_in_a_batch(qr, ctx):
-    """updates enqueued on a caller's stream ahead of a batched launch of
-    several device-updated scenes: each frame equals its host-updated one"""
+    """the updates of several scenes in one launch on a caller's stream,
+    ahead of a batched render of them: each frame equals its host-updated
+    one"""
     import numpy as np
     import torch
     w, h, depth = 128, 72, 4
     s = torch.cuda.Stream()
     scenes = []
     for seed in (1, 2, 3):
-        g, f, sid, fp = _device_scene(qr, ctx, qr.SCN_ANIM, seed, 64, 0, w, h, 0, depth)
+        g, f, sid, fp = _device_scene(qr, ctx, qr.SCN_ANIM, seed, 64, 0, w, h, 0, depth,
+                                      fresh=True)
         scenes.append((g, f, sid, fp))
     b = qr.Batch(ctx, len(scenes))
+    with pytest.raises(RuntimeError):       # one scene twice in one launch
+        ctx.anim_update_many([(scenes[0][2], scenes[0][1].anim_params(16)[1])] * 2)
     for t in (48, 160):
-        outs, reqs = [], []
+        outs, reqs, ups = [], [], []
         for g, f, sid, fp in scenes:
             rc, p = f.anim_params(t)
             assert rc == 0
-            ctx.anim_update(sid, p, s.cuda_stream)
+            ups.append((sid, p))
             out = torch.empty((h, w), dtype=torch.int32, device="cuda")
             q = qr.QrRequest()
             q.scene_id = sid
@@ -153,6 +163,7 @@ def test_device_update_on_a_stream_and_in_a_batch(qr, ctx):
             q.dev_acc = None
             reqs.append(q)
             outs.append(out)
+        ctx.anim_update_many(ups, s.cuda_stream)     # one launch, a block a scene
         b.set(reqs)
         b.launch(s.cuda_stream)
         s.synchronize()

@@ -15,12 +15,13 @@ SCENES = [  # kind, seed, nq, flags, depth
 SIZES = [(64, 48), (96, 54), (128, 72)]
 
 
-def _server(qr, ctx, budget, max_batch):
+def _server(qr, ctx, budget, max_batch, device_anim=False):
     serve = importlib.import_module("quadray-engine_gb300.serve")
-    scenes = [dict(gen=qr.GenScene(k, s, n, f), pt=(k == 3), depth=d)
+    scenes = [dict(gen=qr.GenScene(k, s, n, f), pt=(k == 3), depth=d,
+                   anim=bool(f & qr.GEN_SPIN))
               for (k, s, n, f, d) in SCENES]
     return serve, serve.Server(qr, ctx, scenes, budget_bytes=budget, max_batch=max_batch,
-                               prep_threads=3)
+                               prep_threads=3, device_anim=device_anim)
 
 
 def _alone(qr, ctx, req):
@@ -50,12 +51,17 @@ def _requests(serve, n, seed):
     return out
 
 
-@pytest.mark.parametrize("budget,max_batch", [(120 << 30, 6), (3 << 20, 4)])
-def test_served_frames_equal_frames_alone(qr, budget, max_batch):
+@pytest.mark.parametrize("budget,max_batch,device_anim", [
+    (120 << 30, 6, False), (3 << 20, 4, False), (120 << 30, 6, True), (3 << 20, 4, True)])
+def test_served_frames_equal_frames_alone(qr, budget, max_batch, device_anim):
+    """device_anim: spinning scenes whose copies were prepared for it are
+    updated on the device (qr_scene_anim_update on the serving stream)"""
     ctx = qr.Context(0)
-    serve, srv = _server(qr, ctx, budget, max_batch)
+    serve, srv = _server(qr, ctx, budget, max_batch, device_anim)
     reqs = _requests(serve, 28, 7)
     done, wall = srv.run(reqs, keep_frames=True)
+    if device_anim:
+        assert srv.device_updates > 0
     assert len(done) == len(reqs)
     assert all(r.done >= r.arrival for r in done)
     for r in sorted(done, key=lambda r: r.rid):

@@ -208,3 +208,89 @@ def test_request_over_budget_is_refused():
     with pytest.raises(ValueError):
         srv.run([serve.Request(0, 0, 0, 1920, 1080, 1, 0.0)])
     srv.close()
+
+
+class FakeAnimFlat(FakeFlat):
+    """an animated scene: the table is taken after an update; the animators
+    keep their free rotation until time `lose`"""
+    lose = 10 ** 9
+
+    def __init__(self, gen, w, h, fsaa):
+        super().__init__(gen, w, h, fsaa)
+        self.updated = False
+        self.tables = 0
+
+    def update(self, time, depth):
+        self.updated = True
+        return super().update(time, depth)
+
+    def anim_table(self):
+        assert self.updated
+        self.tables += 1
+        return ["entry"]
+
+    def anim_params(self, time):
+        return (1 if time >= FakeAnimFlat.lose else 0), ["param"]
+
+    def frame_params(self):
+        return FakeParams()
+
+
+class FakeAnimCtx(FakeCtx):
+    def __init__(self):
+        super().__init__()
+        self.inits = self.anim_updates = 0
+
+    def anim_init(self, sid, desc, table):
+        self.inits += 1
+
+    def anim_upload(self, desc, table):
+        self.inits += 1
+        self.uploads += 1
+        return next(self.ids)
+
+    def anim_update_many(self, updates, stream):
+        assert len(set(sid for sid, _ in updates)) == len(updates)
+        self.anim_updates += len(updates)
+
+
+class FakeAnimQr(FakeQr):
+    Flat = FakeAnimFlat
+
+
+def test_animated_scenes_update_on_the_device():
+    """the first request of a scene copy runs the host update phases and
+    prepares the copy for device updates; later requests on that copy run
+    only the animators and one device update; when an animated transform
+    loses its free rotation the host phases run again with a new table"""
+    FakeBatch.order = lambda n: list(range(n))
+    scenes = [dict(gen="g0", pt=False, depth=4, anim=True)]
+    ctx = FakeAnimCtx()
+    srv = HostServer(FakeAnimQr, ctx, scenes, budget_bytes=1 << 30, max_batch=1,
+                     prep_threads=1, device_anim=True)
+    # arrivals 20 ms apart: each request finds the previous one's copy free
+    reqs = [serve.Request(i, 0, 16 * i, 32, 24, 1, 0.02 * i) for i in range(5)]
+    done, _ = srv.run(reqs)
+    assert sorted(r.rid for r in done) == list(range(5))
+    assert ctx.uploads == 1 and ctx.inits == 1 and ctx.updates == 0
+    assert ctx.anim_updates == 4 and srv.device_updates == 4 and srv.host_updates == 1
+    FakeAnimFlat.lose = 16 * 7
+    srv.run([serve.Request(10 + i, 0, 16 * (5 + i), 32, 24, 1, 0.02 * i) for i in range(4)])
+    # times 80, 96 on the device; 112 loses the rotation: host phases and a
+    # new table (which the fake accepts again), then 128 fails the same way
+    assert ctx.anim_updates == 6 and srv.host_updates == 3 and ctx.inits == 3
+    assert srv.flats[(0, 32, 24, 0)].tables == 3
+    FakeAnimFlat.lose = 10 ** 9
+    srv.close()
+
+
+def test_device_updated_copies_are_rebuilt_periodically():
+    FakeBatch.order = lambda n: list(range(n))
+    scenes = [dict(gen="g0", pt=False, depth=4, anim=True)]
+    ctx = FakeAnimCtx()
+    srv = HostServer(FakeAnimQr, ctx, scenes, budget_bytes=1 << 30, max_batch=1,
+                     prep_threads=1, device_anim=True, rebuild_every=3)
+    srv.run([serve.Request(i, 0, 16 * i, 32, 24, 1, 0.02 * i) for i in range(9)])
+    # host, 3 device, host, 3 device, host
+    assert srv.host_updates == 3 and srv.device_updates == 6 and ctx.inits == 3
+    srv.close()
