@@ -171,6 +171,7 @@ def lib():
         L.qrpy_scene_ctx.argtypes = [vp]
         L.qrpy_scene_free.argtypes = [vp]
         L.qrpy_scene_set_pton.argtypes = [vp, i32]
+        L.qrpy_scene_set_device_update.argtypes = [vp, i32]
         L.qr_ctx_create.argtypes = [i32, ctypes.POINTER(vp)]
         L.qr_ctx_destroy.argtypes = [vp]
         L.qr_last_error.restype = ctypes.c_char_p
@@ -510,6 +511,11 @@ class Engine:
     def update(self, time, action):
         """camera movement from user input (rt_Scene::update(time, action))"""
         lib().qrpy_scene_update(self.h, int(time), int(action))
+
+    def set_device_update(self, on):
+        """animated scenes updated on the device (default) or by the host
+        update phases and an upload each render"""
+        return lib().qrpy_scene_set_device_update(self.h, 1 if on else 0)
 
     def set_pton(self, pton):
         """Path-tracer samples per render (rt_Scene::set_pton); returns the

@@ -13,6 +13,7 @@
 #include <string.h>
 #include <new>
 
+#include <string>
 #include "engine.h"
 #include "flatten.h"
 
@@ -97,7 +98,8 @@ rt_Scene::rt_Scene(rt_SCENE *scn_, rt_si32 x_res_, rt_si32 y_res_,
     : pfm(pfm_), scn(scn_), x_res(x_res_), y_res(y_res_), x_row(x_row_),
       frame(frame_), own_frame(RT_NULL), opts(0), pt_on(0), pts_c(0), pt_frame(0),
       depth(10),
-      fl(RT_NULL), scene_id(-1), print(0), next(RT_NULL)
+      fl(RT_NULL), scene_id(-1), print(0), next(RT_NULL), dev_update(1), anim_state(0),
+      since_host(0)
 {
     if (scn == RT_NULL) throw rt_Exception("null-pointer in scene");
     if (scn->lock != RT_NULL)
@@ -149,24 +151,72 @@ rt_void rt_Scene::update(rt_time time, rt_si32 action)
     fl->camera_action(time, action);
 }
 
-rt_void rt_Scene::prepare(rt_time time)
+#define QR_ENGINE_REBUILD 32
+
+/* the scene at `time` on the device: the animators and one device update
+ * (on `stream`, NULL: the context's stream) when the scene allows it, else
+ * the host update phases and an upload */
+rt_void rt_Scene::prepare(rt_time time, rt_pntr stream)
 {
     if (fl->fsaa != pfm->fsaa)
     {
         fl->fsaa = pfm->fsaa;
     }
     fl->depth = depth;
+    qr_ctx *ctx = pfm->get_ctx();
+    int rc;
+    if (dev_update && anim_state == 1 && scene_id >= 0 && since_host < QR_ENGINE_REBUILD)
+    {
+        if (fl->anim_params(time, params) == 0)
+        {
+            rc = qr_scene_anim_update(ctx, scene_id, params.data(), (int)params.size(), stream);
+            if (rc != QR_OK)
+            {
+                fprintf(stderr, "qr scene update: %d %s\n", rc, qr_last_error(ctx));
+                throw rt_Exception("scene update on the GPU failed");
+            }
+            since_host++;
+            return;
+        }
+        anim_state = 0;     /* the table no longer fits: a new one below */
+    }
     fl->update(time);
     qr_scene_desc d;
     fl->desc(&d);
-    int rc = scene_id < 0 ? qr_scene_upload(pfm->get_ctx(), &d, &scene_id)
-                          : qr_scene_update(pfm->get_ctx(), scene_id, &d);
+    if (dev_update && anim_state == 0)
+    {
+        std::string why;
+        anim_state = (fl->anim_table(table, &why) == 0 && !table.empty()) ? 1 : -1;
+    }
+    if (dev_update && anim_state == 1)
+    {
+        fl->anim_params(time, params);      /* the transforms of this frame */
+        rc = scene_id < 0 ? qr_scene_anim_upload(ctx, &d, table.data(), (int)table.size(),
+                                                 RT_NULL, &scene_id)
+                          : qr_scene_anim_init(ctx, scene_id, &d, table.data(),
+                                               (int)table.size(), RT_NULL);
+        since_host = 0;
+    }
+    else
+    {
+        rc = scene_id < 0 ? qr_scene_upload(ctx, &d, &scene_id)
+                          : qr_scene_update(ctx, scene_id, &d);
+    }
     if (rc != QR_OK)
     {
-        fprintf(stderr, "qr scene upload: %d %s\n", rc, qr_last_error(pfm->get_ctx()));
+        fprintf(stderr, "qr scene upload: %d %s\n", rc, qr_last_error(ctx));
         throw rt_Exception("scene upload to the GPU failed");
     }
 }
+
+rt_si32 rt_Scene::set_device_update(rt_si32 on)
+{
+    dev_update = on ? 1 : 0;
+    since_host = QR_ENGINE_REBUILD;     /* the next render updates on the host */
+    return dev_update;
+}
+
+rt_si32 rt_Scene::get_device_update() { return dev_update; }
 
 /* frame parameters of this render; in path-tracer mode the samples
  * accumulate over frames until the scene changes (rt_Scene::render,
@@ -186,6 +236,11 @@ rt_void rt_Scene::frame_setup(qr_frame_params *fp)
     key.insert(key.end(), (const unsigned char *)fp,
                (const unsigned char *)fp + offsetof(qr_frame_params, x_res));
     key.push_back((unsigned char)fl->fsaa);
+    /* a device-updated frame differs from the last host update by the
+     * animated transforms */
+    if (anim_state == 1)
+        key.insert(key.end(), (const unsigned char *)params.data(),
+                   (const unsigned char *)(params.data() + params.size()));
     if (key != pt_key)
     {
         pts_c = 0;
@@ -200,7 +255,7 @@ rt_void rt_Scene::frame_setup(qr_frame_params *fp)
 
 rt_void rt_Scene::render(rt_time time)
 {
-    prepare(time);
+    prepare(time, RT_NULL);
     qr_frame_params fp;
     frame_setup(&fp);
     int rc = qr_render_host(pfm->get_ctx(), scene_id, &fp, frame);
@@ -213,7 +268,9 @@ rt_void rt_Scene::render(rt_time time)
 
 rt_void rt_Scene::render_device(rt_time time, rt_ui32 *dev_frame, rt_pntr stream)
 {
-    prepare(time);
+    prepare(time, stream);
+    /* the legacy default stream does not wait for the context's stream */
+    if (stream == RT_NULL) qr_sync(pfm->get_ctx(), RT_NULL);
     qr_frame_params fp;
     frame_setup(&fp);
     int rc = qr_render_device(pfm->get_ctx(), scene_id, &fp, dev_frame, stream);
@@ -236,6 +293,7 @@ rt_si32 rt_Scene::set_opts(rt_si32 o)
         qr_scene_release(pfm->get_ctx(), scene_id);
         scene_id = -1;
     }
+    anim_state = 0;
     return opts;
 }
 rt_si32 rt_Scene::get_pton() { return pt_on; }

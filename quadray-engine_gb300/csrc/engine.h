@@ -123,6 +123,11 @@ public:
     const qr::Flat *flat() const { return fl; }
     rt_si32     get_depth();
     rt_si32     set_depth(rt_si32 depth);
+    /* update animated scenes on the device (qr_scene_anim_*, on by
+     * default): each render runs only the animators on the host; the
+     * frames are those of the host update phases */
+    rt_si32     set_device_update(rt_si32 on);
+    rt_si32     get_device_update();
 
 private:
     rt_Platform *pfm;
@@ -140,8 +145,17 @@ private:
     int          scene_id;
     int          print;
     rt_Scene    *next;
+    /* device-side updates: 1 prepared, 0 to be tried at the next host
+     * update, -1 the scene does not allow them; host updates come back every
+     * QR_ENGINE_REBUILD device updates (the hierarchy's tree is the first
+     * frame's, refitted) */
+    int          dev_update;
+    int          anim_state;
+    int          since_host;
+    std::vector<qr_anim_node>  table;
+    std::vector<qr_anim_param> params;
 
-    rt_void     prepare(rt_time time);
+    rt_void     prepare(rt_time time, rt_pntr stream);
     rt_void     frame_setup(qr_frame_params *fp);
     friend class rt_Platform;
 };

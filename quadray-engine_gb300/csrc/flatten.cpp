@@ -678,6 +678,7 @@ void Flat::update_matrix(Node *n, float (*mtx)[4])
 void Flat::update_object(Node *n, rt_time time, int flags, Node *trnode,
                          float (*mtx)[4])
 {
+    n->in_flags = flags;
     update_status(n, time, flags, trnode);
     if (n->kind != K_ARRAY)
     {
@@ -1557,6 +1558,16 @@ int Flat::anim_params(rt_time time, std::vector<qr_anim_param> &out)
         }
         obj->time = time;
     }
+    /* cameras as update() leaves them: phase 0.5 status, phase 1 matrix,
+     * and the heading camera actions use */
+    for (size_t i = 0; i < cameras.size(); i++)
+    {
+        Node *c = cameras[i];
+        update_status(c, time, c->in_flags, c->parent != RT_NULL ? c->parent->trnode : RT_NULL);
+        if (c->obj_changed) update_matrix(c, c->pmtx);
+    }
+    hor_sin = sina_(cameras[cam_idx]->trm->rot[RT_Z]);
+    hor_cos = cosa_(cameras[cam_idx]->trm->rot[RT_Z]);
     out.resize(anim_nodes.size());
     int rc = 0;
     for (size_t i = 0; i < anim_nodes.size(); i++)

@@ -87,6 +87,7 @@ struct Node
     int          sgn[4];
     float        scl[4];
     int          obj_changed, obj_has_trm, mtx_has_trm;
+    int          in_flags;      /* update flags handed down by the parent */
     std::vector<Node*> children;
 
     /* surfaces */
@@ -113,7 +114,7 @@ struct Node
     qr_srf       rec;           /* backend record */
 
     Node() : kind(0), tag(0), obj(0), trm(0), parent(0), trnode(0), pmtx(0),
-             obj_changed(0), obj_has_trm(0), mtx_has_trm(0), srf(0),
+             obj_changed(0), obj_has_trm(0), mtx_has_trm(0), in_flags(0), srf(0),
              outer(-1), inner(-1), index(-1), gen(-1), pov(1.0f) {}
 };
 
@@ -146,9 +147,11 @@ public:
      * rotation (all angles multiples of 90 degrees) or a camera under one */
     int anim_table(std::vector<qr_anim_node> &out, std::string *why);
     /* run the animators for `time` (as update() does, without the update
-     * phases) and give each animated transform of the table; nonzero when
-     * one lost its free rotation (1) or changed its scale (2): the frame
-     * then needs update() and a new table */
+     * phases), refresh the cameras (their transforms after camera actions;
+     * no camera moves with an animated object) and give each animated
+     * transform of the table; nonzero when one lost its free rotation (1)
+     * or changed its scale (2): the frame then needs update() and a new
+     * table */
     int anim_params(rt_time time, std::vector<qr_anim_param> &out);
 
     int  opts;

@@ -262,6 +262,11 @@ void *qrpy_scene_ctx(void *h)
     return ((qrpy_engine *)h)->pfm->get_ctx();
 }
 
+int qrpy_scene_set_device_update(void *h, int on)
+{
+    return ((qrpy_engine *)h)->scn->set_device_update(on);
+}
+
 int qrpy_scene_set_pton(void *h, int pton)
 {
     return ((qrpy_engine *)h)->scn->set_pton(pton);

@@ -179,3 +179,27 @@ def test_device_update_on_a_stream_and_in_a_batch(qr, ctx):
     b.close()
     for g, f, sid, fp in scenes:
         ctx.release(sid)
+
+
+@pytest.mark.parametrize("kind,seed,nq,flags,fsaa", [(2, 7, 64, 0, 2), (1, 5, 32, 16, 0),
+                                                     (2, 8, 64, 8, 0)])
+def test_engine_renders_with_device_updates(qr, kind, seed, nq, flags, fsaa):
+    """rt_Scene::render with device updates (the default) against the host
+    update phases every frame: 40 frames (past a periodic host rebuild),
+    with camera actions and a camera switch between renders"""
+    a = qr.Engine(qr.GenScene(kind, seed, nq, flags), 160, 90, fsaa=fsaa, depth=4)
+    b = qr.Engine(qr.GenScene(kind, seed, nq, flags), 160, 90, fsaa=fsaa, depth=4)
+    b.set_device_update(False)
+    for k in range(40):
+        if k % 7 == 3:
+            act = (qr.CAMERA_MOVE_FORWARD, qr.CAMERA_ROTATE_LEFT, qr.CAMERA_MOVE_UP)[k % 3]
+            a.update(16 * k, act)
+            b.update(16 * k, act)
+        if k == 20:
+            a.next_cam()
+            b.next_cam()
+        fa = a.render(16 * k).copy()
+        fb = b.render(16 * k).copy()
+        assert (fa != fb).sum() == 0, k
+    a.close()
+    b.close()
