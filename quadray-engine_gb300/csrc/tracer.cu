@@ -1992,77 +1992,33 @@ __device__ int pt_advance(const qr_dscene &S, PtPend &p, float ret[3], Ray &r,
     return 0;
 }
 
-/* one path-tracer sample: the ray tree as one loop over traced segments.
- * Every node has at most three children (diffuse, transmitted, reflected),
- * so the tree holds at most (3^(depth+1) - 1) / 2 rays; a pixel that traces
- * more (or whose walk gives up) is recorded in the fault word and the
- * sample is black */
-__device__ void trace_pt(const qr_dscene &S, const qr_frame_params &P, Ray r,
-                         int x, int y, int seg_lim, Pcg &g, float col[3], StP st)
+/* the camera ray of a path-tracer sample: tent-jittered position in the
+ * pixel (two draws) */
+__device__ __forceinline__ void pt_camera_ray(const qr_frame_params &P, int x, int y,
+                                              Pcg &g, Ray &r, StP st)
 {
-    PtPend stk[QR_MAX_DEPTH + 1];
-    int sp = 0, off = S.cam_off, num = S.cam_num;
-    float ret[3];
-    int seg = 0;
-    #pragma unroll 1
-    for (;;)
-    {
-        if (++seg > seg_lim)
-        {
-            note_fault(S, QR_FAULT_TREE, x, y);
-            col[0] = col[1] = col[2] = 0.0f;
-            return;
-        }
-        Walk w;
-        w.fault = 0;
-        w.shadow = 0;
-        w.occluded = 0;
-        w.tbuf = r.t_max;
-        w.bestp = -1;
-        w.best.srf = -1;
-        walk(S, P, r, off, num, w, st);
-        if (w.fault)
-        {
-            note_fault(S, w.fault, x, y);
-            col[0] = col[1] = col[2] = 0.0f;
-            return;
-        }
-        if (w.best.srf < 0)
-        {
-            ret[0] = ret[1] = ret[2] = 0.0f;
-        }
-        else
-        {
-            CNT(QR_STAT_SHADE);
-            PtPend &p = stk[sp++];
-            float ddir[3];
-            const Hit hb = w.best;
-            if (pt_begin(S, P, r, hb, p, g, ddir, st))
-            {
-                const qr_srf *__restrict__ s = &S.srf[hb.srf];
-                CNT(QR_STAT_RAY_SECONDARY);
-                child_ray(r, hb.hit, ddir, hb.loc, hb.srf, hb.side, r.depth - 1);
-                off = __ldg(&s->sec_off[hb.side]);
-                num = __ldg(&s->sec_num[hb.side]);
-                continue;
-            }
-        }
-
-        int spawned = 0;
-        #pragma unroll 1
-        while (sp > 0)
-        {
-            if (pt_advance(S, stk[sp - 1], ret, r, off, num, st)) { spawned = 1; break; }
-            sp--;
-        }
-        if (!spawned) break;
-    }
-    #pragma unroll
-    for (int k = 0; k < 3; k++) col[k] = ret[k];
+    float hs = pt_tent(pcg_unit(g));
+    float vs = pt_tent(pcg_unit(g));
+    hs = (float)x + hs;
+    vs = (float)y + vs;
+    camera_ray(P, hs, vs, r);
+    CNT(QR_STAT_RAY_PRIMARY);
 }
 
-/* one pixel of a path-traced frame: pt_on samples added to the running
- * sums, the mean clamped and packed */
+/*
+ * One pixel of a path-traced frame: pt_on samples added to the running
+ * sums, the mean clamped and packed.
+ *
+ * Each sample's ray tree is walked as a loop over traced segments.  Every
+ * node has at most three children (diffuse, transmitted, reflected), so
+ * the tree holds at most (3^(depth+1) - 1) / 2 rays; a sample that traces
+ * more (or whose walk gives up) is recorded in the fault word and is black.
+ * The samples follow one another inside the same loop: a lane whose sample
+ * tree ends starts its next sample at once instead of waiting for the
+ * largest tree of its warp, so the lanes of a warp stay in the walk
+ * together; each pixel draws its stream and sums its samples in the same
+ * order as one sample after the other.
+ */
 __device__ __forceinline__ void pt_pixel(const qr_dscene &S, const qr_frame_params &P,
                                          int x, int y, float *acc, uint32_t *frame, StP st)
 {
@@ -2075,21 +2031,82 @@ __device__ __forceinline__ void pt_pixel(const qr_dscene &S, const qr_frame_para
     for (int d = 0; d <= P.depth; d++) seg_lim *= 3;
     seg_lim = (seg_lim - 1) / 2;
     float sum[3] = {0.0f, 0.0f, 0.0f};
+
+    PtPend stk[QR_MAX_DEPTH + 1];
+    int n = 0, sp = 0, seg = 0, off = S.cam_off, num = S.cam_num;
+    float ret[3];
+    Ray r;
+    if (spp > 0) pt_camera_ray(P, x, y, g, r, st);
     #pragma unroll 1
-    for (int n = 0; n < spp; n++)
+    while (n < spp)
     {
-        /* tent-jittered position in the pixel (two draws) */
-        float hs = pt_tent(pcg_unit(g));
-        float vs = pt_tent(pcg_unit(g));
-        hs = (float)x + hs;
-        vs = (float)y + vs;
-        Ray r;
-        camera_ray(P, hs, vs, r);
-        CNT(QR_STAT_RAY_PRIMARY);
-        float col[3];
-        trace_pt(S, P, r, x, y, seg_lim, g, col, st);
-        #pragma unroll
-        for (int k = 0; k < 3; k++) sum[k] = sum[k] + col[k];
+        int done = 0;
+        if (++seg > seg_lim)
+        {
+            note_fault(S, QR_FAULT_TREE, x, y);
+            ret[0] = ret[1] = ret[2] = 0.0f;
+            done = 1;
+        }
+        else
+        {
+            Walk w;
+            w.fault = 0;
+            w.shadow = 0;
+            w.occluded = 0;
+            w.tbuf = r.t_max;
+            w.bestp = -1;
+            w.best.srf = -1;
+            walk(S, P, r, off, num, w, st);
+            if (w.fault)
+            {
+                note_fault(S, w.fault, x, y);
+                ret[0] = ret[1] = ret[2] = 0.0f;
+                done = 1;
+            }
+            else
+            {
+                int spawned = 0;
+                if (w.best.srf < 0)
+                {
+                    ret[0] = ret[1] = ret[2] = 0.0f;
+                }
+                else
+                {
+                    CNT(QR_STAT_SHADE);
+                    PtPend &p = stk[sp++];
+                    float ddir[3];
+                    const Hit hb = w.best;
+                    if (pt_begin(S, P, r, hb, p, g, ddir, st))
+                    {
+                        const qr_srf *__restrict__ s = &S.srf[hb.srf];
+                        CNT(QR_STAT_RAY_SECONDARY);
+                        child_ray(r, hb.hit, ddir, hb.loc, hb.srf, hb.side, r.depth - 1);
+                        off = __ldg(&s->sec_off[hb.side]);
+                        num = __ldg(&s->sec_num[hb.side]);
+                        spawned = 1;
+                    }
+                }
+                #pragma unroll 1
+                while (!spawned && sp > 0)
+                {
+                    if (pt_advance(S, stk[sp - 1], ret, r, off, num, st)) spawned = 1;
+                    else sp--;
+                }
+                done = !spawned;
+            }
+        }
+        if (done)
+        {
+            /* the sample's colour; the next sample starts in this lane */
+            #pragma unroll
+            for (int k = 0; k < 3; k++) sum[k] = sum[k] + ret[k];
+            n++;
+            sp = 0;
+            seg = 0;
+            off = S.cam_off;
+            num = S.cam_num;
+            if (n < spp) pt_camera_ray(P, x, y, g, r, st);
+        }
     }
     float *a = acc + 3 * ((size_t)y * P.x_row + x);
     float mean[3];
