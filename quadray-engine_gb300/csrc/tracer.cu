@@ -1541,6 +1541,9 @@ __device__ __forceinline__ int tile_y()
 #endif
 /* the path tracer's own bound: 6 (80 registers) 66.5 ms, 8 (64) 67.9 ms
  * on the 1280x720 16-spp frame with 64-byte pending-node records */
+/* samples per launch from which the path tracer runs its samples inside one
+ * segment loop (pt_pixel_flat) */
+#define QR_PT_FLAT_SPP 32
 #ifndef QR_PT_MIN_BLOCKS
 #define QR_PT_MIN_BLOCKS 6
 #endif
@@ -2005,9 +2008,113 @@ __device__ __forceinline__ void pt_camera_ray(const qr_frame_params &P, int x, i
     CNT(QR_STAT_RAY_PRIMARY);
 }
 
+/* one path-tracer sample: the ray tree as one loop over traced segments.
+ * Every node has at most three children (diffuse, transmitted, reflected),
+ * so the tree holds at most (3^(depth+1) - 1) / 2 rays; a pixel that traces
+ * more (or whose walk gives up) is recorded in the fault word and the
+ * sample is black */
+__device__ void trace_pt(const qr_dscene &S, const qr_frame_params &P, Ray r,
+                         int x, int y, int seg_lim, Pcg &g, float col[3], StP st)
+{
+    PtPend stk[QR_MAX_DEPTH + 1];
+    int sp = 0, off = S.cam_off, num = S.cam_num;
+    float ret[3];
+    int seg = 0;
+    #pragma unroll 1
+    for (;;)
+    {
+        if (++seg > seg_lim)
+        {
+            note_fault(S, QR_FAULT_TREE, x, y);
+            col[0] = col[1] = col[2] = 0.0f;
+            return;
+        }
+        Walk w;
+        w.fault = 0;
+        w.shadow = 0;
+        w.occluded = 0;
+        w.tbuf = r.t_max;
+        w.bestp = -1;
+        w.best.srf = -1;
+        walk(S, P, r, off, num, w, st);
+        if (w.fault)
+        {
+            note_fault(S, w.fault, x, y);
+            col[0] = col[1] = col[2] = 0.0f;
+            return;
+        }
+        if (w.best.srf < 0)
+        {
+            ret[0] = ret[1] = ret[2] = 0.0f;
+        }
+        else
+        {
+            CNT(QR_STAT_SHADE);
+            PtPend &p = stk[sp++];
+            float ddir[3];
+            const Hit hb = w.best;
+            if (pt_begin(S, P, r, hb, p, g, ddir, st))
+            {
+                const qr_srf *__restrict__ s = &S.srf[hb.srf];
+                CNT(QR_STAT_RAY_SECONDARY);
+                child_ray(r, hb.hit, ddir, hb.loc, hb.srf, hb.side, r.depth - 1);
+                off = __ldg(&s->sec_off[hb.side]);
+                num = __ldg(&s->sec_num[hb.side]);
+                continue;
+            }
+        }
+
+        int spawned = 0;
+        #pragma unroll 1
+        while (sp > 0)
+        {
+            if (pt_advance(S, stk[sp - 1], ret, r, off, num, st)) { spawned = 1; break; }
+            sp--;
+        }
+        if (!spawned) break;
+    }
+    #pragma unroll
+    for (int k = 0; k < 3; k++) col[k] = ret[k];
+}
+
+/* one pixel of a path-traced frame, one sample after the other: pt_on
+ * samples added to the running sums, the mean clamped and packed */
+__device__ __forceinline__ void pt_pixel_seq(const qr_dscene &S, const qr_frame_params &P,
+                                         int x, int y, float *acc, uint32_t *frame, StP st)
+{
+    Pcg g;
+    pcg_seed(g, P.seed, P.frame_idx, (unsigned long long)y * P.x_res + x);
+    const int spp = P.pt_on;
+    const int n0 = (int)P.pts_c;
+    int seg_lim = 1;
+    #pragma unroll 1
+    for (int d = 0; d <= P.depth; d++) seg_lim *= 3;
+    seg_lim = (seg_lim - 1) / 2;
+    float sum[3] = {0.0f, 0.0f, 0.0f};
+    #pragma unroll 1
+    for (int n = 0; n < spp; n++)
+    {
+        Ray r;
+        pt_camera_ray(P, x, y, g, r, st);
+        float col[3];
+        trace_pt(S, P, r, x, y, seg_lim, g, col, st);
+        #pragma unroll
+        for (int k = 0; k < 3; k++) sum[k] = sum[k] + col[k];
+    }
+    float *a = acc + 3 * ((size_t)y * P.x_row + x);
+    float mean[3];
+    #pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        a[k] = (n0 == 0 ? 0.0f : a[k]) + sum[k];
+        mean[k] = fdiv(a[k], (float)(n0 + spp));
+        mean[k] = clamp1(mean[k]);
+    }
+    frame[(size_t)y * P.x_row + x] = pack(P, mean);
+}
+
 /*
- * One pixel of a path-traced frame: pt_on samples added to the running
- * sums, the mean clamped and packed.
+ * The same with the samples inside one loop over traced segments.
  *
  * Each sample's ray tree is walked as a loop over traced segments.  Every
  * node has at most three children (diffuse, transmitted, reflected), so
@@ -2017,9 +2124,12 @@ __device__ __forceinline__ void pt_camera_ray(const qr_frame_params &P, int x, i
  * tree ends starts its next sample at once instead of waiting for the
  * largest tree of its warp, so the lanes of a warp stay in the walk
  * together; each pixel draws its stream and sums its samples in the same
- * order as one sample after the other.
+ * order as one sample after the other, so the frame is the same.  It pays
+ * from about 32 samples a launch on (fewer samples leave too short a run to
+ * even out, and the longer loop costs instructions): qr_launch_pt picks it
+ * from QR_PT_FLAT_SPP samples on.
  */
-__device__ __forceinline__ void pt_pixel(const qr_dscene &S, const qr_frame_params &P,
+__device__ __forceinline__ void pt_pixel_flat(const qr_dscene &S, const qr_frame_params &P,
                                          int x, int y, float *acc, uint32_t *frame, StP st)
 {
     Pcg g;
@@ -2120,6 +2230,7 @@ __device__ __forceinline__ void pt_pixel(const qr_dscene &S, const qr_frame_para
     frame[(size_t)y * P.x_row + x] = pack(P, mean);
 }
 
+template <int FLAT>
 __global__ void __launch_bounds__(128, QR_PT_MIN_BLOCKS)
 pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *frame,
           qr_dstats *gst)
@@ -2135,7 +2246,8 @@ pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *fram
     StP st = NULL;
     (void)gst;
 #endif
-    pt_pixel(S, P, x, y, acc, frame, st);
+    if (FLAT) pt_pixel_flat(S, P, x, y, acc, frame, st);
+    else pt_pixel_seq(S, P, x, y, acc, frame, st);
 #ifdef QR_STATS
     const unsigned am = __activemask();
     const int leader = __ffs(am) - 1;
@@ -2254,7 +2366,7 @@ batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter
             }
             else if (inside)
             {
-                pt_pixel(sS[wid], sP[wid], x, y, J->acc, J->frame, NULL);
+                pt_pixel_seq(sS[wid], sP[wid], x, y, J->acc, J->frame, NULL);
             }
             /* the tile's pixels are written (the warp barrier orders the
              * lanes' stores before lane 0's fence): count the tile; the
@@ -2318,10 +2430,14 @@ cudaError_t qr_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *
     const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
                     (fp.y_res + 2 * QR_TILE_H - 1) / (2 * QR_TILE_H));
 #ifdef QR_STATS
-    QR_NS::pt_kernel<<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, dstats);
+    qr_dstats *ds = dstats;
 #else
-    QR_NS::pt_kernel<<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, NULL);
+    qr_dstats *ds = NULL;
 #endif
+    if (fp.pt_on >= QR_PT_FLAT_SPP)
+        QR_NS::pt_kernel<1><<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, ds);
+    else
+        QR_NS::pt_kernel<0><<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, ds);
     return cudaGetLastError();
 }
 

@@ -67,14 +67,16 @@ def gpu_means(qr, ctx, sid, params):
     return acc.cpu().numpy()[:, :params.x_res] / params.pt_on
 
 
-@pytest.mark.parametrize("seed", [1, 3])
-def test_pt_bit_exact_vs_float_oracle(qr, oracle, ctx, seed):
+@pytest.mark.parametrize("seed,spp", [(1, 8), (3, 8), (2, 40)])
+def test_pt_bit_exact_vs_float_oracle(qr, oracle, ctx, seed, spp):
+    """spp 40: the launch runs its samples inside one segment loop
+    (from 32 samples on), the same frame as one sample after the other"""
     g, f, desc, params = pt_scene(qr, seed, 96, 54)
     sid = ctx.upload(desc)
     acc = np.zeros((params.y_res, params.x_row, 3), dtype=np.float32)
     for launch in range(2):
         p = qr.QrFrameParams.from_buffer_copy(params)
-        p.pt_on, p.pts_c, p.seed, p.frame_idx = 8, 8.0 * launch, 4242, launch
+        p.pt_on, p.pts_c, p.seed, p.frame_idx = spp, float(spp * launch), 4242, launch
         gpu = ctx.render_host(sid, p)
         ref = np.zeros((p.y_res, p.x_row), dtype=np.uint32)
         oracle_pt(oracle, desc, p, acc, ref)
