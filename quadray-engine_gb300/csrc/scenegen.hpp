@@ -78,6 +78,8 @@
 #define QR_GEN_NOFRESNEL (1 << 9)  /* QR_SCN_ANIM: keep the default, Fresnel off */
 #define QR_GEN_TEXFILE  (1 << 10)  /* with QR_GEN_TEX: textures named as BMP files */
 #define QR_GEN_CAMERAS  (1 << 11)  /* QR_SCN_PLAIN: a second camera */
+#define QR_GEN_RISE     (1 << 12)  /* QR_SCN_PLAIN: the quadrics turn and rise
+                                      (anim_rise: their transforms move) */
 
 namespace qr_gen
 {
@@ -171,6 +173,26 @@ static void anim_spin(rt_time time, rt_time last_time, rt_TRANSFORM3D *trm,
     uint64_t h = pos_hash(trm);
     for (int k = 0; k < 3; k++)
         trm->rot[k] = spin_angle(h, k, time);
+}
+
+/*
+ * Animator of QR_GEN_RISE: the object turns about its three axes at rates
+ * that depend on the time alone (so they never stop at a multiple of 90
+ * degrees at a frame time), and rises by 2 units a second of animation time
+ * since the last call, a move relative to its previous position.
+ */
+static void anim_rise(rt_time time, rt_time last_time, rt_TRANSFORM3D *trm,
+                      rt_pntr pobj)
+{
+    (void)pobj;
+    const float t = (float)time;
+    trm->rot[RT_X] = 17.0f + 0.0371f * t;
+    trm->rot[RT_Y] = -23.0f + 0.0293f * t;
+    trm->rot[RT_Z] = 41.0f + 0.0137f * t;
+    while (trm->rot[RT_X] > 180.0f) trm->rot[RT_X] -= 360.0f;
+    while (trm->rot[RT_Y] > 180.0f) trm->rot[RT_Y] -= 360.0f;
+    while (trm->rot[RT_Z] > 180.0f) trm->rot[RT_Z] -= 360.0f;
+    trm->pos[RT_Z] += 0.002f * (float)(time - last_time);
 }
 
 /*
@@ -570,6 +592,7 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
         float rx = r.uf(-180, 180), ry = r.uf(-180, 180), rz = r.uf(-180, 180);
         Scene::trm_set(&q.trm, 1, 1, 1, rx, ry, rz, px, py, pz);
         if (sc.flags & QR_GEN_SPIN) q.f_anim = anim_spin;
+        if (sc.flags & QR_GEN_RISE) q.f_anim = anim_rise;
         root.push_back(q);
     }
     if (sc.flags & QR_GEN_SHAPES)

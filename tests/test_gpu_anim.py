@@ -107,6 +107,36 @@ def test_device_update_outside_bound_stays_exact(qr, ctx):
     ctx.release(hid)
 
 
+def test_moving_transforms_leave_the_bound_and_stay_exact(qr, ctx):
+    """quadrics that rise (their animators move the transforms): positions
+    come from the animators' parameters, and once the risen surfaces leave
+    the default bound (rotations about fixed origins) the updates open the
+    hierarchy, count the misses, and the frames still equal the host's"""
+    w, h, depth = 160, 96, 4
+    g, f, sid, fp = _device_scene(qr, ctx, qr.SCN_PLAIN, 11, 24, qr.GEN_RISE, w, h, 0, depth)
+    g2 = qr.GenScene(qr.SCN_PLAIN, 11, 24, qr.GEN_RISE)
+    f2 = qr.Flat(g2, w, h, 0)
+    f2.update(0, depth)
+    hid = None
+    times = [16, 160, 1600, 4000, 8000]
+    for t in times:
+        rc, p = f.anim_params(t)
+        assert rc == 0
+        ctx.anim_update(sid, p)
+        dev = ctx.render_host(sid, fp).copy()
+        desc2, params2 = f2.update(t, depth)
+        if hid is None:
+            hid = ctx.upload(desc2)
+        else:
+            ctx.update(hid, desc2)
+        host = ctx.render_host(hid, params2)
+        assert (dev != host).sum() == 0, t
+    frames, missed = ctx.anim_status(sid)
+    assert frames == len(times) and 1 <= missed < len(times)
+    ctx.release(sid)
+    ctx.release(hid)
+
+
 def test_device_update_matches_reference_frames(qr, ctx):
     """the reference's own frames of the animated golden fixtures (no
     camera actions), every frame after the first updated on the device"""

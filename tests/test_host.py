@@ -212,6 +212,7 @@ def test_bmp_textures_load_like_the_reference(qr, tmp_path, monkeypatch):
     (2, 2, 64, 8, -1),          # array-level transform nodes (TARRAY)
     (2, 5, 64, 0, (1 << 20) | (1 << 21) | (1 << 25)),   # the reference's NONE opts
     (1, 3, 32, 16, -1),         # spinning quadrics, no hierarchy of arrays
+    (1, 11, 24, 1 << 12, -1),   # quadrics that turn and rise: moving transforms
 ])
 def test_device_update_table_reproduces_host_update(qr, kind, seed, nq, flags, opts):
     """the device update table taken at one frame, with the animators'
