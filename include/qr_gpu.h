@@ -253,7 +253,12 @@ typedef struct qr_anim_param
     float   pad[3];
 } qr_anim_param;
 
-/* Upload `desc` into scene `scene_id` in place (as qr_scene_update) with
+/* The update calls may come from several host threads: a preparation waits
+ * for the scene's updates still in flight, and no update starts while a
+ * scene is prepared.  As with qr_scene_update, renders of a scene must not
+ * overlap its updates: order them on one stream.
+ *
+ * Upload `desc` into scene `scene_id` in place (as qr_scene_update) with
  * the hierarchy sized for the motion bound (lo[3], hi[3]; NULL: where
  * rotations of the animated transforms about their origins can take the
  * moving records and surfaces, joined with the scene's extent) and prepare the

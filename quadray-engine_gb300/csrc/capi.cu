@@ -344,6 +344,8 @@ static int check_anim_table(const qr_scene_desc *d, const qr_anim_node *nodes, i
         if (N.kind < QR_ANIM_OWN || N.kind > QR_ANIM_NODE) return QR_ERR_ARG;
         if (N.kind == QR_ANIM_OWN ? N.parent != -1 : (N.parent < 0 || N.parent >= i))
             return QR_ERR_ARG;
+        /* only records are transform nodes */
+        if (N.parent >= 0 && nodes[N.parent].rec < 0) return QR_ERR_ARG;
         if (N.param < -1 || (N.kind == QR_ANIM_NODE && N.param != -1)) return QR_ERR_ARG;
         if (N.rec < -1 || N.rec >= d->nsrf || N.light < -1 || N.light >= d->nlgt)
             return QR_ERR_ARG;
@@ -551,6 +553,16 @@ static int anim_prepare(qr_ctx *ctx, qr_scene_slot *sl, const qr_scene_desc *des
         rotation_bound(desc, nodes, n, b);
     }
 
+    /* updates of this scene still in flight write its block: they finish
+     * before the block is replaced, and no update starts meanwhile */
+    std::lock_guard<std::mutex> lock(ctx->amu);
+    if (sl->anim != NULL)
+    {
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < QR_ANIM_RING && e == cudaSuccess; k++)
+            e = cudaEventSynchronize(sl->anim->ev[k]);
+        if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim wait", e);
+    }
     qr_accel_host acc;
     rc = upload(ctx, *sl, desc, false, b, &acc);
     if (rc != QR_OK) return rc;
@@ -658,9 +670,6 @@ static int anim_prepare(qr_ctx *ctx, qr_scene_slot *sl, const qr_scene_desc *des
     }
     a->ok = 0;
     cudaError_t e = cudaSuccess;
-    /* earlier updates may still read the old block and ring */
-    for (int k = 0; k < QR_ANIM_RING && e == cudaSuccess; k++) e = cudaEventSynchronize(a->ev[k]);
-    if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "anim wait", e);
     if (a->bytes < total)
     {
         if (a->block) cudaFree(a->block);
@@ -731,6 +740,7 @@ extern "C" int qr_scene_anim_update_many(qr_ctx *ctx, const qr_anim_request *req
 {
     if (ctx == NULL || n < 0 || (n > 0 && reqs == NULL)) return QR_ERR_ARG;
     if (n == 0) return QR_OK;
+    std::lock_guard<std::mutex> lock(ctx->amu);
     std::vector<qr_scene_slot *> sls(n);
     for (int i = 0; i < n; i++)
     {
@@ -748,7 +758,6 @@ extern "C" int qr_scene_anim_update_many(qr_ctx *ctx, const qr_anim_request *req
         std::sort(u.begin(), u.end());
         if (std::adjacent_find(u.begin(), u.end()) != u.end()) return QR_ERR_ARG;
     }
-    std::lock_guard<std::mutex> lock(ctx->amu);
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "cudaSetDevice", e);
     for (int k = 0; k < QR_ANIM_RING && e == cudaSuccess; k++)

@@ -233,3 +233,38 @@ def test_engine_renders_with_device_updates(qr, kind, seed, nq, flags, fsaa):
         assert (fa != fb).sum() == 0, k
     a.close()
     b.close()
+
+
+def test_malformed_tables_and_updates_are_refused(qr, ctx):
+    """the table's indices are checked before anything is uploaded: parents
+    earlier and carrying a record, records and lights in range and named
+    once; an update gives exactly the table's animated transforms"""
+    g = qr.GenScene(qr.SCN_ANIM, 2, 64, 0)
+    f = qr.Flat(g, 64, 36, 0)
+    desc, params = f.update(0, 4)
+    table = f.anim_table()
+    sid = ctx.upload(desc)
+    n = len(table)
+    under = next(i for i, e in enumerate(table) if e.parent >= 0)
+
+    def refused(mutate):
+        bad = (qr.QrAnimNode * n)()
+        ctypes.memmove(bad, table, ctypes.sizeof(bad))
+        mutate(bad)
+        with pytest.raises(RuntimeError):
+            ctx.anim_init(sid, desc, bad)
+
+    refused(lambda t: setattr(t[under], "parent", under))            # not earlier
+    refused(lambda t: setattr(t[table[under].parent], "rec", -1))    # parent without record
+    refused(lambda t: setattr(t[1], "rec", t[0].rec))                # record named twice
+    refused(lambda t: setattr(t[0], "rec", desc.nsrf))               # out of range
+    refused(lambda t: setattr(t[0], "kind", 7))                      # unknown recipe
+    with pytest.raises(RuntimeError):
+        ctx.anim_init(sid, desc, table, bound=[1, 0, 0, 0, 0, 0])     # lo above hi
+    ctx.anim_init(sid, desc, table)
+    rc, p = f.anim_params(16)
+    with pytest.raises(RuntimeError):
+        ctx.anim_update(sid, (qr.QrAnimParam * (len(p) - 1))())       # too few transforms
+    ctx.anim_update(sid, p)
+    assert ctx.anim_status(sid) == (1, 0)
+    ctx.release(sid)
