@@ -165,11 +165,17 @@ rt_void rt_Scene::prepare(rt_time time, rt_pntr stream)
     fl->depth = depth;
     qr_ctx *ctx = pfm->get_ctx();
     int rc;
-    if (dev_update && anim_state == 1 && scene_id >= 0 && since_host < QR_ENGINE_REBUILD)
+    /* a scene without animated objects (an empty table) changes only by
+     * its cameras, which anim_params refreshes: its records stay as
+     * uploaded and need no rebuild */
+    if (dev_update && anim_state == 1 && scene_id >= 0 &&
+        (table.empty() || since_host < QR_ENGINE_REBUILD))
     {
         if (fl->anim_params(time, params) == 0)
         {
-            rc = qr_scene_anim_update(ctx, scene_id, params.data(), (int)params.size(), stream);
+            rc = table.empty() ? QR_OK
+                               : qr_scene_anim_update(ctx, scene_id, params.data(),
+                                                      (int)params.size(), stream);
             if (rc != QR_OK)
             {
                 fprintf(stderr, "qr scene update: %d %s\n", rc, qr_last_error(ctx));
@@ -186,9 +192,10 @@ rt_void rt_Scene::prepare(rt_time time, rt_pntr stream)
     if (dev_update && anim_state == 0)
     {
         std::string why;
-        anim_state = (fl->anim_table(table, &why) == 0 && !table.empty()) ? 1 : -1;
+        anim_state = fl->anim_table(table, &why) == 0 ? 1 : -1;
+        if (table.empty()) params.clear();
     }
-    if (dev_update && anim_state == 1)
+    if (dev_update && anim_state == 1 && !table.empty())
     {
         fl->anim_params(time, params);      /* the transforms of this frame */
         rc = scene_id < 0 ? qr_scene_anim_upload(ctx, &d, table.data(), (int)table.size(),

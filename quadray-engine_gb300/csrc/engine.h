@@ -124,8 +124,9 @@ public:
     rt_si32     get_depth();
     rt_si32     set_depth(rt_si32 depth);
     /* update animated scenes on the device (qr_scene_anim_*, on by
-     * default): each render runs only the animators on the host; the
-     * frames are those of the host update phases */
+     * default): each render runs only the animators on the host, and a
+     * scene without animated objects is uploaded once; the frames are those
+     * of the host update phases */
     rt_si32     set_device_update(rt_si32 on);
     rt_si32     get_device_update();
 

@@ -212,11 +212,14 @@ def test_device_update_on_a_stream_and_in_a_batch(qr, ctx):
 
 
 @pytest.mark.parametrize("kind,seed,nq,flags,fsaa", [(2, 7, 64, 0, 2), (1, 5, 32, 16, 0),
-                                                     (2, 8, 64, 8, 0)])
+                                                     (2, 8, 64, 8, 0), (1, 9, 24, 0, 0),
+                                                     (1, 13, 24, 1 << 12, 0)])
 def test_engine_renders_with_device_updates(qr, kind, seed, nq, flags, fsaa):
     """rt_Scene::render with device updates (the default) against the host
     update phases every frame: 40 frames (past a periodic host rebuild),
-    with camera actions and a camera switch between renders"""
+    with camera actions and a camera switch between renders; a static scene
+    (uploaded once, only its camera refreshed) and one whose transforms move
+    too"""
     a = qr.Engine(qr.GenScene(kind, seed, nq, flags), 160, 90, fsaa=fsaa, depth=4)
     b = qr.Engine(qr.GenScene(kind, seed, nq, flags), 160, 90, fsaa=fsaa, depth=4)
     b.set_device_update(False)
