@@ -155,6 +155,11 @@ def lib():
                                             ctypes.POINTER(ctypes.c_int)]
         L.qrpy_anim_check.argtypes = [vp, ctypes.POINTER(QrAnimNode), i32,
                                       ctypes.POINTER(QrAnimParam)]
+        L.qrpy_rotation_bound.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(QrAnimNode),
+                                          i32, ctypes.POINTER(ctypes.c_float)]
+        L.qrpy_rotation_bound.restype = None
+        L.qrpy_extent.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(ctypes.c_double)]
+        L.qrpy_extent.restype = None
         L.qr_scene_anim_init.argtypes = [vp, i32, ctypes.POINTER(QrSceneDesc),
                                          ctypes.POINTER(QrAnimNode), i32,
                                          ctypes.POINTER(ctypes.c_float)]

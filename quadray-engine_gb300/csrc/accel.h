@@ -129,6 +129,12 @@ int qr_accel_anim_terms(const qr_scene_desc *d, const qr_accel_host *acc,
                         std::vector<qr_anim_term> &terms,
                         std::vector<qr_anim_target> &targets);
 
+/* where rotations of the table's animated transforms about their origins
+ * can take the moving records and surfaces, joined with the scene's extent
+ * (lo[3], hi[3]): the default motion bound of qr_scene_anim_init */
+void qr_accel_rotation_bound(const qr_scene_desc *d, const qr_anim_node *nodes, int n,
+                             float out[6]);
+
 /* deepest traversal stack the tracer supports */
 #define QR_BVH_STACK 48
 

@@ -365,139 +365,6 @@ static int check_anim_table(const qr_scene_desc *d, const qr_anim_node *nodes, i
     return QR_OK;
 }
 
-/* largest singular value of a 3x3 matrix (power iteration on A^T A) */
-static double sigma_max(const double a[3][3])
-{
-    double g[3][3];
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++)
-            g[i][j] = a[0][i] * a[0][j] + a[1][i] * a[1][j] + a[2][i] * a[2][j];
-    double v[3] = {1.0, 0.7, 0.4}, lam = 0.0;
-    for (int it = 0; it < 64; it++)
-    {
-        double w[3];
-        for (int i = 0; i < 3; i++) w[i] = g[i][0] * v[0] + g[i][1] * v[1] + g[i][2] * v[2];
-        const double n = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-        if (!(n > 0.0)) return 0.0;
-        for (int i = 0; i < 3; i++) v[i] = w[i] / n;
-        lam = n;
-    }
-    /* a little above the estimate: power iteration approaches from below */
-    return sqrt(lam) * (1.0 + 1e-6) + 1e-12;
-}
-
-/*
- * The default motion bound: where moving records and surfaces can be if the
- * animators rotate and never move their transforms' origins.  Along the
- * table (parents first) every entry's origin stays in a ball (c, r) and its
- * linear part has a singular value bound s: an entry of its own keeps its
- * origin, s = |M|; under a parent T the origin is T's origin plus T's linear
- * part applied to a fixed offset, r = r_T + s_T |offset|, s = s_T |P|.  A
- * moving surface stays within its frame's ball widened by s_F times the
- * largest corner of its local box.  The bound holds these balls and the
- * scene's extent; an update that leaves it anyway (an animator that
- * translates) is caught by the update's own check.
- */
-static void rotation_bound(const qr_scene_desc *d, const qr_anim_node *nodes, int n,
-                           float out[6])
-{
-    double ext[6];
-    qr_accel_extent(d, ext);
-    double lo[3] = {ext[0], ext[1], ext[2]}, hi[3] = {ext[3], ext[4], ext[5]};
-    std::vector<double> c(3 * (size_t)n), r(n), sg(n);
-    std::vector<int> of_rec(d->nsrf, -1);
-    auto grow = [&](const double *cc, double rr) {
-        for (int k = 0; k < 3; k++)
-        {
-            lo[k] = std::min(lo[k], cc[k] - rr);
-            hi[k] = std::max(hi[k], cc[k] + rr);
-        }
-    };
-    for (int e = 0; e < n; e++)
-    {
-        const qr_anim_node &N = nodes[e];
-        double P[3][3];
-        for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) P[i][j] = N.p[4 * j + i];   /* column-major */
-        double o[3] = {0.0, 0.0, 0.0};
-        double M[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-        if (N.rec >= 0)
-        {
-            const qr_srf &s = d->srf[N.rec];
-            float f[9];
-            if (qr_accel_record_frame(s, f))
-                for (int i = 0; i < 3; i++)
-                    for (int j = 0; j < 3; j++) M[i][j] = f[3 * i + j];
-            for (int k = 0; k < 3; k++) o[k] = s.pos[k];
-            of_rec[N.rec] = e;
-        }
-        else if (N.light >= 0)
-        {
-            for (int k = 0; k < 3; k++) o[k] = d->lgt[N.light].pos[k];
-        }
-        if (N.kind == QR_ANIM_OWN)
-        {
-            for (int k = 0; k < 3; k++) c[3 * e + k] = o[k];
-            r[e] = 0.0;
-            sg[e] = sigma_max(M);
-        }
-        else
-        {
-            const int t = N.parent;
-            const qr_srf &T = d->srf[nodes[t].rec >= 0 ? nodes[t].rec : 0];
-            /* the offset in T's frame: T's transform rows applied to the
-             * origins' difference */
-            double q = 0.0;
-            const float *row[3] = {T.tci, T.tcj, T.tck};
-            for (int i = 0; i < 3; i++)
-            {
-                double v = 0.0;
-                for (int k = 0; k < 3; k++) v += (double)row[i][k] * (o[k] - (double)T.pos[k]);
-                q += v * v;
-            }
-            for (int k = 0; k < 3; k++) c[3 * e + k] = c[3 * t + k];
-            r[e] = r[t] + sg[t] * sqrt(q) * (1.0 + 1e-5) + 1e-5;
-            sg[e] = sg[t] * sigma_max(P);
-        }
-        if (N.rec >= 0) grow(&c[3 * e], r[e]);
-    }
-    /* moving surfaces: their frame's ball and the reach of their local box */
-    std::vector<char> dyn(d->nsrf, 0);
-    for (int e = 0; e < n; e++)
-        if (nodes[e].rec >= 0) dyn[nodes[e].rec] = 1;
-    qr_accel_host none;
-    std::vector<qr_anim_term> terms;
-    std::vector<qr_anim_target> targets;
-    for (int l = 0; l < QR_BVH_LEVELS; l++) none.lbounded[l].assign(d->nsrf, 1);
-    qr_accel_anim_terms(d, &none, NULL, dyn, terms, targets);
-    for (size_t i = 0; i < targets.size(); i++)
-    {
-        const qr_anim_term &t = terms[targets[i].t0];
-        const bool node = t.mode == QR_TERM_NODE || t.mode == QR_TERM_NODE_SHIFT;
-        const int fr = node ? t.xf : t.srf;
-        if (fr < 0 || of_rec[fr] < 0) continue;
-        const int e = of_rec[fr];
-        const qr_srf &s = d->srf[t.srf];
-        double rho = 0.0;
-        bool fin = true;
-        for (int k = 0; k < 3; k++)
-        {
-            const double a = t.u[QR_BVH_LEVELS][k], b = t.u[QR_BVH_LEVELS][3 + k];
-            const double sh = node ? (double)s.pos[k] : 0.0;
-            if (!(a > -HUGE_VAL && b < HUGE_VAL && a <= b)) fin = false;
-            const double m = std::max(fabs(a + sh), fabs(b + sh));
-            rho += m * m;
-        }
-        if (!fin) continue;
-        grow(&c[3 * e], r[e] + sg[e] * sqrt(rho) * (1.0 + 1e-5) + 1e-5);
-    }
-    for (int k = 0; k < 3; k++)
-    {
-        out[k] = (float)lo[k];
-        out[3 + k] = (float)hi[k];
-    }
-}
-
 static int anim_prepare(qr_ctx *ctx, qr_scene_slot *sl, const qr_scene_desc *desc,
                         const qr_anim_node *nodes, int n, const float *bound);
 
@@ -550,7 +417,7 @@ static int anim_prepare(qr_ctx *ctx, qr_scene_slot *sl, const qr_scene_desc *des
     }
     else
     {
-        rotation_bound(desc, nodes, n, b);
+        qr_accel_rotation_bound(desc, nodes, n, b);
     }
 
     /* updates of this scene still in flight write its block: they finish

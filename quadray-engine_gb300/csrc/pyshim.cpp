@@ -13,6 +13,7 @@
 #include "scenegen.hpp"
 #include "flatten.h"
 #include "xform.h"
+#include "accel.h"
 #include "engine.h"
 
 extern "C"
@@ -124,6 +125,18 @@ int qrpy_flat_anim_params(void *f, long long time, qr_anim_param *out, int cap, 
     if ((int)p.size() > cap) return -1;
     if (!p.empty()) memcpy(out, p.data(), sizeof(qr_anim_param) * p.size());
     return rc;
+}
+
+/* the default motion bound of a device update table (lo[3], hi[3]) and the
+ * scene extent it is joined with, for host tests of the bound */
+void qrpy_rotation_bound(const qr_scene_desc *d, const qr_anim_node *t, int n, float *out)
+{
+    qr_accel_rotation_bound(d, t, n, out);
+}
+
+void qrpy_extent(const qr_scene_desc *d, double *out)
+{
+    qr_accel_extent(d, out);
 }
 
 /* host restatement of the device update's transform stages (anim.cu stages

@@ -241,3 +241,51 @@ def test_static_scene_has_an_empty_update_table(qr):
     assert len(f.anim_table()) == 0
     rc, p = f.anim_params(16)
     assert rc == 0 and len(p) == 0
+
+
+def _bound(qr, desc, table):
+    out = (ctypes.c_float * 6)()
+    qr.lib().qrpy_rotation_bound(ctypes.byref(desc), table, len(table), out)
+    return list(out)
+
+
+def _extent(qr, desc):
+    out = (ctypes.c_double * 6)()
+    qr.lib().qrpy_extent(ctypes.byref(desc), out)
+    return list(out)
+
+
+@pytest.mark.parametrize("kind,seed,nq,flags", [
+    (2, 1, 64, 0),          # spinning 3-level hierarchy, every surface a node
+    (2, 5, 64, 8),          # array-level transform nodes (TARRAY)
+    (2, 3, 256, 0),
+    (1, 3, 64, 16),         # spinning quadrics
+])
+def test_rotation_bound_holds_every_later_frame(qr, kind, seed, nq, flags):
+    """the default motion bound of a device update table, taken at the first
+    frame: for animators that only rotate, the scene's extent (surface boxes
+    without rounding allowance and record positions) at every later frame
+    lies inside it"""
+    f = qr.Flat(qr.GenScene(kind, seed, nq, flags), 64, 48, 0)
+    desc, _ = f.update(0, 4)
+    table = f.anim_table()
+    b = _bound(qr, desc, table)
+    e0 = _extent(qr, desc)
+    assert all(b[k] <= e0[k] and b[3 + k] >= e0[3 + k] for k in range(3))
+    for t in [16 * k for k in range(1, 400, 7)]:
+        desc, _ = f.update(t, 4)
+        e = _extent(qr, desc)
+        for k in range(3):
+            assert b[k] <= e[k] + 1e-4 and e[3 + k] - 1e-4 <= b[3 + k], (t, k, b, e)
+
+
+def test_moving_transforms_leave_the_rotation_bound(qr):
+    """animators that move their transforms (quadrics that rise) are not
+    covered by the default bound: later frames leave it, which the device
+    update's own check catches"""
+    f = qr.Flat(qr.GenScene(qr.SCN_PLAIN, 11, 24, 1 << 12), 64, 48, 0)
+    desc, _ = f.update(0, 4)
+    b = _bound(qr, desc, f.anim_table())
+    desc, _ = f.update(16000, 4)
+    e = _extent(qr, desc)
+    assert e[5] > b[5]
