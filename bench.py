@@ -33,8 +33,9 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 # algorithmic FP32 operations per unit of work (div / sqrt count 1, FMA 2;
-# this build issues no FMAs): per solver test, transform, clip evaluation,
-# shaded hit, light evaluation, refraction and reflection
+# the library is compiled without FMA contraction): per solver test,
+# transform, clip evaluation, shaded hit, light evaluation, refraction and
+# reflection
 FLOPS = {
     "test_plane": 3, "test_quadric": 40, "test_twoplane": 28, "xform": 33,
     "clip_root": 12, "clip_custom": 15, "shade": 30, "light": 55,
