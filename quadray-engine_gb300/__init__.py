@@ -160,6 +160,8 @@ def lib():
         L.qrpy_rotation_bound.restype = None
         L.qrpy_extent.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(ctypes.c_double)]
         L.qrpy_extent.restype = None
+        L.qrpy_anim_box_check.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(QrAnimNode),
+                                          i32, ctypes.POINTER(QrSceneDesc)]
         L.qr_scene_anim_init.argtypes = [vp, i32, ctypes.POINTER(QrSceneDesc),
                                          ctypes.POINTER(QrAnimNode), i32,
                                          ctypes.POINTER(ctypes.c_float)]

@@ -759,13 +759,21 @@ static void term_local(qr_anim_term &t, int l, const Box &u)
     }
 }
 
-bool qr_accel_record_frame(const qr_srf &t, float a[9])
+bool qr_accel_record_frame_d(const qr_srf &t, double a[9])
 {
     double m[3][3], r[3][3];
     record_matrix(t, m);
     if (!invert3(m, r)) return false;
     for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) a[3 * i + j] = (float)r[i][j];
+        for (int j = 0; j < 3; j++) a[3 * i + j] = r[i][j];
+    return true;
+}
+
+bool qr_accel_record_frame(const qr_srf &t, float a[9])
+{
+    double r[9];
+    if (!qr_accel_record_frame_d(t, r)) return false;
+    for (int k = 0; k < 9; k++) a[k] = (float)r[k];
     return true;
 }
 

@@ -120,6 +120,7 @@ struct qr_anim_target
  * inverse of the record's transform rows (record_matrix), row-major, in
  * float; false when singular */
 bool qr_accel_record_frame(const qr_srf &t, float a[9]);
+bool qr_accel_record_frame_d(const qr_srf &t, double a[9]);     /* the same in double */
 
 /* the terms of every bounded surface whose box depends on a record marked
  * in dyn (its own, its transform node's, a bounding clipper's or that

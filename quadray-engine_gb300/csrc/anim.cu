@@ -26,6 +26,7 @@
 #include <float.h>
 #include <math.h>
 #include "anim.cuh"
+#include "anim_box.h"
 #include "xform.h"
 
 namespace
@@ -41,87 +42,6 @@ __device__ void store16(float *p, const float (*m)[4])
 {
     for (int i = 0; i < 4; i++)
         for (int j = 0; j < 4; j++) p[4 * i + j] = m[i][j];
-}
-
-/* world-from-local matrix of a record's frame (accel.cpp
- * qr_accel_record_frame, in float): the inverse of the transform rows as the
- * tracer applies them (diagonal only when amap[3] == 1, "scaling only") */
-__device__ void record_frame(const qr_srf &t, float *f)
-{
-    float m[3][3];
-    const float *row[3] = {t.tci, t.tcj, t.tck};
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++)
-            m[i][j] = (t.amap[3] == 1 && i != j) ? 0.0f : row[i][j];
-    const float c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1];
-    const float c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2];
-    const float c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
-    const float det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
-    if (!(fabsf(det) > 1e-30f))
-    {
-        f[9] = 1.0f;
-        return;
-    }
-    const float id = 1.0f / det;
-    f[0] = c00 * id;
-    f[1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
-    f[2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
-    f[3] = c01 * id;
-    f[4] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
-    f[5] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
-    f[6] = c02 * id;
-    f[7] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
-    f[8] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
-    f[9] = 0.0f;
-}
-
-/* world box of one term at level l (accel.h, QR_TERM_*); false when the
- * frame's transform is singular */
-__device__ bool term_box(const qr_anim_dev &A, const qr_anim_term &t, int l,
-                         float lo[3], float hi[3])
-{
-    const qr_srf &s = A.srf[t.srf];
-    const bool node = t.mode == QR_TERM_NODE || t.mode == QR_TERM_NODE_SHIFT;
-    const int fr = node ? t.xf : t.srf;
-    const qr_srf &F = A.srf[fr];
-    float u[6];
-    for (int k = 0; k < 6; k++) u[k] = t.u[l][k];
-    if (node)
-    {
-        for (int k = 0; k < 3; k++)
-        {
-            u[k] += s.pos[k];
-            u[3 + k] += s.pos[k];
-        }
-    }
-    if (t.mode == QR_TERM_NODE_SHIFT || t.mode == QR_TERM_OWN_SHIFT)
-    {
-        for (int k = 0; k < 3; k++)
-        {
-            lo[k] = u[k] + F.pos[k];
-            hi[k] = u[3 + k] + F.pos[k];
-        }
-        return true;
-    }
-    const float *a = A.frame + 10 * (size_t)fr;
-    if (a[9] != 0.0f) return false;
-    /* interval image of u under h = a u + o (accel.cpp affine_image) */
-    for (int i = 0; i < 3; i++)
-    {
-        float l0 = F.pos[i], h0 = F.pos[i];
-        for (int j = 0; j < 3; j++)
-        {
-            const float c = a[3 * i + j];
-            if (c == 0.0f) continue;
-            const float p = c * u[j], q = c * u[3 + j];
-            if (isnan(p) || isnan(q)) { l0 = -HUGE_VALF; h0 = HUGE_VALF; break; }
-            l0 += fminf(p, q);
-            h0 += fmaxf(p, q);
-        }
-        lo[i] = l0;
-        hi[i] = h0;
-    }
-    return true;
 }
 
 __device__ bool inside(const float ext[6], const float lo[3], const float hi[3])
@@ -202,7 +122,7 @@ __global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev *devs)
                 s.tck[k] = inv[k][2];
                 s.pos[k] = M[3][k];
             }
-            record_frame(s, A.frame + 10 * (size_t)N.rec);
+            qr::record_frame(s, A.frame + 10 * (size_t)N.rec);
             /* record positions bound the local coordinates the walk forms
              * (light positions take no part, as in the host build) */
             const float p[3] = {M[3][0], M[3][1], M[3][2]};
@@ -223,41 +143,21 @@ __global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev *devs)
         const qr_anim_target tg = A.targets[w / (L + 1)];
         const int l = w % (L + 1);
         if (l < L && ((tg.levels >> l) & 1) == 0) continue;
-        float lo[3] = {-HUGE_VALF, -HUGE_VALF, -HUGE_VALF};
-        float hi[3] = {HUGE_VALF, HUGE_VALF, HUGE_VALF};
-        const int nterm = l == L ? 1 : tg.tn;
-        bool ok = true;
-        for (int j = 0; j < nterm && ok; j++)
-        {
-            float tl[3], th[3];
-            ok = term_box(A, A.terms[tg.t0 + j], l, tl, th);
-            for (int k = 0; k < 3 && ok; k++)
-            {
-                lo[k] = fmaxf(lo[k], tl[k]);
-                hi[k] = fminf(hi[k], th[k]);
-            }
-        }
         if (l == L)
         {
             /* the extent holds the finite ones of these boxes (a quadric
              * that only its clippers bound has none), as in the host build */
+            float lo[3], hi[3];
+            const bool ok = qr::term_box(A.srf, A.frame, A.terms[tg.t0], L, lo, hi);
             bool fin = ok;
             for (int k = 0; k < 3; k++)
                 fin = fin && lo[k] > -HUGE_VALF && hi[k] < HUGE_VALF && lo[k] <= hi[k];
             if (!ok || (fin && !inside(A.ext, lo, hi))) fail = 1;
             continue;
         }
-        for (int k = 0; k < 3 && ok; k++)
-            ok = lo[k] <= hi[k] && lo[k] > -HUGE_VALF && hi[k] < HUGE_VALF;
-        if (!ok) { fail = 1; continue; }
-        float *b = A.lboxes + ((size_t)l * A.nsrf + tg.srf) * 6;
-        for (int k = 0; k < 3; k++)
-        {
-            /* accel.cpp pad */
-            const float m = 1e-3f + 1e-4f * (fabsf(lo[k]) + fabsf(hi[k]));
-            b[k] = lo[k] - m;
-            b[3 + k] = hi[k] + m;
-        }
+        if (!qr::target_box(A.srf, A.frame, A.terms, tg, l,
+                            A.lboxes + ((size_t)l * A.nsrf + tg.srf) * 6))
+            fail = 1;
     }
     __syncthreads();
 

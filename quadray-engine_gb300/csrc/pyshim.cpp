@@ -14,6 +14,7 @@
 #include "flatten.h"
 #include "xform.h"
 #include "accel.h"
+#include "anim_box.h"
 #include "engine.h"
 
 extern "C"
@@ -137,6 +138,82 @@ void qrpy_rotation_bound(const qr_scene_desc *d, const qr_anim_node *t, int n, f
 void qrpy_extent(const qr_scene_desc *d, double *out)
 {
     qr_accel_extent(d, out);
+}
+
+/* the device update's box stage (anim_box.h, the kernel's own float steps)
+ * run on the host for the records of scene dt, with the terms and targets
+ * taken from scene d0 and its table under the default motion bound;
+ * returns how many (surface, level) boxes fail to contain the exact box of
+ * the same terms (double arithmetic, no pad), counting a box the float
+ * stage refuses (singular or unbounded) a thousand times */
+int qrpy_anim_box_check(const qr_scene_desc *d0, const qr_anim_node *table, int n,
+                        const qr_scene_desc *dt)
+{
+    float b[6];
+    qr_accel_rotation_bound(d0, table, n, b);
+    qr_accel_host acc;
+    int root[QR_BVH_LEVELS], aoff[QR_BVH_LEVELS], anum[QR_BVH_LEVELS];
+    float r2[QR_BVH_LEVELS];
+    qr_accel_build_levels(d0, &acc, root, aoff, anum, r2, b);
+    std::vector<char> dyn(d0->nsrf, 0);
+    for (int e = 0; e < n; e++)
+        if (table[e].rec >= 0) dyn[table[e].rec] = 1;
+    std::vector<qr_anim_term> terms;
+    std::vector<qr_anim_target> targets;
+    qr_accel_anim_terms(d0, &acc, b, dyn, terms, targets);
+    std::vector<float> fr((size_t)dt->nsrf * 10);
+    for (int i = 0; i < dt->nsrf; i++) qr::record_frame(dt->srf[i], &fr[10 * (size_t)i]);
+    int bad = 0;
+    for (size_t g = 0; g < targets.size(); g++)
+    {
+        const qr_anim_target &tg = targets[g];
+        for (int l = 0; l < QR_BVH_LEVELS; l++)
+        {
+            if (((tg.levels >> l) & 1) == 0) continue;
+            float fb[6];
+            if (!qr::target_box(dt->srf, fr.data(), terms.data(), tg, l, fb))
+            {
+                bad += 1000;
+                continue;
+            }
+            double lo[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+            double hi[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL};
+            for (int j = 0; j < tg.tn; j++)
+            {
+                const qr_anim_term &t = terms[tg.t0 + j];
+                const bool node = t.mode == QR_TERM_NODE || t.mode == QR_TERM_NODE_SHIFT;
+                const qr_srf &s = dt->srf[t.srf];
+                const qr_srf &F = dt->srf[node ? t.xf : t.srf];
+                double v[6];
+                for (int k = 0; k < 3; k++)
+                {
+                    const double sh = node ? (double)s.pos[k] : 0.0;
+                    v[k] = (double)t.u[l][k] + sh;
+                    v[3 + k] = (double)t.u[l][3 + k] + sh;
+                }
+                double a[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+                if (t.mode == QR_TERM_NODE || t.mode == QR_TERM_OWN)
+                    qr_accel_record_frame_d(F, a);
+                for (int i = 0; i < 3; i++)
+                {
+                    double l0 = F.pos[i], h0 = F.pos[i];
+                    for (int k = 0; k < 3; k++)
+                    {
+                        const double c = a[3 * i + k];
+                        if (c == 0.0) continue;
+                        const double p = c * v[k], q = c * v[3 + k];
+                        l0 += p < q ? p : q;
+                        h0 += p < q ? q : p;
+                    }
+                    if (l0 > lo[i]) lo[i] = l0;
+                    if (h0 < hi[i]) hi[i] = h0;
+                }
+            }
+            for (int k = 0; k < 3; k++)
+                if (!((double)fb[k] <= lo[k] && (double)fb[3 + k] >= hi[k])) { bad++; break; }
+        }
+    }
+    return bad;
 }
 
 /* host restatement of the device update's transform stages (anim.cu stages

@@ -289,3 +289,20 @@ def test_moving_transforms_leave_the_rotation_bound(qr):
     desc, _ = f.update(16000, 4)
     e = _extent(qr, desc)
     assert e[5] > b[5]
+
+
+@pytest.mark.parametrize("kind,seed,nq,flags", [
+    (2, 1, 64, 0), (2, 5, 64, 8), (2, 3, 256, 0), (1, 3, 64, 16),
+])
+def test_float_box_stage_contains_the_exact_boxes(qr, kind, seed, nq, flags):
+    """the device update's box stage (the kernel's float steps, run here on
+    the host) gives, at later frames, boxes that contain the exact boxes of
+    the same terms in double arithmetic: the pad covers float rounding"""
+    f0 = qr.Flat(qr.GenScene(kind, seed, nq, flags), 64, 48, 0)
+    d0, _ = f0.update(0, 4)
+    table = f0.anim_table()
+    ft = qr.Flat(qr.GenScene(kind, seed, nq, flags), 64, 48, 0)
+    for t in (16, 16 * 37, 16 * 211, 16 * 997):
+        dt, _ = ft.update(t, 4)
+        assert qr.lib().qrpy_anim_box_check(ctypes.byref(d0), table, len(table),
+                                            ctypes.byref(dt)) == 0, t
