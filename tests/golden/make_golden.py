@@ -40,7 +40,7 @@ DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 #   reference's load_image reads (the driver writes them to
 #   ../data/textures/ of its working directory); fsaa 1 = 2x alternating,
 #   2 = 4x rotated grid; 2048 = a second camera (next_cam before the frames
-#   listed in NEXTCAM);
+#   listed in NEXTCAM); 16 = plain scene whose quadrics spin;
 #   opts "none" renders the reference without its list optimisations
 CASES = {
     "plain_s1_160x96":      (1, 1, 16, 160, 96, 0, 1, 0, "full"),
@@ -77,6 +77,10 @@ CASES = {
     "anim_s1_tarray_none_160x90_d4": (2, 1, 64, 160, 90, 0, 1, 8, "none", 4),
     "anim_s6_nofresnel_160x90_d4": (2, 6, 64, 160, 90, 0, 2, 512, "full", 4),
     "anim_s8_nofresnel_96x54_d10": (2, 8, 64, 96, 54, 0, 1, 512, "none", 10),
+    # six frames in a row (t = 0 .. 80 ms): a longer sequence for animated
+    # scenes updated from frame to frame, and spinning plain quadrics (16)
+    "anim_s12_full_128x72_d4":    (2, 12, 64, 128, 72, 0, 6, 0, "full", 4),
+    "plain_s26_spin_160x96":      (1, 26, 16, 160, 96, 0, 6, 16, "full"),
     # path tracer (kind 3): the reference's running mean after 256 frames of
     # one sample each (its own random streams); only the last frame is kept
     "pt_s1_ref256_80x45_d8":      (3, 1, 32, 80, 45, 0, 256, 0, "full", 8, "last"),
