@@ -895,9 +895,9 @@ static double sigma_max(const double a[3][3])
 void qr_accel_rotation_bound(const qr_scene_desc *d, const qr_anim_node *nodes, int n,
                              float out[6])
 {
-    double ext[6];
-    qr_accel_extent(d, ext);
-    double lo[3] = {ext[0], ext[1], ext[2]}, hi[3] = {ext[3], ext[4], ext[5]};
+    Extent x;
+    scene_extent(d, NULL, x);
+    double lo[3] = {x.clo[0], x.clo[1], x.clo[2]}, hi[3] = {x.chi[0], x.chi[1], x.chi[2]};
     std::vector<double> c(3 * (size_t)n), r(n), sg(n);
     std::vector<int> of_rec(d->nsrf, -1);
     auto grow = [&](const double *cc, double rr) {
@@ -955,28 +955,25 @@ void qr_accel_rotation_bound(const qr_scene_desc *d, const qr_anim_node *nodes, 
         }
         if (N.rec >= 0) grow(&c[3 * e], r[e]);
     }
-    /* moving surfaces: their frame's ball and the reach of their local box */
-    std::vector<char> dyn(d->nsrf, 0);
-    for (int e = 0; e < n; e++)
-        if (nodes[e].rec >= 0) dyn[nodes[e].rec] = 1;
-    qr_accel_host none;
-    std::vector<qr_anim_term> terms;
-    std::vector<qr_anim_target> targets;
-    for (int l = 0; l < QR_BVH_LEVELS; l++) none.lbounded[l].assign(d->nsrf, 1);
-    qr_accel_anim_terms(d, &none, NULL, dyn, terms, targets);
-    for (size_t i = 0; i < targets.size(); i++)
+    /* moving surfaces: their frame's ball and the reach of their local box
+     * (without rounding allowance, as the extent has it) */
+    for (int i = 0; i < d->nsrf; i++)
     {
-        const qr_anim_term &t = terms[targets[i].t0];
-        const bool node = t.mode == QR_TERM_NODE || t.mode == QR_TERM_NODE_SHIFT;
-        const int fr = node ? t.xf : t.srf;
+        const qr_srf &s = d->srf[i];
+        if (s.is_node || x.srf_xf[i] == -2) continue;
+        const int sx = x.srf_xf[i];
+        const int mode = term_mode(d, s, sx, false);
+        const bool node = mode == QR_TERM_NODE || mode == QR_TERM_NODE_SHIFT;
+        const int fr = node ? sx : i;
         if (fr < 0 || of_rec[fr] < 0) continue;
         const int e = of_rec[fr];
-        const qr_srf &s = d->srf[t.srf];
+        const Box u = local_surface_box(s, 0.0);
         double rho = 0.0;
         bool fin = true;
         for (int k = 0; k < 3; k++)
         {
-            const double a = t.u[QR_BVH_LEVELS][k], b = t.u[QR_BVH_LEVELS][3 + k];
+            /* the box in float, rounded outwards, as the terms hold it */
+            const double a = down(u.lo[k]), b = up(u.hi[k]);
             const double sh = node ? (double)s.pos[k] : 0.0;
             if (!(a > -HUGE_VAL && b < HUGE_VAL && a <= b)) fin = false;
             const double m = std::max(fabs(a + sh), fabs(b + sh));
