@@ -33,6 +33,7 @@ GEN_NOFRESNEL = 1 << 9   # animated scene without Fresnel terms (the default)
 GEN_TEXFILE = 1 << 10    # with GEN_TEX: textures named as BMP files (write_textures)
 GEN_CAMERAS = 1 << 11    # plain scene with a second camera (next_cam)
 GEN_RISE = 1 << 12       # plain scene whose quadrics turn and rise (transforms move)
+GEN_SETTLE = 1 << 13     # plain scene whose quadrics grow (from 1 s), rest at right angles (2 s)
 # camera actions (rt_Scene::update; codes of core/engine/object.h:47-63)
 CAMERA_MOVE_DOWN, CAMERA_MOVE_UP, CAMERA_MOVE_LEFT, CAMERA_MOVE_RIGHT = 2, 3, 4, 5
 CAMERA_MOVE_BACK, CAMERA_MOVE_FORWARD = 6, 7

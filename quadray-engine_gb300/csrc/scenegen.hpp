@@ -80,6 +80,9 @@
 #define QR_GEN_CAMERAS  (1 << 11)  /* QR_SCN_PLAIN: a second camera */
 #define QR_GEN_RISE     (1 << 12)  /* QR_SCN_PLAIN: the quadrics turn and rise
                                       (anim_rise: their transforms move) */
+#define QR_GEN_SETTLE   (1 << 13)  /* QR_SCN_PLAIN: the quadrics turn, grow
+                                      from 1 s and rest at right angles from
+                                      2 s (anim_settle) */
 
 namespace qr_gen
 {
@@ -193,6 +196,33 @@ static void anim_rise(rt_time time, rt_time last_time, rt_TRANSFORM3D *trm,
     while (trm->rot[RT_Y] > 180.0f) trm->rot[RT_Y] -= 360.0f;
     while (trm->rot[RT_Z] > 180.0f) trm->rot[RT_Z] -= 360.0f;
     trm->pos[RT_Z] += 0.002f * (float)(time - last_time);
+}
+
+/*
+ * Animator of QR_GEN_SETTLE: the object turns (as anim_rise), from 1000 ms
+ * on it is scaled by 1.5, and from 2000 ms on it rests at right angles (the
+ * update phases then give it no rotation of its own).
+ */
+static void anim_settle(rt_time time, rt_time last_time, rt_TRANSFORM3D *trm,
+                        rt_pntr pobj)
+{
+    (void)pobj;
+    const float t = (float)time;
+    if (time < 2000)
+    {
+        trm->rot[RT_X] = 17.0f + 0.0371f * t;
+        trm->rot[RT_Y] = -23.0f + 0.0293f * t;
+        trm->rot[RT_Z] = 41.0f + 0.0137f * t;
+    }
+    else
+    {
+        trm->rot[RT_X] = 90.0f;
+        trm->rot[RT_Y] = 0.0f;
+        trm->rot[RT_Z] = -90.0f;
+    }
+    const float sc = time >= 1000 ? 1.5f : 1.0f;
+    trm->scl[RT_X] = trm->scl[RT_Y] = trm->scl[RT_Z] = sc;
+    (void)last_time;
 }
 
 /*
@@ -593,6 +623,7 @@ static void build_plain(Scene &sc, uint64_t seed, int nq, int nl)
         Scene::trm_set(&q.trm, 1, 1, 1, rx, ry, rz, px, py, pz);
         if (sc.flags & QR_GEN_SPIN) q.f_anim = anim_spin;
         if (sc.flags & QR_GEN_RISE) q.f_anim = anim_rise;
+        if (sc.flags & QR_GEN_SETTLE) q.f_anim = anim_settle;
         root.push_back(q);
     }
     if (sc.flags & QR_GEN_SHAPES)

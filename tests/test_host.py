@@ -306,3 +306,31 @@ def test_float_box_stage_contains_the_exact_boxes(qr, kind, seed, nq, flags):
         dt, _ = ft.update(t, 4)
         assert qr.lib().qrpy_anim_box_check(ctypes.byref(d0), table, len(table),
                                             ctypes.byref(dt)) == 0, t
+
+
+def test_update_table_refusals(qr):
+    """anim_params reports a frame the table no longer fits: an animated
+    transform whose scale changes (2), one that comes to rest at right
+    angles (1); a table taken where an animated object has no free rotation
+    is refused"""
+    f = qr.Flat(qr.GenScene(qr.SCN_PLAIN, 5, 8, qr.GEN_SETTLE), 64, 48, 0)
+    f.update(0, 4)
+    table = f.anim_table()
+    assert len(table) == 8
+    rc, p = f.anim_params(500)
+    assert rc == 0
+    f.update(500, 4)
+    assert f.anim_check(table, p) == 0
+    rc, _ = f.anim_params(1200)
+    assert rc == 2
+    f.update(1200, 4)
+    table = f.anim_table()          # a new table at the new scale fits again
+    rc, p = f.anim_params(1500)
+    assert rc == 0
+    f.update(1500, 4)
+    assert f.anim_check(table, p) == 0
+    rc, _ = f.anim_params(2500)
+    assert rc == 1
+    f.update(2500, 4)
+    with pytest.raises(ValueError):
+        f.anim_table()
