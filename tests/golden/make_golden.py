@@ -81,6 +81,8 @@ CASES = {
     # scenes updated from frame to frame, and spinning plain quadrics (16)
     "anim_s12_full_128x72_d4":    (2, 12, 64, 128, 72, 0, 6, 0, "full", 4),
     "plain_s26_spin_160x96":      (1, 26, 16, 160, 96, 0, 6, 16, "full"),
+    "anim_s13_full_aa4_96x54_d4": (2, 13, 64, 96, 54, 2, 4, 0, "full", 4),
+    "anim_s14_none_96x54_d10":    (2, 14, 64, 96, 54, 0, 4, 0, "none", 10),
     # path tracer (kind 3): the reference's running mean after 256 frames of
     # one sample each (its own random streams); only the last frame is kept
     "pt_s1_ref256_80x45_d8":      (3, 1, 32, 80, 45, 0, 256, 0, "full", 8, "last"),
