@@ -39,7 +39,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 FLOPS = {
     "test_plane": 3, "test_quadric": 40, "test_twoplane": 28, "xform": 33,
     "clip_root": 12, "clip_custom": 15, "shade": 30, "light": 55,
-    "refract": 40, "reflect": 25,
+    "refract": 40, "reflect": 25, "box_test": 12,
 }
 STAT_NAMES = ["ray_primary", "ray_shadow", "ray_secondary", "test_plane",
               "test_quadric", "test_twoplane", "xform", "clip_root",
@@ -50,7 +50,9 @@ WORKLOADS = {
     # animated Whitted frame: 1920x1080, 4x AA, 64 quadrics cut by 1-2 planes
     # each plus 8 boolean-minus pairs, 3-level spinning hierarchy, 4 lights,
     # reflection + refraction with Fresnel to depth 4
-    "anim": dict(kind=2, seed=1, nq=64, w=1920, h=1080, fsaa=2, depth=4, anim=True),
+    # (300 frames at t = 16 ms apart)
+    "anim": dict(kind=2, seed=1, nq=64, w=1920, h=1080, fsaa=2, depth=4, anim=True,
+                 frames=300),
     # plain Whitted frame: 800x480, 1 spp, 1 ground plane + 16 quadrics,
     # 2 lights, shadows
     "plain": dict(kind=1, seed=1, nq=16, w=800, h=480, fsaa=0, depth=10, anim=False),
@@ -460,16 +462,24 @@ class ClockSampler:
 
 def cpu_baseline(qr, wl, seconds=12.0):
     """The CPU restatement of the reference tracer on the host cores, on a
-    bounded sample of rows of the workload's first frame; returns rays/s and
-    the setup."""
+    bounded sample of rows of the workload: rows in a stride order over the
+    whole frame, and for the animated workload over 8 frames spread over its
+    animation (frame k of the sample takes rows k, k + 8, ... of that
+    order); returns rays/s and the setup."""
     import build as oracle_build
     O = oracle_build.load_oracle()
-    g = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)
-    f = qr.Flat(g, wl["w"], wl["h"], wl["fsaa"])
-    desc, params = f.update(0, wl["depth"])
+    nfr = wl.get("frames", 1)
+    times = [16 * int((i + 0.5) * nfr / 8) for i in range(8)] if wl["anim"] else [0]
     spp = wl.get("pt", 0)
-    if spp:
-        params.pt_on, params.pts_c, params.seed, params.frame_idx = spp, 0.0, 1, 0
+    frames = []
+    for t in times:
+        g = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)
+        f = qr.Flat(g, wl["w"], wl["h"], wl["fsaa"])
+        desc, params = f.update(t, wl["depth"])
+        if spp:
+            params.pt_on, params.pts_c, params.seed, params.frame_idx = spp, 0.0, 1, 0
+        frames.append((g, f, desc, params))
+    params = frames[0][3]
     acc = np.zeros((params.y_res, params.x_row, 3), dtype=np.float32)
     cores = os.cpu_count() or 1
     out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
@@ -489,14 +499,15 @@ def cpu_baseline(qr, wl, seconds=12.0):
             with lock:
                 i = nxt[0]
                 nxt[0] += 1
-            yy = (i * stride) % params.y_res
+            _, _, desc, prm = frames[i % len(frames)]
+            yy = ((i // len(frames)) * stride) % prm.y_res
             nr = ctypes.c_uint64()
             if spp:
-                O.qr_oracle_pt(ctypes.addressof(desc), ctypes.addressof(params),
+                O.qr_oracle_pt(ctypes.addressof(desc), ctypes.addressof(prm),
                                acc.ctypes.data, out.ctypes.data, yy, yy + 1,
                                ctypes.byref(nr))
             else:
-                O.qr_oracle_render(ctypes.addressof(desc), ctypes.addressof(params),
+                O.qr_oracle_render(ctypes.addressof(desc), ctypes.addressof(prm),
                                    out.ctypes.data, yy, yy + 1, ctypes.byref(nr))
             with lock:
                 rows_done[0] += 1
@@ -509,9 +520,11 @@ def cpu_baseline(qr, wl, seconds=12.0):
     for t in th:
         t.join()
     dt = time.perf_counter() - t0
+    what = ("rows of %d frames spread over the %d-frame animation" % (len(frames), nfr)
+            if wl["anim"] else "rows of the frame")
     return {"value": rays[0] / dt, "unit": "rays/s", "cores": cores, "kind": "port",
-            "sample": "%d rows of the %dx%d frame (%.1f s, %d threads)" % (
-                rows_done[0], wl["w"], wl["h"], dt, cores)}
+            "sample": "%d %s, %dx%d (%.1f s, %d threads)" % (
+                rows_done[0], what, wl["w"], wl["h"], dt, cores)}
 
 
 def run_reference(args, wl):
@@ -527,12 +540,253 @@ def run_reference(args, wl):
     line = {"impl": "reference", "metric": "rays_per_s", "value": v, "unit": "rays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, **{k: wl[k] for k in ("w", "h", "fsaa", "nq", "seed")}},
+            "config": config_of(args.workload, wl),
             "cpu_baseline": {"value": v, "unit": "rays/s", "cores": cb["cores"],
                              "kind": cb["kind"], "sample": cb["sample"]},
             "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def config_of(name, wl):
+    """the workload's identity, the same in both arms' lines"""
+    spp = wl.get("pt", 0)
+    return {"workload": name, "width": wl["w"], "height": wl["h"], "fsaa": wl["fsaa"],
+            "quadrics": wl["nq"], "seed": wl["seed"], "depth": wl["depth"],
+            "animated": wl["anim"], "frames": wl.get("frames", 1),
+            "samples_per_pixel": spp if spp else (4 if wl["fsaa"] == 2 else 1)}
+
+
+def frame_stats(qr, ctx, sid, params):
+    """work counters of one frame (instrumented build of the same kernels)"""
+    counts = (ctypes.c_uint64 * len(STAT_NAMES))()
+    host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+    rc = qr.lib().qr_render_stats(ctx.h, sid, ctypes.byref(params),
+                                  host.ctypes.data_as(ctypes.c_void_p), counts)
+    assert rc == 0, ctx.error()
+    return dict(zip(STAT_NAMES, (int(c) for c in counts)))
+
+
+def rays_of(st):
+    return st["ray_primary"] + st["ray_shadow"] + st["ray_secondary"]
+
+
+def fp32_peaks(qr, local):
+    """measured FP32 issue rates (TFLOP/s) of plain operations and of fused
+    multiply-adds (qr_fp32_peak)"""
+    out = {}
+    for name, fma in (("plain", 0), ("fma", 1)):
+        v = ctypes.c_double(0.0)
+        rc = qr.lib().qr_fp32_peak(local, fma, ctypes.byref(v))
+        out[name] = v.value if rc == 0 else None
+    return out
+
+
+REBUILD_EVERY = 32      # host update phases every 32nd frame of rt_Scene (engine.cpp)
+
+
+def run_frames(args, wl, rank, world, dist, local):
+    """one frame a step: the animated workload renders frames spread over its
+    animation, each after its device-side update; plain and path-traced
+    workloads render their frame"""
+    import torch
+    qr = importlib.import_module("quadray-engine_gb300")
+    ctx = qr.Context(local)
+    depth = wl["depth"]
+    spp = wl.get("pt", 0)
+    nfr = wl.get("frames", 1)
+    K, W = args.steps, args.warmup
+
+    def pt_params(p):
+        if spp:
+            p.pt_on, p.pts_c, p.seed, p.frame_idx = spp, 0.0, 1, 0
+        return p
+
+    # work counters of every frame of the workload (host update phases,
+    # upload, instrumented render): rays per frame and algorithmic FLOPs
+    sflat = qr.Flat(qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0), wl["w"], wl["h"],
+                    wl["fsaa"])
+    ssid = None
+    per_frame = []
+    scene_bytes = 0
+    for j in range(nfr):
+        desc, params = sflat.update(16 * j, depth)
+        if ssid is None:
+            ssid = ctx.upload(desc)
+        else:
+            ctx.update(ssid, desc)
+        per_frame.append(frame_stats(qr, ctx, ssid, pt_params(params)))
+        scene_bytes = (desc.nsrf * 256 + desc.nmat * 112 + desc.nlgt * 48 +
+                       desc.nelem * 16 + desc.nlelem * 16 + desc.ntex * 4)
+    nsrf = int(desc.nsrf)
+
+    # timed frames: spread over the animation (the first warm-up frames
+    # untimed); a frame j of an animated scene is rendered as rt_Scene does
+    # in its steady state: the scene prepared by the host update phases at
+    # the last rebuild frame j0 = 32 floor(j / 32) (untimed: the input
+    # arriving), then the device-side update to frame j and the render
+    timed = [int((i + 0.5) * nfr / K) for i in range(K)] if wl["anim"] else [0] * K
+    warm = list(range(min(W, nfr))) if wl["anim"] else [0] * W
+    warm += [warm[-1]] * (W - len(warm))
+    dflat = qr.Flat(qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0), wl["w"], wl["h"],
+                    wl["fsaa"])
+    dsid = [None]
+    if not wl["anim"]:
+        desc, params = dflat.update(0, depth)
+        dsid[0] = ctx.upload(desc)
+        fixed = pt_params(qr.QrFrameParams.from_buffer_copy(params))
+
+    def prepare(j):
+        """untimed: the scene state of the last rebuild before frame j;
+        returns the device update's parameters and the frame parameters"""
+        if not wl["anim"]:
+            return None, fixed
+        j0 = REBUILD_EVERY * (j // REBUILD_EVERY)
+        desc, _ = dflat.update(16 * j0, depth)
+        table = dflat.anim_table()
+        if dsid[0] is None:
+            dsid[0] = ctx.anim_upload(desc, table)
+        else:
+            ctx.anim_init(dsid[0], desc, table)
+        rc, prm = dflat.anim_params(16 * j)
+        assert rc == 0, rc
+        return prm, pt_params(dflat.frame_params())
+
+    frame = torch.empty((wl["h"], wl["w"] + 64), dtype=torch.int32, device="cuda")
+    acc = torch.empty((wl["h"], wl["w"] + 64, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step(prm, fp):
+        if prm is not None:
+            ctx.anim_update(dsid[0], prm, sp)
+        if spp:
+            ctx.render_pt(dsid[0], fp, acc.data_ptr(), frame.data_ptr(), sp)
+        else:
+            ctx.render_device(dsid[0], fp, frame.data_ptr(), sp)
+
+    for j in warm:
+        prm, fp = prepare(j)
+        step(prm, fp)
+    torch.cuda.synchronize()
+    assert fp.x_row <= wl["w"] + 64
+
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(K)]
+    torch.cuda.synchronize()
+    for i, j in enumerate(timed):
+        prm, fp = prepare(j)
+        flush.zero_()
+        ev[i][0].record(stream)
+        step(prm, fp)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    rays = sum(rays_of(per_frame[j]) for j in timed) / K          # per frame (mean)
+    value, t_total = whole_job(rays, K, sum(ms) / 1000.0, dist, "cuda")
+    if dist is not None:
+        dist.barrier()
+    fps = K * world / t_total
+    anim_status = ctx.anim_status(dsid[0]) if wl["anim"] else None
+    # the timed frames' work as rendered (the refitted hierarchy of a
+    # device-updated frame tests more boxes than a fresh one; the traced
+    # segments are the same)
+    tstats = []
+    for j in sorted(set(timed)):
+        prm, fp = prepare(j)
+        if prm is not None:
+            ctx.anim_update(dsid[0], prm, sp)
+            torch.cuda.synchronize()
+        st = frame_stats(qr, ctx, dsid[0], fp)
+        assert rays_of(st) == rays_of(per_frame[j]), j
+        tstats += [st] * timed.count(j)
+    stats = dict((k, sum(st[k] for st in tstats) / K) for k in STAT_NAMES)
+    flops = sum(stats[k] * v for k, v in FLOPS.items())
+
+    # end to end through the engine API (rt_Scene::render(time)) into the
+    # caller's host frame: the animated workload renders its whole
+    # animation in order and times every frame after the warm-up ones, so
+    # the host rebuild of every 32nd frame and the loosening of the refitted
+    # hierarchy between rebuilds are inside; other workloads render K frames
+    eng = qr.Engine(qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0), wl["w"], wl["h"],
+                    fsaa=wl["fsaa"], depth=depth, pton=spp)
+    e2e_frames = list(range(nfr)) if wl["anim"] else [0] * (W + K)
+    lat = []
+    for n, j in enumerate(e2e_frames):
+        t0 = time.perf_counter()
+        eng.render(16 * j)                      # into the caller-owned host frame
+        if n >= W:
+            lat.append(time.perf_counter() - t0)
+    eng.close()
+    e2e_timed = e2e_frames[W:]
+    e2e_rays = sum(rays_of(per_frame[j]) for j in e2e_timed)
+    if wl["anim"]:
+        nparams = len(dflat.anim_params(0)[1])
+        # the animated transforms each frame (48 bytes each); the whole
+        # scene on the frames of a host rebuild
+        h2d = sum(scene_bytes if j % REBUILD_EVERY == 0 else 48 * nparams
+                  for j in e2e_timed) / len(e2e_timed)
+    else:
+        h2d = 0                                 # the scene stays resident
+    d2h = wl["w"] * wl["h"] * 4
+
+    # FP32 issue rates measured on this device: the bit-exact arithmetic
+    # issues no fused multiply-add, so the plain rate is the roofline; the
+    # FMA rate is reported beside it
+    pk = fp32_peaks(qr, local)
+    achieved = flops * K / t_total / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh).get(args.workload, {}).get("bytes_per_launch")
+    roof = {"bound": "fp32", "achieved": achieved, "peak": pk["plain"], "unit": "TFLOP/s",
+            "frac": achieved / pk["plain"] if pk["plain"] else None, "traffic": traffic,
+            "peak_fma": pk["fma"], "frac_fma": achieved / pk["fma"] if pk["fma"] else None,
+            "peak_source": "measured on this device (qr_fp32_peak): FP32 additions, every "
+                           "SM filled, CUDA events; peak_fma: fused multiply-adds as 2 ops",
+            "flops_per_frame": flops}
+    cfg = config_of(args.workload, wl)
+    cfg.update({"surfaces": nsrf, "rays_per_frame": rays,
+                "timed_frames": timed if wl["anim"] else None,
+                "l2": "256 MiB buffer written between timed steps",
+                "parallelism": "replicas" if world > 1 else "single"})
+    line = {
+        "metric": "rays_per_s", "value": value, "unit": "rays/s",
+        "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": 1000.0 * t_total / K,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": cfg,
+        "step": ("device-side update of the animated transforms + render of the frame"
+                 if wl["anim"] else "render of the frame"),
+        "frames_per_s": fps,
+        "frame_ms_p50": float(np.percentile(ms, 50)),
+        "frame_ms_p99": float(np.percentile(ms, 99)),
+        "e2e": {"value": e2e_rays / sum(lat), "unit": "rays/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "frames": len(lat),
+                "host_rebuilds": sum(1 for j in e2e_timed if j % REBUILD_EVERY == 0)
+                if wl["anim"] else 0,
+                "frame_ms_p50": 1000.0 * float(np.percentile(lat, 50)),
+                "frame_ms_p99": 1000.0 * float(np.percentile(lat, 99))},
+        "roofline": roof,
+        "work_per_frame": stats,
+        "anim_status": anim_status,
+        "gpu_launches": K * (2 if wl["anim"] else 1),
+        "clocks": ck,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(qr, wl)
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
 
 
 def main():
@@ -577,135 +831,9 @@ def main():
             dist.destroy_process_group()
         return
 
-    qr = importlib.import_module("quadray-engine_gb300")
-    gen = qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0)
-    flat = qr.Flat(gen, wl["w"], wl["h"], wl["fsaa"])
-    ctx = qr.Context(local)
-    nframes = args.warmup + args.steps if wl["anim"] else 1
-    sids, scene_bytes = [], 0
-    for j in range(nframes):
-        desc, params = flat.update(16 * j, wl["depth"])
-        sids.append(ctx.upload(desc))
-        scene_bytes = (desc.nsrf * 256 + desc.nmat * 112 + desc.nlgt * 48 +
-                       desc.nelem * 16 + desc.nlelem * 16 + desc.ntex * 4)
-
-    def sid_of(j):
-        return sids[j] if wl["anim"] else sids[0]
-
-    spp = wl.get("pt", 0)
-    if spp:
-        params.pt_on, params.pts_c, params.seed, params.frame_idx = spp, 0.0, 1, 0
-
-    # instrumented launches: rays and work counters of every timed frame
-    host = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
-    stats = dict((k, 0) for k in STAT_NAMES)
-    frame_rays = []
-    for i in range(args.steps if wl["anim"] else 1):
-        counts = (ctypes.c_uint64 * len(STAT_NAMES))()
-        rc = qr.lib().qr_render_stats(ctx.h, sid_of(args.warmup + i), ctypes.byref(params),
-                                      host.ctypes.data_as(ctypes.c_void_p), counts)
-        assert rc == 0, ctx.error()
-        for k, c in zip(STAT_NAMES, counts):
-            stats[k] += int(c)
-        frame_rays.append(int(counts[0]) + int(counts[1]) + int(counts[2]))
-    nstat = len(frame_rays)
-    rays = sum(frame_rays) / nstat                      # per frame (mean)
-    flops = sum(stats[k] * v for k, v in FLOPS.items()) / nstat
-
-    frame = torch.empty((params.y_res, params.x_row), dtype=torch.int32, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
-    sp = stream.cuda_stream
-    for j in range(args.warmup):
-        ctx.render_device(sid_of(j), params, frame.data_ptr(), sp)
-    torch.cuda.synchronize()
-
-    if dist is not None:
-        dist.barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    torch.cuda.synchronize()
-    for i in range(args.steps):
-        flush.zero_()
-        ev[i][0].record(stream)
-        ctx.render_device(sid_of(args.warmup + i), params, frame.data_ptr(), sp)
-        ev[i][1].record(stream)
-    torch.cuda.synchronize()
-    ck = clocks.stop()
-    ms = [a.elapsed_time(b) for a, b in ev]
-    value, t_total = whole_job(rays, args.steps, sum(ms) / 1000.0, dist, "cuda")
-    if dist is not None:
-        dist.barrier()
-    fps = args.steps * world / t_total
-
-    # end to end through the engine API with a host frame buffer
-    eng = qr.Engine(qr.GenScene(wl["kind"], wl["seed"], wl["nq"], 0), wl["w"], wl["h"],
-                    fsaa=wl["fsaa"], depth=wl["depth"], pton=spp)
-    step_t = (lambda j: 16 * j) if wl["anim"] else (lambda j: 0)
-    for j in range(args.warmup):
-        eng.render(step_t(j))
-    lat = []
-    for i in range(args.steps):
-        t0 = time.perf_counter()
-        eng.render(step_t(args.warmup + i))     # into the caller-owned host frame
-        lat.append(time.perf_counter() - t0)
-    e2e_t = sum(lat)
-    h2d = scene_bytes
-    d2h = wl["w"] * wl["h"] * 4
-    eng.close()
-
-    # FP32 issue rate: the bit-exact arithmetic issues no fused multiply-add,
-    # so one FP32 operation per lane and clock (152 SMs x 128 lanes); the
-    # clock is the median sampled during the timed region
-    pk, pk_kind = peaks()
-    sm_mhz = ck.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * sm_mhz * 1e6 / 1e12   # TFLOP/s
-    achieved = flops * args.steps / t_total / 1e12
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as fh:
-            traffic = json.load(fh).get(args.workload, {}).get("bytes_per_launch")
-    line = {
-        "metric": "rays_per_s", "value": value, "unit": "rays/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * t_total / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "width": wl["w"], "height": wl["h"],
-                   "fsaa": wl["fsaa"], "quadrics": wl["nq"], "seed": wl["seed"],
-                   "depth": wl["depth"], "animated": wl["anim"],
-                   "samples_per_pixel": spp if spp else (4 if wl["fsaa"] == 2 else 1),
-                   "surfaces": int(desc.nsrf), "rays_per_frame": rays,
-                   "l2": "256 MiB buffer written between timed steps",
-                   "parallelism": "replicas" if world > 1 else "single"},
-        "frames_per_s": fps,
-        "frame_ms_p50": float(np.percentile(ms, 50)),
-        "frame_ms_p99": float(np.percentile(ms, 99)),
-        "e2e": {"value": rays * args.steps / e2e_t, "unit": "rays/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "frame_ms_p50": 1000.0 * float(np.percentile(lat, 50)),
-                "frame_ms_p99": 1000.0 * float(np.percentile(lat, 99))},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
-                     "peak_source": "nominal FP32 issue rate, no FMA (152 SMs x 128 "
-                                    "lanes x sampled SM clock); MEASURED_PEAKS.json "
-                                    "has no FP32 figure",
-                     "flops_per_frame": flops},
-        "work_per_frame": dict((k, v / nstat) for k, v in stats.items()),
-        "gpu_launches": args.steps,
-        "clocks": ck,
-    }
-    if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(qr, wl)
-    if rank == 0:
-        print(json.dumps(line))
-    ctx.close()
+    run_frames(args, wl, rank, world, dist, local)
     if dist is not None:
         dist.destroy_process_group()
-
 
 if __name__ == "__main__":
     main()

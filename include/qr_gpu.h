@@ -313,14 +313,20 @@ int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
 int qr_render_pt(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                  float *dev_acc, uint32_t *dev_frame, void *stream);
 /* path tracer without any device allocation.  This entry point has no
- * counterpart in the reference: it is qr_render_pt with its running sums in
- * a fixed array inside the library (QR_NOALLOC_MAX_PX pixels of 3 floats,
- * x_row * y_res may not exceed it: QR_ERR_LIMIT).  The first call on a
- * device looks the array up (cudaGetSymbolAddress) and should come before
- * any stream capture.  A call with pts_c == 0 starts the sums for its frame
- * size, later calls of that size add to them (QR_ERR_STATE if none were
- * started); nothing has to be cleared first.  The array is shared by every
- * context and scene on a device: overlapping calls race on it. */
+ * counterpart in the reference.  It serves callers that may not allocate
+ * device memory inside their render loop (a server that keeps allocations
+ * out of its steady state, a host application that owns the device heap):
+ * it is qr_render_pt with its running sums in a fixed array inside the
+ * library (QR_NOALLOC_MAX_PX pixels of 3 floats, 12 MiB a device, held
+ * until the process exits; x_row * y_res may not exceed it: QR_ERR_LIMIT).
+ * The first call on a device looks the array up (cudaGetSymbolAddress) with
+ * that device current and should come before any stream capture; the
+ * caller's current device is restored before the call returns.  A call with
+ * pts_c == 0 starts the sums for its context, scene and frame shape (x_row,
+ * y_res); later calls add to them and must name the same context, scene and
+ * shape (else QR_ERR_STATE); nothing has to be cleared first.  The array is
+ * shared by every context and scene on a device: calls that overlap on the
+ * GPU race on it. */
 #define QR_NOALLOC_MAX_PX   (1 << 20)
 int qr_render_pt_noalloc(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,
                          uint32_t *dev_frame, void *stream);
@@ -407,6 +413,14 @@ int qr_batch_wait(qr_batch *b);
  * finished (qr_batch_poll / qr_batch_wait); read them as volatile.  No
  * counterpart in the reference (it renders one frame per call) */
 int qr_batch_done(qr_batch *b, const volatile uint32_t **flags);
+
+/* measured FP32 issue rate of `device` in TFLOP/s (*tflops): plain FP32
+ * additions (fma == 0, one operation a lane and instruction, the rate of
+ * this tracer's arithmetic, which issues no fused multiply-add) or fused
+ * multiply-adds (fma != 0, counted as two operations), every SM filled,
+ * timed with CUDA events at the clock the device runs.  The roofline
+ * denominator of the render kernels; no counterpart in the reference */
+int qr_fp32_peak(int device, int fma, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,9 @@ ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libqr_oracle.so")
 LIB64 = os.path.join(OUT, "libqr_oracle64.so")     # QR_ORACLE_FP64 build
-REF_DIR = os.environ.get("QR_REFERENCE", "/root/reference")
+# the reference checkout: QR_REFERENCE, else the checkout this container
+# provides (read-only; absent on the GPU hosts, where nothing here needs it)
+REF_DIR = os.environ.get("QR_REFERENCE") or "/root/reference"
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
 
 

@@ -116,6 +116,7 @@ class QrAnimRequest(ctypes.Structure):
 
 ANIM_OWN, ANIM_UNDER, ANIM_NODE = 0, 1, 2
 QR_ERR_STATE = 5
+QR_ERR_LIMIT = 7
 QR_ERR_BUSY = 8
 QR_ERR_TRACE = 9
 FAULT_TREE, FAULT_STACK = 1, 2
@@ -204,6 +205,7 @@ def lib():
         L.qr_batch_done.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p)]
         L.qr_batch_wait.argtypes = [vp]
         L.qr_sync.argtypes = [vp, vp]
+        L.qr_fp32_peak.argtypes = [i32, i32, ctypes.POINTER(ctypes.c_double)]
         L.qr_fault.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
         L.qr_render_stats.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp,
                                       ctypes.POINTER(ctypes.c_uint64)]

@@ -44,6 +44,56 @@ def oracle_render(oracle, desc, params, y0=0, y1=None):
     return out[:, :params.x_res], nr.value
 
 
+def oracle_render_par(oracle, desc, params, y0=0, y1=None, threads=None):
+    """oracle_render over row bands on all host cores (the oracle call
+    releases the interpreter lock); returns (frame, traced rays)"""
+    import threading
+    y1 = params.y_res if y1 is None else y1
+    out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+    nt = max(1, min(threads or (os.cpu_count() or 1), y1 - y0))
+    # interleaved bands of 4 rows even out the work of dense and empty rows
+    rows = list(range(y0, y1, 4))
+    counts = [0] * nt
+    rcs = [0] * nt
+
+    def work(t):
+        for r0 in rows[t::nt]:
+            nr = ctypes.c_uint64()
+            rc = oracle.qr_oracle_render(ctypes.addressof(desc), ctypes.addressof(params),
+                                         out.ctypes.data, r0, min(r0 + 4, y1),
+                                         ctypes.byref(nr))
+            rcs[t] |= rc
+            counts[t] += nr.value
+
+    th = [threading.Thread(target=work, args=(t,)) for t in range(nt)]
+    [t.start() for t in th]
+    [t.join() for t in th]
+    assert not any(rcs)
+    return out[:, :params.x_res], sum(counts)
+
+
+def oracle_pt_par(oracle, desc, params, y0, y1, threads=None):
+    """the oracle's path tracer over rows [y0, y1) on all host cores;
+    returns (frame, running sums)"""
+    import threading
+    out = np.zeros((params.y_res, params.x_row), dtype=np.uint32)
+    acc = np.zeros((params.y_res, params.x_row, 3), dtype=np.float32)
+    nt = max(1, min(threads or (os.cpu_count() or 1), y1 - y0))
+    rows = list(range(y0, y1))
+    rcs = [0] * nt
+
+    def work(t):
+        for r in rows[t::nt]:
+            rcs[t] |= oracle.qr_oracle_pt(ctypes.addressof(desc), ctypes.addressof(params),
+                                          acc.ctypes.data, out.ctypes.data, r, r + 1, None)
+
+    th = [threading.Thread(target=work, args=(t,)) for t in range(nt)]
+    [t.start() for t in th]
+    [t.join() for t in th]
+    assert not any(rcs)
+    return out[:, :params.x_res], acc[:, :params.x_res]
+
+
 def channels(frame):
     f = frame.astype(np.int64)
     return np.stack([(f >> 16) & 255, (f >> 8) & 255, f & 255], axis=-1)

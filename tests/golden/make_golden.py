@@ -83,6 +83,13 @@ CASES = {
     "plain_s26_spin_160x96":      (1, 26, 16, 160, 96, 0, 6, 16, "full"),
     "anim_s13_full_aa4_96x54_d4": (2, 13, 64, 96, 54, 2, 4, 0, "full", 4),
     "anim_s14_none_96x54_d10":    (2, 14, 64, 96, 54, 0, 4, 0, "none", 10),
+    # the benchmarked configurations at their sizes: the plain frame at
+    # 800x480 (seeds 1-3), the animated frame with 4x AA at 480x270 (two
+    # frames, the bench's default options)
+    "plain_s1_800x480":           (1, 1, 16, 800, 480, 0, 1, 0, "full"),
+    "plain_s2_800x480":           (1, 2, 16, 800, 480, 0, 1, 0, "full"),
+    "plain_s3_800x480":           (1, 3, 16, 800, 480, 0, 1, 0, "full"),
+    "anim_s1_full_aa4_480x270_d4": (2, 1, 64, 480, 270, 2, 2, 0, "full", 4),
     # path tracer (kind 3): the reference's running mean after 256 frames of
     # one sample each (its own random streams); only the last frame is kept
     "pt_s1_ref256_80x45_d8":      (3, 1, 32, 80, 45, 0, 256, 0, "full", 8, "last"),
