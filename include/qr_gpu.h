@@ -190,6 +190,11 @@ typedef struct qr_frame_params
                                    thread a sub-sample (the frame is the
                                    same; for tests; single-frame renders
                                    only, batches ignore it) */
+#define QR_FP_PIXEL_PT      4   /* path tracer: one thread a pixel with its
+                                   samples in turn (the per-pixel kernel)
+                                   instead of the wavefront stages (the
+                                   frame is the same; for tests and
+                                   comparisons) */
 
 typedef struct qr_ctx qr_ctx;
 
@@ -301,8 +306,11 @@ int qr_scene_anim_status(qr_ctx *ctx, int scene_id, int32_t out[2]);
  * With fp->pt_on > 0 the frame is path traced: pt_on samples per pixel are
  * added to the context's running sums (reset when fp->pts_c == 0, which
  * counts the samples already summed) and the frame shows the mean over
- * pts_c + pt_on samples; the samples come from PCG32 streams seeded by
- * (fp->seed, fp->frame_idx, pixel).  This replaces the reference's
+ * pts_c + pt_on samples; every random draw is a counter-based hash of
+ * (fp->seed, fp->frame_idx, pixel, sample number pts_c + i, the drawing
+ * node's place in the sample's ray tree, the draw's purpose), so the frame
+ * does not depend on the order the GPU evaluates paths in.  This replaces
+ * the reference's
  * path-tracer accumulation planes (rt_Scene::render with set_pton,
  * core/engine/engine.cpp:2914-2919, 3674; tracer.cpp:2115-2139) */
 int qr_render_device(qr_ctx *ctx, int scene_id, const qr_frame_params *fp,

@@ -1208,10 +1208,14 @@ int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
  *   weight c_trn / (1 - P) (4685-4723); point lights and ambient are not
  *   used (no next-event estimation); colour = rc c_rfl + (tc c_trn + local);
  *   the pixel is the mean of its samples (2115-2139, 2250-2263).
- * Random numbers come from one PCG32 stream (O'Neill 2014) per pixel and
- * launch, seeded from (seed, frame index, pixel index), in the order the
- * samples and their depth-first ray trees use them; the CUDA path tracer
- * draws the same stream in the same order.
+ * Random numbers are counter-based: every draw is a hash of (seed, frame
+ * index, pixel index, sample, the drawing node's position in the sample's
+ * ray tree, the draw's purpose), so any order of evaluation (depth first
+ * here, breadth first in the CUDA wavefront) draws the same numbers.  The
+ * hash is the SplitMix64 finaliser (Steele, Lea, Flood 2014) chained over
+ * the key; a node's position is its code in base 3: the camera ray 0, the
+ * diffuse, refracted and reflected children of node c are 3c + 1, 3c + 2,
+ * 3c + 3.
  */
 
 /* depth left at which roulette and the dielectric split start: the
@@ -1221,31 +1225,41 @@ int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
 #define PT_RR_DEPTH     (10 - 5)
 #define PT_SPLIT_DEPTH  (10 - 2)
 
-typedef struct pcg_s { uint64_t state, inc; } pcg_t;
-
-static uint32_t pcg_next(pcg_t *g)
+/* counter-based draws (see the header of this section) */
+static uint64_t mix64(uint64_t z)
 {
-    uint64_t old = g->state;
-    uint32_t xs, rot;
-    g->state = old * 6364136223846793005ull + g->inc;
-    xs = (uint32_t)(((old >> 18) ^ old) >> 27);
-    rot = (uint32_t)(old >> 59);
-    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
 }
 
-static void pcg_seed(pcg_t *g, uint64_t seed, int frame, uint64_t pixel)
+#define PT_GOLDEN   0x9E3779B97F4A7C15ull
+#define PT_CODEMUL  0xD6E8FEB86659FD93ull
+
+/* the key of sample n of a pixel */
+static uint64_t pt_sample_key(uint64_t seed, int frame, uint64_t pixel, int n)
 {
-    g->state = 0u;
-    g->inc = (pixel << 1) | 1u;
-    pcg_next(g);
-    g->state += seed ^ ((uint64_t)(uint32_t)frame * 0x9E3779B97F4A7C15ull);
-    pcg_next(g);
+    uint64_t kp = mix64(seed ^ mix64(((uint64_t)(uint32_t)frame << 40) ^ pixel));
+    return mix64(kp + (uint64_t)(uint32_t)n * PT_GOLDEN);
 }
 
-/* uniform in [0, 1) with 24 bits, exact in either precision */
-static real pcg_unit(pcg_t *g)
+/* the key of the node with tree code `code` in a sample */
+static uint64_t pt_node_key(uint64_t ks, uint32_t code)
 {
-    return (real)(int32_t)(pcg_next(g) >> 8) * (real)(1.0f / 16777216.0f);
+    return mix64(ks ^ ((uint64_t)code * PT_CODEMUL));
+}
+
+/* draw d of a node: uniform in [0, 1) with 24 bits, exact in either
+ * precision; draws 0 roulette, 1-2 bounce, 3 dielectric split, 4-5 the
+ * camera ray's jitter (node 0) */
+#define PT_DRAW_RR      0
+#define PT_DRAW_BOUNCE  1
+#define PT_DRAW_SPLIT   3
+#define PT_DRAW_JITTER  4
+static real pt_draw(uint64_t kn, int d)
+{
+    uint32_t u = (uint32_t)(mix64(kn + (uint64_t)(d + 1) * PT_GOLDEN) >> 40);
+    return (real)(int32_t)u * (real)(1.0f / 16777216.0f);
 }
 
 /* power series of sin and cos on [-pi, pi], evaluated with fused
@@ -1488,7 +1502,7 @@ static void pt_secondary(const scene_t *sc, const ray_t *r, const hit_t *h,
 }
 
 static void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
-                     pcg_t *g, real col[3]);
+                     uint64_t ks, uint32_t code, real col[3]);
 
 static void child(ray_t *cr, const hit_t *h, const real dir[3], int flags, int depth)
 {
@@ -1507,8 +1521,9 @@ static void child(ray_t *cr, const hit_t *h, const real dir[3], int flags, int d
 }
 
 static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
-                     pcg_t *g, real col[3])
+                     uint64_t ks, uint32_t code, real col[3])
 {
+    const uint64_t kn = pt_node_key(ks, code);
     const qr_srf *s = &sc->srf[h->srf];
     int side = h->side;
     int props = s->props[side];
@@ -1526,7 +1541,7 @@ static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
         real p = tex[0] > tex[1] ? tex[0] : tex[1];
         real u;
         p = p > tex[2] ? p : tex[2];
-        u = pcg_unit(g);
+        u = pt_draw(kn, PT_DRAW_RR);
         if (!(u < p)) dif = 0;
         else
         {
@@ -1536,14 +1551,14 @@ static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
     }
     if (dif)
     {
-        real u1 = pcg_unit(g);
-        real u2 = pcg_unit(g);
+        real u1 = pt_draw(kn, PT_DRAW_BOUNCE);
+        real u2 = pt_draw(kn, PT_DRAW_BOUNCE + 1);
         pt_bounce(nrm, u1, u2, ddir);
     }
     pt_secondary(sc, r, h, nrm, &o);
     if (o.split && o.trn && o.rfl && r->depth != 0 && r->depth <= PT_SPLIT_DEPTH)
     {
-        real u = pcg_unit(g);
+        real u = pt_draw(kn, PT_DRAW_SPLIT);
         real re = o.c_rfl / (o.c_trn + o.c_rfl);
         real pr = re * 0.5f;
         pr = pr + 0.25f;
@@ -1566,7 +1581,7 @@ static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
         ray_t cr;
         real lc[3];
         child(&cr, h, ddir, side, r->depth - 1);
-        pt_trace(sc, &cr, s->sec_off[side], s->sec_num[side], dmax, g, lc);
+        pt_trace(sc, &cr, s->sec_off[side], s->sec_num[side], dmax, ks, 3 * code + 1, lc);
         for (k = 0; k < 3; k++)
         {
             c[k] = lc[k] * m->l_dff;
@@ -1582,7 +1597,8 @@ static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
         {
             ray_t cr;
             child(&cr, h, o.nw, side | FLAG_PASS, r->depth - 1);
-            pt_trace(sc, &cr, s->sec_off[1 - side], s->sec_num[1 - side], dmax, g, tc);
+            pt_trace(sc, &cr, s->sec_off[1 - side], s->sec_num[1 - side], dmax, ks,
+                     3 * code + 2, tc);
             for (k = 0; k < 3; k++) tc[k] = tc[k] * o.c_trn;
         }
         for (k = 0; k < 3; k++) c[k] = tc[k] + c[k];
@@ -1594,7 +1610,7 @@ static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
         {
             ray_t cr;
             child(&cr, h, o.rw, side, r->depth - 1);
-            pt_trace(sc, &cr, s->sec_off[side], s->sec_num[side], dmax, g, rc);
+            pt_trace(sc, &cr, s->sec_off[side], s->sec_num[side], dmax, ks, 3 * code + 3, rc);
             for (k = 0; k < 3; k++) rc[k] = rc[k] * o.c_rfl;
         }
         for (k = 0; k < 3; k++) c[k] = rc[k] + c[k];
@@ -1603,7 +1619,7 @@ static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
 }
 
 static void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
-                     pcg_t *g, real col[3])
+                     uint64_t ks, uint32_t code, real col[3])
 {
     walk_t w;
     memset(&w, 0, sizeof(w));
@@ -1616,7 +1632,7 @@ static void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
         col[0] = col[1] = col[2] = 0.0f;
         return;
     }
-    pt_shade(sc, r, &w.best, dmax, g, col);
+    pt_shade(sc, r, &w.best, dmax, ks, code, col);
 }
 
 /* tent filter on [-1, 1] from one uniform number (2267-2342), halved */
@@ -1649,16 +1665,17 @@ int qr_oracle_pt(const qr_scene_desc *d, const qr_frame_params *fp, void *acc_,
     {
         for (x = 0; x < fp->x_res; x++)
         {
-            pcg_t g;
             real sum[3] = {0.0f, 0.0f, 0.0f}, mean[3];
             real *a = &acc[3 * ((size_t)y * fp->x_row + x)];
-            pcg_seed(&g, fp->seed, fp->frame_idx, (uint64_t)y * fp->x_res + x);
+            const uint64_t pixel = (uint64_t)y * fp->x_res + x;
             for (n = 0; n < spp; n++)
             {
                 real hs, vs, col[3];
                 ray_t r;
-                hs = pt_tent(pcg_unit(&g));
-                vs = pt_tent(pcg_unit(&g));
+                const uint64_t ks = pt_sample_key(fp->seed, fp->frame_idx, pixel, n0 + n);
+                const uint64_t k0 = pt_node_key(ks, 0);
+                hs = pt_tent(pt_draw(k0, PT_DRAW_JITTER));
+                vs = pt_tent(pt_draw(k0, PT_DRAW_JITTER + 1));
                 hs = (real)x + hs;
                 vs = (real)y + vs;
                 for (k = 0; k < 3; k++)
@@ -1675,7 +1692,7 @@ int qr_oracle_pt(const qr_scene_desc *d, const qr_frame_params *fp, void *acc_,
                 r.from = -1;
                 r.flags = 0;
                 r.depth = fp->depth;
-                pt_trace(&sc, &r, d->cam_off, d->cam_num, fp->depth, &g, col);
+                pt_trace(&sc, &r, d->cam_off, d->cam_num, fp->depth, ks, 0, col);
                 for (k = 0; k < 3; k++) sum[k] = sum[k] + col[k];
             }
             for (k = 0; k < 3; k++)

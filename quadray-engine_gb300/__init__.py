@@ -47,6 +47,8 @@ OPTS_NONE = (1 << 20) | (1 << 21) | (1 << 25)
 QR_OK = 0
 FP_LINEAR_WALK = 1        # qr_frame_params.flags: no BVH (same frame)
 FP_PIXEL_THREADS = 2      # qr_frame_params.flags: 4x AA, a thread per pixel (same frame)
+FP_PIXEL_PT = 4           # qr_frame_params.flags: path tracer, a thread per pixel instead
+                          # of the wavefront stages (same frame)
 
 
 class QrSceneDesc(ctypes.Structure):

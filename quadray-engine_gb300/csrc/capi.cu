@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 #include <algorithm>
 #include <mutex>
@@ -19,6 +20,7 @@
 #include "tracer.cuh"
 #include "accel.h"
 #include "anim.cuh"
+#include "wavefront.h"
 
 
 /* device update of an animated scene (qr_scene_anim_*) */
@@ -79,7 +81,27 @@ struct qr_ctx
     size_t       adevs_n;
     cudaEvent_t  aev[4];
     int          anext;
+    /* scratch of the wavefront path tracer (queues, node pool, sample and
+     * pixel sums), grown as frames need; one frame at a time uses it: a
+     * frame on another stream waits for the last one (wf_ev) */
+    std::mutex   wfmu;
+    void        *wf;
+    size_t       wf_bytes;
+    cudaEvent_t  wf_ev;
+    cudaStream_t wf_last;
+    int          sms;
+    long long    wf_paths;      /* paths of a chunk at most */
+    int          wf_q, wf_pool; /* queue rays, pool nodes a path */
 };
+
+/* the wavefront's chunks: 2^21 paths, queues of 2 rays and a pool of 8
+ * nodes a path: about 1.1 KB a path, 2.2 GB.  QR_WF_CAPS="paths,q,pool" in
+ * the environment of the process (read when a context is created) sets
+ * other capacities (tests use small ones to exercise chunks and the
+ * overflow path) */
+#define QR_WF_MAX_PATHS (2ll << 20)
+#define QR_WF_Q_PER_PATH 2
+#define QR_WF_POOL_PER_PATH 8
 
 static int fail(qr_ctx *ctx, int code, const char *what, cudaError_t e)
 {
@@ -110,7 +132,31 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
     ctx->adevs_n = 0;
     ctx->anext = 0;
     for (int k = 0; k < 4; k++) ctx->aev[k] = NULL;
+    ctx->wf = NULL;
+    ctx->wf_bytes = 0;
+    ctx->wf_ev = NULL;
+    ctx->wf_last = 0;
+    ctx->sms = 0;
+    ctx->wf_paths = QR_WF_MAX_PATHS;
+    ctx->wf_q = QR_WF_Q_PER_PATH;
+    ctx->wf_pool = QR_WF_POOL_PER_PATH;
+    {
+        const char *ev = getenv("QR_WF_CAPS");
+        long long a = 0;
+        int b = 0, c = 0;
+        if (ev != NULL && sscanf(ev, "%lld,%d,%d", &a, &b, &c) == 3 && a >= 32 &&
+            a <= (1ll << 24) && b >= 1 && b <= 16 && c >= 1 && c <= 64 &&
+            a * c <= (1ll << 28))         /* pool nodes << 2 stay in an int */
+        {
+            ctx->wf_paths = a;
+            ctx->wf_q = b;
+            ctx->wf_pool = c;
+        }
+    }
     cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount,
+                                                     device);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->wf_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->dfault, 4 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dfault, 0, 4 * sizeof(uint32_t), ctx->stream);
@@ -120,6 +166,7 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
         fprintf(stderr, "qr_ctx_create: %s\n", cudaGetErrorString(e));
         if (ctx->dfault) cudaFree(ctx->dfault);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        if (ctx->wf_ev) cudaEventDestroy(ctx->wf_ev);
         delete ctx;
         return QR_ERR_CUDA;
     }
@@ -146,6 +193,8 @@ extern "C" int qr_ctx_destroy(qr_ctx *ctx)
     if (ctx->adevs) cudaFreeHost(ctx->adevs);
     for (int k = 0; k < 4; k++)
         if (ctx->aev[k]) cudaEventDestroy(ctx->aev[k]);
+    if (ctx->wf) cudaFree(ctx->wf);
+    if (ctx->wf_ev) cudaEventDestroy(ctx->wf_ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return QR_OK;
@@ -805,12 +854,44 @@ static int ensure_acc(qr_ctx *ctx, size_t px)
     return QR_OK;
 }
 
+/* path-tracer samples: the wavefront stages over the context's scratch, or
+ * the per-pixel kernel (QR_FP_PIXEL_PT, or when the scratch cannot be had);
+ * both give the same frame */
+static cudaError_t launch_pt(qr_ctx *ctx, const qr_scene_slot *sl, const qr_frame_params *fp,
+                             float *acc, uint32_t *dev_frame, cudaStream_t stream)
+{
+    if (fp->flags & QR_FP_PIXEL_PT) return qr_launch_pt(sl->d, *fp, acc, dev_frame, stream);
+    std::lock_guard<std::mutex> lock(ctx->wfmu);
+    const qr_wf_caps caps = qr_wf_caps_for(*fp, ctx->wf_paths, ctx->wf_q, ctx->wf_pool);
+    const size_t need = qr_wf_bytes(caps);
+    if (ctx->wf_bytes < need)
+    {
+        /* cudaFree waits for the device: no frame still uses the old block */
+        if (ctx->wf) cudaFree(ctx->wf);
+        ctx->wf = NULL;
+        ctx->wf_bytes = 0;
+        if (cudaMalloc(&ctx->wf, need) != cudaSuccess)
+        {
+            ctx->wf = NULL;
+            cudaGetLastError();             /* clear the allocation error */
+            return qr_launch_pt(sl->d, *fp, acc, dev_frame, stream);
+        }
+        ctx->wf_bytes = need;
+    }
+    cudaError_t e = cudaSuccess;
+    if (ctx->wf_last != stream) e = cudaStreamWaitEvent(stream, ctx->wf_ev, 0);
+    if (e == cudaSuccess)
+        e = qr_wf_launch_pt(sl->d, *fp, acc, dev_frame, ctx->wf, caps, ctx->sms, stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->wf_ev, stream);
+    ctx->wf_last = stream;
+    return e;
+}
+
 /* Whitted frame, or path-tracer samples when fp->pt_on > 0 */
 static cudaError_t launch(qr_ctx *ctx, const qr_scene_slot *sl, const qr_frame_params *fp,
                           float *acc, uint32_t *dev_frame, cudaStream_t stream)
 {
-    (void)ctx;
-    if (fp->pt_on > 0) return qr_launch_pt(sl->d, *fp, acc, dev_frame, stream);
+    if (fp->pt_on > 0) return launch_pt(ctx, sl, fp, acc, dev_frame, stream);
     return qr_launch_whitted(sl->d, *fp, dev_frame, stream);
 }
 
@@ -844,7 +925,7 @@ extern "C" int qr_render_pt(qr_ctx *ctx, int scene_id, const qr_frame_params *fp
     if (fp->pt_on <= 0 || dev_acc == NULL || dev_frame == NULL) return QR_ERR_ARG;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess)
-        e = qr_launch_pt(sl->d, *fp, dev_acc, dev_frame, (cudaStream_t)stream);
+        e = launch_pt(ctx, sl, fp, dev_acc, dev_frame, (cudaStream_t)stream);
     if (e != cudaSuccess) return fail(ctx, QR_ERR_CUDA, "path-tracer launch", e);
     return QR_OK;
 }

@@ -144,6 +144,11 @@ struct rt_TEX
 #define RT_TEX(tag, val)                                                      \
     { RT_TEX_##tag, RT_COL(val), RT_NULL, 0, RT_NULL, 0, 0, 0 }
 
+/* a texture named by its BMP file, loaded when the scene is built (from
+ * the directory of QR_PATH_TEXTURES, else data/textures/) */
+#define RT_TEX_LOAD(tag, pstr)                                                \
+    { RT_TEX_##tag, RT_COL(0x0), (rt_pntr)pstr, 0, RT_NULL, 0, 0, 0 }
+
 #define RT_TEX_BIND(tag, ptex)                                                \
     { RT_TEX_##tag, RT_COL(0x0), *ptex, 0, RT_NULL, 0,                        \
       (rt_si32)RT_ARR_SIZE(**ptex), (rt_si32)RT_ARR_SIZE(*ptex) }

@@ -1,0 +1,532 @@
+/*
+ * wavefront.cu: the path tracer as wavefront stages over ray queues in HBM.
+ *
+ * The reference bins its path-tracer rays per surface, side and depth in
+ * SIMD buffers and shades a buffer once a full SIMD group waits in it, which
+ * keeps its lanes busy while paths end at different depths
+ * (core/tracer/tracer.cpp:783-1100 SLICE_FRAG / STORE_BUFF / SLICE_SPTR,
+ * 6686-6915, end-of-frame flush 7239-7375).  Here every level of the
+ * samples' ray trees is one stage over a compacted queue:
+ *
+ *   wf_gen    camera rays of a chunk of samples, pixel tiles of 8 x 4 in a
+ *             warp, appended to level 0's queue;
+ *   wf_step   level d: each ray walks the scene (nearest hit), the hit is
+ *             shaded (the node's random draws, emission, roulette,
+ *             cosine-weighted bounce, the dielectric split) into a node
+ *             record, and the node's children are appended to level d+1's
+ *             queue: the lanes of a warp count their children, a warp scan
+ *             gives each lane its offset and one atomic reserves the warp's
+ *             run (warp-vote compaction: level d+1 holds no dead lanes);
+ *   wf_fold   levels from the deepest up: a node's colour from its
+ *             children's colours (written into its record by their fold),
+ *             in the reference's order colour = rc c_rfl + (tc c_trn +
+ *             (bounce l_dff tex + emission)), handed to its parent's record
+ *             or, at level 0, to the sample's slot;
+ *   wf_accum  each pixel adds its samples of the chunk in sample order;
+ *   wf_final  running sums, mean, clamp and pack (as pt_kernel).
+ *
+ * Random draws are counter-based (tracer_dev.cuh pt_node_key / pt_draw), so
+ * breadth-first evaluation draws what the depth-first oracle draws and the
+ * frame is the per-pixel kernel's (pt_kernel) bit for bit.
+ *
+ * Chunks.  A frame's samples are numbered sample-major (path q = s * Ppad +
+ * t, t the pixel's place in the tile order over Ppad padded pixels) and cut
+ * into chunks of at most cap_paths paths, rendered one after the other; a
+ * pixel's samples are summed in ascending s whatever the chunking.  Queues
+ * and the node pool have fixed capacities: a level whose children would not
+ * fit sets the overflow word; every later stage of the frame then does
+ * nothing and wf_fallback renders the whole frame with the per-pixel kernel
+ * (the same frame).  No host synchronisation is needed: every kernel reads
+ * its level's count from device memory and strides over it.
+ */
+#include "tracer_dev.cuh"
+#include "wavefront.h"
+
+namespace qr_dev
+{
+
+/* a queued ray, 80 bytes */
+struct WRay
+{
+    float4 o;       /* origin, t_min */
+    float4 d;       /* direction, t_max */
+    float4 p;       /* originating surface's local hit, surface (int bits) */
+    int4   m;       /* flags | depth << 8, owner, tree code, list offset */
+    int4   k;       /* sample key (low, high), list length, pixel tile place */
+};
+
+/* a shaded node (or a miss), 96 bytes; its children write cl / ct / cr */
+struct WNode
+{
+    float4 t;       /* tex scaled by roulette, l_dff (diffuse child) */
+    float4 e;       /* emission, c_trn */
+    float4 f;       /* c_rfl, bits (int), owner (int), - */
+    float4 cl;      /* the diffuse child's colour */
+    float4 ct;      /* the refracted child's colour */
+    float4 cr;      /* the reflected child's colour */
+};
+
+#define WN_HIT      1
+#define WN_DIF      2
+#define WN_TRN      4
+#define WN_RFL      8
+#define WN_SPAWN    16
+
+/* owners: level-0 rays own a sample slot of the chunk; deeper rays own a
+ * child slot (0 diffuse, 1 refracted, 2 reflected) of a node in the pool */
+__device__ __forceinline__ int owner_of(int node, int slot) { return (node << 2) | slot; }
+
+/* the device-side control block of a frame */
+struct WCtl
+{
+    int cnt[QR_MAX_DEPTH + 2];      /* rays of each level in this chunk */
+    int off[QR_MAX_DEPTH + 2];      /* first pool node of each level */
+    int next[QR_MAX_DEPTH + 2];     /* rays of each level handed to warps */
+    int overflow;                   /* a queue or the pool ran full */
+    int pad[3];
+};
+
+#ifndef QR_WF_MIN_BLOCKS
+#define QR_WF_MIN_BLOCKS 6
+#endif
+
+/* exclusive warp scan of small counts; returns the warp's total in *tot */
+__device__ __forceinline__ int warp_excl_scan(int v, int *tot)
+{
+    const int lane = threadIdx.x & 31;
+    int x = v;
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    *tot = __shfl_sync(0xFFFFFFFFu, x, 31);
+    return x - v;
+}
+
+/* reserve the warp's run of `total` entries in a queue counter */
+__device__ __forceinline__ int warp_reserve(int *counter, int total)
+{
+    int base = 0;
+    if ((threadIdx.x & 31) == 0 && total > 0) base = atomicAdd(counter, total);
+    return __shfl_sync(0xFFFFFFFFu, base, 0);
+}
+
+__device__ __forceinline__ void put_ray(WRay *q, int i, const float org[3], float t_min,
+                                        const float dir[3], float t_max, const float phit[3],
+                                        int from, int flags, int depth, int owner,
+                                        uint32_t code, int off, int num,
+                                        unsigned long long ks, int tp)
+{
+    WRay r;
+    r.o = make_float4(org[0], org[1], org[2], t_min);
+    r.d = make_float4(dir[0], dir[1], dir[2], t_max);
+    r.p = make_float4(phit[0], phit[1], phit[2], __int_as_float(from));
+    r.m = make_int4(flags | (depth << 8), owner, (int)code, off);
+    r.k = make_int4((int)(uint32_t)ks, (int)(uint32_t)(ks >> 32), num, tp);
+    q[i] = r;
+}
+
+/* pixel of tile place t: tiles of 8 x 4 pixels, tile rows of tx tiles */
+__device__ __forceinline__ void tile_pixel(int t, int tx, int &x, int &y)
+{
+    const int tile = t >> 5, in = t & 31;
+    x = (tile % tx) * 8 + (in & 7);
+    y = (tile / tx) * 4 + (in >> 3);
+}
+
+/* level 0: camera rays of paths [c0, c1) */
+__global__ void __launch_bounds__(128)
+wf_gen(const qr_frame_params P, long long c0, long long c1, int ppad, int tx,
+       WRay *q0, WCtl *ctl)
+{
+    if (ctl->overflow) return;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q00 = c0 + (((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll);
+         q00 < c1; q00 += stride)
+    {
+        const long long q = q00 + (threadIdx.x & 31);
+        int x = 0, y = 0, ok = 0, s = 0, t = 0;
+        if (q < c1)
+        {
+            s = (int)(q / ppad);
+            t = (int)(q - (long long)s * ppad);
+            tile_pixel(t, tx, x, y);
+            ok = x < P.x_res && y < P.y_res;
+        }
+        int tot;
+        const int ex = warp_excl_scan(ok, &tot);
+        const int base = warp_reserve(&ctl->cnt[0], tot);
+        if (!ok) continue;
+        const unsigned long long pixel = (unsigned long long)y * P.x_res + x;
+        const unsigned long long ks = pt_sample_key(P.seed, P.frame_idx, pixel,
+                                                    (int)P.pts_c + s);
+        Ray r;
+        pt_camera_ray(P, x, y, ks, r, NULL);
+        put_ray(q0, base + ex, r.org, r.t_min, r.dir, r.t_max, r.phit, r.from, r.flags,
+                r.depth, (int)(q - c0), 0u, -1, 0, ks, t);
+    }
+}
+
+/* level d: walk, shade, append the children to level d + 1 */
+__global__ void __launch_bounds__(128, QR_WF_MIN_BLOCKS)
+wf_step(const qr_dscene S, const qr_frame_params P, int d, const WRay *__restrict__ qin,
+        WRay *qout, WNode *pool, WCtl *ctl, int cap_q, int cap_pool)
+{
+    if (ctl->overflow) return;
+    const int n = ctl->cnt[d];
+    const int base = d == 0 ? 0 : ctl->off[d];
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->off[d + 1] = base + n;
+    const int lane = threadIdx.x & 31;
+    /* warps take runs of 32 rays as they come free (rays differ widely in
+     * cost) */
+    #pragma unroll 1
+    for (;;)
+    {
+        int i0 = 0;
+        if (lane == 0) i0 = atomicAdd(&ctl->next[d], 32);
+        i0 = __shfl_sync(0xFFFFFFFFu, i0, 0);
+        if (i0 >= n) break;
+        const int i = i0 + lane;
+        int nch = 0, dif = 0, trn = 0, rfl = 0, side = 0, srf = -1, depth = 0;
+        float hit[3], loc[3], ddir[3], nw[3], rw[3];
+        uint32_t code = 0u;
+        unsigned long long ks = 0ull;
+        int tp = 0;
+        if (i < n)
+        {
+            const WRay q = qin[i];
+            Ray r;
+            r.org[0] = q.o.x; r.org[1] = q.o.y; r.org[2] = q.o.z; r.t_min = q.o.w;
+            r.dir[0] = q.d.x; r.dir[1] = q.d.y; r.dir[2] = q.d.z; r.t_max = q.d.w;
+            r.phit[0] = q.p.x; r.phit[1] = q.p.y; r.phit[2] = q.p.z;
+            r.from = __float_as_int(q.p.w);
+            r.flags = q.m.x & 255;
+            r.depth = q.m.x >> 8;
+            const int owner = q.m.y;
+            code = (uint32_t)q.m.z;
+            const int off = q.m.w >= 0 ? q.m.w : S.cam_off;
+            const int num = q.m.w >= 0 ? q.k.z : S.cam_num;
+            ks = (unsigned long long)(uint32_t)q.k.x |
+                 ((unsigned long long)(uint32_t)q.k.y << 32);
+            tp = q.k.w;
+            Walk w;
+            w.fault = 0;
+            w.shadow = 0;
+            w.occluded = 0;
+            w.tbuf = r.t_max;
+            w.bestp = -1;
+            w.best.srf = -1;
+            walk(S, P, r, off, num, w, NULL);
+            WNode &N = pool[base + i];
+            if (w.fault)
+            {
+                int x, y;
+                tile_pixel(tp, (P.x_res + 7) / 8, x, y);
+                note_fault(S, w.fault, x, y);
+                w.best.srf = -1;
+            }
+            if (w.best.srf < 0)
+            {
+                N.f = make_float4(0.0f, __int_as_float(0), __int_as_float(owner), 0.0f);
+            }
+            else
+            {
+                const Hit h = w.best;
+                PtPend pp;
+                dif = pt_begin(S, P, r, h, pp, ks, code, ddir, NULL);
+                const int bits = pt_bits(pp);
+                trn = (bits & PT_TRN) != 0;
+                rfl = (bits & PT_RFL) != 0;
+                const int spawn = r.depth != 0;
+                side = h.side;
+                srf = h.srf;
+                depth = r.depth;
+                #pragma unroll
+                for (int k = 0; k < 3; k++) { hit[k] = h.hit[k]; loc[k] = h.loc[k]; }
+                if (spawn && trn) { nw[0] = pp.n.x; nw[1] = pp.n.y; nw[2] = pp.n.z; }
+                if (spawn && rfl) { rw[0] = pp.m.x; rw[1] = pp.m.y; rw[2] = pp.m.z; }
+                /* the node: pt_begin's fields, repacked */
+                if (dif) N.t = pp.a;
+                N.e = make_float4(dif ? pp.b.x : pp.a.x, dif ? pp.b.y : pp.a.y,
+                                  dif ? pp.b.z : pp.a.z, (dif || trn) ? pp.b.w : 0.0f);
+                N.f = make_float4(rfl ? pp.h.w : 0.0f,
+                                  __int_as_float(WN_HIT | (dif ? WN_DIF : 0) |
+                                                 (trn ? WN_TRN : 0) | (rfl ? WN_RFL : 0) |
+                                                 (spawn ? WN_SPAWN : 0)),
+                                  __int_as_float(owner), 0.0f);
+                nch = dif + (spawn && trn) + (spawn && rfl);
+                trn = spawn && trn;
+                rfl = spawn && rfl;
+            }
+        }
+        int tot;
+        const int ex = warp_excl_scan(nch, &tot);
+        int qb = warp_reserve(&ctl->cnt[d + 1], tot);
+        /* the children of level d + 1 take pool nodes base + n + [0, cnt) */
+        if (qb + tot > cap_q || base + n + qb + tot > cap_pool)
+        {
+            if (lane == 0 && tot > 0) atomicExch(&ctl->overflow, 1);
+            continue;
+        }
+        if (nch == 0) continue;
+        const qr_srf *__restrict__ s = &S.srf[srf];
+        int at = qb + ex;
+        const int node = base + i;
+        const float fmax = FLT_MAX;
+        if (dif)
+        {
+            put_ray(qout, at++, hit, 0.0f, ddir, fmax, loc, srf, side, depth - 1,
+                    owner_of(node, 0), 3u * code + 1u, __ldg(&s->sec_off[side]),
+                    __ldg(&s->sec_num[side]), ks, tp);
+        }
+        if (trn)
+        {
+            put_ray(qout, at++, hit, 0.0f, nw, fmax, loc, srf, side | FLAG_PASS, depth - 1,
+                    owner_of(node, 1), 3u * code + 2u, __ldg(&s->sec_off[1 - side]),
+                    __ldg(&s->sec_num[1 - side]), ks, tp);
+        }
+        if (rfl)
+        {
+            put_ray(qout, at++, hit, 0.0f, rw, fmax, loc, srf, side, depth - 1,
+                    owner_of(node, 2), 3u * code + 3u, __ldg(&s->sec_off[side]),
+                    __ldg(&s->sec_num[side]), ks, tp);
+        }
+    }
+}
+
+/* level d, deepest first: the node's colour to its owner */
+__global__ void __launch_bounds__(128)
+wf_fold(int d, WNode *pool, float4 *samples, const WCtl *ctl)
+{
+    if (ctl->overflow) return;
+    const int n = ctl->cnt[d];
+    const int base = d == 0 ? 0 : ctl->off[d];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const WNode &N = pool[base + i];
+        const float4 f = N.f;
+        const int bits = __float_as_int(f.y), owner = __float_as_int(f.z);
+        float c[3] = {0.0f, 0.0f, 0.0f};
+        if (bits & WN_HIT)
+        {
+            const float4 e = N.e;
+            if (bits & WN_DIF)
+            {
+                const float4 t = N.t, cl = N.cl;
+                float v;
+                v = cl.x * t.w; c[0] = v * t.x;
+                v = cl.y * t.w; c[1] = v * t.y;
+                v = cl.z * t.w; c[2] = v * t.z;
+            }
+            c[0] = c[0] + e.x;
+            c[1] = c[1] + e.y;
+            c[2] = c[2] + e.z;
+            if (bits & WN_TRN)
+            {
+                float tc[3] = {0.0f, 0.0f, 0.0f};
+                if (bits & WN_SPAWN)
+                {
+                    const float4 ct = N.ct;
+                    tc[0] = ct.x * e.w; tc[1] = ct.y * e.w; tc[2] = ct.z * e.w;
+                }
+                c[0] = tc[0] + c[0]; c[1] = tc[1] + c[1]; c[2] = tc[2] + c[2];
+            }
+            if (bits & WN_RFL)
+            {
+                float rc[3] = {0.0f, 0.0f, 0.0f};
+                if (bits & WN_SPAWN)
+                {
+                    const float4 cr = N.cr;
+                    rc[0] = cr.x * f.x; rc[1] = cr.y * f.x; rc[2] = cr.z * f.x;
+                }
+                c[0] = rc[0] + c[0]; c[1] = rc[1] + c[1]; c[2] = rc[2] + c[2];
+            }
+        }
+        const float4 cv = make_float4(c[0], c[1], c[2], 0.0f);
+        if (d == 0)
+        {
+            samples[owner] = cv;
+        }
+        else
+        {
+            WNode &Pn = pool[owner >> 2];
+            const int slot = owner & 3;
+            if (slot == 0) Pn.cl = cv;
+            else if (slot == 1) Pn.ct = cv;
+            else Pn.cr = cv;
+        }
+    }
+}
+
+/* each pixel adds its samples of paths [c0, c1) in sample order */
+__global__ void __launch_bounds__(128)
+wf_accum(const qr_frame_params P, long long c0, long long c1, int ppad, int tx,
+         const float4 *__restrict__ samples, float4 *sums, const WCtl *ctl)
+{
+    if (ctl->overflow) return;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ppad; t += gridDim.x * blockDim.x)
+    {
+        int x, y;
+        tile_pixel(t, tx, x, y);
+        if (x >= P.x_res || y >= P.y_res) continue;
+        /* samples s with c0 <= s * ppad + t < c1 */
+        long long s0 = c0 - t <= 0 ? 0 : (c0 - t + ppad - 1) / ppad;
+        const size_t px = (size_t)y * P.x_res + x;
+        float4 a = sums[px];
+        int any = 0;
+        for (long long s = s0; s * ppad + t < c1; s++)
+        {
+            const float4 v = samples[s * ppad + t - c0];
+            a.x = a.x + v.x;
+            a.y = a.y + v.y;
+            a.z = a.z + v.z;
+            any = 1;
+        }
+        if (any) sums[px] = a;
+    }
+}
+
+/* the running sums and the frame (pt_pixel_seq's end) */
+__global__ void __launch_bounds__(128)
+wf_final(const qr_frame_params P, const float4 *__restrict__ sums, float *acc,
+         uint32_t *frame, const WCtl *ctl)
+{
+    if (ctl->overflow) return;
+    const int npx = P.x_res * P.y_res;
+    const int n0 = (int)P.pts_c, spp = P.pt_on;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x)
+    {
+        const int y = i / P.x_res, x = i - y * P.x_res;
+        const float4 sv = sums[i];
+        const float sum[3] = {sv.x, sv.y, sv.z};
+        float *a = acc + 3 * ((size_t)y * P.x_row + x);
+        float mean[3];
+        #pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            a[k] = (n0 == 0 ? 0.0f : a[k]) + sum[k];
+            mean[k] = fdiv(a[k], (float)(n0 + spp));
+            mean[k] = clamp1(mean[k]);
+        }
+        frame[(size_t)y * P.x_row + x] = pack(P, mean);
+    }
+}
+
+/* the whole frame by the per-pixel kernel's path, when a queue overflowed */
+__global__ void __launch_bounds__(128, QR_PT_MIN_BLOCKS)
+wf_fallback(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *frame,
+            const WCtl *ctl)
+{
+    if (!ctl->overflow) return;
+    const int x = tile_x(), y = tile_y();
+    if (x >= P.x_res || y >= P.y_res) return;
+    pt_pixel_seq(S, P, x, y, acc, frame, NULL);
+}
+
+} /* namespace qr_dev */
+
+using namespace qr_dev;
+
+size_t qr_wf_bytes(const qr_wf_caps &c)
+{
+    return sizeof(WCtl) + 2 * (size_t)c.cap_q * sizeof(WRay) +
+           (size_t)c.cap_pool * sizeof(WNode) + (size_t)c.cap_paths * sizeof(float4) +
+           (size_t)c.cap_px * sizeof(float4) + 5 * 256;
+}
+
+qr_wf_caps qr_wf_caps_for(const qr_frame_params &fp, long long max_paths, int q_per_path,
+                          int pool_per_path)
+{
+    qr_wf_caps c;
+    const int tx = (fp.x_res + 7) / 8, ty = (fp.y_res + 3) / 4;
+    const long long ppad = (long long)tx * ty * 32;
+    long long paths = ppad * (long long)fp.pt_on;
+    if (paths > max_paths) paths = max_paths;
+    if (paths < 32) paths = 32;
+    c.cap_paths = paths;
+    c.cap_q = (long long)q_per_path * paths;
+    c.cap_pool = (long long)pool_per_path * paths;
+    if (c.cap_q < paths) c.cap_q = paths;
+    if (c.cap_pool < paths) c.cap_pool = paths;
+    c.cap_px = (long long)fp.x_res * fp.y_res;
+    return c;
+}
+
+static inline size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *acc,
+                            uint32_t *frame, void *scratch, const qr_wf_caps &caps,
+                            int sms, cudaStream_t stream)
+{
+    unsigned char *b = (unsigned char *)scratch;
+    WCtl *ctl = (WCtl *)b;
+    b += al256(sizeof(WCtl));
+    WRay *qa = (WRay *)b;
+    b += al256((size_t)caps.cap_q * sizeof(WRay));
+    WRay *qb = (WRay *)b;
+    b += al256((size_t)caps.cap_q * sizeof(WRay));
+    WNode *pool = (WNode *)b;
+    b += al256((size_t)caps.cap_pool * sizeof(WNode));
+    float4 *samples = (float4 *)b;
+    b += al256((size_t)caps.cap_paths * sizeof(float4));
+    float4 *sums = (float4 *)b;
+
+    const int tx = (fp.x_res + 7) / 8, ty = (fp.y_res + 3) / 4;
+    const int ppad = tx * ty * 32;
+    const long long total = (long long)ppad * fp.pt_on;
+    const int levels = fp.depth + 1;
+    /* every kernel strides over its level: as many blocks as are resident */
+    static int step_per_sm = 0;
+    if (step_per_sm == 0)
+    {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, wf_step, 128, 0) != cudaSuccess ||
+            nb <= 0)
+            nb = QR_WF_MIN_BLOCKS;
+        step_per_sm = nb;
+    }
+    const int blocks = sms * 8;             /* memory-bound stages: 8 blocks of 128 a SM */
+    const int sblocks = sms * step_per_sm;
+    cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(WCtl), stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(sums, 0, (size_t)fp.x_res * fp.y_res * sizeof(float4), stream);
+    for (long long c0 = 0; c0 < total && e == cudaSuccess; c0 += caps.cap_paths)
+    {
+        const long long c1 = c0 + caps.cap_paths < total ? c0 + caps.cap_paths : total;
+        /* counts of this chunk (the overflow word stays) */
+        e = cudaMemsetAsync(ctl, 0, offsetof(WCtl, overflow), stream);   /* cnt, off, next */
+        if (e != cudaSuccess) break;
+        wf_gen<<<blocks, 128, 0, stream>>>(fp, c0, c1, ppad, tx, qa, ctl);
+        for (int d = 0; d < levels; d++)
+        {
+            WRay *qi = (d & 1) ? qb : qa, *qo = (d & 1) ? qa : qb;
+            wf_step<<<sblocks, 128, 0, stream>>>(sc, fp, d, qi, qo, pool, ctl,
+                                                 (int)caps.cap_q, (int)caps.cap_pool);
+        }
+        for (int d = levels - 1; d >= 0; d--)
+            wf_fold<<<blocks, 128, 0, stream>>>(d, pool, samples, ctl);
+        wf_accum<<<blocks, 128, 0, stream>>>(fp, c0, c1, ppad, tx, samples, sums, ctl);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+    {
+        wf_final<<<blocks, 128, 0, stream>>>(fp, sums, acc, frame, ctl);
+        const dim3 block(32, 4);
+        const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
+                        (fp.y_res + 2 * QR_TILE_H - 1) / (2 * QR_TILE_H));
+        wf_fallback<<<grid, block, 0, stream>>>(sc, fp, acc, frame, ctl);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+int qr_wf_overflowed(const void *scratch, cudaStream_t stream, int *out)
+{
+    const WCtl *ctl = (const WCtl *)scratch;
+    cudaError_t e = cudaMemcpyAsync(out, &ctl->overflow, sizeof(int), cudaMemcpyDeviceToHost,
+                                    stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    return e == cudaSuccess ? 0 : -1;
+}

@@ -1,0 +1,35 @@
+/*
+ * wavefront.h: host side of the wavefront path tracer (wavefront.cu).
+ */
+#ifndef QR_WAVEFRONT_H
+#define QR_WAVEFRONT_H
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include "tracer.cuh"
+
+/* capacities of a frame's scratch: paths of a chunk, rays of a level's
+ * queue, nodes of a chunk's pool, pixels of the frame */
+struct qr_wf_caps
+{
+    long long cap_paths, cap_q, cap_pool, cap_px;
+};
+
+/* the capacities for a frame: chunks of at most max_paths paths, queues
+ * of q_per_path rays and a pool of pool_per_path nodes a path of a chunk
+ * (at least one each) */
+qr_wf_caps qr_wf_caps_for(const qr_frame_params &fp, long long max_paths, int q_per_path,
+                          int pool_per_path);
+/* device bytes of a scratch block with these capacities */
+size_t qr_wf_bytes(const qr_wf_caps &caps);
+/* path-trace fp.pt_on samples a pixel into acc / frame (as qr_launch_pt)
+ * with the wavefront stages, using `scratch` (qr_wf_bytes(caps) bytes, 256
+ * aligned, not shared with work in flight); `sms` = the device's SMs */
+cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *acc,
+                            uint32_t *frame, void *scratch, const qr_wf_caps &caps,
+                            int sms, cudaStream_t stream);
+/* whether the last frame rendered with this scratch overflowed its queues
+ * (and was rendered by the per-pixel kernel instead); synchronises stream */
+int qr_wf_overflowed(const void *scratch, cudaStream_t stream, int *out);
+
+#endif /* QR_WAVEFRONT_H */
