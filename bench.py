@@ -641,6 +641,9 @@ def run_frames(args, wl, rank, world, dist, local):
         returns the device update's parameters and the frame parameters"""
         if not wl["anim"]:
             return None, fixed
+        # the in-place upload rewrites the scene's block: the previous
+        # frame's render (on another stream) must have finished reading it
+        torch.cuda.synchronize()
         j0 = REBUILD_EVERY * (j // REBUILD_EVERY)
         desc, _ = dflat.update(16 * j0, depth)
         table = dflat.anim_table()
@@ -652,13 +655,16 @@ def run_frames(args, wl, rank, world, dist, local):
         assert rc == 0, rc
         return prm, pt_params(dflat.frame_params())
 
-    frame = torch.empty((wl["h"], wl["w"] + 64), dtype=torch.int32, device="cuda")
-    acc = torch.empty((wl["h"], wl["w"] + 64, 3), dtype=torch.float32, device="cuda")
+    x_row = int(params.x_row)           # the same for every frame of the workload
+    assert x_row >= wl["w"] and params.y_res == wl["h"]
+    frame = torch.empty((wl["h"], x_row), dtype=torch.int32, device="cuda")
+    acc = torch.empty((wl["h"], x_row, 3), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
 
     def step(prm, fp):
+        assert fp.x_row == x_row and fp.y_res == wl["h"]
         if prm is not None:
             ctx.anim_update(dsid[0], prm, sp)
         if spp:
@@ -670,7 +676,6 @@ def run_frames(args, wl, rank, world, dist, local):
         prm, fp = prepare(j)
         step(prm, fp)
     torch.cuda.synchronize()
-    assert fp.x_row <= wl["w"] + 64
 
     if dist is not None:
         dist.barrier()
