@@ -14,7 +14,11 @@
  *
  * usage: ref_driver KIND SEED NQ W H FSAA FRAMES FLAGS OPTS OUT [THREADS]
  *                   [DEPTH] [DUMP]
- *   KIND    1 plain Whitted, 2 animated, 3 path tracer
+ *   KIND    1 plain Whitted, 2 animated, 3 path tracer; 101-118 the
+ *           reference's own test scene 1-18 (test/scenes/scn_testNN.h, as
+ *           test/core_test.cpp:193-475 builds them; SEED, NQ and FLAGS are
+ *           ignored), 201-218 the same scene path traced (one sample a
+ *           frame, FRAMES frames accumulated: the last frame is the mean)
  *   FSAA    0 none, 2 4x
  *   FRAMES  frames rendered at t = i*16 ms; all are written (PT: accumulated)
  *   FLAGS   scenegen flags (1 = hit-ID materials)
@@ -41,6 +45,38 @@
 #undef protected
 
 #include "../quadray-engine_gb300/csrc/scenegen.hpp"
+
+/* the reference's test scenes (test/scenes, found on the include path) */
+#include "scn_test01.h"
+#include "scn_test02.h"
+#include "scn_test03.h"
+#include "scn_test04.h"
+#include "scn_test05.h"
+#include "scn_test06.h"
+#include "scn_test07.h"
+#include "scn_test08.h"
+#include "scn_test09.h"
+#include "scn_test10.h"
+#include "scn_test11.h"
+#include "scn_test12.h"
+#include "scn_test13.h"
+#include "scn_test14.h"
+#include "scn_test15.h"
+#include "scn_test16.h"
+#include "scn_test17.h"
+#include "scn_test18.h"
+
+static rt_SCENE *test_scene(int n)
+{
+    static rt_SCENE *const all[18] = {
+        &scn_test01::sc_root, &scn_test02::sc_root, &scn_test03::sc_root,
+        &scn_test04::sc_root, &scn_test05::sc_root, &scn_test06::sc_root,
+        &scn_test07::sc_root, &scn_test08::sc_root, &scn_test09::sc_root,
+        &scn_test10::sc_root, &scn_test11::sc_root, &scn_test12::sc_root,
+        &scn_test13::sc_root, &scn_test14::sc_root, &scn_test15::sc_root,
+        &scn_test16::sc_root, &scn_test17::sc_root, &scn_test18::sc_root};
+    return n >= 1 && n <= 18 ? all[n - 1] : NULL;
+}
 
 static rt_pntr sys_alloc(rt_size size)
 {
@@ -230,7 +266,15 @@ int main(int argc, char **argv)
             return 1;
         }
     }
-    qr_gen::Scene *sc = qr_gen::build(kind, seed, nq, flags);
+    const int ref_scene = kind > 200 ? kind - 200 : kind > 100 ? kind - 100 : 0;
+    const int ref_pt = kind > 200;
+    qr_gen::Scene *sc = ref_scene ? NULL : qr_gen::build(kind, seed, nq, flags);
+    rt_SCENE *scn = ref_scene ? test_scene(ref_scene) : &sc->scn;
+    if (scn == NULL)
+    {
+        fprintf(stderr, "unknown scene kind %d\n", kind);
+        return 2;
+    }
 
     rt_Platform *pfm;
     if (thnum > 1)
@@ -247,12 +291,12 @@ int main(int argc, char **argv)
     double tsum = 0.0;
     try
     {
-        rt_Scene *scene = new(pfm) rt_Scene(&sc->scn, w, h, w, RT_NULL, pfm);
+        rt_Scene *scene = new(pfm) rt_Scene(scn, w, h, w, RT_NULL, pfm);
         g_cur = scene;
         if (strcmp(opts, "none") == 0) scene->set_opts(RT_OPTS_NONE);
         else if (strcmp(opts, "full") == 0) scene->set_opts(RT_OPTS_FULL);
         else scene->set_opts((rt_si32)strtoul(opts, NULL, 0));
-        if (kind == QR_SCN_PT) scene->set_pton(1);
+        if (kind == QR_SCN_PT || ref_pt) scene->set_pton(1);
         scene->depth = depth;
 
         /* QR_ACTIONS="a,b,...": camera action a_k (object.h:47-62) through
@@ -322,6 +366,6 @@ int main(int argc, char **argv)
     fclose(fo);
     fprintf(stderr, "ms_per_frame %.3f threads %d\n", tsum / frames, thnum);
     delete pfm;
-    delete sc;
+    if (sc != NULL) delete sc;
     return 0;
 }

@@ -94,6 +94,39 @@ def oracle_pt_par(oracle, desc, params, y0, y1, threads=None):
     return out[:, :params.x_res], acc[:, :params.x_res]
 
 
+def load_qrsf(qr, raw):
+    """a flattened scene written by tests/golden/scene_fixture.cpp (QRSF):
+    returns (QrSceneDesc, QrFrameParams, arrays the descriptor points into)"""
+    b = bytes(raw)
+    hdr = np.frombuffer(b[:40], dtype="<i4")
+    assert hdr[0] == 0x46535251 and hdr[1] == 1
+    ns, nm, nl, ne, nle, nt, co, cn = (int(x) for x in hdr[2:])
+    off, arrs = 40, []
+    for n, sz in ((ns, 256), (nm, 112), (nl, 48), (ne, 16), (nle, 16), (nt, 4)):
+        a = np.frombuffer(b[off:off + n * sz], dtype=np.uint8).copy()
+        arrs.append(a if a.size else np.zeros(16, dtype=np.uint8))
+        off += n * sz
+    fp = qr.QrFrameParams.from_buffer_copy(b[off:off + ctypes.sizeof(qr.QrFrameParams)])
+    d = qr.QrSceneDesc()
+    d.nsrf, d.nmat, d.nlgt, d.nelem, d.nlelem, d.ntex = ns, nm, nl, ne, nle, nt
+    d.cam_off, d.cam_num = co, cn
+    d.srf, d.mat, d.lgt, d.elems, d.lelems, d.texels = (a.ctypes.data for a in arrs)
+    return d, fp, arrs
+
+
+def frame_cmp(a, b, t_diff=3):
+    """the reference's own frame comparison (test/core_test.cpp:98-148): a
+    pixel differs when a channel differs by more than t_diff, and a
+    differing pixel counts only when one of its 8 neighbours differs too;
+    returns the count of such pixels"""
+    bad = max_channel_diff(a, b) > t_diff
+    h, w = bad.shape
+    p = np.pad(bad, 1)
+    nb = sum(p[1 + dy:1 + dy + h, 1 + dx:1 + dx + w]
+             for dy in (-1, 0, 1) for dx in (-1, 0, 1) if dy or dx)
+    return int((bad & (nb > 0)).sum())
+
+
 def channels(frame):
     f = frame.astype(np.int64)
     return np.stack([(f >> 16) & 255, (f >> 8) & 255, f & 255], axis=-1)

@@ -148,13 +148,119 @@ def run_case(name, case):
     return data
 
 
+# ---- the reference's own regression scenes (test/scenes/scn_test01-18.h)
+#
+# Each fixture holds the reference's frame of the scene (rt_Scene::render
+# with RT_OPTS_NONE, as test/core_test.cpp:993 renders its first run, and
+# with RT_OPTS_FULL, its second run at :1033) and the scene as this
+# repository's host engine flattens it from the unchanged scene header
+# (oracle/_ref/scene_fixture, built from tests/golden/scene_fixture.cpp):
+# the records the tests render.  The library's one image texture (the crate
+# of data/objects, named tex_crate01.bmp when images are not compiled in) is
+# replaced on both sides by a synthetic image of this script, so no image
+# data of the reference enters the fixtures.  Scenes 17 and 18 are the
+# reference's path-tracer scenes: their fixtures hold the mean of 256
+# one-sample frames of the reference's path tracer.
+SCN_W, SCN_H = 400, 240
+PT_SCENES = {17: (80, 48, 256), 18: (80, 48, 256)}
+FIXTURE = os.path.join(ROOT, "oracle", "_ref", "scene_fixture")
+
+
+def write_bmp24(path, w, h, rgb):
+    """24-bit bottom-up BMP of rgb[h][w] (XRGB integers)"""
+    row = (w * 3 + 3) & ~3
+    img = row * h
+    hd = bytearray(54)
+    hd[0:2] = b"BM"
+    for at, v in ((2, 54 + img), (10, 54), (14, 40), (18, w), (22, h), (34, img)):
+        hd[at:at + 4] = int(v).to_bytes(4, "little")
+    hd[26] = 1
+    hd[28] = 24
+    body = bytearray()
+    for y in range(h - 1, -1, -1):
+        line = bytearray()
+        for x in range(w):
+            c = int(rgb[y][x])
+            line += bytes((c & 255, (c >> 8) & 255, (c >> 16) & 255))
+        body += line + bytes(row - len(line))
+    with open(path, "wb") as f:
+        f.write(bytes(hd) + bytes(body))
+
+
+def crate_standin(n=64):
+    """a synthetic plank pattern standing in for the crate image"""
+    rgb = np.zeros((n, n), dtype=np.int64)
+    for y in range(n):
+        for x in range(n):
+            plank = (y * 4) // n
+            edge = x < 3 or x >= n - 3 or y < 3 or y >= n - 3 or (y * 4) % n < 2
+            h = (x * 2654435761 + plank * 40503 + y * 97) & 0xFFFFFFFF
+            grain = 150 + ((h >> 13) % 40) - 20
+            if edge:
+                grain = 70
+            r, g, b = grain, (grain * 3) // 4, grain // 3
+            rgb[y, x] = (r << 16) | (g << 8) | b
+    return rgb
+
+
+def scene_dir(td):
+    run = os.path.join(td, "run")
+    tex = os.path.join(td, "data", "textures")
+    os.makedirs(run, exist_ok=True)
+    os.makedirs(tex, exist_ok=True)
+    write_bmp24(os.path.join(tex, "tex_crate01.bmp"), 64, 64, crate_standin(64))
+    return run, tex
+
+
+def ref_scene_frames(kind, w, h, frames, opts, run):
+    out = os.path.join(run, "frame.bin")
+    subprocess.run([DRIVER, str(kind), "0", "0", str(w), str(h), "0", str(frames), "0",
+                    opts, out, str(min(8, os.cpu_count() or 1)), "10"],
+                   check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, cwd=run)
+    return np.fromfile(out, dtype="<u4").reshape(frames, h, w)
+
+
+def flat_scene(n, w, h, tex, run):
+    out = os.path.join(run, "scene.qrsf")
+    env = dict(os.environ, QR_PATH_TEXTURES=tex + os.sep)
+    subprocess.run([FIXTURE, str(n), str(w), str(h), "0", "none", "10", out],
+                   check=True, env=env)
+    with open(out, "rb") as f:
+        return np.frombuffer(f.read(), dtype=np.uint8)
+
+
+def run_ref_scene(n):
+    with tempfile.TemporaryDirectory() as td:
+        run, tex = scene_dir(td)
+        none = ref_scene_frames(100 + n, SCN_W, SCN_H, 1, "none", run)
+        full = ref_scene_frames(100 + n, SCN_W, SCN_H, 1, "full", run)
+        qrsf = flat_scene(n, SCN_W, SCN_H, tex, run)
+        meta = dict(scene=n, w=SCN_W, h=SCN_H, fsaa=0, depth=10, frames=1, opts="none",
+                    flags=0)
+        np.savez_compressed(os.path.join(HERE, "scn_test%02d_%dx%d.npz" % (n, SCN_W, SCN_H)),
+                            frames=none, frames_full=full, qrsf=qrsf, meta=json.dumps(meta))
+        if n in PT_SCENES:
+            w, h, spp = PT_SCENES[n]
+            # the reference's path tracer converges under its full options
+            # only (with RT_OPTS_NONE its frames do not accumulate)
+            pt = ref_scene_frames(200 + n, w, h, spp, "full", run)[-1:]
+            qrsf = flat_scene(n, w, h, tex, run)
+            meta = dict(scene=n, w=w, h=h, fsaa=0, depth=10, frames=1, samples=spp,
+                        opts="full", flags=0)
+            np.savez_compressed(os.path.join(HERE, "scn_test%02d_pt%d_%dx%d.npz" % (n, spp, w, h)),
+                                frames=pt, qrsf=qrsf, meta=json.dumps(meta))
+        return none
+
+
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("oracle/_ref/ref_driver is missing: run `make -C oracle ref`")
-    names = sys.argv[1:] or list(CASES)
+    names = sys.argv[1:] or list(CASES) + ["scn_test%02d" % n for n in range(1, 19)]
     for name in names:
-        case = CASES[name]
-        data = run_case(name, case)
+        if name.startswith("scn_test"):
+            data = run_ref_scene(int(name[8:10]))
+        else:
+            data = run_case(name, CASES[name])
         print("%-24s %s nonzero=%d" % (name, data.shape, int((data != 0).sum())))
 
 
