@@ -190,6 +190,12 @@ typedef struct qr_frame_params
                                    thread a sub-sample (the frame is the
                                    same; for tests; single-frame renders
                                    only, batches ignore it) */
+#define QR_FP_WAVEFRONT     8   /* Whitted: wavefront stages (queues of
+                                   camera, shadow and secondary rays)
+                                   instead of a thread a pixel or 4x AA
+                                   sub-sample tracing its whole ray tree
+                                   (the frame is the same; slower on the
+                                   benchmarked frames) */
 #define QR_FP_PIXEL_PT      4   /* path tracer: one thread a pixel with its
                                    samples in turn (the per-pixel kernel)
                                    instead of the wavefront stages (the

@@ -49,6 +49,8 @@ FP_LINEAR_WALK = 1        # qr_frame_params.flags: no BVH (same frame)
 FP_PIXEL_THREADS = 2      # qr_frame_params.flags: 4x AA, a thread per pixel (same frame)
 FP_PIXEL_PT = 4           # qr_frame_params.flags: path tracer, a thread per pixel instead
                           # of the wavefront stages (same frame)
+FP_WAVEFRONT = 8          # qr_frame_params.flags: Whitted, wavefront stages instead of a
+                          # thread per pixel or sub-sample tracing its whole ray tree
 
 
 class QrSceneDesc(ctypes.Structure):

@@ -23,7 +23,8 @@ DEV_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-prec-div=true",
 HOST_FLAGS = ["-Xcompiler", "-fPIC,-O2,-ffp-contract=off,-fno-fast-math"]
 INCS = ["-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
 
-SOURCES = ["tracer.cu", "tracer_stats.cu", "wavefront.cu", "capi.cu", "noalloc.cu", "batch.cu",
+SOURCES = ["tracer.cu", "tracer_stats.cu", "wavefront.cu", "whitted_wf.cu", "capi.cu", "noalloc.cu",
+           "batch.cu",
            "anim.cu", "peak.cu",
            "accel.cpp", "flatten.cpp", "engine.cpp", "pyshim.cpp"]
 # sources that textually include another translation unit

@@ -39,21 +39,11 @@
  * (the same frame).  No host synchronisation is needed: every kernel reads
  * its level's count from device memory and strides over it.
  */
-#include "tracer_dev.cuh"
+#include "wf_common.cuh"
 #include "wavefront.h"
 
 namespace qr_dev
 {
-
-/* a queued ray, 80 bytes */
-struct WRay
-{
-    float4 o;       /* origin, t_min */
-    float4 d;       /* direction, t_max */
-    float4 p;       /* originating surface's local hit, surface (int bits) */
-    int4   m;       /* flags | depth << 8, owner, tree code, list offset */
-    int4   k;       /* sample key (low, high), list length, pixel tile place */
-};
 
 /* a shaded node (or a miss), 96 bytes; its children write cl / ct / cr */
 struct WNode
@@ -72,69 +62,9 @@ struct WNode
 #define WN_RFL      8
 #define WN_SPAWN    16
 
-/* owners: level-0 rays own a sample slot of the chunk; deeper rays own a
- * child slot (0 diffuse, 1 refracted, 2 reflected) of a node in the pool */
-__device__ __forceinline__ int owner_of(int node, int slot) { return (node << 2) | slot; }
-
-/* the device-side control block of a frame */
-struct WCtl
-{
-    int cnt[QR_MAX_DEPTH + 2];      /* rays of each level in this chunk */
-    int off[QR_MAX_DEPTH + 2];      /* first pool node of each level */
-    int next[QR_MAX_DEPTH + 2];     /* rays of each level handed to warps */
-    int overflow;                   /* a queue or the pool ran full */
-    int pad[3];
-};
-
 #ifndef QR_WF_MIN_BLOCKS
 #define QR_WF_MIN_BLOCKS 6
 #endif
-
-/* exclusive warp scan of small counts; returns the warp's total in *tot */
-__device__ __forceinline__ int warp_excl_scan(int v, int *tot)
-{
-    const int lane = threadIdx.x & 31;
-    int x = v;
-    #pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane >= o) x += y;
-    }
-    *tot = __shfl_sync(0xFFFFFFFFu, x, 31);
-    return x - v;
-}
-
-/* reserve the warp's run of `total` entries in a queue counter */
-__device__ __forceinline__ int warp_reserve(int *counter, int total)
-{
-    int base = 0;
-    if ((threadIdx.x & 31) == 0 && total > 0) base = atomicAdd(counter, total);
-    return __shfl_sync(0xFFFFFFFFu, base, 0);
-}
-
-__device__ __forceinline__ void put_ray(WRay *q, int i, const float org[3], float t_min,
-                                        const float dir[3], float t_max, const float phit[3],
-                                        int from, int flags, int depth, int owner,
-                                        uint32_t code, int off, int num,
-                                        unsigned long long ks, int tp)
-{
-    WRay r;
-    r.o = make_float4(org[0], org[1], org[2], t_min);
-    r.d = make_float4(dir[0], dir[1], dir[2], t_max);
-    r.p = make_float4(phit[0], phit[1], phit[2], __int_as_float(from));
-    r.m = make_int4(flags | (depth << 8), owner, (int)code, off);
-    r.k = make_int4((int)(uint32_t)ks, (int)(uint32_t)(ks >> 32), num, tp);
-    q[i] = r;
-}
-
-/* pixel of tile place t: tiles of 8 x 4 pixels, tile rows of tx tiles */
-__device__ __forceinline__ void tile_pixel(int t, int tx, int &x, int &y)
-{
-    const int tile = t >> 5, in = t & 31;
-    x = (tile % tx) * 8 + (in & 7);
-    y = (tile / tx) * 4 + (in >> 3);
-}
 
 /* level 0: camera rays of paths [c0, c1) */
 __global__ void __launch_bounds__(128)
