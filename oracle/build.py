@@ -6,8 +6,11 @@ fast-math).  ``build_ref()`` compiles the reference engine's own renderer
 from its sources with ``oracle/Makefile`` into ``oracle/_ref/`` when the
 reference tree is available (the golden-fixture generator uses it).
 
-``load_oracle()`` returns a ctypes handle; only tests, the graft smoke check
-and the CPU-baseline leg of bench.py call it.
+``build_oracle_gpu()`` compiles the same source in double for the device
+(``qr_oracle_gpu.cu``: the FP64 path-tracer oracle on the GPU).
+
+``load_oracle()`` and ``load_oracle_gpu()`` return ctypes handles; only
+tests, the smoke check and the CPU-baseline leg of bench.py call them.
 """
 import ctypes
 import os
@@ -39,6 +42,36 @@ def build_oracle(fp64=False):
           [src, "-lm", "-o", lib]
     subprocess.run(cmd, check=True)
     return lib
+
+
+LIBGPU = os.path.join(OUT, "libqr_oracle_gpu.so")   # FP64 oracle on the GPU
+
+
+def build_oracle_gpu():
+    """Compile qr_oracle_gpu.cu (qr_oracle.c in double, for the device) for
+    sm_103a; nvcc cross-compiles it without a GPU"""
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "qr_oracle_gpu.cu")
+    deps = [src, os.path.join(HERE, "qr_oracle.c"), os.path.join(HERE, "qr_oracle.h"),
+            os.path.join(ROOT, "include", "qr_gpu.h")]
+    if os.path.exists(LIBGPU) and all(os.path.getmtime(d) <= os.path.getmtime(LIBGPU)
+                                      for d in deps):
+        return LIBGPU
+    nvcc = os.environ.get("NVCC") or (
+        "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+           "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
+           "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-I" + HERE,
+           "-I" + os.path.join(ROOT, "include"), "-shared", src, "-o", LIBGPU]
+    subprocess.run(cmd, check=True)
+    return LIBGPU
+
+
+def load_oracle_gpu():
+    L = ctypes.CDLL(build_oracle_gpu())
+    L.qr_oracle_pt_gpu.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    return L
 
 
 def build_ref():

@@ -32,6 +32,14 @@
 #include "qr_gpu.h"
 #include "qr_oracle.h"
 
+/* the restatement's functions are plain static C; the FP64 GPU oracle
+ * (qr_oracle_gpu.cu) compiles this file for the device as well */
+#ifdef __CUDACC__
+#define ORC static __host__ __device__
+#else
+#define ORC static
+#endif
+
 /* precision of the restatement: float (the checker of the GPU tracer and
  * the CPU baseline) or, built with QR_ORACLE_FP64, double (the FP64 oracle
  * of the path tracer); both builds come from this one source.  The scene
@@ -101,16 +109,16 @@ typedef struct hit_s
 
 /* sign-bit operations of the reference's SIMD code (xor with the sign
  * mask), written as negation so they hold in either precision */
-static inline real fxor(real a, uint32_t m) { return (m & 0x80000000u) ? -a : a; }
-static inline uint32_t sgnbit(real a) { return signbit(a) ? 0x80000000u : 0u; }
+ORC inline real fxor(real a, uint32_t m) { return (m & 0x80000000u) ? -a : a; }
+ORC inline uint32_t sgnbit(real a) { return signbit(a) ? 0x80000000u : 0u; }
 
 /* reciprocal square root and reciprocal in the reference's full-precision
  * compat mode (core/config/rtconf.h: rsq = 1/sqrt, rcp = 1/x) */
-static inline real rsq(real x) { return 1.0f / R_SQRT(x); }
+ORC inline real rsq(real x) { return 1.0f / R_SQRT(x); }
 
 /* M * v with the transform-node coefficients, diagonal terms first
  * (tracer.cpp:2537-2568); fast path keeps only the diagonal (2546) */
-static void xform(const qr_srf *t, const real v[3], real o[3])
+ORC void xform(const qr_srf *t, const real v[3], real o[3])
 {
     real x = t->tci[0] * v[0];
     real y = t->tcj[1] * v[1];
@@ -137,7 +145,7 @@ static void xform(const qr_srf *t, const real v[3], real o[3])
  *   tbuf   current depth buffer
  *   dmask  this lane's near-zero-determinant flag, amask sign of a
  */
-static int clip_root(const scene_t *sc, const ray_t *r, int si, real t,
+ORC int clip_root(const scene_t *sc, const ray_t *r, int si, real t,
                      real tbuf, const real ldff[3], const real lray[3],
                      int side, int dmask, uint32_t amask, real hit[3],
                      real loc[3])
@@ -327,7 +335,7 @@ typedef struct walk_s
 } walk_t;
 
 /* record a root that passed the clipper; shadow rays test occlusion */
-static void accept_root(const scene_t *sc, walk_t *w, int si, int side,
+ORC void accept_root(const scene_t *sc, walk_t *w, int si, int side,
                         real t, const real hit[3], const real loc[3],
                         uint32_t amask)
 {
@@ -352,7 +360,7 @@ static void accept_root(const scene_t *sc, walk_t *w, int si, int side,
 
 /* CHECK_SIDE (558-567): a ray leaving surface s cannot hit it again from
  * the side it could not reach */
-static int side_blocked(const ray_t *r, int si, int side)
+ORC int side_blocked(const ray_t *r, int si, int side)
 {
     int f;
     if (r->from != si) return 0;
@@ -360,11 +368,10 @@ static int side_blocked(const ray_t *r, int si, int side)
     return f == 1 - side || f == 2 + side;
 }
 
-static void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
+ORC void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
                       const real ldff[3], const real lray[3],
                       real a, real b, real c, real d)
 {
-    const qr_srf *s = &sc->srf[si];
     real nb, sd, q, t1n, t1d, t2n, t2d, t1, t2;
     int dmask, m_pos, m_neg, t1m, t2m, first, k;
     uint32_t amask;
@@ -439,10 +446,9 @@ static void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
             if (w->shadow && w->occluded) return;
         }
     }
-    (void)s;
 }
 
-static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
+ORC void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
 {
     real cdff[3] = {0, 0, 0}, cray[3] = {0, 0, 0};
     int cache_last = -1;
@@ -573,10 +579,10 @@ static void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
  *      transform (3273-3352), material (3356-3416), lights (3929-4436),
  *      transparency (4438-4936), reflection (4938-5359) -------------------- */
 
-static void trace(scene_t *sc, const ray_t *r, int off, int num, real col[3]);
+ORC void trace(scene_t *sc, const ray_t *r, int off, int num, real col[3]);
 
 /* normal (side-oriented, world frame) and texel colour of a hit */
-static void hit_surface(const scene_t *sc, const hit_t *h, real nrm[3], real tex[3])
+ORC void hit_surface(const scene_t *sc, const hit_t *h, real nrm[3], real tex[3])
 {
     const qr_srf *s = &sc->srf[h->srf];
     int side = h->side;
@@ -681,7 +687,7 @@ static void hit_surface(const scene_t *sc, const hit_t *h, real nrm[3], real tex
 
 }
 
-static void shade(scene_t *sc, const ray_t *r, const hit_t *h, real col[3])
+ORC void shade(scene_t *sc, const ray_t *r, const hit_t *h, real col[3])
 {
     const qr_srf *s = &sc->srf[h->srf];
     int side = h->side;
@@ -1054,7 +1060,7 @@ static void shade(scene_t *sc, const ray_t *r, const hit_t *h, real col[3])
     memcpy(col, c, sizeof(c));
 }
 
-static void trace(scene_t *sc, const ray_t *r, int off, int num, real col[3])
+ORC void trace(scene_t *sc, const ray_t *r, int off, int num, real col[3])
 {
     walk_t w;
     memset(&w, 0, sizeof(w));
@@ -1084,7 +1090,7 @@ static const real aa2_h[2][2] = {{-0.08f + 0.25f, +0.08f - 0.25f},
 static const real aa2_v[2][2] = {{+0.08f + 0.25f, -0.08f - 0.25f},
                                  {+0.08f + 0.25f, -0.08f - 0.25f}};
 
-static void primary(scene_t *sc, const qr_scene_desc *d,
+ORC void primary(scene_t *sc, const qr_scene_desc *d,
                     const qr_frame_params *fp, real hs, real vs,
                     real col[3])
 {
@@ -1108,11 +1114,11 @@ static void primary(scene_t *sc, const qr_scene_desc *d,
     trace(sc, &r, d->cam_off, d->cam_num, col);
 }
 
-static uint32_t pack(const qr_frame_params *fp, const real col[3])
+ORC uint32_t pack(const qr_frame_params *fp, const real col[3])
 {
     uint32_t px = 0;
     int k;
-    static const int sh[3] = {16, 8, 0};
+    const int sh[3] = {16, 8, 0};
     for (k = 0; k < 3; k++)
     {
         real v = col[k];
@@ -1126,7 +1132,7 @@ static uint32_t pack(const qr_frame_params *fp, const real col[3])
     return px;
 }
 
-static inline real clamp1(real v) { return v < 1.0f ? v : 1.0f; }
+ORC inline real clamp1(real v) { return v < 1.0f ? v : 1.0f; }
 
 int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
                      uint32_t *frame, int y0, int y1, uint64_t *nrays)
@@ -1226,7 +1232,7 @@ int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
 #define PT_SPLIT_DEPTH  (10 - 2)
 
 /* counter-based draws (see the header of this section) */
-static uint64_t mix64(uint64_t z)
+ORC uint64_t mix64(uint64_t z)
 {
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
@@ -1237,14 +1243,14 @@ static uint64_t mix64(uint64_t z)
 #define PT_CODEMUL  0xD6E8FEB86659FD93ull
 
 /* the key of sample n of a pixel */
-static uint64_t pt_sample_key(uint64_t seed, int frame, uint64_t pixel, int n)
+ORC uint64_t pt_sample_key(uint64_t seed, int frame, uint64_t pixel, int n)
 {
     uint64_t kp = mix64(seed ^ mix64(((uint64_t)(uint32_t)frame << 40) ^ pixel));
     return mix64(kp + (uint64_t)(uint32_t)n * PT_GOLDEN);
 }
 
 /* the key of the node with tree code `code` in a sample */
-static uint64_t pt_node_key(uint64_t ks, uint32_t code)
+ORC uint64_t pt_node_key(uint64_t ks, uint32_t code)
 {
     return mix64(ks ^ ((uint64_t)code * PT_CODEMUL));
 }
@@ -1256,7 +1262,7 @@ static uint64_t pt_node_key(uint64_t ks, uint32_t code)
 #define PT_DRAW_BOUNCE  1
 #define PT_DRAW_SPLIT   3
 #define PT_DRAW_JITTER  4
-static real pt_draw(uint64_t kn, int d)
+ORC real pt_draw(uint64_t kn, int d)
 {
     uint32_t u = (uint32_t)(mix64(kn + (uint64_t)(d + 1) * PT_GOLDEN) >> 40);
     return (real)(int32_t)u * (real)(1.0f / 16777216.0f);
@@ -1265,7 +1271,7 @@ static real pt_draw(uint64_t kn, int d)
 /* power series of sin and cos on [-pi, pi], evaluated with fused
  * multiply-adds like the reference's sinps/cosps (Taylor terms to x^9 and
  * x^8) */
-static real pt_sin(real x)
+ORC real pt_sin(real x)
 {
     real t = x * x, s = x, p = x * t;
     s = R_FMA(p, (real)(-1.0 / 6.0), s);
@@ -1278,7 +1284,7 @@ static real pt_sin(real x)
     return s;
 }
 
-static real pt_cos(real x)
+ORC real pt_cos(real x)
 {
     real t = x * x, c = 1.0f, p = t;
     c = R_FMA(p, (real)(-0.5), c);
@@ -1298,7 +1304,7 @@ static real pt_cos(real x)
 #endif
 
 /* cosine-weighted direction about the unit normal w */
-static void pt_bounce(const real w[3], real u1, real u2, real d[3])
+ORC void pt_bounce(const real w[3], real u1, real u2, real d[3])
 {
     real a[3] = {0.0f, 0.0f, 0.0f}, u[3], v[3], l, inv, s0, s1, ph, cp, sp;
     int k;
@@ -1336,7 +1342,7 @@ typedef struct pt_sec_s
     real nw[3], rw[3];
 } pt_sec_t;
 
-static void pt_secondary(const scene_t *sc, const ray_t *r, const hit_t *h,
+ORC void pt_secondary(const scene_t *sc, const ray_t *r, const hit_t *h,
                          const real nrm[3], pt_sec_t *o)
 {
     const qr_srf *s = &sc->srf[h->srf];
@@ -1501,10 +1507,10 @@ static void pt_secondary(const scene_t *sc, const ray_t *r, const hit_t *h,
     o->c_rfl = c_rfl;
 }
 
-static void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
+ORC void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
                      uint64_t ks, uint32_t code, real col[3]);
 
-static void child(ray_t *cr, const hit_t *h, const real dir[3], int flags, int depth)
+ORC void child(ray_t *cr, const hit_t *h, const real dir[3], int flags, int depth)
 {
     int k;
     for (k = 0; k < 3; k++)
@@ -1520,7 +1526,7 @@ static void child(ray_t *cr, const hit_t *h, const real dir[3], int flags, int d
     cr->depth = depth;
 }
 
-static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
+ORC void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
                      uint64_t ks, uint32_t code, real col[3])
 {
     const uint64_t kn = pt_node_key(ks, code);
@@ -1618,7 +1624,7 @@ static void pt_shade(scene_t *sc, const ray_t *r, const hit_t *h, int dmax,
     for (k = 0; k < 3; k++) col[k] = c[k];
 }
 
-static void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
+ORC void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
                      uint64_t ks, uint32_t code, real col[3])
 {
     walk_t w;
@@ -1636,7 +1642,7 @@ static void pt_trace(scene_t *sc, const ray_t *r, int off, int num, int dmax,
 }
 
 /* tent filter on [-1, 1] from one uniform number (2267-2342), halved */
-static real pt_tent(real u)
+ORC real pt_tent(real u)
 {
     real r = u + u, d;
     if (r < 1.0f) d = R_SQRT(r) - 1.0f;
@@ -1644,64 +1650,81 @@ static real pt_tent(real u)
     return d * 0.5f;
 }
 
+/* the scene view of a descriptor for the walk */
+ORC void scene_of(scene_t *sc, const qr_scene_desc *d, const qr_frame_params *fp)
+{
+    int k;
+    memset(sc, 0, sizeof(*sc));
+    sc->srf = d->srf;
+    sc->mat = d->mat;
+    sc->lgt = d->lgt;
+    sc->elems = d->elems;
+    sc->lelems = d->lelems;
+    sc->texels = d->texels;
+    for (k = 0; k < 3; k++) sc->amb[k] = fp->amb[k];
+    sc->ctx_props = fp->ctx_props;
+}
+
+/* fp->pt_on samples of pixel (x, y) added to its running sums a[3]; the
+ * mean is returned packed */
+ORC uint32_t pt_pixel(scene_t *sc, const qr_scene_desc *d, const qr_frame_params *fp,
+                      int x, int y, real *a)
+{
+    real sum[3] = {0.0f, 0.0f, 0.0f}, mean[3];
+    const int spp = fp->pt_on, n0 = (int)fp->pts_c;
+    const uint64_t pixel = (uint64_t)y * fp->x_res + x;
+    int n, k;
+    for (n = 0; n < spp; n++)
+    {
+        real hs, vs, col[3];
+        ray_t r;
+        const uint64_t ks = pt_sample_key(fp->seed, fp->frame_idx, pixel, n0 + n);
+        const uint64_t k0 = pt_node_key(ks, 0);
+        hs = pt_tent(pt_draw(k0, PT_DRAW_JITTER));
+        vs = pt_tent(pt_draw(k0, PT_DRAW_JITTER + 1));
+        hs = (real)x + hs;
+        vs = (real)y + vs;
+        for (k = 0; k < 3; k++)
+        {
+            real hx = fp->hor[k] * hs;
+            real vx = fp->ver[k] * vs;
+            hx = hx + vx;
+            r.ray[k] = hx + fp->dir[k];
+            r.org[k] = fp->org[k];
+            r.phit[k] = 0.0f;
+        }
+        r.t_min = fp->t_min;
+        r.t_max = fp->t_max;
+        r.from = -1;
+        r.flags = 0;
+        r.depth = fp->depth;
+        pt_trace(sc, &r, d->cam_off, d->cam_num, fp->depth, ks, 0, col);
+        for (k = 0; k < 3; k++) sum[k] = sum[k] + col[k];
+    }
+    for (k = 0; k < 3; k++)
+    {
+        a[k] = (n0 == 0 ? 0.0f : a[k]) + sum[k];
+        mean[k] = a[k] / (real)(n0 + spp);
+        mean[k] = clamp1(mean[k]);
+    }
+    return pack(fp, mean);
+}
+
 int qr_oracle_pt(const qr_scene_desc *d, const qr_frame_params *fp, void *acc_,
                  uint32_t *frame, int y0, int y1, uint64_t *nrays)
 {
     scene_t sc;
     real *acc = (real *)acc_;
-    int x, y, k, n, spp = fp->pt_on;
-    int n0 = (int)fp->pts_c;
-    memset(&sc, 0, sizeof(sc));
-    sc.srf = d->srf;
-    sc.mat = d->mat;
-    sc.lgt = d->lgt;
-    sc.elems = d->elems;
-    sc.lelems = d->lelems;
-    sc.texels = d->texels;
-    for (k = 0; k < 3; k++) sc.amb[k] = fp->amb[k];
-    sc.ctx_props = fp->ctx_props;
-    if (spp <= 0) return 1;
+    int x, y;
+    scene_of(&sc, d, fp);
+    if (fp->pt_on <= 0) return 1;
     for (y = y0; y < y1; y++)
     {
         for (x = 0; x < fp->x_res; x++)
         {
-            real sum[3] = {0.0f, 0.0f, 0.0f}, mean[3];
-            real *a = &acc[3 * ((size_t)y * fp->x_row + x)];
-            const uint64_t pixel = (uint64_t)y * fp->x_res + x;
-            for (n = 0; n < spp; n++)
-            {
-                real hs, vs, col[3];
-                ray_t r;
-                const uint64_t ks = pt_sample_key(fp->seed, fp->frame_idx, pixel, n0 + n);
-                const uint64_t k0 = pt_node_key(ks, 0);
-                hs = pt_tent(pt_draw(k0, PT_DRAW_JITTER));
-                vs = pt_tent(pt_draw(k0, PT_DRAW_JITTER + 1));
-                hs = (real)x + hs;
-                vs = (real)y + vs;
-                for (k = 0; k < 3; k++)
-                {
-                    real hx = fp->hor[k] * hs;
-                    real vx = fp->ver[k] * vs;
-                    hx = hx + vx;
-                    r.ray[k] = hx + fp->dir[k];
-                    r.org[k] = fp->org[k];
-                    r.phit[k] = 0.0f;
-                }
-                r.t_min = fp->t_min;
-                r.t_max = fp->t_max;
-                r.from = -1;
-                r.flags = 0;
-                r.depth = fp->depth;
-                pt_trace(&sc, &r, d->cam_off, d->cam_num, fp->depth, ks, 0, col);
-                for (k = 0; k < 3; k++) sum[k] = sum[k] + col[k];
-            }
-            for (k = 0; k < 3; k++)
-            {
-                a[k] = (n0 == 0 ? 0.0f : a[k]) + sum[k];
-                mean[k] = a[k] / (real)(n0 + spp);
-                mean[k] = clamp1(mean[k]);
-            }
-            if (frame != NULL) frame[(size_t)y * fp->x_row + x] = pack(fp, mean);
+            const uint32_t px = pt_pixel(&sc, d, fp, x, y,
+                                         &acc[3 * ((size_t)y * fp->x_row + x)]);
+            if (frame != NULL) frame[(size_t)y * fp->x_row + x] = px;
         }
     }
     if (nrays != NULL) *nrays = sc.nrays;
