@@ -138,6 +138,46 @@ ORC void xform(const qr_srf *t, const real v[3], real o[3])
 /* ---- clipping subroutine CC_clp (tracer.cpp:2686-3249) ------------------ */
 
 /*
+ * Boundary tracking (qr_oracle_boundary, the hit-ID exclusion mask): while
+ * a walk carries a tracker, every decision taken for a root that can still
+ * matter (its depth test passes or is marginal) records the root's distance
+ * when the quantity it compares lies within QR_MARGIN (1e-5) of the
+ * decision's boundary, relative to the size of the terms compared: the
+ * quadric's discriminant (tangent rays), the depth test between surfaces,
+ * the near plane, the axis clippers and the custom clippers.  A pixel whose
+ * primary ray recorded such a root no farther than its hit is ill
+ * conditioned: float rounding may give it either surface.  Walks without a
+ * tracker (every render) skip all of this.
+ */
+#define QR_MARGIN       1e-5
+#define QR_MARGIN_EV    8
+
+typedef struct margin_s
+{
+    int  nev;                   /* marginal decisions seen */
+    real t[QR_MARGIN_EV];       /* their roots' distances */
+} margin_t;
+
+ORC void margin_note(margin_t *mg, real t, real num, real den)
+{
+    if (mg == NULL) return;
+    if (!(R_FABS(num) <= (real)QR_MARGIN * den)) return;
+    /* beyond the slots, the last one keeps the nearest distance */
+    if (mg->nev < QR_MARGIN_EV) mg->t[mg->nev] = t;
+    else if (t < mg->t[QR_MARGIN_EV - 1]) mg->t[QR_MARGIN_EV - 1] = t;
+    mg->nev++;
+}
+
+ORC real rmax3(real a, real b, real c)
+{
+    a = R_FABS(a);
+    b = R_FABS(b);
+    c = R_FABS(c);
+    if (b > a) a = b;
+    return c > a ? c : a;
+}
+
+/*
  * Returns 1 if root t of surface s survives depth test, near clip, axis
  * clippers and custom clippers; fills the world hit and the local hit.
  *   ldff   the surface's local diff (ctx DFF in the solver's frame)
@@ -148,7 +188,7 @@ ORC void xform(const qr_srf *t, const real v[3], real o[3])
 ORC int clip_root(const scene_t *sc, const ray_t *r, int si, real t,
                      real tbuf, const real ldff[3], const real lray[3],
                      int side, int dmask, uint32_t amask, real hit[3],
-                     real loc[3])
+                     real loc[3], margin_t *mg)
 {
     const qr_srf *s = &sc->srf[si];
     int valid = 1;
@@ -156,6 +196,16 @@ ORC int clip_root(const scene_t *sc, const ray_t *r, int si, real t,
 
     if (!(tbuf > t)) valid = 0;             /* depth test */
     if (!(r->t_min < t)) valid = 0;         /* near plane */
+    if (mg != NULL)
+    {
+        const int dm = R_FABS(tbuf - t) <= (real)QR_MARGIN * rmax3(t, tbuf, 0.0f);
+        const int nm = R_FABS(t - r->t_min) <= (real)QR_MARGIN * rmax3(t, r->t_min, 0.0f);
+        if (dm) margin_note(mg, t, 0.0f, 1.0f);
+        if (nm) margin_note(mg, t, 0.0f, 1.0f);
+        /* the decisions below matter only for a root the depth test and the
+         * near plane let through, or nearly so */
+        if (!valid && !dm && !nm) mg = NULL;
+    }
 
     for (k = 0; k < 3; k++)
     {
@@ -230,10 +280,12 @@ ORC int clip_root(const scene_t *sc, const ray_t *r, int si, real t,
         if ((s->mint >> k) & 1)
         {
             if (!(s->bmin[k] <= loc[k])) valid = 0;
+            margin_note(mg, t, loc[k] - s->bmin[k], rmax3(loc[k], s->bmin[k], 1.0f));
         }
         if ((s->maxt >> k) & 1)
         {
             if (!(s->bmax[k] >= loc[k])) valid = 0;
+            margin_note(mg, t, loc[k] - s->bmax[k], rmax3(loc[k], s->bmax[k], 1.0f));
         }
     }
 
@@ -296,6 +348,7 @@ ORC int clip_root(const scene_t *sc, const ray_t *r, int si, real t,
             if (c->clpk == 1)
             {
                 v = fxor(p[c->amap[2]], c->asgn[2] ? 0x80000000u : 0u);
+                margin_note(mg, t, v, rmax3(p[0], p[1], p[2]) + 1.0f);
             }
             else if (c->clpk == 2)
             {
@@ -306,12 +359,16 @@ ORC int clip_root(const scene_t *sc, const ray_t *r, int si, real t,
                     d2[k] = p[k] * p[k] * c->sci[k] - d1;
                 }
                 v = ((d2[0] - c->sci[3]) + d2[1]) + d2[2];
+                margin_note(mg, t, v, R_FABS(d2[0]) + R_FABS(d2[1]) + R_FABS(d2[2]) +
+                                      R_FABS(c->sci[3]));
             }
             else
             {
                 real d2[3];
                 for (k = 0; k < 3; k++) d2[k] = p[k] * p[k] * c->sci[k];
                 v = ((d2[0] - c->sci[3]) + d2[1]) + d2[2];
+                margin_note(mg, t, v, R_FABS(d2[0]) + R_FABS(d2[1]) + R_FABS(d2[2]) +
+                                      R_FABS(c->sci[3]));
             }
             /* APPLY_CLIP (515-523): minus inner keeps v >= 0,
              * minus outer keeps v <= 0 */
@@ -332,6 +389,7 @@ typedef struct walk_s
     int     occluded;
     real   tbuf;
     hit_t   best;
+    margin_t *mg;           /* boundary tracker (NULL: none) */
 } walk_t;
 
 /* record a root that passed the clipper; shadow rays test occlusion */
@@ -377,6 +435,9 @@ ORC void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
     uint32_t amask;
     real hit[3], loc[3];
 
+    /* a tangent ray: the double root -b / a */
+    if (w->mg != NULL && a != 0.0f)
+        margin_note(w->mg, -b / a, d, b * b + R_FABS(c * a));
     /* QD_rts (5785-5799) */
     if (!(0.0f <= d)) return;               /* xmask */
     nb = fxor(b, 0x80000000u);
@@ -440,7 +501,7 @@ ORC void root_pair(const scene_t *sc, const ray_t *r, walk_t *w, int si,
         if (side_blocked(r, si, side)) continue;
         if (!tm) continue;
         if (clip_root(sc, r, si, t, w->tbuf, ldff, lray, side, dmask, amask,
-                      hit, loc))
+                      hit, loc, w->mg))
         {
             accept_root(sc, w, si, side, t, hit, loc, amask);
             if (w->shadow && w->occluded) return;
@@ -526,7 +587,7 @@ ORC void walk(const scene_t *sc, const ray_t *r, int off, int num, walk_t *w)
             if (!(rk != 0.0f)) continue;
             t = dk / rk;
             if (!clip_root(sc, r, el->ref, t, w->tbuf, ldff, lray, 0, 0, 0,
-                           hit, loc))
+                           hit, loc, w->mg))
             {
                 continue;
             }
@@ -1134,6 +1195,21 @@ ORC uint32_t pack(const qr_frame_params *fp, const real col[3])
 
 ORC inline real clamp1(real v) { return v < 1.0f ? v : 1.0f; }
 
+/* the scene view of a descriptor for the walk */
+ORC void scene_of(scene_t *sc, const qr_scene_desc *d, const qr_frame_params *fp)
+{
+    int k;
+    memset(sc, 0, sizeof(*sc));
+    sc->srf = d->srf;
+    sc->mat = d->mat;
+    sc->lgt = d->lgt;
+    sc->elems = d->elems;
+    sc->lelems = d->lelems;
+    sc->texels = d->texels;
+    for (k = 0; k < 3; k++) sc->amb[k] = fp->amb[k];
+    sc->ctx_props = fp->ctx_props;
+}
+
 int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
                      uint32_t *frame, int y0, int y1, uint64_t *nrays)
 {
@@ -1194,6 +1270,68 @@ int qr_oracle_render(const qr_scene_desc *d, const qr_frame_params *fp,
         }
     }
     if (nrays) *nrays = sc.nrays;
+    return QR_OK;
+}
+
+/* 1 when the camera ray through (hs, vs) meets a decision within QR_MARGIN
+ * of its boundary no farther than its hit (see margin_t) */
+ORC int primary_marginal(scene_t *sc, const qr_scene_desc *d, const qr_frame_params *fp,
+                         real hs, real vs)
+{
+    ray_t r;
+    walk_t w;
+    margin_t mg;
+    int k;
+    for (k = 0; k < 3; k++)
+    {
+        real hx = fp->hor[k] * hs;
+        real vx = fp->ver[k] * vs;
+        hx = hx + vx;
+        r.ray[k] = hx + fp->dir[k];
+        r.org[k] = fp->org[k];
+        r.phit[k] = 0.0f;
+    }
+    r.t_min = fp->t_min;
+    r.t_max = fp->t_max;
+    r.from = -1;
+    r.flags = 0;
+    r.depth = fp->depth;
+    memset(&w, 0, sizeof(w));
+    memset(&mg, 0, sizeof(mg));
+    w.tbuf = r.t_max;
+    w.best.srf = -1;
+    w.mg = &mg;
+    walk(sc, &r, d->cam_off, d->cam_num, &w);
+    for (k = 0; k < mg.nev && k < QR_MARGIN_EV; k++)
+        if (w.best.srf < 0 || mg.t[k] <= w.tbuf + (real)QR_MARGIN * R_FABS(w.tbuf)) return 1;
+    return 0;
+}
+
+int qr_oracle_boundary(const qr_scene_desc *d, const qr_frame_params *fp, uint8_t *mask,
+                       int y0, int y1)
+{
+    scene_t sc;
+    int x, y, s;
+    if (d == NULL || fp == NULL || mask == NULL) return QR_ERR_ARG;
+    scene_of(&sc, d, fp);
+    if (y1 > fp->y_res) y1 = fp->y_res;
+    for (y = y0; y < y1; y++)
+    {
+        for (x = 0; x < fp->x_res; x++)
+        {
+            int m = 0;
+            if (fp->fsaa == 2)
+                for (s = 0; s < 4; s++)
+                    m |= primary_marginal(&sc, d, fp, (real)x + aa4_h[s], (real)y + aa4_v[s]);
+            else if (fp->fsaa == 1)
+                for (s = 0; s < 2; s++)
+                    m |= primary_marginal(&sc, d, fp, (real)x + aa2_h[x & 1][s],
+                                          (real)y + aa2_v[x & 1][s]);
+            else
+                m = primary_marginal(&sc, d, fp, (real)x, (real)y);
+            mask[(size_t)y * fp->x_res + x] = (uint8_t)m;
+        }
+    }
     return QR_OK;
 }
 
@@ -1650,20 +1788,6 @@ ORC real pt_tent(real u)
     return d * 0.5f;
 }
 
-/* the scene view of a descriptor for the walk */
-ORC void scene_of(scene_t *sc, const qr_scene_desc *d, const qr_frame_params *fp)
-{
-    int k;
-    memset(sc, 0, sizeof(*sc));
-    sc->srf = d->srf;
-    sc->mat = d->mat;
-    sc->lgt = d->lgt;
-    sc->elems = d->elems;
-    sc->lelems = d->lelems;
-    sc->texels = d->texels;
-    for (k = 0; k < 3; k++) sc->amb[k] = fp->amb[k];
-    sc->ctx_props = fp->ctx_props;
-}
 
 /* fp->pt_on samples of pixel (x, y) added to its running sums a[3]; the
  * mean is returned packed */

@@ -44,6 +44,26 @@ def oracle_render(oracle, desc, params, y0=0, y1=None):
     return out[:, :params.x_res], nr.value
 
 
+_ORACLE64 = []
+
+
+def boundary_mask(desc, params):
+    """the hit-ID exclusion mask of a frame (qr_oracle_boundary of the FP64
+    oracle): 1 where a camera ray meets a solver or clipper decision within
+    1e-5 relative of its boundary no farther than its hit"""
+    if not _ORACLE64:
+        import build as oracle_build
+        L = oracle_build.load_oracle(fp64=True)
+        L.qr_oracle_boundary.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_int, ctypes.c_int]
+        _ORACLE64.append(L)
+    mask = np.zeros((params.y_res, params.x_res), dtype=np.uint8)
+    rc = _ORACLE64[0].qr_oracle_boundary(ctypes.addressof(desc), ctypes.addressof(params),
+                                         mask.ctypes.data, 0, params.y_res)
+    assert rc == 0
+    return mask.astype(bool)
+
+
 def oracle_render_par(oracle, desc, params, y0=0, y1=None, threads=None):
     """oracle_render over row bands on all host cores (the oracle call
     releases the interpreter lock); returns (frame, traced rays)"""

@@ -161,7 +161,12 @@ def test_device_update_matches_reference_frames(qr, ctx):
                 assert rc == 0
                 ctx.anim_update(sid, p)
             img = ctx.render_host(sid, fp)
-            check_against_golden(img, frames[k], meta)
+            mask = None
+            if meta["flags"] & 1:
+                from conftest import boundary_mask
+                _, _, dk, pk = flatten_case(qr, meta, 16 * k)
+                mask = boundary_mask(dk, pk)
+            check_against_golden(img, frames[k], meta, mask)
         ctx.release(sid)
         done += 1
     assert done >= 4, os.listdir(os.path.dirname(path))

@@ -186,13 +186,15 @@ def test_anim_full_size_frame_properties(qr, ctx):
 # ---- the reference's own frames (tests/golden), through the GPU
 
 def test_gpu_matches_reference_goldens(qr, ctx):
+    from conftest import boundary_mask
     from test_oracle_golden import EXACT, load_golden, check_against_golden, frames_of
     for path in EXACT:
         frames, meta = load_golden(path)
         for k, (desc, params) in enumerate(frames_of(qr, meta)):
             sid = ctx.upload(desc)
             img = ctx.render_host(sid, params)
-            check_against_golden(img, frames[k], meta)
+            mask = boundary_mask(desc, params) if meta["flags"] & 1 else None
+            check_against_golden(img, frames[k], meta, mask)
             ctx.release(sid)
 
 

@@ -27,7 +27,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import channels, max_channel_diff, oracle_render
+from conftest import boundary_mask, channels, max_channel_diff, oracle_render
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # generated-scene fixtures (the reference's own test scenes, scn_test*, are
@@ -38,8 +38,11 @@ FIXTURES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
 # colour: fraction of pixels allowed to differ, and by at most this many LSBs
 COLOR_FRAC = 1e-3
 COLOR_LSB = 1
-# hit IDs: host libm differences across machines may move a boundary pixel
-ID_FRAC = 1e-3
+# hit IDs: exact outside the exclusion mask (conftest.boundary_mask: a root
+# within 1e-5 relative of a tangent, a clip boundary or another surface's
+# distance, where float rounding may pick either surface); the mask itself
+# must stay a small share of the frame
+ID_MASK_FRAC = 0.03
 
 
 def load_golden(path):
@@ -88,12 +91,20 @@ def frames_of(qr, meta):
         yield desc, params
 
 
-def check_against_golden(img, ref, meta):
+def check_against_golden(img, ref, meta, mask=None):
+    """the golden bar: hit-ID frames exact outside the exclusion mask (exact
+    everywhere when no mask is given), colour frames within COLOR_LSB on all
+    but COLOR_FRAC of the pixels"""
     assert img.shape == ref.shape
     n = img.size
     if meta["flags"] & 1:
-        bad = int((img != ref).sum())
-        assert bad <= ID_FRAC * n, "hit IDs differ on %d of %d pixels" % (bad, n)
+        diff = img != ref
+        if mask is not None:
+            assert mask.shape == img.shape
+            assert mask.mean() <= ID_MASK_FRAC, "exclusion mask %.4f" % mask.mean()
+            diff = diff & ~mask
+        bad = int(diff.sum())
+        assert bad == 0, "hit IDs differ on %d of %d pixels outside the mask" % (bad, n)
         return bad
     d = max_channel_diff(img, ref)
     bad = int((d > COLOR_LSB).sum())
@@ -124,7 +135,8 @@ def test_oracle_matches_reference(qr, oracle, path):
     for k, (desc, params) in enumerate(frames_of(qr, meta)):
         img, nrays = oracle_render(oracle, desc, params)
         assert nrays > 0
-        check_against_golden(img, frames[k], meta)
+        mask = boundary_mask(desc, params) if meta["flags"] & 1 else None
+        check_against_golden(img, frames[k], meta, mask)
 
 
 @pytest.mark.xfail(reason="with RT_OPTS_TARRAY the reference's shadow and "
@@ -163,9 +175,32 @@ def test_planted_error_is_caught(qr, oracle):
     g, f, desc, params = flatten_case(qr, meta)
     img, _ = oracle_render(oracle, desc, params)
     img = img.copy()
-    img[::4, :] ^= 2                   # 25% of hit IDs moved to the other side
+    mask = boundary_mask(desc, params)
+    moved = img.copy()
+    moved[::4, :] ^= 2                 # 25% of hit IDs moved to the other side
     with pytest.raises(AssertionError):
-        check_against_golden(img, frames[0], meta)
+        check_against_golden(moved, frames[0], meta, mask)
+    one = img.copy()                   # one ID moved where the mask is clear
+    yy, xx = np.argwhere(~mask)[len(np.argwhere(~mask)) // 2]
+    one[yy, xx] ^= 2
+    with pytest.raises(AssertionError):
+        check_against_golden(one, frames[0], meta, mask)
+    inside = img.copy()                # IDs moved only inside the mask pass
+    inside[mask] ^= 2
+    check_against_golden(inside, frames[0], meta, mask)
+
+
+def test_boundary_mask_marks_tangents_and_clips(qr):
+    """the exclusion mask is a thin set: a small share of the frame, and in
+    the animated scene (clippers, booleans) larger than in the plain one"""
+    g, f, desc, params = flatten_case(qr, dict(kind=1, seed=1, nq=16, w=160, h=96, fsaa=0,
+                                               flags=1, opts="full", depth=10))
+    m1 = boundary_mask(desc, params)
+    g, f, desc, params = flatten_case(qr, dict(kind=2, seed=5, nq=64, w=160, h=90, fsaa=0,
+                                               flags=1, opts="full", depth=4))
+    m2 = boundary_mask(desc, params)
+    assert 0 < m1.mean() < 0.01
+    assert m1.mean() < m2.mean() < ID_MASK_FRAC
 
 
 # ---- path tracer: same estimator as the reference, different random streams
