@@ -176,7 +176,13 @@ def run_serve(args, wl, rank, world, dist, local):
             rays_of[key] = int(counts[0]) + int(counts[1]) + int(counts[2])
         return rays_of[key] * (req.spp if sc["pt"] else 1)
 
+    urgent = None
+    if args.serve_urgent:
+        # 1080p Whitted frames, whose latency has a target, go first
+        def urgent(r):
+            return (r.w, r.h) == (1920, 1080) and not scenes[r.scene]["pt"]
     srv = serve.Server(qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
+                       max_batch_pixels=args.serve_batch_px, urgent=urgent,
                        prep_threads=min(8, os.cpu_count() or 1),
                        device_anim=not args.serve_host_update)
     # warm-up: every scene once at every size
@@ -186,8 +192,10 @@ def run_serve(args, wl, rank, world, dist, local):
     results = []
     clocks = ClockSampler(local)
     clocks.start()
-    for rate in wl["serve"]:
-        reqs = serve.poisson_requests(32, rate, wl["seconds"], SERVE_SIZES, 16,
+    rates = [float(x) for x in args.serve_rates.split(",")] if args.serve_rates else wl["serve"]
+    seconds = args.serve_seconds or wl["seconds"]
+    for rate in rates:
+        reqs = serve.poisson_requests(32, rate, seconds, SERVE_SIZES, 16,
                                       wl["seed"] + int(rate))
         total = sum(rays(r) for r in reqs)
         done, wall = srv.run(reqs)
@@ -217,7 +225,9 @@ def run_serve(args, wl, rank, world, dist, local):
         "config": {"workload": "serve", "scenes": 32, "animated_plain": 32,
                    "quadrics": [16, 256], "sizes": SERVE_SIZES, "spp": [1, 16],
                    "sampling": "spp 1: one camera ray a pixel; spp > 1: 4x AA",
-                   "budget_bytes": 120 << 30, "seconds_per_rate": wl["seconds"],
+                   "budget_bytes": 120 << 30, "seconds_per_rate": seconds,
+                   "max_batch_pixels": args.serve_batch_px,
+                   "urgent_first": "1080p Whitted" if args.serve_urgent else None,
                    "parallelism": "replicas" if world > 1 else "single"},
         "rates": results,
         "scene_updates": counts,
@@ -802,6 +812,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="anim", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-rates", default="",
+                    help="serve: arrival rates per second, comma-separated")
+    ap.add_argument("--serve-seconds", type=float, default=0.0,
+                    help="serve: seconds of arrivals per rate")
+    ap.add_argument("--serve-batch-px", type=int, default=24 << 20,
+                    help="serve: pixels of a batched launch at most")
+    ap.add_argument("--serve-urgent", action="store_true",
+                    help="serve: 1080p Whitted requests go into the next batch first")
     ap.add_argument("--serve-host-update", action="store_true",
                     help="serve: update animated scenes on the host (update phases, "
                          "hierarchy build and upload per request) instead of the device")

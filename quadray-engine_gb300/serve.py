@@ -62,11 +62,14 @@ class Server:
 
     def __init__(self, qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
                  max_batch_pixels=24 << 20, prep_threads=4, per_request=True,
-                 device_anim=False, rebuild_every=32):
+                 device_anim=False, rebuild_every=32, urgent=None):
         """scenes: list of dicts with keys gen (a GenScene), pt (path-traced
         scene), depth and anim (animated); per_request: complete each request
         when its frame is done (else when its batch is); device_anim: update
-        animated scenes on the device (qr_scene_anim_*) where they allow it"""
+        animated scenes on the device (qr_scene_anim_*) where they allow it;
+        urgent: a predicate on requests whose latency has a target (e.g.
+        1080p Whitted frames): prepared urgent requests go into the next
+        batch ahead of the others"""
         self.per_request = per_request
         self.device_anim = device_anim
         self.tables = {}                # (scene, w, h, fsaa) -> update table or None
@@ -94,6 +97,8 @@ class Server:
         self.waiting = collections.deque()      # arrived, not admitted
         self.preparing = []                      # futures
         self.ready = collections.deque()         # prepared, not launched
+        self.ready_urgent = collections.deque()  # the same, urgent ones
+        self.urgent = urgent
         self.inflight = collections.deque()      # (batch, [requests])
         self.completed = []
         self.idle_sleep = 100e-6
@@ -197,7 +202,10 @@ class Server:
             if f.done():
                 r = f.result()
                 r.prepared = now_fn()
-                self.ready.append(r)
+                if self.urgent is not None and self.urgent(r):
+                    self.ready_urgent.append(r)
+                else:
+                    self.ready.append(r)
             else:
                 keep.append(f)
         self.preparing = keep
@@ -205,15 +213,16 @@ class Server:
     # ---- batches ------------------------------------------------------
     def _launch(self):
         qr = self.qr
-        while self.ready and self.free_batches:
+        while (self.ready or self.ready_urgent) and self.free_batches:
             reqs, px = [], 0
-            while self.ready and len(reqs) < self.max_batch:
-                r = self.ready[0]
-                if reqs and px + r.w * r.h > self.max_batch_pixels:
-                    break
-                self.ready.popleft()
-                reqs.append(r)
-                px += r.w * r.h
+            for q in (self.ready_urgent, self.ready):
+                while q and len(reqs) < self.max_batch:
+                    r = q[0]
+                    if reqs and px + r.w * r.h > self.max_batch_pixels:
+                        break
+                    q.popleft()
+                    reqs.append(r)
+                    px += r.w * r.h
             table = []
             for r in reqs:
                 q = qr.QrRequest()
@@ -262,15 +271,19 @@ class Server:
 
     def step(self, now_fn):
         """one turn of the loop; returns whether anything moved"""
-        n = len(self.completed) + len(self.waiting) + len(self.ready) + len(self.inflight)
+        def count():
+            return (len(self.completed) + len(self.waiting) + len(self.ready) +
+                    len(self.ready_urgent) + len(self.inflight))
+        n = count()
         self._complete(now_fn)
         self._admit()
         self._collect_prepared(now_fn)
         self._launch()
-        return n != len(self.completed) + len(self.waiting) + len(self.ready) + len(self.inflight)
+        return n != count()
 
     def busy(self):
-        return bool(self.waiting or self.preparing or self.ready or self.inflight)
+        return bool(self.waiting or self.preparing or self.ready or self.ready_urgent or
+                    self.inflight)
 
     def run(self, arrivals, keep_frames=False):
         """serve a list of Requests (their arrival in seconds from the
