@@ -70,7 +70,8 @@ def build_oracle_gpu():
 def load_oracle_gpu():
     L = ctypes.CDLL(build_oracle_gpu())
     L.qr_oracle_pt_gpu.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                   ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+                                   ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
     return L
 
 

@@ -3,14 +3,16 @@
  * of include/qr_gpu.h).
  *
  * A batch holds up to max_requests requests on resident scenes of one
- * context, Whitted or path-traced, of any size.  Each request is cut into
- * warp tiles; one persistent kernel per mode walks the tiles of all its
- * requests (tracer.cu batch_kernel), the path-tracer kernel on a second
- * stream so the two overlap in each other's tail.  The counter reset and the
- * two launches are captured once into a CUDA graph and replayed by every
- * launch until the requests or the tile configuration change.  The tile
- * shape and the tiles a warp claims at once come from qr_batch_tune, which
- * times each configuration on the batch itself and keeps the fastest.
+ * context, Whitted or path-traced, of any size.  The Whitted requests are
+ * cut into warp tiles and one persistent kernel walks the tiles of all of
+ * them (tracer.cu batch_kernel).  The path-traced requests run, one after
+ * the other on a second stream, as frames of the wavefront path tracer
+ * (wavefront.cu) over the batch's own scratch, so the two classes overlap
+ * in each other's tail.  The counter reset and all the launches are
+ * captured once into a CUDA graph and replayed by every launch until the
+ * requests or the tile configuration change.  The tile shape and the tiles
+ * a warp claims at once come from qr_batch_tune, which times each
+ * configuration on the batch itself and keeps the fastest.
  *
  * Completion per request: the warp that finishes a request's last tile sets
  * the request's flag in host memory mapped into the device
@@ -20,11 +22,13 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
+#include <algorithm>
 #include <new>
 #include <vector>
 
 #include "qr_gpu.h"
 #include "tracer.cuh"
+#include "wavefront.h"
 
 int qr_internal_scene(qr_ctx *ctx, int scene_id, const qr_dscene **sc, int *device);
 int qr_internal_check_fp(const qr_frame_params *fp);
@@ -53,7 +57,17 @@ struct qr_batch
     cudaGraphExec_t exec;
     int          graph_ok;
     int          launched;
+    int          sms;
+    /* path-traced requests: wavefront capacities of each PT job, and the
+     * scratch that fits the largest */
+    std::vector<qr_wf_caps> pt_caps;
+    void        *wf;
+    size_t       wf_bytes;
+    std::vector<qr_job> pt_jobs;    /* host copies of the path-traced jobs */
 };
+
+/* wavefront chunks of the batch's path-traced requests (as a context's) */
+#define QR_BATCH_WF_PATHS (2ll << 20)
 
 static int bfail(qr_batch *b, int code, const char *what, cudaError_t e)
 {
@@ -100,6 +114,8 @@ extern "C" int qr_batch_create(qr_ctx *ctx, int max_requests, qr_batch **out)
         int per = qr_batch_blocks_per_sm(m);
         b->blocks[m] = sms * (per > 0 ? per : 1);
     }
+    b->sms = sms;
+    qr_wf_prepare();
     *out = b;
     return QR_OK;
 }
@@ -117,6 +133,7 @@ extern "C" int qr_batch_destroy(qr_batch *b)
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->join) cudaEventDestroy(b->join);
     if (b->done) cudaEventDestroy(b->done);
+    if (b->wf) cudaFree(b->wf);
     delete b;
     return QR_OK;
 }
@@ -165,6 +182,26 @@ static int upload_jobs(qr_batch *b)
                                    cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch job upload", e);
     }
+    /* the path-traced jobs' wavefront capacities and the scratch for the
+     * largest */
+    b->pt_caps.clear();
+    size_t need = 0;
+    for (int j = b->nw; j < b->nw + b->np; j++)
+    {
+        const qr_wf_caps c = qr_wf_caps_for(jobs[j].P, QR_BATCH_WF_PATHS, 2, 8);
+        b->pt_caps.push_back(c);
+        need = std::max(need, qr_wf_bytes(c));
+    }
+    if (need > b->wf_bytes)
+    {
+        if (b->wf) cudaFree(b->wf);
+        b->wf = NULL;
+        b->wf_bytes = 0;
+        cudaError_t e = cudaMalloc(&b->wf, need);
+        if (e != cudaSuccess) return bfail(b, QR_ERR_OOM, "batch wavefront scratch", e);
+        b->wf_bytes = need;
+    }
+    b->pt_jobs.assign(jobs.begin() + b->nw, jobs.end());
     if (b->exec)
     {
         cudaGraphExecDestroy(b->exec);
@@ -219,10 +256,14 @@ static cudaError_t enqueue(qr_batch *b)
     if (e == cudaSuccess)
         e = qr_launch_batch(0, b->djobs, b->nw, b->tiles[0], b->dcount, b->tw, b->th,
                             b->grab, b->blocks[0], b->dtiles, b->ddone, b->main);
-    if (e == cudaSuccess)
-        e = qr_launch_batch(1, b->djobs + b->nw, b->np, b->tiles[1], b->dcount + 1,
-                            b->tw, b->th, b->grab, b->blocks[1], b->dtiles + b->nw,
-                            b->ddone, b->side);
+    /* the path-traced requests one after the other on the side stream,
+     * each marked done as soon as its frame is in device memory */
+    for (int j = 0; j < b->np && e == cudaSuccess; j++)
+    {
+        const qr_job &J = b->pt_jobs[j];
+        e = qr_wf_launch_pt(J.S, J.P, J.acc, J.frame, b->wf, b->pt_caps[j], b->sms, b->side);
+        if (e == cudaSuccess) e = qr_wf_mark_done(b->ddone, J.req, b->side);
+    }
     if (e == cudaSuccess) e = cudaEventRecord(b->join, b->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->main, b->join, 0);
     return e;

@@ -359,6 +359,35 @@ wf_fallback(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *fr
 
 using namespace qr_dev;
 
+static int g_step_per_sm = 0;
+
+int qr_wf_prepare(void)
+{
+    if (g_step_per_sm == 0)
+    {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, wf_step, 128, 0) != cudaSuccess ||
+            nb <= 0)
+            nb = QR_WF_MIN_BLOCKS;
+        g_step_per_sm = nb;
+    }
+    return g_step_per_sm;
+}
+
+/* a batched request's completion word, once the frame before it on the
+ * stream is in device memory */
+__global__ void wf_mark_done(uint32_t *done, int req)
+{
+    __threadfence_system();
+    *(volatile uint32_t *)&done[req] = 1u;
+}
+
+cudaError_t qr_wf_mark_done(uint32_t *done, int req, cudaStream_t stream)
+{
+    wf_mark_done<<<1, 1, 0, stream>>>(done, req);
+    return cudaGetLastError();
+}
+
 size_t qr_wf_bytes(const qr_wf_caps &c)
 {
     return sizeof(WCtl) + 2 * (size_t)c.cap_q * sizeof(WRay) +
@@ -408,15 +437,7 @@ cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, floa
     const long long total = (long long)ppad * fp.pt_on;
     const int levels = fp.depth + 1;
     /* every kernel strides over its level: as many blocks as are resident */
-    static int step_per_sm = 0;
-    if (step_per_sm == 0)
-    {
-        int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, wf_step, 128, 0) != cudaSuccess ||
-            nb <= 0)
-            nb = QR_WF_MIN_BLOCKS;
-        step_per_sm = nb;
-    }
+    const int step_per_sm = qr_wf_prepare();
     const int blocks = sms * 8;             /* memory-bound stages: 8 blocks of 128 a SM */
     const int sblocks = sms * step_per_sm;
     cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(WCtl), stream);

@@ -28,6 +28,12 @@ size_t qr_wf_bytes(const qr_wf_caps &caps);
 cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *acc,
                             uint32_t *frame, void *scratch, const qr_wf_caps &caps,
                             int sms, cudaStream_t stream);
+/* resident blocks a SM of the stages' tracing kernel (queried once; call it
+ * before a stream capture that holds wavefront launches) */
+int qr_wf_prepare(void);
+/* set done[req] to 1 on `stream` once the work before it has run (done may
+ * be host memory mapped into the device) */
+cudaError_t qr_wf_mark_done(uint32_t *done, int req, cudaStream_t stream);
 /* whether the last frame rendered with this scratch overflowed its queues
  * (and was rendered by the per-pixel kernel instead); synchronises stream */
 int qr_wf_overflowed(const void *scratch, cudaStream_t stream, int *out);
