@@ -194,6 +194,7 @@ def run_serve(args, wl, rank, world, dist, local):
     clocks.start()
     rates = [float(x) for x in args.serve_rates.split(",")] if args.serve_rates else wl["serve"]
     seconds = args.serve_seconds or wl["seconds"]
+    l0 = qr.kernel_launches()
     for rate in rates:
         reqs = serve.poisson_requests(32, rate, seconds, SERVE_SIZES, 16,
                                       wl["seed"] + int(rate))
@@ -212,6 +213,7 @@ def run_serve(args, wl, rank, world, dist, local):
                         "whitted_1080p_ms_p99": float(np.percentile(big, 99)) if len(big) else None,
                         "prepared_ms_p99": float(np.percentile(prep, 99)) if len(prep) else None})
     ck = clocks.stop()
+    launches = qr.kernel_launches() - l0
     counts = {"device_updates": srv.device_updates, "host_updates": srv.host_updates}
     srv.close()
     anim_us = anim_update_time(qr, ctx, wl["seed"])
@@ -238,6 +240,7 @@ def run_serve(args, wl, rank, world, dist, local):
                         "update phases on the device (host update phases and "
                         "uploads for a scene copy's first frame), batched "
                         "launches; frames stay on the device"},
+        "gpu_launches": launches,
         "clocks": ck,
     }
     if rank == 0:
@@ -309,11 +312,13 @@ def run_batch(args, wl, rank, world, dist, local):
     clocks.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
+    l0 = qr.kernel_launches()
     for i in range(args.steps):
         ev[i][0].record(stream)
         b.launch(sp)
         ev[i][1].record(stream)
     torch.cuda.synchronize()
+    launches = qr.kernel_launches() - l0
     ck = clocks.stop()
     ms = [a.elapsed_time(c) for a, c in ev]
     value, t_total = whole_job(rays, args.steps, sum(ms) / 1000.0, dist, "cuda")
@@ -384,7 +389,7 @@ def run_batch(args, wl, rank, world, dist, local):
         "e2e": {"value": rays * len(lat) / sum(lat), "unit": "rays/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_p50": 1000.0 * float(np.percentile(lat, 50))},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches,
         "clocks": ck,
     }
     if rank == 0:
@@ -694,11 +699,14 @@ def run_frames(args, wl, rank, world, dist, local):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(K)]
     torch.cuda.synchronize()
+    launches = 0                        # the library's kernels in the timed steps
     for i, j in enumerate(timed):
         prm, fp = prepare(j)
         flush.zero_()
         ev[i][0].record(stream)
+        l0 = qr.kernel_launches()
         step(prm, fp)
+        launches += qr.kernel_launches() - l0
         ev[i][1].record(stream)
     torch.cuda.synchronize()
     ck = clocks.stop()
@@ -794,7 +802,7 @@ def run_frames(args, wl, rank, world, dist, local):
         "roofline": roof,
         "work_per_frame": stats,
         "anim_status": anim_status,
-        "gpu_launches": K * (2 if wl["anim"] else 1),
+        "gpu_launches": launches,
         "clocks": ck,
     }
     if rank == 0 and not args.no_cpu:

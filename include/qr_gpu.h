@@ -436,6 +436,11 @@ int qr_batch_done(qr_batch *b, const volatile uint32_t **flags);
  * denominator of the render kernels; no counterpart in the reference */
 int qr_fp32_peak(int device, int fma, double *tflops);
 
+/* Kernels the library has launched in this process, all contexts together:
+ * renders, path-tracer stages, device updates, batches (a batch counts the
+ * kernels of its graph at each launch).  No counterpart in the reference. */
+unsigned long long qr_kernel_launches(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -210,6 +210,8 @@ def lib():
         L.qr_batch_wait.argtypes = [vp]
         L.qr_sync.argtypes = [vp, vp]
         L.qr_fp32_peak.argtypes = [i32, i32, ctypes.POINTER(ctypes.c_double)]
+        L.qr_kernel_launches.argtypes = []
+        L.qr_kernel_launches.restype = ctypes.c_ulonglong
         L.qr_fault.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
         L.qr_render_stats.argtypes = [vp, i32, ctypes.POINTER(QrFrameParams), vp,
                                       ctypes.POINTER(ctypes.c_uint64)]
@@ -240,6 +242,11 @@ class GenScene:
             self.close()
         except Exception:
             pass
+
+
+def kernel_launches():
+    """kernels the library has launched in this process (qr_kernel_launches)"""
+    return int(lib().qr_kernel_launches())
 
 
 def write_textures(seed, directory):

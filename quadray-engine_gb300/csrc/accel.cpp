@@ -407,6 +407,19 @@ int build_node(std::vector<Prim> &p, int lo, int hi, int depth, qr_accel_host *o
             if (mid <= lo || mid >= hi) mid = -1;
         }
     }
+    if (mid < 0 && n > QR_BVH_LEAF_MAX)
+    {
+        /* a leaf holds at most QR_BVH_LEAF_MAX items: halve the node at
+         * the median centroid of its widest axis (or in list order) */
+        int ax = 0;
+        for (int k = 1; k < 3; k++)
+            if (cb.hi[k] - cb.lo[k] > cb.hi[ax] - cb.lo[ax]) ax = k;
+        mid = lo + n / 2;
+        if (cb.hi[ax] > cb.lo[ax])
+            std::nth_element(&p[lo], &p[mid], &p[lo] + n, [ax](const Prim &u, const Prim &v) {
+                return u.c[ax] < v.c[ax];
+            });
+    }
     qr_bnode nd;
     memset(&nd, 0, sizeof(nd));
     for (int k = 0; k < 3; k++)
@@ -440,6 +453,28 @@ int build_node(std::vector<Prim> &p, int lo, int hi, int depth, qr_accel_host *o
 }
 
 } /* namespace */
+
+void qr_accel_pairs(const std::vector<qr_bnode> &nodes, std::vector<qr_bpair> &pairs)
+{
+    pairs.assign(nodes.size(), qr_bpair());
+    for (size_t i = 0; i < nodes.size(); i++)
+    {
+        const qr_bnode &nd = nodes[i];
+        qr_bpair &pr = pairs[i];
+        memset(&pr, 0, sizeof(pr));
+        if (nd.count > 0) continue;
+        const qr_bnode &a = nodes[nd.a], &b = nodes[nd.b];
+        for (int k = 0; k < 3; k++)
+        {
+            pr.lo_a[k] = a.lo[k];
+            pr.hi_a[k] = a.hi[k];
+            pr.lo_b[k] = b.lo[k];
+            pr.hi_b[k] = b.hi[k];
+        }
+        pr.code_a = qr_bnode_code(a, nd.a);
+        pr.code_b = qr_bnode_code(b, nd.b);
+    }
+}
 
 /* node boxes of a tree whose items' boxes changed, bottom-up: nodes are
  * stored parent before children (build_node), so a reverse sweep sees
@@ -700,7 +735,8 @@ void qr_accel_build_levels(const qr_scene_desc *d, qr_accel_host *out,
         out->lbounded[l] = lv.bounded;
         const int i0 = (int)out->items.size();
         anum[l] = (int)lv.always.size();
-        r2[l] = (lv.depth < QR_BVH_STACK - 2 && !lv.nodes.empty()) ? lv.ray_r2 : -1.0f;
+        r2[l] = (lv.depth < QR_BVH_STACK - 2 && !lv.nodes.empty() &&
+                 i0 + lv.items.size() <= (size_t)QR_BVH_MAX_ITEMS) ? lv.ray_r2 : -1.0f;
         if (l == 0)
         {
             for (int k = 0; k < 3; k++) out->ray_c[k] = lv.ray_c[k];

@@ -41,6 +41,37 @@ struct qr_bnode
     int32_t pad[3];
 };
 
+/* leaves hold at most QR_BVH_LEAF_MAX items, and a level at most
+ * QR_BVH_MAX_ITEMS items: a leaf is then coded in one int (qr_bpair) */
+#define QR_BVH_LEAF_MAX 15
+#define QR_BVH_MAX_ITEMS (1 << 26)
+
+/* the two children of an inner node as the walk reads them, 64 bytes:
+ * each child's box, and in the fourth word of its lo group the child's
+ * code: an inner node's index, or for a leaf ~(first item << 4 | count).
+ * One record a node (a leaf's is unused); the device update rewrites the
+ * boxes from the nodes' after each refit */
+struct qr_bpair
+{
+    float   lo_a[3];
+    int32_t code_a;
+    float   hi_a[3];
+    int32_t pad_a;
+    float   lo_b[3];
+    int32_t code_b;
+    float   hi_b[3];
+    int32_t pad_b;
+};
+
+/* the walk's code of node i (see qr_bpair) */
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+static inline int32_t qr_bnode_code(const qr_bnode &n, int32_t i)
+{
+    return n.count > 0 ? (int32_t)~(((uint32_t)n.a << 4) | (uint32_t)n.count) : i;
+}
+
 /* one surface of the list: its position in the list (tie order), record
  * index, and the transform node whose cached transform the walk applies
  * (-1: the surface's own transform or translation) */
@@ -77,6 +108,9 @@ struct qr_accel_host
  * level l serves rays starting within 8^l times the base radius of the
  * scene's centre, its boxes allowing for their rounding; returns 0 */
 int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level);
+
+/* the walk's child records of `nodes` (one a node) */
+void qr_accel_pairs(const std::vector<qr_bnode> &nodes, std::vector<qr_bpair> &pairs);
 
 /* all levels concatenated into `out` (node indices and item ranges shifted
  * by the preceding levels); per level its root node, its unbounded surfaces

@@ -26,6 +26,7 @@
 #include <float.h>
 #include <math.h>
 #include "anim.cuh"
+#include "tracer.cuh"
 #include "anim_box.h"
 #include "xform.h"
 
@@ -208,6 +209,24 @@ __global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev *devs)
             __syncthreads();
         }
     }
+    __syncthreads();
+
+    /* stage 5: the walk's child records take the children's new boxes (the
+     * codes, which follow the topology, stay) */
+    for (int i = tid; i < A.nbvh; i += nt)
+    {
+        const qr_bnode &nd = A.bvh[i];
+        if (nd.count > 0) continue;
+        const qr_bnode &ca = A.bvh[nd.a], &cb = A.bvh[nd.b];
+        qr_bpair &pr = A.pairs[i];
+        for (int k = 0; k < 3; k++)
+        {
+            pr.lo_a[k] = ca.lo[k];
+            pr.hi_a[k] = ca.hi[k];
+            pr.lo_b[k] = cb.lo[k];
+            pr.hi_b[k] = cb.hi[k];
+        }
+    }
     if (tid == 0)
     {
         A.status[0] += 1;
@@ -221,5 +240,6 @@ cudaError_t qr_launch_anim(const qr_anim_dev *devs, int n, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
     anim_kernel<<<n, 512, 0, stream>>>(devs);
+    qr_note_launches(stream, 1);
     return cudaGetLastError();
 }

@@ -26,6 +26,7 @@ struct qr_anim_dev
     int32_t              ntargets, nsrf;
     float               *lboxes;    /* [QR_BVH_LEVELS][nsrf][6] surface boxes */
     qr_bnode            *bvh;       /* hierarchy nodes, all levels */
+    qr_bpair            *pairs;     /* the walk's child records of the nodes */
     const qr_bitem      *items;
     const int32_t       *rorder;    /* nodes by depth, deepest first */
     const int32_t       *depth_off; /* depth band b: rorder[depth_off[b], depth_off[b+1]) */

@@ -58,6 +58,7 @@ struct qr_batch
     int          graph_ok;
     int          launched;
     int          sms;
+    int          graph_kernels;  /* kernel nodes of the captured graph */
     /* path-traced requests: wavefront capacities of each PT job, and the
      * scratch that fits the largest */
     std::vector<qr_wf_caps> pt_caps;
@@ -285,6 +286,20 @@ extern "C" int qr_batch_launch(qr_batch *b, void *stream)
             if (e2 != cudaSuccess) e = e2;
         }
         if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+        b->graph_kernels = 0;
+        size_t nn = 0;
+        if (e == cudaSuccess) e = cudaGraphGetNodes(g, NULL, &nn);
+        if (e == cudaSuccess && nn > 0)
+        {
+            std::vector<cudaGraphNode_t> nodes(nn);
+            e = cudaGraphGetNodes(g, nodes.data(), &nn);
+            for (size_t i = 0; i < nn && e == cudaSuccess; i++)
+            {
+                cudaGraphNodeType t;
+                e = cudaGraphNodeGetType(nodes[i], &t);
+                if (e == cudaSuccess && t == cudaGraphNodeTypeKernel) b->graph_kernels++;
+            }
+        }
         if (g) cudaGraphDestroy(g);
         if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch graph capture", e);
         b->graph_ok = 1;
@@ -293,6 +308,7 @@ extern "C" int qr_batch_launch(qr_batch *b, void *stream)
      * the completion flags before the graph can set them */
     memset(b->hdone, 0, sizeof(uint32_t) * b->reqs.size());
     e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
+    if (e == cudaSuccess) qr_note_launches((cudaStream_t)stream, b->graph_kernels);
     if (e == cudaSuccess) e = cudaEventRecord(b->done, (cudaStream_t)stream);
     if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch graph launch", e);
     b->launched = 1;

@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -108,6 +109,22 @@ struct qr_ctx
 #define QR_WH_MAX_SAMPLES (2ll << 20)
 #define QR_WF_Q_PER_PATH 2
 #define QR_WF_POOL_PER_PATH 8
+
+/* kernels the library has launched (graph launches count their kernels) */
+static std::atomic<unsigned long long> g_launches(0);
+
+void qr_note_launches(cudaStream_t stream, int n)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+        return;
+    g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed);
+}
+
+extern "C" unsigned long long qr_kernel_launches(void)
+{
+    return g_launches.load(std::memory_order_relaxed);
+}
 
 static int fail(qr_ctx *ctx, int code, const char *what, cudaError_t e)
 {
@@ -321,9 +338,12 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     size_t o_lel = o_elm + al16(sizeof(qr_elem) * d->nelem);
     size_t o_tex = o_lel + al16(sizeof(qr_lelem) * d->nlelem);
     size_t o_nod = o_tex + al16(sizeof(uint32_t) * d->ntex);
-    size_t o_itm = o_nod + al16(sizeof(qr_bnode) * acc.nodes.size());
+    size_t o_par = o_nod + al16(sizeof(qr_bnode) * acc.nodes.size());
+    size_t o_itm = o_par + al16(sizeof(qr_bpair) * acc.nodes.size());
     size_t o_alw = o_itm + al16(sizeof(qr_bitem) * acc.items.size());
     size_t total = o_alw + al16(sizeof(qr_bitem) * acc.always.size());
+    std::vector<qr_bpair> pairs;
+    qr_accel_pairs(acc.nodes, pairs);
 
     std::vector<unsigned char> h(total, 0);
     memcpy(&h[o_srf], d->srf, sizeof(qr_srf) * d->nsrf);
@@ -333,7 +353,10 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     memcpy(&h[o_lel], d->lelems, sizeof(qr_lelem) * d->nlelem);
     memcpy(&h[o_tex], d->texels, sizeof(uint32_t) * d->ntex);
     if (!acc.nodes.empty())
+    {
         memcpy(&h[o_nod], acc.nodes.data(), sizeof(qr_bnode) * acc.nodes.size());
+        memcpy(&h[o_par], pairs.data(), sizeof(qr_bpair) * pairs.size());
+    }
     if (!acc.items.empty())
         memcpy(&h[o_itm], acc.items.data(), sizeof(qr_bitem) * acc.items.size());
     if (!acc.always.empty())
@@ -369,6 +392,7 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     sl.d.cam_off = d->cam_off;
     sl.d.cam_num = d->cam_num;
     sl.d.nodes = (const qr_bnode *)(b + o_nod);
+    sl.d.pairs = (const qr_bpair *)(b + o_par);
     sl.d.items = (const qr_bitem *)(b + o_itm);
     sl.d.always = (const qr_bitem *)(b + o_alw);
     sl.d.nnodes = use_bvh ? (int32_t)acc.nodes.size() : -1;
@@ -643,6 +667,7 @@ static int anim_prepare(qr_ctx *ctx, qr_scene_slot *sl, const qr_scene_desc *des
     D.nsrf = desc->nsrf;
     D.lboxes = (float *)(blk + o_lbx);
     D.bvh = const_cast<qr_bnode *>(sl->d.nodes);
+    D.pairs = const_cast<qr_bpair *>(sl->d.pairs);
     D.items = sl->d.items;
     D.rorder = (const int32_t *)(blk + o_ror);
     D.depth_off = (const int32_t *)(blk + o_dof);

@@ -282,6 +282,7 @@ cudaError_t qr_launch_batch(int mode, const qr_job *jobs, int njobs, int total_t
         QR_NS::batch_kernel<1><<<blocks, block, 0, stream>>>(jobs, njobs, total_tiles,
                                                             counter, tw, th, grab,
                                                             tiles_done, done);
+    qr_note_launches(stream, 1);
     return cudaGetLastError();
 }
 
@@ -316,6 +317,7 @@ cudaError_t qr_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *
         QR_NS::pt_kernel<1><<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, ds);
     else
         QR_NS::pt_kernel<0><<<grid, block, 0, stream>>>(sc, fp, acc, dev_frame, ds);
+    qr_note_launches(stream, 1);
     return cudaGetLastError();
 }
 
@@ -336,11 +338,13 @@ cudaError_t qr_launch_whitted(const qr_dscene &sc, const qr_frame_params &fp,
     {
         const dim3 grid((fp.x_res + 7) / 8, (fp.y_res + 3) / 4);
         QR_NS::whitted_aa_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, dstats);
+        qr_note_launches(stream, 1);
         return cudaGetLastError();
     }
     const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
                     (fp.y_res + 2 * QR_TILE_H - 1) / (2 * QR_TILE_H));
     QR_NS::whitted_kernel<<<grid, block, 0, stream>>>(sc, fp, dev_frame, dstats);
+    qr_note_launches(stream, 1);
     return cudaGetLastError();
 }
 

@@ -28,6 +28,7 @@ struct qr_dscene
      * when the scene has none.  The shadow list [shd_off, shd_off + shd_num)
      * holds the same surfaces, so shadow rays use it too */
     const qr_bnode *nodes;          /* all levels, concatenated */
+    const qr_bpair *pairs;          /* the walk's child records, one a node */
     const qr_bitem *items;
     const qr_bitem *always;
     int32_t nnodes, nitems, nalways;
@@ -42,6 +43,11 @@ struct qr_dscene
      * pixel that set one, count of such pixels (NULL: not recorded) */
     uint32_t *fault;
 };
+
+/* count n kernel launches on `stream` in the library's total
+ * (qr_kernel_launches); launches into a stream capture are not counted
+ * there: a graph's kernels count when the graph is launched */
+void qr_note_launches(cudaStream_t stream, int n);
 
 /* per-launch counters (instrumented runs only) */
 struct qr_dstats

@@ -38,6 +38,7 @@
 #define D_EPS       0.00000000001f  /* root-sorting threshold, object.h:41 */
 #define T_EPS       0.0000001f      /* root-split threshold, object.h:42 */
 #define SIGN_BIT    0x80000000u
+#define QR_CODE_NONE ((int)0x80000000)  /* no code (qr_bpair codes are above it) */
 
 /*
  * Work counters: with QR_STATS defined (tracer_stats.cu) the code lives in
@@ -492,13 +493,12 @@ __device__ __forceinline__ void local_ray(const qr_dscene &S, const Ray &r, int 
  * fused multiply-add (oinv = org * inv per ray).  The test only prunes
  * nodes and every box carries a margin far above this rounding, so which
  * surfaces are tested, and the frame, do not depend on it. */
-__device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray &r,
-                                       const float inv[3], const float oinv[3], float tmax,
-                                       float &tn, StP st)
+__device__ __forceinline__ int box_hit4(const float4 l4, const float4 h4, const Ray &r,
+                                        const float inv[3], const float oinv[3], float tmax,
+                                        float &tn, StP st)
 {
     CNT(QR_STAT_BOX_TEST);
     float t0 = -FLT_MAX, t1 = FLT_MAX;
-    const float4 l4 = ldf4(n->lo), h4 = ldf4(n->hi);
     const float los[3] = {l4.x, l4.y, l4.z}, his[3] = {h4.x, h4.y, h4.z};
     #pragma unroll
     for (int k = 0; k < 3; k++)
@@ -516,6 +516,13 @@ __device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray
     }
     tn = t0;
     return t0 <= t1 && t1 >= r.t_min && t0 <= tmax;
+}
+
+__device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray &r,
+                                       const float inv[3], const float oinv[3], float tmax,
+                                       float &tn, StP st)
+{
+    return box_hit4(ldf4(n->lo), ldf4(n->hi), r, inv, oinv, tmax, tn, st);
 }
 
 /*
@@ -549,8 +556,8 @@ static __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const 
     float cdff[3] = {0.0f, 0.0f, 0.0f}, cray[3] = {0.0f, 0.0f, 0.0f};
     /* hierarchy source */
     int ai = 0, ia = 0, ib = 0, sp = 0;
-    int2 stk[QR_BVH_STACK];         /* node, entry distance (float bits) */
-    int cur = -1;                   /* node to visit next without a pop */
+    int2 stk[QR_BVH_STACK];         /* code, entry distance (float bits) */
+    int cur = QR_CODE_NONE;         /* code (qr_bpair) to take next without a pop */
     float inv[3], oinv[3];
     int aend = 0;
     if (use_bvh)
@@ -568,7 +575,7 @@ static __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const 
         if (box_hit(&S.nodes[root], r, inv, oinv, w.tbuf, tn, st))
         {
             (void)tn;
-            cur = root;
+            cur = qr_bnode_code(S.nodes[root], root);
         }
     }
 
@@ -623,43 +630,46 @@ static __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const 
                 /* near child first: it is visited at once, the far one
                  * pushed with its entry distance and skipped on the pop
                  * if a hit nearer than that has been found meanwhile */
+                /* an inner node's record holds both children's boxes and
+                 * codes: one fetch a visit; a leaf is taken from its code */
                 #pragma unroll 1
                 while (ia >= ib)
                 {
-                    int node = cur;
-                    if (node >= 0)
+                    int code = cur;
+                    if (code != QR_CODE_NONE)
                     {
-                        cur = -1;
+                        cur = QR_CODE_NONE;
                     }
                     else
                     {
                         if (sp <= 0) break;
                         const int2 e = stk[--sp];
                         if (__int_as_float(e.y) > w.tbuf) continue;
-                        node = e.x;
+                        code = e.x;
                     }
-                    const qr_bnode *__restrict__ n = &S.nodes[node];
-                    const int cnt = __ldg(&n->count);
-                    const int a = __ldg(&n->a);
-                    if (cnt > 0)
+                    if (code < 0)
                     {
-                        ia = a;
-                        ib = a + cnt;
+                        const int lc = ~code;
+                        ia = lc >> 4;
+                        ib = ia + (lc & 15);
                         continue;
                     }
-                    const int b = __ldg(&n->b);
+                    const qr_bpair *__restrict__ pr = &S.pairs[code];
+                    const float4 la = ldf4(pr->lo_a), ha4 = ldf4(pr->hi_a);
+                    const float4 lb = ldf4(pr->lo_b), hb4 = ldf4(pr->hi_b);
                     float ta, tb;
-                    const int ha = box_hit(&S.nodes[a], r, inv, oinv, w.tbuf, ta, st);
-                    const int hb = box_hit(&S.nodes[b], r, inv, oinv, w.tbuf, tb, st);
+                    const int ha = box_hit4(la, ha4, r, inv, oinv, w.tbuf, ta, st);
+                    const int hb = box_hit4(lb, hb4, r, inv, oinv, w.tbuf, tb, st);
+                    const int ca = __float_as_int(la.w), cb = __float_as_int(lb.w);
                     if (ha && hb)
                     {
                         if (sp >= QR_BVH_STACK) { w.fault = QR_FAULT_STACK; return; }
                         const int near_a = ta <= tb;
-                        stk[sp++] = make_int2(near_a ? b : a, __float_as_int(near_a ? tb : ta));
-                        cur = near_a ? a : b;
+                        stk[sp++] = make_int2(near_a ? cb : ca, __float_as_int(near_a ? tb : ta));
+                        cur = near_a ? ca : cb;
                     }
-                    else if (ha) cur = a;
-                    else if (hb) cur = b;
+                    else if (ha) cur = ca;
+                    else if (hb) cur = cb;
                 }
                 if (ia >= ib) break;
                 it = &S.items[ia++];
@@ -1541,10 +1551,13 @@ __device__ __forceinline__ int tile_y()
 
 /* blocks of 32x4 threads; QR_MIN_BLOCKS resident blocks per SM bound the
  * registers per thread (65536 / (128 * QR_MIN_BLOCKS)).  Measured on the
- * 1920x1080 4x AA animated frame: 1 (152 registers) 55.0 ms, unbounded (128)
- * 48.0 ms, 5 (96) 44.8 ms, 6 (80) 44.0 ms, 8 (64) 46.5 ms */
+ * 1920x1080 4x AA animated frame with a thread a pixel: 1 (152 registers)
+ * 55.0 ms, unbounded (128) 48.0 ms, 5 (96) 44.8 ms, 6 (80) 44.0 ms, 8 (64)
+ * 46.5 ms; with a thread a sub-sample (whitted_aa_kernel): 6 (80) 21.07 ms,
+ * 7 (72) 20.67 ms, and with 256 quadrics 65.0 against 61.8 ms (the
+ * 800x480 plain frame 0.105 ms both) */
 #ifndef QR_MIN_BLOCKS
-#define QR_MIN_BLOCKS 6
+#define QR_MIN_BLOCKS 7
 #endif
 /* the path tracer's own bound: 6 (80 registers) 66.5 ms, 8 (64) 67.9 ms
  * on the 1280x720 16-spp frame with 64-byte pending-node records */

@@ -385,6 +385,7 @@ __global__ void wf_mark_done(uint32_t *done, int req)
 cudaError_t qr_wf_mark_done(uint32_t *done, int req, cudaStream_t stream)
 {
     wf_mark_done<<<1, 1, 0, stream>>>(done, req);
+    qr_note_launches(stream, 1);
     return cudaGetLastError();
 }
 
@@ -459,6 +460,7 @@ cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, floa
         for (int d = levels - 1; d >= 0; d--)
             wf_fold<<<blocks, 128, 0, stream>>>(d, pool, samples, ctl);
         wf_accum<<<blocks, 128, 0, stream>>>(fp, c0, c1, ppad, tx, samples, sums, ctl);
+        qr_note_launches(stream, 2 + 2 * levels);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -468,6 +470,7 @@ cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, floa
         const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
                         (fp.y_res + 2 * QR_TILE_H - 1) / (2 * QR_TILE_H));
         wf_fallback<<<grid, block, 0, stream>>>(sc, fp, acc, frame, ctl);
+        qr_note_launches(stream, 2);
         e = cudaGetLastError();
     }
     return e;

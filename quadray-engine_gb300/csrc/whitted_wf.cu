@@ -498,6 +498,7 @@ cudaError_t qr_wh_launch(const qr_dscene &sc, const qr_frame_params &fp, uint32_
         for (int d = levels - 1; d >= 0; d--)
             wh_fold<<<blocks, 128, 0, stream>>>(d, pool, samples, ctl);
         wh_pack<<<blocks, 128, 0, stream>>>(fp, c0, c1, ns, tx, samples, frame, ctl);
+        qr_note_launches(stream, 2 + 4 * levels);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -506,6 +507,7 @@ cudaError_t qr_wh_launch(const qr_dscene &sc, const qr_frame_params &fp, uint32_
         const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
                         (fp.y_res + 2 * QR_TILE_H - 1) / (2 * QR_TILE_H));
         wh_fallback<<<grid, block, 0, stream>>>(sc, fp, frame, ctl);
+        qr_note_launches(stream, 1);
         e = cudaGetLastError();
     }
     return e;
