@@ -176,6 +176,33 @@ def run_serve(args, wl, rank, world, dist, local):
             rays_of[key] = int(counts[0]) + int(counts[1]) + int(counts[2])
         return rays_of[key] * (req.spp if sc["pt"] else 1)
 
+    alone_ms = {}
+
+    def alone(req):
+        """device time of the request's frame rendered alone (its scene at
+        t = 0, CUDA events, the median of 3)"""
+        sc = scenes[req.scene]
+        fsaa = 0 if (sc["pt"] or req.spp <= 1) else 2
+        key = (req.scene, req.w, req.h, fsaa)
+        if key not in alone_ms:
+            g = qr.GenScene(sc["kind"], wl["seed"] + req.scene, sc["nq"], qr.GEN_SPIN)
+            f = qr.Flat(g, req.w, req.h, fsaa)
+            desc, params = f.update(0, sc["depth"])
+            sid = ctx.upload(desc)
+            fr = torch.empty((req.h, params.x_row), dtype=torch.int32, device="cuda")
+            s = torch.cuda.current_stream()
+            ts = []
+            for _ in range(4):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                ctx.render_device(sid, params, fr.data_ptr(), s.cuda_stream)
+                e1.record(s)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ctx.release(sid)
+            alone_ms[key] = float(np.median(ts[1:]))
+        return alone_ms[key]
+
     urgent = None
     if args.serve_urgent:
         # 1080p Whitted frames, whose latency has a target, go first
@@ -204,6 +231,8 @@ def run_serve(args, wl, rank, world, dist, local):
         big = np.array([r.done - r.arrival for r in done
                         if (r.w, r.h) == (1920, 1080) and not scenes[r.scene]["pt"]]) * 1000.0
         prep = np.array([r.prepared - r.arrival for r in done if r.prepared]) * 1000.0
+        big_alone = np.array([alone(r) for r in done
+                              if (r.w, r.h) == (1920, 1080) and not scenes[r.scene]["pt"]])
         results.append({"rate_per_s": rate, "requests": len(reqs), "seconds": wall,
                         "rays_per_s": total / wall,
                         "frames_per_s": len(reqs) / wall,
@@ -211,6 +240,10 @@ def run_serve(args, wl, rank, world, dist, local):
                         "latency_ms_p99": float(np.percentile(lat, 99)),
                         "whitted_1080p_ms_p50": float(np.percentile(big, 50)) if len(big) else None,
                         "whitted_1080p_ms_p99": float(np.percentile(big, 99)) if len(big) else None,
+                        "whitted_1080p_alone_ms_p50": float(np.percentile(big_alone, 50))
+                        if len(big_alone) else None,
+                        "whitted_1080p_alone_ms_p99": float(np.percentile(big_alone, 99))
+                        if len(big_alone) else None,
                         "prepared_ms_p99": float(np.percentile(prep, 99)) if len(prep) else None})
     ck = clocks.stop()
     launches = qr.kernel_launches() - l0

@@ -30,6 +30,12 @@
 #include "tracer.cuh"
 #include "wavefront.h"
 
+/* side streams of the path-traced requests: their frames run side by side,
+ * so one frame's stage tails overlap another's work */
+#ifndef QR_BATCH_PT_STREAMS
+#define QR_BATCH_PT_STREAMS 2
+#endif
+
 int qr_internal_scene(qr_ctx *ctx, int scene_id, const qr_dscene **sc, int *device);
 int qr_internal_check_fp(const qr_frame_params *fp);
 int qr_internal_device(qr_ctx *ctx);
@@ -52,18 +58,21 @@ struct qr_batch
     int          tiles[2];      /* tiles per mode */
     int          tw, th, grab;
     int          blocks[2];
-    cudaStream_t main, side;
-    cudaEvent_t  fork, join, done;
+    cudaStream_t main, side[QR_BATCH_PT_STREAMS];
+    cudaEvent_t  fork, join[QR_BATCH_PT_STREAMS], done;
     cudaGraphExec_t exec;
     int          graph_ok;
     int          launched;
     int          sms;
     int          graph_kernels;  /* kernel nodes of the captured graph */
-    /* path-traced requests: wavefront capacities of each PT job, and the
-     * scratch that fits the largest */
+    /* path-traced requests: wavefront capacities of each PT job, the side
+     * stream each runs on, and a scratch per side stream that fits the
+     * largest */
     std::vector<qr_wf_caps> pt_caps;
-    void        *wf;
+    std::vector<int> pt_stream;
+    void        *wf[QR_BATCH_PT_STREAMS];
     size_t       wf_bytes;
+    int          nwf;            /* scratch blocks allocated */
     std::vector<qr_job> pt_jobs;    /* host copies of the path-traced jobs */
 };
 
@@ -98,9 +107,12 @@ extern "C" int qr_batch_create(qr_ctx *ctx, int max_requests, qr_batch **out)
     if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&b->ddone, b->hdone, 0);
     if (e == cudaSuccess) memset(b->hdone, 0, sizeof(uint32_t) * (size_t)max_requests);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    for (int k = 0; k < QR_BATCH_PT_STREAMS && e == cudaSuccess; k++)
+    {
+        e = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     int sms = 0;
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
@@ -130,11 +142,14 @@ extern "C" int qr_batch_destroy(qr_batch *b)
     if (b->dtiles) cudaFree(b->dtiles);
     if (b->hdone) cudaFreeHost(b->hdone);
     if (b->main) cudaStreamDestroy(b->main);
-    if (b->side) cudaStreamDestroy(b->side);
+    for (int k = 0; k < QR_BATCH_PT_STREAMS; k++)
+    {
+        if (b->side[k]) cudaStreamDestroy(b->side[k]);
+        if (b->join[k]) cudaEventDestroy(b->join[k]);
+        if (b->wf[k]) cudaFree(b->wf[k]);
+    }
     if (b->fork) cudaEventDestroy(b->fork);
-    if (b->join) cudaEventDestroy(b->join);
     if (b->done) cudaEventDestroy(b->done);
-    if (b->wf) cudaFree(b->wf);
     delete b;
     return QR_OK;
 }
@@ -183,9 +198,11 @@ static int upload_jobs(qr_batch *b)
                                    cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return bfail(b, QR_ERR_CUDA, "batch job upload", e);
     }
-    /* the path-traced jobs' wavefront capacities and the scratch for the
-     * largest */
+    /* the path-traced jobs' wavefront capacities, their side streams (each
+     * job to the stream with the least work so far, by pixels x samples,
+     * largest jobs first) and a scratch per stream used for the largest */
     b->pt_caps.clear();
+    b->pt_stream.assign(b->np, 0);
     size_t need = 0;
     for (int j = b->nw; j < b->nw + b->np; j++)
     {
@@ -193,14 +210,41 @@ static int upload_jobs(qr_batch *b)
         b->pt_caps.push_back(c);
         need = std::max(need, qr_wf_bytes(c));
     }
-    if (need > b->wf_bytes)
     {
-        if (b->wf) cudaFree(b->wf);
-        b->wf = NULL;
+        std::vector<int> ord(b->np);
+        for (int j = 0; j < b->np; j++) ord[j] = j;
+        auto work = [&](int j) {
+            const qr_frame_params &P = jobs[b->nw + j].P;
+            return (double)P.x_res * P.y_res * P.pt_on;
+        };
+        std::stable_sort(ord.begin(), ord.end(), [&](int u, int v) { return work(u) > work(v); });
+        double load[QR_BATCH_PT_STREAMS] = {0.0};
+        for (int j : ord)
+        {
+            int k = 0;
+            for (int q = 1; q < QR_BATCH_PT_STREAMS; q++)
+                if (load[q] < load[k]) k = q;
+            b->pt_stream[j] = k;
+            load[k] += work(j);
+        }
+    }
+    const int nwf = std::min(b->np, QR_BATCH_PT_STREAMS);
+    if (need > b->wf_bytes || nwf > b->nwf)
+    {
+        for (int k = 0; k < QR_BATCH_PT_STREAMS; k++)
+        {
+            if (b->wf[k]) cudaFree(b->wf[k]);
+            b->wf[k] = NULL;
+        }
         b->wf_bytes = 0;
-        cudaError_t e = cudaMalloc(&b->wf, need);
-        if (e != cudaSuccess) return bfail(b, QR_ERR_OOM, "batch wavefront scratch", e);
+        b->nwf = 0;
+        for (int k = 0; k < nwf; k++)
+        {
+            cudaError_t e = cudaMalloc(&b->wf[k], need);
+            if (e != cudaSuccess) return bfail(b, QR_ERR_OOM, "batch wavefront scratch", e);
+        }
         b->wf_bytes = need;
+        b->nwf = nwf;
     }
     b->pt_jobs.assign(jobs.begin() + b->nw, jobs.end());
     if (b->exec)
@@ -246,27 +290,34 @@ extern "C" int qr_batch_config(qr_batch *b, int tile_w, int grab)
     return upload_jobs(b);
 }
 
-/* the two persistent launches on b->main (and b->side) */
+/* the Whitted persistent launch on b->main, the path-traced frames on the
+ * side streams */
 static cudaError_t enqueue(qr_batch *b)
 {
     cudaError_t e = cudaMemsetAsync(b->dcount, 0, 2 * sizeof(int), b->main);
     if (e == cudaSuccess && b->nw + b->np > 0)
         e = cudaMemsetAsync(b->dtiles, 0, sizeof(int) * (size_t)(b->nw + b->np), b->main);
     if (e == cudaSuccess) e = cudaEventRecord(b->fork, b->main);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork, 0);
+    for (int k = 0; k < QR_BATCH_PT_STREAMS && e == cudaSuccess; k++)
+        e = cudaStreamWaitEvent(b->side[k], b->fork, 0);
     if (e == cudaSuccess)
         e = qr_launch_batch(0, b->djobs, b->nw, b->tiles[0], b->dcount, b->tw, b->th,
                             b->grab, b->blocks[0], b->dtiles, b->ddone, b->main);
-    /* the path-traced requests one after the other on the side stream,
+    /* the path-traced requests one after the other on each side stream,
      * each marked done as soon as its frame is in device memory */
     for (int j = 0; j < b->np && e == cudaSuccess; j++)
     {
         const qr_job &J = b->pt_jobs[j];
-        e = qr_wf_launch_pt(J.S, J.P, J.acc, J.frame, b->wf, b->pt_caps[j], b->sms, b->side);
-        if (e == cudaSuccess) e = qr_wf_mark_done(b->ddone, J.req, b->side);
+        const int k = b->pt_stream[j];
+        e = qr_wf_launch_pt(J.S, J.P, J.acc, J.frame, b->wf[k], b->pt_caps[j], b->sms,
+                            b->side[k]);
+        if (e == cudaSuccess) e = qr_wf_mark_done(b->ddone, J.req, b->side[k]);
     }
-    if (e == cudaSuccess) e = cudaEventRecord(b->join, b->side);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->main, b->join, 0);
+    for (int k = 0; k < QR_BATCH_PT_STREAMS && e == cudaSuccess; k++)
+    {
+        e = cudaEventRecord(b->join[k], b->side[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->main, b->join[k], 0);
+    }
     return e;
 }
 

@@ -10,7 +10,9 @@
  *
  *   wf_gen    camera rays of a chunk of samples, pixel tiles of 8 x 4 in a
  *             warp, appended to level 0's queue;
- *   wf_step   level d: each ray walks the scene (nearest hit), the hit is
+ *   wf_trace  level d: each ray walks the scene to its nearest hit, which
+ *             is stored for the next stage (32 bytes a ray);
+ *   wf_step   level d: each ray's hit is
  *             shaded (the node's random draws, emission, roulette,
  *             cosine-weighted bounce, the dielectric split) into a node
  *             record, and the node's children are appended to level d+1's
@@ -65,6 +67,56 @@ struct WNode
 #ifndef QR_WF_MIN_BLOCKS
 #define QR_WF_MIN_BLOCKS 6
 #endif
+#ifndef QR_WF_TRACE_MIN_BLOCKS
+#define QR_WF_TRACE_MIN_BLOCKS 6
+#endif
+
+/* a ray's nearest hit from the tracing stage, 32 bytes: hit point and
+ * surface (-1: none), local hit point and side | walk fault << 8 */
+struct WHit
+{
+    float4 h;
+    float4 l;
+};
+
+/* level d's nearest hits: warps take runs of 32 rays as they come free.
+ * The walk in a kernel of its own, ahead of the shading: each kernel is
+ * smaller (the shading's registers no longer spill around the walk), and
+ * the 1280x720 64-spp frame takes 175.0 against 181.9 ms with the walk
+ * inside the shading stage (at 8 resident blocks for the shading 177.0,
+ * and for both 178.6 ms) */
+__global__ void __launch_bounds__(128, QR_WF_TRACE_MIN_BLOCKS)
+wf_trace(const qr_dscene S, const qr_frame_params P, int d, const WRay *__restrict__ qin,
+         WHit *hits, WCtl *ctl)
+{
+    if (ctl->overflow) return;
+    const int n = ctl->cnt[d];
+    const int lane = threadIdx.x & 31;
+    #pragma unroll 1
+    for (;;)
+    {
+        int i0 = 0;
+        if (lane == 0) i0 = atomicAdd(&ctl->tnext[d], 32);
+        i0 = __shfl_sync(0xFFFFFFFFu, i0, 0);
+        if (i0 >= n) break;
+        const int i = i0 + lane;
+        if (i >= n) continue;
+        Ray r;
+        int off, num;
+        get_ray(qin[i], S, r, off, num);
+        Walk w;
+        walk_init(w, r, 0);
+        walk(S, P, r, off, num, w, NULL);
+        /* a ray without a hit has no side (the field is not set) */
+        const int side = w.best.srf >= 0 ? (w.best.side & 1) : 0;
+        WHit hh;
+        hh.h = make_float4(w.best.hit[0], w.best.hit[1], w.best.hit[2],
+                           __int_as_float(w.best.srf));
+        hh.l = make_float4(w.best.loc[0], w.best.loc[1], w.best.loc[2],
+                           __int_as_float(side | (w.fault << 8)));
+        hits[i] = hh;
+    }
+}
 
 /* level 0: camera rays of paths [c0, c1) */
 __global__ void __launch_bounds__(128)
@@ -99,10 +151,12 @@ wf_gen(const qr_frame_params P, long long c0, long long c1, int ppad, int tx,
     }
 }
 
-/* level d: walk, shade, append the children to level d + 1 */
+/* level d: take the tracing stage's hit, shade, append the children to
+ * level d + 1 */
 __global__ void __launch_bounds__(128, QR_WF_MIN_BLOCKS)
 wf_step(const qr_dscene S, const qr_frame_params P, int d, const WRay *__restrict__ qin,
-        WRay *qout, WNode *pool, WCtl *ctl, int cap_q, int cap_pool)
+        const WHit *__restrict__ hits, WRay *qout, WNode *pool, WCtl *ctl, int cap_q,
+        int cap_pool)
 {
     if (ctl->overflow) return;
     const int n = ctl->cnt[d];
@@ -148,7 +202,15 @@ wf_step(const qr_dscene S, const qr_frame_params P, int d, const WRay *__restric
             w.tbuf = r.t_max;
             w.bestp = -1;
             w.best.srf = -1;
-            walk(S, P, r, off, num, w, NULL);
+            {
+                const WHit hh = hits[i];
+                const int bits = __float_as_int(hh.l.w);
+                w.best.srf = __float_as_int(hh.h.w);
+                w.best.side = bits & 1;
+                w.fault = (int)((unsigned)bits >> 8);
+                w.best.hit[0] = hh.h.x; w.best.hit[1] = hh.h.y; w.best.hit[2] = hh.h.z;
+                w.best.loc[0] = hh.l.x; w.best.loc[1] = hh.l.y; w.best.loc[2] = hh.l.z;
+            }
             WNode &N = pool[base + i];
             if (w.fault)
             {
@@ -392,6 +454,7 @@ cudaError_t qr_wf_mark_done(uint32_t *done, int req, cudaStream_t stream)
 size_t qr_wf_bytes(const qr_wf_caps &c)
 {
     return sizeof(WCtl) + 2 * (size_t)c.cap_q * sizeof(WRay) +
+           (size_t)c.cap_q * sizeof(WHit) + 256 +
            (size_t)c.cap_pool * sizeof(WNode) + (size_t)c.cap_paths * sizeof(float4) +
            (size_t)c.cap_px * sizeof(float4) + 5 * 256;
 }
@@ -427,6 +490,8 @@ cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, floa
     b += al256((size_t)caps.cap_q * sizeof(WRay));
     WRay *qb = (WRay *)b;
     b += al256((size_t)caps.cap_q * sizeof(WRay));
+    WHit *hits = (WHit *)b;
+    b += al256((size_t)caps.cap_q * sizeof(WHit));
     WNode *pool = (WNode *)b;
     b += al256((size_t)caps.cap_pool * sizeof(WNode));
     float4 *samples = (float4 *)b;
@@ -454,13 +519,14 @@ cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, floa
         for (int d = 0; d < levels; d++)
         {
             WRay *qi = (d & 1) ? qb : qa, *qo = (d & 1) ? qa : qb;
-            wf_step<<<sblocks, 128, 0, stream>>>(sc, fp, d, qi, qo, pool, ctl,
+            wf_trace<<<sblocks, 128, 0, stream>>>(sc, fp, d, qi, hits, ctl);
+            wf_step<<<sblocks, 128, 0, stream>>>(sc, fp, d, qi, hits, qo, pool, ctl,
                                                  (int)caps.cap_q, (int)caps.cap_pool);
         }
         for (int d = levels - 1; d >= 0; d--)
             wf_fold<<<blocks, 128, 0, stream>>>(d, pool, samples, ctl);
         wf_accum<<<blocks, 128, 0, stream>>>(fp, c0, c1, ppad, tx, samples, sums, ctl);
-        qr_note_launches(stream, 2 + 2 * levels);
+        qr_note_launches(stream, 2 + 3 * levels);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)

@@ -33,6 +33,7 @@ struct WCtl
     int cnt[QR_MAX_DEPTH + 2];      /* rays of each level in this chunk */
     int off[QR_MAX_DEPTH + 2];      /* first pool node of each level */
     int next[QR_MAX_DEPTH + 2];     /* rays of each level handed to warps */
+    int tnext[QR_MAX_DEPTH + 2];    /* the same for the tracing stage */
     int overflow;                   /* a queue or the pool ran full */
     int pad[3];
 };

@@ -94,19 +94,26 @@ class Server:
         self.stream = self._new_stream()
         self.batches = [qr.Batch(ctx, max_batch), qr.Batch(ctx, max_batch)]
         self.free_batches = collections.deque(self.batches)
+        # urgent requests: batches of their own on a stream of the highest
+        # priority, so that their blocks take the SMs as soon as a running
+        # batch frees them, ahead of the batches queued on the other stream
+        self.ustream = self._new_stream(priority=-1) if urgent is not None else None
+        self.ubatches = ([qr.Batch(ctx, max_batch), qr.Batch(ctx, max_batch)]
+                         if urgent is not None else [])
+        self.free_ubatches = collections.deque(self.ubatches)
         self.waiting = collections.deque()      # arrived, not admitted
         self.preparing = []                      # futures
         self.ready = collections.deque()         # prepared, not launched
         self.ready_urgent = collections.deque()  # the same, urgent ones
         self.urgent = urgent
-        self.inflight = collections.deque()      # (batch, [requests])
+        self.inflight = collections.deque()      # (batch, [requests], words, pool)
         self.completed = []
         self.idle_sleep = 100e-6
 
     # ---- device memory ------------------------------------------------
-    def _new_stream(self):
+    def _new_stream(self, priority=0):
         import torch
-        return torch.cuda.Stream()
+        return torch.cuda.Stream(priority=priority)
 
     def _alloc(self, req, pt):
         """the request's frame (and path-tracer sums) in device memory"""
@@ -212,10 +219,17 @@ class Server:
 
     # ---- batches ------------------------------------------------------
     def _launch(self):
+        if self.urgent is None:
+            self._launch_from((self.ready_urgent, self.ready), self.free_batches, self.stream)
+        else:
+            self._launch_from((self.ready_urgent,), self.free_ubatches, self.ustream)
+            self._launch_from((self.ready,), self.free_batches, self.stream)
+
+    def _launch_from(self, queues, free, stream):
         qr = self.qr
-        while (self.ready or self.ready_urgent) and self.free_batches:
+        while any(queues) and free:
             reqs, px = [], 0
-            for q in (self.ready_urgent, self.ready):
+            for q in queues:
                 while q and len(reqs) < self.max_batch:
                     r = q[0]
                     if reqs and px + r.w * r.h > self.max_batch_pixels:
@@ -232,17 +246,17 @@ class Server:
                 q.dev_frame = r.frame.data_ptr()
                 q.dev_acc = r.acc.data_ptr() if r.acc is not None else None
                 table.append(q)
-            b = self.free_batches.popleft()
+            b = free.popleft()
             b.set(table)
             ups = [(r.slot, r.anim) for r in reqs if r.anim is not None]
             if ups:
                 # the batch's scene updates: one launch ahead of the batch
-                self.ctx.anim_update_many(ups, self.stream.cuda_stream)
+                self.ctx.anim_update_many(ups, stream.cuda_stream)
                 for r in reqs:
                     r.anim = None
-            b.launch(self.stream.cuda_stream)
+            b.launch(stream.cuda_stream)
             flags = np.frombuffer(b.done_flags(len(reqs)), dtype=np.uint32)
-            self.inflight.append((b, reqs, flags))
+            self.inflight.append((b, reqs, flags, free))
 
     def _finish(self, r, t):
         r.done = t
@@ -254,7 +268,9 @@ class Server:
         # each request completes when its own frame is done (the batch's
         # per-request completion words), its batch is recycled when all are
         t = None
-        for b, reqs, flags in (self.inflight if self.per_request else ()):
+        for b, reqs, flags, _ in (self.inflight if self.per_request else ()):
+            if b is None:               # recycled: its words belong to a new launch
+                continue
             for i in np.flatnonzero(flags.copy()):    # a snapshot: the device
                                                       # writes the words live
                 r = reqs[i]
@@ -262,12 +278,19 @@ class Server:
                     if t is None:
                         t = now_fn()
                     self._finish(r, t)
-        while self.inflight and self.inflight[0][0].poll():
-            b, reqs, flags = self.inflight.popleft()
+        # batches are recycled in order per stream; either stream's batch at
+        # the head of the in-flight list may finish first
+        for k in range(len(self.inflight)):
+            b, reqs, flags, free = self.inflight[k]
+            if b is None or not b.poll():
+                continue
             for r in reqs:
                 if r.done is None:
                     self._finish(r, now_fn())
-            self.free_batches.append(b)
+            free.append(b)
+            self.inflight[k] = (None, reqs, flags, free)
+        while self.inflight and self.inflight[0][0] is None:
+            self.inflight.popleft()
 
     def step(self, now_fn):
         """one turn of the loop; returns whether anything moved"""
@@ -318,7 +341,7 @@ class Server:
         return done, now()
 
     def close(self):
-        for b in self.batches:
+        for b in self.batches + self.ubatches:
             b.close()
         self.pool.shutdown()
 

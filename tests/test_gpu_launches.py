@@ -1,6 +1,6 @@
 """The library's kernel-launch count (qr_kernel_launches), which the
 benchmark reports as its launches in the timed region: a Whitted frame is
-one kernel, a path-traced frame of the wavefront one chunk of (2 + 2 levels)
+one kernel, a path-traced frame of the wavefront one chunk of (2 + 3 levels)
 stage kernels plus the final and fallback kernels, a device update one
 kernel, and a batch the kernels of its graph at every launch."""
 import pytest
@@ -29,8 +29,9 @@ def test_launch_counts(qr):
     p3.pt_on, p3.pts_c, p3.seed, p3.frame_idx = 8, 0.0, 1, 0
     n0 = qr.kernel_launches()
     ctx.render_pt(sid3, p3, acc.data_ptr(), frame.data_ptr(), sp)
-    # 12 x 14 tiles of 32 paths, 8 samples: one chunk of 9 levels
-    assert qr.kernel_launches() - n0 == (2 + 2 * 9) + 2
+    # 12 x 14 tiles of 32 paths, 8 samples: one chunk of 9 levels (a tracing,
+    # a shading and a folding kernel each)
+    assert qr.kernel_launches() - n0 == (2 + 3 * 9) + 2
     p3.flags = p3.flags | qr.FP_PIXEL_PT
     n0 = qr.kernel_launches()
     ctx.render_pt(sid3, p3, acc.data_ptr(), frame.data_ptr(), sp)
@@ -54,6 +55,6 @@ def test_launch_counts(qr):
     b.launch(sp)
     torch.cuda.synchronize()
     # the Whitted batch kernel, the path-traced frame's kernels, its done mark
-    assert qr.kernel_launches() - n0 == 1 + (2 + 2 * 9) + 2 + 1
+    assert qr.kernel_launches() - n0 == 1 + (2 + 3 * 9) + 2 + 1
     b.close()
     ctx.close()

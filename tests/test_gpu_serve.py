@@ -15,13 +15,13 @@ SCENES = [  # kind, seed, nq, flags, depth
 SIZES = [(64, 48), (96, 54), (128, 72)]
 
 
-def _server(qr, ctx, budget, max_batch, device_anim=False):
+def _server(qr, ctx, budget, max_batch, device_anim=False, urgent=None):
     serve = importlib.import_module("quadray-engine_gb300.serve")
     scenes = [dict(gen=qr.GenScene(k, s, n, f), pt=(k == 3), depth=d,
                    anim=bool(f & qr.GEN_SPIN))
               for (k, s, n, f, d) in SCENES]
     return serve, serve.Server(qr, ctx, scenes, budget_bytes=budget, max_batch=max_batch,
-                               prep_threads=3, device_anim=device_anim)
+                               prep_threads=3, device_anim=device_anim, urgent=urgent)
 
 
 def _alone(qr, ctx, req):
@@ -51,13 +51,17 @@ def _requests(serve, n, seed):
     return out
 
 
-@pytest.mark.parametrize("budget,max_batch,device_anim", [
-    (120 << 30, 6, False), (3 << 20, 4, False), (120 << 30, 6, True), (3 << 20, 4, True)])
-def test_served_frames_equal_frames_alone(qr, budget, max_batch, device_anim):
+@pytest.mark.parametrize("budget,max_batch,device_anim,urgent", [
+    (120 << 30, 6, False, False), (3 << 20, 4, False, False), (120 << 30, 6, True, False),
+    (3 << 20, 4, True, False), (120 << 30, 6, True, True)])
+def test_served_frames_equal_frames_alone(qr, budget, max_batch, device_anim, urgent):
     """device_anim: spinning scenes whose copies were prepared for it are
-    updated on the device (qr_scene_anim_update on the serving stream)"""
+    updated on the device (qr_scene_anim_update on the serving stream);
+    urgent: the largest frames go into batches of their own on a stream of
+    high priority, overlapping the others on the device"""
     ctx = qr.Context(0)
-    serve, srv = _server(qr, ctx, budget, max_batch, device_anim)
+    serve, srv = _server(qr, ctx, budget, max_batch, device_anim,
+                         (lambda r: r.w == 128) if urgent else None)
     reqs = _requests(serve, 28, 7)
     done, wall = srv.run(reqs, keep_frames=True)
     if device_anim:

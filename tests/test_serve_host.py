@@ -98,9 +98,9 @@ class FakeTensor:
 
 
 class HostServer(serve.Server):
-    def _new_stream(self):
+    def _new_stream(self, priority=0):
         class S:
-            cuda_stream = 0
+            cuda_stream = 1 if priority else 0
         return S()
 
     def _alloc(self, req, pt):
@@ -108,10 +108,10 @@ class HostServer(serve.Server):
         req.acc = FakeTensor() if pt else None
 
 
-def _server(budget, max_batch=4, per_request=True):
+def _server(budget, max_batch=4, per_request=True, urgent=None):
     scenes = [dict(gen="g%d" % i, pt=(i == 2), depth=4) for i in range(3)]
     return HostServer(FakeQr, FakeCtx(), scenes, budget_bytes=budget, max_batch=max_batch,
-                      prep_threads=2, per_request=per_request)
+                      prep_threads=2, per_request=per_request, urgent=urgent)
 
 
 def _requests(n, w=64, h=48, spp=1):
@@ -164,7 +164,7 @@ def test_requests_complete_on_their_own_word():
             srv.used += r.bytes
         b.pending = ["running"]                 # poll: not finished
         flags = np.frombuffer(b.done_flags(4), dtype=np.uint32)
-        srv.inflight.append((b, reqs, flags))
+        srv.inflight.append((b, reqs, flags, srv.free_batches))
         b.flags[2] = 1
         srv._complete(lambda: 1.0)
         assert [r.rid for r in srv.completed] == ([2] if per_request else [])
@@ -178,6 +178,41 @@ def test_requests_complete_on_their_own_word():
         assert srv.used == 0 and not srv.inflight and b in srv.free_batches
         assert sorted(srv.slots[0]) == [100, 101, 102, 103]
         srv.close()
+
+
+def test_urgent_requests_get_batches_of_their_own():
+    """urgent requests go into batches of their own, launched on the
+    high-priority stream ahead of the others; every request completes once
+    and batches of both pools come back to their pools"""
+    FakeBatch.order = lambda n: list(range(n))
+    launched = []
+    orig = FakeBatch.launch
+
+    def launch(self, stream):
+        launched.append((stream, [q.fp.urgent for q in self.table]))
+        orig(self, stream)
+    FakeBatch.launch = launch
+    try:
+        srv = _server(1 << 30, max_batch=4, urgent=lambda r: r.w == 128)
+        reqs = [serve.Request(i, i % 2, 16 * i, 128 if i % 3 == 0 else 64, 48, 1, 0.0)
+                for i in range(12)]
+        orig_prep = srv._prepare
+
+        def prepare(req):
+            r = orig_prep(req)
+            r.fp.urgent = req.w == 128
+            return r
+        srv._prepare = prepare
+        done, wall = srv.run(reqs)
+    finally:
+        FakeBatch.launch = orig
+    assert sorted(r.rid for r in done) == list(range(12))
+    for stream, flags in launched:
+        assert all(flags) if stream == 1 else not any(flags)
+    assert any(s == 1 for s, _ in launched) and any(s == 0 for s, _ in launched)
+    assert len(srv.free_batches) == 2 and len(srv.free_ubatches) == 2
+    assert srv.used == 0 and not srv.busy()
+    srv.close()
 
 
 def test_scene_copies_are_reused():
