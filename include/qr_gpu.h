@@ -411,6 +411,12 @@ int qr_batch_set(qr_batch *b, const qr_request *reqs, int n);
 /* tile width (4, 8, 16 or 32; tiles are 32 pixels) and tiles a warp claims
  * at once (1-64) */
 int qr_batch_config(qr_batch *b, int tile_w, int grab);
+/* on (the default): the Whitted requests' kernel is persistent, a block
+ * for each resident slot, its warps claiming runs of tiles until none are
+ * left; off: a block for every 4 runs of tiles, each warp taking one run,
+ * so that blocks retire as they finish and kernels on streams of higher
+ * priority take the SMs between them (a server's urgent requests) */
+int qr_batch_persistent(qr_batch *b, int on);
 /* time every tile configuration on the batch and keep the fastest;
  * tile_w, grab and ms (optional) receive the choice and its time */
 int qr_batch_tune(qr_batch *b, int *tile_w, int *grab, float *ms);

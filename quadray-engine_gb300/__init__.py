@@ -202,6 +202,7 @@ def lib():
         L.qr_batch_destroy.argtypes = [vp]
         L.qr_batch_set.argtypes = [vp, ctypes.POINTER(QrRequest), i32]
         L.qr_batch_config.argtypes = [vp, i32, i32]
+        L.qr_batch_persistent.argtypes = [vp, i32]
         L.qr_batch_tune.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                     ctypes.POINTER(ctypes.c_float)]
         L.qr_batch_launch.argtypes = [vp, vp]
@@ -478,6 +479,9 @@ class Batch:
 
     def config(self, tile_w, grab):
         self._check(lib().qr_batch_config(self.h, tile_w, grab), "qr_batch_config")
+
+    def persistent(self, on):
+        self._check(lib().qr_batch_persistent(self.h, 1 if on else 0), "qr_batch_persistent")
 
     def tune(self):
         tw, gr, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()

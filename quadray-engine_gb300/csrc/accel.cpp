@@ -476,6 +476,96 @@ void qr_accel_pairs(const std::vector<qr_bnode> &nodes, std::vector<qr_bpair> &p
     }
 }
 
+static double node_area(const qr_bnode &n)
+{
+    const double dx = (double)n.hi[0] - n.lo[0], dy = (double)n.hi[1] - n.lo[1],
+                 dz = (double)n.hi[2] - n.lo[2];
+    return 2.0 * (dx * dy + dy * dz + dz * dx);
+}
+
+/* the record of inner node i and, recursively, of its inner slots; returns
+ * its index; *need: the deepest stack below it */
+static int32_t make_quad(const std::vector<qr_bnode> &nodes, int32_t i,
+                         std::vector<qr_bquad> &quads, std::vector<int32_t> &src,
+                         int32_t *need)
+{
+    int32_t ch[4] = {nodes[i].a, nodes[i].b, -1, -1};
+    int n = 2;
+    while (n < 4)
+    {
+        /* open the inner child with the largest box */
+        int best = -1;
+        double ba = -1.0;
+        for (int k = 0; k < n; k++)
+        {
+            const qr_bnode &c = nodes[ch[k]];
+            if (c.count == 0 && node_area(c) > ba) { ba = node_area(c); best = k; }
+        }
+        if (best < 0) break;
+        const qr_bnode &c = nodes[ch[best]];
+        ch[best] = c.a;
+        ch[n++] = c.b;
+    }
+    const int32_t q = (int32_t)quads.size();
+    quads.push_back(qr_bquad());
+    src.resize(4 * quads.size(), -1);
+    qr_bquad rec;
+    memset(&rec, 0, sizeof(rec));
+    int32_t below = 0;
+    for (int k = 0; k < 4; k++)
+    {
+        if (k >= n)
+        {
+            rec.lo_x[k] = rec.lo_y[k] = rec.lo_z[k] = HUGE_VALF;
+            rec.hi_x[k] = rec.hi_y[k] = rec.hi_z[k] = -HUGE_VALF;
+            rec.code[k] = QR_BQUAD_EMPTY;
+            src[4 * q + k] = -1;
+            continue;
+        }
+        const qr_bnode &c = nodes[ch[k]];
+        rec.lo_x[k] = c.lo[0]; rec.lo_y[k] = c.lo[1]; rec.lo_z[k] = c.lo[2];
+        rec.hi_x[k] = c.hi[0]; rec.hi_y[k] = c.hi[1]; rec.hi_z[k] = c.hi[2];
+        src[4 * q + k] = ch[k];
+        if (c.count > 0)
+        {
+            rec.code[k] = qr_bnode_code(c, ch[k]);
+        }
+        else
+        {
+            int32_t nb = 0;
+            rec.code[k] = make_quad(nodes, ch[k], quads, src, &nb);
+            below = std::max(below, nb);
+        }
+    }
+    quads[q] = rec;
+    /* a visit pushes the hit slots but the nearest: n - 1 entries */
+    *need = (n - 1) + below;
+    return q;
+}
+
+void qr_accel_quads(const std::vector<qr_bnode> &nodes, const int *root, int nlev,
+                    std::vector<qr_bquad> &quads, std::vector<int32_t> &src,
+                    int32_t *quad_root, int32_t *stack_need)
+{
+    quads.clear();
+    src.clear();
+    for (int l = 0; l < nlev; l++)
+    {
+        quad_root[l] = QR_BQUAD_EMPTY;
+        stack_need[l] = 0;
+        if (root[l] < 0 || root[l] >= (int)nodes.size()) continue;
+        const qr_bnode &r = nodes[root[l]];
+        if (r.count > 0)
+        {
+            quad_root[l] = qr_bnode_code(r, root[l]);
+            continue;
+        }
+        int32_t need = 0;
+        quad_root[l] = make_quad(nodes, root[l], quads, src, &need);
+        stack_need[l] = need;
+    }
+}
+
 /* node boxes of a tree whose items' boxes changed, bottom-up: nodes are
  * stored parent before children (build_node), so a reverse sweep sees
  * children first */

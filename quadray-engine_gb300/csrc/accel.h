@@ -63,6 +63,22 @@ struct qr_bpair
     int32_t pad_b;
 };
 
+/* the walk's 4-wide view of the tree, 128 bytes a record: up to four
+ * children's boxes (structure of arrays, one 16-byte group per bound and
+ * axis) and codes (qr_bpair's, QR_BQUAD_EMPTY for an unused slot, whose
+ * box is empty).  A record collapses a node of the binary tree with its
+ * children (and theirs) until it holds four, the largest boxes opened
+ * first; each slot's box is the box of a node of the binary tree (its
+ * source), which the device update copies after each refit */
+#define QR_BQUAD_EMPTY ((int32_t)0x80000000)
+struct qr_bquad
+{
+    float   lo_x[4], lo_y[4], lo_z[4];
+    float   hi_x[4], hi_y[4], hi_z[4];
+    int32_t code[4];
+    int32_t pad[4];
+};
+
 /* the walk's code of node i (see qr_bpair) */
 #if defined(__CUDACC__)
 __host__ __device__
@@ -111,6 +127,15 @@ int qr_accel_build(const qr_scene_desc *d, qr_accel_host *out, int level);
 
 /* the walk's child records of `nodes` (one a node) */
 void qr_accel_pairs(const std::vector<qr_bnode> &nodes, std::vector<qr_bpair> &pairs);
+
+/* the 4-wide records of the trees rooted at root[l] (l < nlev; roots past
+ * the node array are skipped): quads, each slot's source node (src, 4 a
+ * record, -1 for an empty slot), and per level the code of its root
+ * (quad_root) and the deepest stack its walk can need (stack_need: 3 a
+ * record on the way down) */
+void qr_accel_quads(const std::vector<qr_bnode> &nodes, const int *root, int nlev,
+                    std::vector<qr_bquad> &quads, std::vector<int32_t> &src,
+                    int32_t *quad_root, int32_t *stack_need);
 
 /* all levels concatenated into `out` (node indices and item ranges shifted
  * by the preceding levels); per level its root node, its unbounded surfaces

@@ -211,8 +211,18 @@ __global__ void __launch_bounds__(512) anim_kernel(const qr_anim_dev *devs)
     }
     __syncthreads();
 
-    /* stage 5: the walk's child records take the children's new boxes (the
-     * codes, which follow the topology, stay) */
+    /* stage 5: the walk's records take the nodes' new boxes (the codes,
+     * which follow the topology, stay) */
+    for (int w = tid; w < 4 * A.nquads; w += nt)
+    {
+        const int sn = A.quad_src[w];
+        if (sn < 0) continue;
+        const qr_bnode &c = A.bvh[sn];
+        qr_bquad &q = A.quads[w >> 2];
+        const int k = w & 3;
+        q.lo_x[k] = c.lo[0]; q.lo_y[k] = c.lo[1]; q.lo_z[k] = c.lo[2];
+        q.hi_x[k] = c.hi[0]; q.hi_y[k] = c.hi[1]; q.hi_z[k] = c.hi[2];
+    }
     for (int i = tid; i < A.nbvh; i += nt)
     {
         const qr_bnode &nd = A.bvh[i];

@@ -27,6 +27,9 @@ struct qr_anim_dev
     float               *lboxes;    /* [QR_BVH_LEVELS][nsrf][6] surface boxes */
     qr_bnode            *bvh;       /* hierarchy nodes, all levels */
     qr_bpair            *pairs;     /* the walk's child records of the nodes */
+    qr_bquad            *quads;     /* the walk's 4-wide records */
+    const int32_t       *quad_src;  /* each slot's node (-1: empty) */
+    int32_t              nquads;
     const qr_bitem      *items;
     const int32_t       *rorder;    /* nodes by depth, deepest first */
     const int32_t       *depth_off; /* depth band b: rorder[depth_off[b], depth_off[b+1]) */

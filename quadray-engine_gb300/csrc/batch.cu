@@ -57,6 +57,8 @@ struct qr_batch
     int          nw, np;        /* jobs per mode */
     int          tiles[2];      /* tiles per mode */
     int          tw, th, grab;
+    int          once;          /* Whitted kernel: a block for every 4 runs
+                                   of tiles (qr_batch_persistent(b, 0)) */
     int          blocks[2];
     cudaStream_t main, side[QR_BATCH_PT_STREAMS];
     cudaEvent_t  fork, join[QR_BATCH_PT_STREAMS], done;
@@ -290,8 +292,21 @@ extern "C" int qr_batch_config(qr_batch *b, int tile_w, int grab)
     return upload_jobs(b);
 }
 
-/* the Whitted persistent launch on b->main, the path-traced frames on the
- * side streams */
+extern "C" int qr_batch_persistent(qr_batch *b, int on)
+{
+    if (b == NULL) return QR_ERR_ARG;
+    b->once = on ? 0 : 1;
+    if (b->exec)
+    {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = NULL;
+    }
+    b->graph_ok = 0;
+    return QR_OK;
+}
+
+/* the Whitted launch on b->main, the path-traced frames on the side
+ * streams */
 static cudaError_t enqueue(qr_batch *b)
 {
     cudaError_t e = cudaMemsetAsync(b->dcount, 0, 2 * sizeof(int), b->main);
@@ -302,7 +317,7 @@ static cudaError_t enqueue(qr_batch *b)
         e = cudaStreamWaitEvent(b->side[k], b->fork, 0);
     if (e == cudaSuccess)
         e = qr_launch_batch(0, b->djobs, b->nw, b->tiles[0], b->dcount, b->tw, b->th,
-                            b->grab, b->blocks[0], b->dtiles, b->ddone, b->main);
+                            b->grab, b->blocks[0], b->once, b->dtiles, b->ddone, b->main);
     /* the path-traced requests one after the other on each side stream,
      * each marked done as soon as its frame is in device memory */
     for (int j = 0; j < b->np && e == cudaSuccess; j++)

@@ -338,12 +338,20 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     size_t o_lel = o_elm + al16(sizeof(qr_elem) * d->nelem);
     size_t o_tex = o_lel + al16(sizeof(qr_lelem) * d->nlelem);
     size_t o_nod = o_tex + al16(sizeof(uint32_t) * d->ntex);
-    size_t o_par = o_nod + al16(sizeof(qr_bnode) * acc.nodes.size());
-    size_t o_itm = o_par + al16(sizeof(qr_bpair) * acc.nodes.size());
-    size_t o_alw = o_itm + al16(sizeof(qr_bitem) * acc.items.size());
-    size_t total = o_alw + al16(sizeof(qr_bitem) * acc.always.size());
     std::vector<qr_bpair> pairs;
     qr_accel_pairs(acc.nodes, pairs);
+    std::vector<qr_bquad> quads;
+    std::vector<int32_t> quad_src;
+    int32_t lvl_quad[QR_BVH_LEVELS], stack_need[QR_BVH_LEVELS];
+    qr_accel_quads(acc.nodes, lvl_root, QR_BVH_LEVELS, quads, quad_src, lvl_quad, stack_need);
+    for (int l = 0; l < QR_BVH_LEVELS; l++)
+        if (stack_need[l] > QR_BVH_STACK) lvl_r2[l] = -1.0f;   /* that level walks the list */
+    size_t o_par = o_nod + al16(sizeof(qr_bnode) * acc.nodes.size());
+    size_t o_qud = o_par + al16(sizeof(qr_bpair) * acc.nodes.size());
+    size_t o_qsr = o_qud + al16(sizeof(qr_bquad) * quads.size());
+    size_t o_itm = o_qsr + al16(sizeof(int32_t) * quad_src.size());
+    size_t o_alw = o_itm + al16(sizeof(qr_bitem) * acc.items.size());
+    size_t total = o_alw + al16(sizeof(qr_bitem) * acc.always.size());
 
     std::vector<unsigned char> h(total, 0);
     memcpy(&h[o_srf], d->srf, sizeof(qr_srf) * d->nsrf);
@@ -356,6 +364,11 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     {
         memcpy(&h[o_nod], acc.nodes.data(), sizeof(qr_bnode) * acc.nodes.size());
         memcpy(&h[o_par], pairs.data(), sizeof(qr_bpair) * pairs.size());
+    }
+    if (!quads.empty())
+    {
+        memcpy(&h[o_qud], quads.data(), sizeof(qr_bquad) * quads.size());
+        memcpy(&h[o_qsr], quad_src.data(), sizeof(int32_t) * quad_src.size());
     }
     if (!acc.items.empty())
         memcpy(&h[o_itm], acc.items.data(), sizeof(qr_bitem) * acc.items.size());
@@ -393,6 +406,9 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     sl.d.cam_num = d->cam_num;
     sl.d.nodes = (const qr_bnode *)(b + o_nod);
     sl.d.pairs = (const qr_bpair *)(b + o_par);
+    sl.d.quads = (const qr_bquad *)(b + o_qud);
+    sl.d.quad_src = (const int32_t *)(b + o_qsr);
+    sl.d.nquads = (int32_t)quads.size();
     sl.d.items = (const qr_bitem *)(b + o_itm);
     sl.d.always = (const qr_bitem *)(b + o_alw);
     sl.d.nnodes = use_bvh ? (int32_t)acc.nodes.size() : -1;
@@ -403,6 +419,7 @@ static int upload(qr_ctx *ctx, qr_scene_slot &sl, const qr_scene_desc *d, bool f
     for (int l = 0; l < QR_BVH_LEVELS; l++)
     {
         sl.d.lvl_root[l] = lvl_root[l];
+        sl.d.lvl_quad[l] = lvl_quad[l];
         sl.d.lvl_aoff[l] = lvl_aoff[l];
         sl.d.lvl_anum[l] = lvl_anum[l];
         sl.d.lvl_r2[l] = lvl_r2[l];
@@ -668,6 +685,9 @@ static int anim_prepare(qr_ctx *ctx, qr_scene_slot *sl, const qr_scene_desc *des
     D.lboxes = (float *)(blk + o_lbx);
     D.bvh = const_cast<qr_bnode *>(sl->d.nodes);
     D.pairs = const_cast<qr_bpair *>(sl->d.pairs);
+    D.quads = const_cast<qr_bquad *>(sl->d.quads);
+    D.quad_src = sl->d.quad_src;
+    D.nquads = sl->d.nquads;
     D.items = sl->d.items;
     D.rorder = (const int32_t *)(blk + o_ror);
     D.depth_off = (const int32_t *)(blk + o_dof);

@@ -70,7 +70,8 @@
 #define QR_GEN_NOSPEC   (1 << 1)   /* debug: no specular */
 #define QR_GEN_ONELIGHT (1 << 2)   /* debug: a single light */
 #define QR_GEN_TARRAY   (1 << 3)   /* QR_SCN_ANIM: keep RT_OPTS_TARRAY on */
-#define QR_GEN_SPIN     (1 << 4)   /* QR_SCN_PLAIN: the quadrics spin (anim_spin) */
+#define QR_GEN_SPIN     (1 << 4)   /* QR_SCN_PLAIN, QR_SCN_PT: the quadrics spin
+                                      (anim_spin) */
 #define QR_GEN_TEX      (1 << 5)   /* QR_SCN_PLAIN: textured ground and quadrics */
 #define QR_GEN_GAMMA    (1 << 6)   /* opt out of RT_OPTS_GAMMA: gamma on */
 #define QR_GEN_SHAPES   (1 << 7)   /* QR_SCN_PLAIN: the other quadric kinds too */
@@ -942,6 +943,7 @@ static void build_pt(Scene &sc, uint64_t seed, int nq)
         float ry = r.uf(-180, 180);
         float rz = r.uf(-180, 180);
         Scene::trm_set(&q.trm, 1, 1, 1, rx, ry, rz, p[0], p[1], p[2]);
+        if (sc.flags & QR_GEN_SPIN) q.f_anim = anim_spin;
         root.push_back(q);
     }
     rt_OBJECT ro = sc.array(root);

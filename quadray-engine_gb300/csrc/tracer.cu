@@ -152,15 +152,18 @@ pt_kernel(const qr_dscene S, const qr_frame_params P, float *acc, uint32_t *fram
 template <int MODE>
 __global__ void __launch_bounds__(128, MODE == 0 ? QR_MIN_BLOCKS : QR_PT_MIN_BLOCKS)
 batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter,
-             int tw, int th, int grab, int *tiles_done, uint32_t *done)
+             int tw, int th, int grab, int once, int *tiles_done, uint32_t *done)
 {
     __shared__ qr_dscene sS[4];
     __shared__ qr_frame_params sP[4];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.y;
     int cur = -1;
+    /* once: a warp takes one run of tiles and its block retires when its
+     * warps are done, so kernels of higher-priority streams get SMs as
+     * blocks finish; else warps claim runs until none are left */
     #pragma unroll 1
-    for (;;)
+    for (int claim = 0; !once || claim == 0; claim++)
     {
         int t0 = 0;
         if (lane == 0) t0 = atomicAdd(counter, grab);
@@ -269,18 +272,20 @@ batch_kernel(const qr_job *__restrict__ jobs, int njobs, int total, int *counter
 
 #ifndef QR_STATS
 cudaError_t qr_launch_batch(int mode, const qr_job *jobs, int njobs, int total_tiles,
-                            int *counter, int tw, int th, int grab, int blocks,
+                            int *counter, int tw, int th, int grab, int blocks, int once,
                             int *tiles_done, uint32_t *done, cudaStream_t stream)
 {
     if (njobs <= 0 || total_tiles <= 0) return cudaSuccess;
     const dim3 block(32, 4);
+    /* one run of grab tiles a warp: as many blocks as runs / 4 */
+    if (once) blocks = (int)(((long long)total_tiles + 4ll * grab - 1) / (4ll * grab));
     if (mode == 0)
         QR_NS::batch_kernel<0><<<blocks, block, 0, stream>>>(jobs, njobs, total_tiles,
-                                                            counter, tw, th, grab,
+                                                            counter, tw, th, grab, once,
                                                             tiles_done, done);
     else
         QR_NS::batch_kernel<1><<<blocks, block, 0, stream>>>(jobs, njobs, total_tiles,
-                                                            counter, tw, th, grab,
+                                                            counter, tw, th, grab, once,
                                                             tiles_done, done);
     qr_note_launches(stream, 1);
     return cudaGetLastError();

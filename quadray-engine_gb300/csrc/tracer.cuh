@@ -29,6 +29,9 @@ struct qr_dscene
      * holds the same surfaces, so shadow rays use it too */
     const qr_bnode *nodes;          /* all levels, concatenated */
     const qr_bpair *pairs;          /* the walk's child records, one a node */
+    const qr_bquad *quads;          /* the walk's 4-wide records */
+    const int32_t  *quad_src;       /* each quad slot's node (-1: empty) */
+    int32_t nquads;
     const qr_bitem *items;
     const qr_bitem *always;
     int32_t nnodes, nitems, nalways;
@@ -37,6 +40,7 @@ struct qr_dscene
      * and the rays it serves: origin within sqrt(r2) of ray_c (r2 < 0: the
      * level is missing) */
     int32_t lvl_root[QR_BVH_LEVELS], lvl_aoff[QR_BVH_LEVELS], lvl_anum[QR_BVH_LEVELS];
+    int32_t lvl_quad[QR_BVH_LEVELS];    /* code of level l's root in the 4-wide view */
     float   lvl_r2[QR_BVH_LEVELS];
     float   ray_c[3];
     /* the owning context's fault word: QR_FAULT_* bits, x, y of the first
@@ -87,12 +91,13 @@ struct qr_job
     int32_t         req;            /* its index in the batch */
 };
 
-/* persistent launch over the tiles of njobs requests of one mode (0
- * Whitted, 1 path tracer); *counter and tiles_done[0, njobs) must hold 0.
+/* launch over the tiles of njobs requests of one mode (0 Whitted, 1 path
+ * tracer): `blocks` persistent blocks, or with `once` a block for every 4
+ * runs of grab tiles; *counter and tiles_done[0, njobs) must hold 0.
  * The warp that finishes a request's last tile sets done[req] to 1 (done
  * may be host memory mapped into the device) */
 cudaError_t qr_launch_batch(int mode, const qr_job *jobs, int njobs, int total_tiles,
-                            int *counter, int tw, int th, int grab, int blocks,
+                            int *counter, int tw, int th, int grab, int blocks, int once,
                             int *tiles_done, uint32_t *done, cudaStream_t stream);
 /* resident blocks of 128 threads per SM of the batch kernel of a mode */
 int qr_batch_blocks_per_sm(int mode);

@@ -535,8 +535,9 @@ __device__ __forceinline__ int box_hit(const qr_bnode *__restrict__ n, const Ray
  * Hits are accepted by (distance, list position), so both give the in-order
  * walk's result.  There is one solver site for both sources.
  */
-static __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
-                     int off, int num, Walk &w, StP st)
+template <int QUADS>
+static __device__ void walk_t(const qr_dscene &S, const qr_frame_params &P, const Ray &r,
+                              int off, int num, Walk &w, StP st)
 {
     const float dx = r.org[0] - S.ray_c[0], dy = r.org[1] - S.ray_c[1],
                 dz = r.org[2] - S.ray_c[2];
@@ -575,7 +576,7 @@ static __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const 
         if (box_hit(&S.nodes[root], r, inv, oinv, w.tbuf, tn, st))
         {
             (void)tn;
-            cur = qr_bnode_code(S.nodes[root], root);
+            cur = QUADS ? S.lvl_quad[lvl] : qr_bnode_code(S.nodes[root], root);
         }
     }
 
@@ -654,6 +655,50 @@ static __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const 
                         ib = ia + (lc & 15);
                         continue;
                     }
+                    if (QUADS)
+                    {
+                    /* a 4-wide record: the hit slots' codes, the nearest
+                     * taken next and the others pushed farthest first (so
+                     * the nearer pop first) */
+                    const qr_bquad *__restrict__ qd = &S.quads[code];
+                    const float4 lx = ldf4(qd->lo_x), ly = ldf4(qd->lo_y), lz = ldf4(qd->lo_z);
+                    const float4 hx = ldf4(qd->hi_x), hy = ldf4(qd->hi_y), hz = ldf4(qd->hi_z);
+                    const int4 cd = ldi4(qd->code);
+                    const float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, lys[4] = {ly.x, ly.y, ly.z, ly.w};
+                    const float lzs[4] = {lz.x, lz.y, lz.z, lz.w}, hxs[4] = {hx.x, hx.y, hx.z, hx.w};
+                    const float hys[4] = {hy.x, hy.y, hy.z, hy.w}, hzs[4] = {hz.x, hz.y, hz.z, hz.w};
+                    const int cds[4] = {cd.x, cd.y, cd.z, cd.w};
+                    float td[4];
+                    int tc[4], nh = 0;
+                    #pragma unroll
+                    for (int k = 0; k < 4; k++)
+                    {
+                        float t;
+                        const int h = cds[k] != QR_BQUAD_EMPTY &&
+                                      box_hit4(make_float4(lxs[k], lys[k], lzs[k], 0.0f),
+                                               make_float4(hxs[k], hys[k], hzs[k], 0.0f),
+                                               r, inv, oinv, w.tbuf, t, st);
+                        td[k] = h ? t : __int_as_float(0x7f800000);   /* misses last */
+                        tc[k] = cds[k];
+                        nh += h;
+                    }
+                    if (nh == 0) continue;
+                    /* ascending distance: a sorting network of 4 */
+#define QR_CSWAP(a, b)                                                            \
+                    if (td[b] < td[a])                                            \
+                    {                                                             \
+                        const float tt = td[a]; td[a] = td[b]; td[b] = tt;        \
+                        const int cc = tc[a]; tc[a] = tc[b]; tc[b] = cc;          \
+                    }
+                    QR_CSWAP(0, 1) QR_CSWAP(2, 3) QR_CSWAP(0, 2) QR_CSWAP(1, 3) QR_CSWAP(1, 2)
+#undef QR_CSWAP
+                    if (sp + nh - 1 > QR_BVH_STACK) { w.fault = QR_FAULT_STACK; return; }
+                    #pragma unroll
+                    for (int m = 3; m > 0; m--)
+                        if (m < nh) stk[sp++] = make_int2(tc[m], __float_as_int(td[m]));
+                    cur = tc[0];
+                    continue;
+                    }
                     const qr_bpair *__restrict__ pr = &S.pairs[code];
                     const float4 la = ldf4(pr->lo_a), ha4 = ldf4(pr->hi_a);
                     const float4 lb = ldf4(pr->lo_b), hb4 = ldf4(pr->hi_b);
@@ -713,6 +758,18 @@ static __device__ void walk(const qr_dscene &S, const qr_frame_params &P, const 
         solve_surface(S, r, w, si, p, ldff, lray, st);
         if (w.shadow && w.occluded) return;
     }
+}
+
+/* the walk over the binary tree's child records (qr_bpair): the Whitted
+ * kernels' form.  Over the 4-wide records (qr_bquad) the animated 1080p
+ * frame took 22.9 against 20.1 ms and the plain frame 0.111 against
+ * 0.103 ms (the Whitted kernels' registers spill around the sort), the
+ * 256-quadric frame 57.5 against 60.4 ms; the path tracer's tracing stage,
+ * with 80 registers and incoherent rays, gains from them (wf_trace) */
+static __device__ __forceinline__ void walk(const qr_dscene &S, const qr_frame_params &P,
+                                            const Ray &r, int off, int num, Walk &w, StP st)
+{
+    walk_t<0>(S, P, r, off, num, w, st);
 }
 
 /* shading state of one hit, kept while its shadow rays are traced */

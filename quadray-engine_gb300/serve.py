@@ -101,6 +101,11 @@ class Server:
         self.ubatches = ([qr.Batch(ctx, max_batch), qr.Batch(ctx, max_batch)]
                          if urgent is not None else [])
         self.free_ubatches = collections.deque(self.ubatches)
+        if urgent is not None:
+            # the other batches' blocks retire as they finish, so that an
+            # urgent batch's blocks take their SMs at once
+            for b in self.batches:
+                b.persistent(False)
         self.waiting = collections.deque()      # arrived, not admitted
         self.preparing = []                      # futures
         self.ready = collections.deque()         # prepared, not launched

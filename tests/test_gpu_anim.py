@@ -280,3 +280,47 @@ def test_malformed_tables_and_updates_are_refused(qr, ctx):
     ctx.anim_update(sid, p)
     assert ctx.anim_status(sid) == (1, 0)
     ctx.release(sid)
+
+
+@pytest.mark.parametrize("seed,nq", [(1, 32), (4, 96)])
+def test_device_update_path_traced_equals_host_update(qr, ctx, seed, nq):
+    """the path tracer's tracing stage walks the 4-wide records, which the
+    device update refits after the nodes: path-traced frames of the closed
+    box with spinning quadrics, updated on the device, equal those of the
+    host-updated scene, and those of the per-pixel kernel (which walks the
+    binary records)"""
+    import torch
+    w, h, depth = 96, 54, 6
+    g, f, sid, fp = _device_scene(qr, ctx, qr.SCN_PT, seed, nq, qr.GEN_SPIN, w, h, 0, depth)
+    g2 = qr.GenScene(qr.SCN_PT, seed, nq, qr.GEN_SPIN)
+    f2 = qr.Flat(g2, w, h, 0)
+    hid = None
+    sp = torch.cuda.current_stream().cuda_stream
+
+    def pt(scene, params, flags=0):
+        p = _copy(qr, params)
+        p.pt_on, p.pts_c, p.seed, p.frame_idx = 16, 0.0, 9, 0
+        p.flags |= flags
+        acc = torch.zeros((p.y_res, p.x_row, 3), dtype=torch.float32, device="cuda")
+        fr = torch.zeros((p.y_res, p.x_row), dtype=torch.int32, device="cuda")
+        ctx.render_pt(scene, p, acc.data_ptr(), fr.data_ptr(), sp)
+        torch.cuda.synchronize()
+        return fr.cpu().numpy(), acc.cpu().numpy()
+
+    for t in [16, 16 * 40, 16 * 97]:
+        rc, p = f.anim_params(t)
+        assert rc == 0
+        ctx.anim_update(sid, p)
+        dev, dacc = pt(sid, fp)
+        desc2, params2 = f2.update(t, depth)
+        if hid is None:
+            hid = ctx.upload(desc2)
+        else:
+            ctx.update(hid, desc2)
+        host, hacc = pt(hid, params2)
+        assert (dev != host).sum() == 0 and (dacc != hacc).sum() == 0, t
+        pix, pacc = pt(sid, fp, qr.FP_PIXEL_PT)
+        assert (dev != pix).sum() == 0 and (dacc != pacc).sum() == 0, t
+        assert (dev != 0).mean() > 0.05       # 16 samples: a noisy, not a black frame
+    ctx.release(sid)
+    ctx.release(hid)

@@ -48,15 +48,18 @@ def test_batch_frames_equal_single_frames(qr):
     alone = [_alone(qr, ctx, r).copy() for r in reqs]
     b = qr.Batch(ctx, 16)
     b.set(reqs)
-    for tw, grab in [(8, 1), (16, 4), (32, 1), (4, 2)]:
+    for tw, grab, persistent in [(8, 1, 1), (16, 4, 1), (32, 1, 1), (4, 2, 1), (8, 1, 0),
+                                 (16, 4, 0)]:
         for fr, _ in bufs:
             fr.zero_()
         b.config(tw, grab)
+        b.persistent(persistent)
         b.launch(torch.cuda.current_stream().cuda_stream)
         b.wait()
         for i, (fr, _) in enumerate(bufs):
             got = fr.cpu().numpy().view(np.uint32)[:, :reqs[i].fp.x_res]
-            assert (got != alone[i]).sum() == 0, (tw, grab, i)
+            assert (got != alone[i]).sum() == 0, (tw, grab, persistent, i)
+    b.persistent(1)
     tw, grab, ms = b.tune()
     assert tw in (4, 8, 16, 32) and grab >= 1 and ms > 0
     b.launch(0)

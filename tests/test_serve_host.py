@@ -54,6 +54,9 @@ class FakeBatch:
         assert len(table) <= self.max
         self.table = list(table)
 
+    def persistent(self, on):
+        self.is_persistent = on
+
     def launch(self, stream):
         for i in range(self.max):
             self.flags[i] = 0
@@ -211,6 +214,8 @@ def test_urgent_requests_get_batches_of_their_own():
         assert all(flags) if stream == 1 else not any(flags)
     assert any(s == 1 for s, _ in launched) and any(s == 0 for s, _ in launched)
     assert len(srv.free_batches) == 2 and len(srv.free_ubatches) == 2
+    # the other batches yield their SMs between blocks
+    assert all(b.is_persistent is False for b in srv.batches)
     assert srv.used == 0 and not srv.busy()
     srv.close()
 
