@@ -763,8 +763,9 @@ static __device__ void walk_t(const qr_dscene &S, const qr_frame_params &P, cons
 /* the walk over the binary tree's child records (qr_bpair): the Whitted
  * kernels' form.  Over the 4-wide records (qr_bquad) the animated 1080p
  * frame took 22.9 against 20.1 ms and the plain frame 0.111 against
- * 0.103 ms (the Whitted kernels' registers spill around the sort), the
- * 256-quadric frame 57.5 against 60.4 ms; the path tracer's tracing stage,
+ * 0.103 ms (the Whitted kernels' registers spill around the sort; at 6 and
+ * 5 resident blocks 22.9 and 21.4 ms), the 256-quadric frame 57.5 against
+ * 60.4 ms; the path tracer's tracing stage,
  * with 80 registers and incoherent rays, gains from them (wf_trace) */
 static __device__ __forceinline__ void walk(const qr_dscene &S, const qr_frame_params &P,
                                             const Ray &r, int off, int num, Walk &w, StP st)
