@@ -79,7 +79,7 @@ struct qr_batch
 };
 
 /* wavefront chunks of the batch's path-traced requests (as a context's) */
-#define QR_BATCH_WF_PATHS (2ll << 20)
+#define QR_BATCH_WF_PATHS (4ll << 20)
 
 static int bfail(qr_batch *b, int code, const char *what, cudaError_t e)
 {

@@ -98,12 +98,14 @@ struct qr_ctx
     long long    wh_samples;    /* Whitted: camera rays of a chunk at most */
 };
 
-/* the wavefront's chunks: 2^21 paths, queues of 2 rays and a pool of 8
- * nodes a path: about 1.1 KB a path, 2.2 GB.  QR_WF_CAPS="paths,q,pool" in
- * the environment of the process (read when a context is created) sets
+/* the wavefront's chunks: 2^22 paths, queues of 2 rays and a pool of 8
+ * nodes a path: about 1.2 KB a path, 4.9 GB.  Fewer, larger chunks leave
+ * fewer stage tails: the 1280x720 64-spp frame takes 183.9 / 169.6 / 162.9
+ * / 161.9 ms at 2^20 / 2^21 / 2^22 / 2^23 paths.  QR_WF_CAPS="paths,q,pool"
+ * in the environment of the process (read when a context is created) sets
  * other capacities (tests use small ones to exercise chunks and the
  * overflow path) */
-#define QR_WF_MAX_PATHS (2ll << 20)
+#define QR_WF_MAX_PATHS (4ll << 20)
 /* Whitted chunks: 2^21 camera rays (about 1.3 KB a ray with four lights,
  * 2.7 GB); QR_WH_SAMPLES in the environment sets another number */
 #define QR_WH_MAX_SAMPLES (2ll << 20)
