@@ -588,7 +588,9 @@ def run_reference(args, wl):
     line = {"impl": "reference", "metric": "rays_per_s", "value": v, "unit": "rays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": config_of(args.workload, wl),
+            "config": dict(config_of(args.workload, wl),
+                           l2="none: the scalar port on the host cores",
+                           parallelism="single"),
             "cpu_baseline": {"value": v, "unit": "rays/s", "cores": cb["cores"],
                              "kind": cb["kind"], "sample": cb["sample"]},
             "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0,
@@ -808,10 +810,11 @@ def run_frames(args, wl, rank, world, dist, local):
             "peak_source": "measured on this device (qr_fp32_peak): FP32 additions, every "
                            "SM filled, CUDA events; peak_fma: fused multiply-adds as 2 ops",
             "flops_per_frame": flops}
+    # config: the workload's identity (the reference arm's line carries the
+    # same keys and values) and how it was timed; the measured workload
+    # quantities go beside it
     cfg = config_of(args.workload, wl)
-    cfg.update({"surfaces": nsrf, "rays_per_frame": rays,
-                "timed_frames": timed if wl["anim"] else None,
-                "l2": "256 MiB buffer written between timed steps",
+    cfg.update({"l2": "256 MiB buffer written between timed steps",
                 "parallelism": "replicas" if world > 1 else "single"})
     line = {
         "metric": "rays_per_s", "value": value, "unit": "rays/s",
@@ -820,6 +823,8 @@ def run_frames(args, wl, rank, world, dist, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": cfg,
+        "workload": {"surfaces": nsrf, "rays_per_frame": rays,
+                     "timed_frames": timed if wl["anim"] else None},
         "step": ("device-side update of the animated transforms + render of the frame"
                  if wl["anim"] else "render of the frame"),
         "frames_per_s": fps,
