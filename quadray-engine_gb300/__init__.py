@@ -165,6 +165,7 @@ def lib():
                                           i32, ctypes.POINTER(ctypes.c_float)]
         L.qrpy_rotation_bound.restype = None
         L.qrpy_extent.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(ctypes.c_double)]
+        L.qrpy_accel_check.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(ctypes.c_int)]
         L.qrpy_extent.restype = None
         L.qrpy_anim_box_check.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(QrAnimNode),
                                           i32, ctypes.POINTER(QrSceneDesc)]

@@ -140,6 +140,102 @@ void qrpy_extent(const qr_scene_desc *d, double *out)
     qr_accel_extent(d, out);
 }
 
+/* the walk's views of the hierarchy of scene d against its binary tree:
+ * per built level, the items a walk of the 4-wide records reaches are
+ * those of the binary tree, each once; every slot's box is its source
+ * node's and its code the node's (or the record made of it); pairs hold
+ * their children's boxes and codes; leaves hold at most QR_BVH_LEAF_MAX
+ * items; a level's stack need bounds what its walk pushes.  Returns the
+ * number of violations; *levels receives the levels checked */
+int qrpy_accel_check(const qr_scene_desc *d, int *levels)
+{
+    qr_accel_host acc;
+    int root[QR_BVH_LEVELS], aoff[QR_BVH_LEVELS], anum[QR_BVH_LEVELS];
+    float r2[QR_BVH_LEVELS];
+    qr_accel_build_levels(d, &acc, root, aoff, anum, r2, NULL);
+    std::vector<qr_bpair> pairs;
+    qr_accel_pairs(acc.nodes, pairs);
+    std::vector<qr_bquad> quads;
+    std::vector<int32_t> src;
+    int32_t qroot[QR_BVH_LEVELS], need[QR_BVH_LEVELS];
+    qr_accel_quads(acc.nodes, root, QR_BVH_LEVELS, quads, src, qroot, need);
+    int bad = 0, nl = 0;
+    const int nn = (int)acc.nodes.size();
+    for (int i = 0; i < nn; i++)
+    {
+        const qr_bnode &n = acc.nodes[i];
+        if (n.count > 0)
+        {
+            if (n.count > QR_BVH_LEAF_MAX) bad++;
+            continue;
+        }
+        const qr_bpair &p = pairs[i];
+        const qr_bnode &a = acc.nodes[n.a], &b = acc.nodes[n.b];
+        for (int k = 0; k < 3; k++)
+            if (p.lo_a[k] != a.lo[k] || p.hi_a[k] != a.hi[k] ||
+                p.lo_b[k] != b.lo[k] || p.hi_b[k] != b.hi[k]) bad++;
+        if (p.code_a != qr_bnode_code(a, n.a) || p.code_b != qr_bnode_code(b, n.b)) bad++;
+    }
+    for (int l = 0; l < QR_BVH_LEVELS; l++)
+    {
+        if (r2[l] < 0.0f || root[l] < 0 || root[l] >= nn) continue;
+        nl++;
+        /* items under the binary tree */
+        std::vector<int> want(acc.items.size(), 0), got(acc.items.size(), 0);
+        std::vector<int> st(1, root[l]);
+        while (!st.empty())
+        {
+            const int i = st.back();
+            st.pop_back();
+            const qr_bnode &n = acc.nodes[i];
+            if (n.count > 0)
+                for (int j = n.a; j < n.a + n.count; j++) want[j]++;
+            else { st.push_back(n.a); st.push_back(n.b); }
+        }
+        /* items the 4-wide walk reaches, with its deepest stack */
+        std::vector<std::pair<int32_t, int>> qs(1, std::make_pair(qroot[l], 0));
+        int deepest = 0;
+        while (!qs.empty())
+        {
+            const int32_t c = qs.back().first;
+            const int depth = qs.back().second;
+            qs.pop_back();
+            if (c < 0)
+            {
+                const uint32_t lc = ~(uint32_t)c;
+                for (int j = (int)(lc >> 4); j < (int)(lc >> 4) + (int)(lc & 15); j++)
+                    if (j >= 0 && j < (int)got.size()) got[j]++; else bad++;
+                continue;
+            }
+            if (c >= (int32_t)quads.size()) { bad++; continue; }
+            const qr_bquad &q = quads[c];
+            int used = 0;
+            for (int k = 0; k < 4; k++)
+            {
+                const int s = src[4 * (size_t)c + k];
+                if (q.code[k] == QR_BQUAD_EMPTY) { if (s != -1) bad++; continue; }
+                used++;
+                if (s < 0 || s >= nn) { bad++; continue; }
+                const qr_bnode &n = acc.nodes[s];
+                if (q.lo_x[k] != n.lo[0] || q.lo_y[k] != n.lo[1] || q.lo_z[k] != n.lo[2] ||
+                    q.hi_x[k] != n.hi[0] || q.hi_y[k] != n.hi[1] || q.hi_z[k] != n.hi[2]) bad++;
+                if (n.count > 0 && q.code[k] != qr_bnode_code(n, s)) bad++;
+                if (n.count == 0 && q.code[k] < 0) bad++;
+            }
+            if (used < 2) bad++;
+            deepest = std::max(deepest, depth + used - 1);
+            for (int k = 0; k < 4; k++)
+                if (q.code[k] != QR_BQUAD_EMPTY)
+                    qs.push_back(std::make_pair(q.code[k], depth + used - 1));
+        }
+        if (deepest > need[l]) bad++;
+        for (size_t j = 0; j < want.size(); j++)
+            if (want[j] != got[j] || want[j] > 1) bad++;
+    }
+    if (levels != NULL) *levels = nl;
+    return bad;
+}
+
 /* the device update's box stage (anim_box.h, the kernel's own float steps)
  * run on the host for the records of scene dt, with the terms and targets
  * taken from scene d0 and its table under the default motion bound;

@@ -334,3 +334,22 @@ def test_update_table_refusals(qr):
     f.update(2500, 4)
     with pytest.raises(ValueError):
         f.anim_table()
+
+
+@pytest.mark.parametrize("kind,seed,nq,flags", [
+    (1, 1, 16, 0), (1, 5, 256, 0), (2, 1, 64, 0), (2, 4, 256, 0), (2, 9, 512, 0),
+    (3, 1, 32, 0), (3, 2, 96, 1 << 4)])
+def test_walk_views_of_the_hierarchy(qr, kind, seed, nq, flags):
+    """the binary child records and the 4-wide records the walks read
+    reach exactly the binary tree's items, each once, with its boxes and
+    codes; leaves hold at most 15 items; the stack need bounds the 4-wide
+    walk (qrpy_accel_check, on the host)"""
+    g = qr.GenScene(kind, seed, nq, flags)
+    f = qr.Flat(g, 320, 240, 0)
+    desc, _ = f.update(0, 4)
+    levels = ctypes.c_int(0)
+    bad = qr.lib().qrpy_accel_check(ctypes.byref(desc), ctypes.byref(levels))
+    assert bad == 0
+    assert levels.value >= 1
+    if nq >= 256 and kind == 2:
+        assert levels.value == 3          # the outer levels are built and checked
