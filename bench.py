@@ -210,6 +210,8 @@ def run_serve(args, wl, rank, world, dist, local):
             return (r.w, r.h) == (1920, 1080) and not scenes[r.scene]["pt"]
     srv = serve.Server(qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
                        max_batch_pixels=args.serve_batch_px, urgent=urgent,
+                       urgent_batch_pixels=args.serve_urgent_px or None,
+                       urgent_batches=args.serve_urgent_batches,
                        prep_threads=min(8, os.cpu_count() or 1),
                        device_anim=not args.serve_host_update)
     # warm-up: every scene once at every size
@@ -263,6 +265,9 @@ def run_serve(args, wl, rank, world, dist, local):
                    "budget_bytes": 120 << 30, "seconds_per_rate": seconds,
                    "max_batch_pixels": args.serve_batch_px,
                    "urgent_first": "1080p Whitted" if args.serve_urgent else None,
+                   "urgent_batch_pixels": (args.serve_urgent_px or args.serve_batch_px)
+                   if args.serve_urgent else None,
+                   "urgent_batches": args.serve_urgent_batches if args.serve_urgent else None,
                    "parallelism": "replicas" if world > 1 else "single"},
         "rates": results,
         "scene_updates": counts,
@@ -865,7 +870,12 @@ def main():
     ap.add_argument("--serve-batch-px", type=int, default=24 << 20,
                     help="serve: pixels of a batched launch at most")
     ap.add_argument("--serve-urgent", action="store_true",
-                    help="serve: 1080p Whitted requests go into the next batch first")
+                    help="serve: 1080p Whitted requests in batches of their own on a "
+                         "high-priority stream")
+    ap.add_argument("--serve-urgent-px", type=int, default=0,
+                    help="serve: pixels of an urgent batch at most (default: as the others)")
+    ap.add_argument("--serve-urgent-batches", type=int, default=2,
+                    help="serve: urgent batches in flight at most")
     ap.add_argument("--serve-host-update", action="store_true",
                     help="serve: update animated scenes on the host (update phases, "
                          "hierarchy build and upload per request) instead of the device")

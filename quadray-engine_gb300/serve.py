@@ -62,14 +62,16 @@ class Server:
 
     def __init__(self, qr, ctx, scenes, budget_bytes=120 << 30, max_batch=64,
                  max_batch_pixels=24 << 20, prep_threads=4, per_request=True,
-                 device_anim=False, rebuild_every=32, urgent=None):
+                 device_anim=False, rebuild_every=32, urgent=None,
+                 urgent_batch_pixels=None, urgent_batches=2):
         """scenes: list of dicts with keys gen (a GenScene), pt (path-traced
         scene), depth and anim (animated); per_request: complete each request
         when its frame is done (else when its batch is); device_anim: update
         animated scenes on the device (qr_scene_anim_*) where they allow it;
         urgent: a predicate on requests whose latency has a target (e.g.
-        1080p Whitted frames): prepared urgent requests go into the next
-        batch ahead of the others"""
+        1080p Whitted frames): prepared urgent requests go into batches of
+        their own (urgent_batches of them, of urgent_batch_pixels at most,
+        default max_batch_pixels) on a stream of the highest priority"""
         self.per_request = per_request
         self.device_anim = device_anim
         self.tables = {}                # (scene, w, h, fsaa) -> update table or None
@@ -98,8 +100,9 @@ class Server:
         # priority, so that their blocks take the SMs as soon as a running
         # batch frees them, ahead of the batches queued on the other stream
         self.ustream = self._new_stream(priority=-1) if urgent is not None else None
-        self.ubatches = ([qr.Batch(ctx, max_batch), qr.Batch(ctx, max_batch)]
+        self.ubatches = ([qr.Batch(ctx, max_batch) for _ in range(urgent_batches)]
                          if urgent is not None else [])
+        self.urgent_batch_pixels = urgent_batch_pixels or max_batch_pixels
         self.free_ubatches = collections.deque(self.ubatches)
         if urgent is not None:
             # the other batches' blocks retire as they finish, so that an
@@ -225,19 +228,22 @@ class Server:
     # ---- batches ------------------------------------------------------
     def _launch(self):
         if self.urgent is None:
-            self._launch_from((self.ready_urgent, self.ready), self.free_batches, self.stream)
+            self._launch_from((self.ready_urgent, self.ready), self.free_batches, self.stream,
+                              self.max_batch_pixels)
         else:
-            self._launch_from((self.ready_urgent,), self.free_ubatches, self.ustream)
-            self._launch_from((self.ready,), self.free_batches, self.stream)
+            self._launch_from((self.ready_urgent,), self.free_ubatches, self.ustream,
+                              self.urgent_batch_pixels)
+            self._launch_from((self.ready,), self.free_batches, self.stream,
+                              self.max_batch_pixels)
 
-    def _launch_from(self, queues, free, stream):
+    def _launch_from(self, queues, free, stream, max_px):
         qr = self.qr
         while any(queues) and free:
             reqs, px = [], 0
             for q in queues:
                 while q and len(reqs) < self.max_batch:
                     r = q[0]
-                    if reqs and px + r.w * r.h > self.max_batch_pixels:
+                    if reqs and px + r.w * r.h > max_px:
                         break
                     q.popleft()
                     reqs.append(r)
