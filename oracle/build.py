@@ -21,8 +21,8 @@ ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libqr_oracle.so")
 LIB64 = os.path.join(OUT, "libqr_oracle64.so")     # QR_ORACLE_FP64 build
-# the reference checkout: QR_REFERENCE, else the checkout this container
-# provides (read-only; absent on the GPU hosts, where nothing here needs it)
+# the reference checkout: QR_REFERENCE, else /root/reference (read-only);
+# where neither holds the reference's sources its build is skipped
 REF_DIR = os.environ.get("QR_REFERENCE") or "/root/reference"
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
 
