@@ -92,6 +92,12 @@ struct qr_ctx
     size_t       wf_bytes;
     cudaEvent_t  wf_ev;
     cudaStream_t wf_last;
+    /* the path tracer's second chunk in flight: its scratch, stream and
+     * events (without the scratch, chunks run one at a time) */
+    void        *wf2;
+    size_t       wf2_bytes;
+    cudaStream_t wf_side;
+    cudaEvent_t  wf_sev[3];
     int          sms;
     long long    wf_paths;      /* paths of a chunk at most */
     int          wf_q, wf_pool; /* queue rays, pool nodes a path */
@@ -161,6 +167,10 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
     ctx->wf_bytes = 0;
     ctx->wf_ev = NULL;
     ctx->wf_last = 0;
+    ctx->wf2 = NULL;
+    ctx->wf2_bytes = 0;
+    ctx->wf_side = NULL;
+    for (int k = 0; k < 3; k++) ctx->wf_sev[k] = NULL;
     ctx->sms = 0;
     ctx->wf_paths = QR_WF_MAX_PATHS;
     ctx->wf_q = QR_WF_Q_PER_PATH;
@@ -188,6 +198,9 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount,
                                                      device);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->wf_ev, cudaEventDisableTiming);
+    for (int k = 0; k < 3 && e == cudaSuccess; k++)
+        e = cudaEventCreateWithFlags(&ctx->wf_sev[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->wf_side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->dfault, 4 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dfault, 0, 4 * sizeof(uint32_t), ctx->stream);
@@ -197,7 +210,10 @@ extern "C" int qr_ctx_create(int device, qr_ctx **out)
         fprintf(stderr, "qr_ctx_create: %s\n", cudaGetErrorString(e));
         if (ctx->dfault) cudaFree(ctx->dfault);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        if (ctx->wf_side) cudaStreamDestroy(ctx->wf_side);
         if (ctx->wf_ev) cudaEventDestroy(ctx->wf_ev);
+        for (int k = 0; k < 3; k++)
+            if (ctx->wf_sev[k]) cudaEventDestroy(ctx->wf_sev[k]);
         delete ctx;
         return QR_ERR_CUDA;
     }
@@ -225,7 +241,11 @@ extern "C" int qr_ctx_destroy(qr_ctx *ctx)
     for (int k = 0; k < 4; k++)
         if (ctx->aev[k]) cudaEventDestroy(ctx->aev[k]);
     if (ctx->wf) cudaFree(ctx->wf);
+    if (ctx->wf2) cudaFree(ctx->wf2);
     if (ctx->wf_ev) cudaEventDestroy(ctx->wf_ev);
+    for (int k = 0; k < 3; k++)
+        if (ctx->wf_sev[k]) cudaEventDestroy(ctx->wf_sev[k]);
+    if (ctx->wf_side) cudaStreamDestroy(ctx->wf_side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return QR_OK;
@@ -936,6 +956,24 @@ static bool wf_scratch(qr_ctx *ctx, size_t need)
     return true;
 }
 
+/* the second chunk's scratch, at least `need` bytes (ctx->wfmu held);
+ * false when it cannot be had (chunks then run one at a time) */
+static bool wf_scratch2(qr_ctx *ctx, size_t need)
+{
+    if (ctx->wf2_bytes >= need) return true;
+    if (ctx->wf2) cudaFree(ctx->wf2);
+    ctx->wf2 = NULL;
+    ctx->wf2_bytes = 0;
+    if (cudaMalloc(&ctx->wf2, need) != cudaSuccess)
+    {
+        ctx->wf2 = NULL;
+        cudaGetLastError();
+        return false;
+    }
+    ctx->wf2_bytes = need;
+    return true;
+}
+
 /* a frame on `stream` may use the scratch once the last frame that used it
  * (perhaps on another stream) is done; returns the wait's status */
 static cudaError_t wf_begin(qr_ctx *ctx, cudaStream_t stream)
@@ -961,9 +999,22 @@ static cudaError_t launch_pt(qr_ctx *ctx, const qr_scene_slot *sl, const qr_fram
     const qr_wf_caps caps = qr_wf_caps_for(*fp, ctx->wf_paths, ctx->wf_q, ctx->wf_pool);
     if (!wf_scratch(ctx, qr_wf_bytes(caps)))
         return qr_launch_pt(sl->d, *fp, acc, dev_frame, stream);
+    /* a frame of two chunks or more keeps two in flight */
+    const int tx = (fp->x_res + 7) / 8, ty = (fp->y_res + 3) / 4;
+    const long long paths = (long long)tx * ty * 32 * fp->pt_on;
+    qr_wf_second sec;
+    const qr_wf_second *second = NULL;
+    if (paths > caps.cap_paths && wf_scratch2(ctx, qr_wf_bytes(caps)))
+    {
+        sec.scratch = ctx->wf2;
+        sec.stream = ctx->wf_side;
+        for (int k = 0; k < 3; k++) sec.ev[k] = ctx->wf_sev[k];
+        second = &sec;
+    }
     cudaError_t e = wf_begin(ctx, stream);
     if (e == cudaSuccess)
-        e = qr_wf_launch_pt(sl->d, *fp, acc, dev_frame, ctx->wf, caps, ctx->sms, stream);
+        e = qr_wf_launch_pt(sl->d, *fp, acc, dev_frame, ctx->wf, caps, ctx->sms, stream,
+                            second);
     return wf_end(ctx, stream, e);
 }
 

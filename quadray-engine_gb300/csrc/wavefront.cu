@@ -483,58 +483,110 @@ qr_wf_caps qr_wf_caps_for(const qr_frame_params &fp, long long max_paths, int q_
 
 static inline size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+/* the stages' arrays in a scratch block */
+struct WPipe
+{
+    WCtl   *ctl;
+    WRay   *qa, *qb;
+    WHit   *hits;
+    WNode  *pool;
+    float4 *samples, *sums;
+};
+
+static WPipe carve(void *scratch, const qr_wf_caps &caps)
+{
+    WPipe p;
+    unsigned char *b = (unsigned char *)scratch;
+    p.ctl = (WCtl *)b;
+    b += al256(sizeof(WCtl));
+    p.qa = (WRay *)b;
+    b += al256((size_t)caps.cap_q * sizeof(WRay));
+    p.qb = (WRay *)b;
+    b += al256((size_t)caps.cap_q * sizeof(WRay));
+    p.hits = (WHit *)b;
+    b += al256((size_t)caps.cap_q * sizeof(WHit));
+    p.pool = (WNode *)b;
+    b += al256((size_t)caps.cap_pool * sizeof(WNode));
+    p.samples = (float4 *)b;
+    b += al256((size_t)caps.cap_paths * sizeof(float4));
+    p.sums = (float4 *)b;
+    return p;
+}
+
+/* the second pipeline's overflow word into the first's */
+__global__ void wf_merge(WCtl *a, const WCtl *b)
+{
+    if (b->overflow) a->overflow = 1;
+}
+
 cudaError_t qr_wf_launch_pt(const qr_dscene &sc, const qr_frame_params &fp, float *acc,
                             uint32_t *frame, void *scratch, const qr_wf_caps &caps,
-                            int sms, cudaStream_t stream)
+                            int sms, cudaStream_t stream, const qr_wf_second *second)
 {
-    unsigned char *b = (unsigned char *)scratch;
-    WCtl *ctl = (WCtl *)b;
-    b += al256(sizeof(WCtl));
-    WRay *qa = (WRay *)b;
-    b += al256((size_t)caps.cap_q * sizeof(WRay));
-    WRay *qb = (WRay *)b;
-    b += al256((size_t)caps.cap_q * sizeof(WRay));
-    WHit *hits = (WHit *)b;
-    b += al256((size_t)caps.cap_q * sizeof(WHit));
-    WNode *pool = (WNode *)b;
-    b += al256((size_t)caps.cap_pool * sizeof(WNode));
-    float4 *samples = (float4 *)b;
-    b += al256((size_t)caps.cap_paths * sizeof(float4));
-    float4 *sums = (float4 *)b;
-
     const int tx = (fp.x_res + 7) / 8, ty = (fp.y_res + 3) / 4;
     const int ppad = tx * ty * 32;
     const long long total = (long long)ppad * fp.pt_on;
+    const long long nchunks = (total + caps.cap_paths - 1) / caps.cap_paths;
     const int levels = fp.depth + 1;
+    /* two pipelines only when there are two chunks to overlap */
+    const int np = second != NULL && nchunks >= 2 ? 2 : 1;
+    WPipe P[2];
+    P[0] = carve(scratch, caps);
+    P[1] = np == 2 ? carve(second->scratch, caps) : P[0];
+    cudaStream_t st[2] = {stream, np == 2 ? second->stream : stream};
+    float4 *sums = P[0].sums;
     /* every kernel strides over its level: as many blocks as are resident */
     const int step_per_sm = qr_wf_prepare();
     const int blocks = sms * 8;             /* memory-bound stages: 8 blocks of 128 a SM */
     const int sblocks = sms * step_per_sm;
-    cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(WCtl), stream);
+    cudaError_t e = cudaMemsetAsync(P[0].ctl, 0, sizeof(WCtl), stream);
+    if (e == cudaSuccess && np == 2) e = cudaMemsetAsync(P[1].ctl, 0, sizeof(WCtl), stream);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(sums, 0, (size_t)fp.x_res * fp.y_res * sizeof(float4), stream);
-    for (long long c0 = 0; c0 < total && e == cudaSuccess; c0 += caps.cap_paths)
+    if (e == cudaSuccess && np == 2) e = cudaEventRecord(second->ev[0], stream);
+    if (e == cudaSuccess && np == 2) e = cudaStreamWaitEvent(st[1], second->ev[0], 0);
+    long long c = 0;
+    for (long long c0 = 0; c0 < total && e == cudaSuccess; c0 += caps.cap_paths, c++)
     {
+        const int p = (int)(c % np);
+        const WPipe &W = P[p];
+        cudaStream_t s = st[p];
         const long long c1 = c0 + caps.cap_paths < total ? c0 + caps.cap_paths : total;
         /* counts of this chunk (the overflow word stays) */
-        e = cudaMemsetAsync(ctl, 0, offsetof(WCtl, overflow), stream);   /* cnt, off, next */
+        e = cudaMemsetAsync(W.ctl, 0, offsetof(WCtl, overflow), s);   /* cnt, off, next */
         if (e != cudaSuccess) break;
-        wf_gen<<<blocks, 128, 0, stream>>>(fp, c0, c1, ppad, tx, qa, ctl);
+        wf_gen<<<blocks, 128, 0, s>>>(fp, c0, c1, ppad, tx, W.qa, W.ctl);
         for (int d = 0; d < levels; d++)
         {
-            WRay *qi = (d & 1) ? qb : qa, *qo = (d & 1) ? qa : qb;
-            wf_trace<<<sblocks, 128, 0, stream>>>(sc, fp, d, qi, hits, ctl);
-            wf_step<<<sblocks, 128, 0, stream>>>(sc, fp, d, qi, hits, qo, pool, ctl,
-                                                 (int)caps.cap_q, (int)caps.cap_pool);
+            WRay *qi = (d & 1) ? W.qb : W.qa, *qo = (d & 1) ? W.qa : W.qb;
+            wf_trace<<<sblocks, 128, 0, s>>>(sc, fp, d, qi, W.hits, W.ctl);
+            wf_step<<<sblocks, 128, 0, s>>>(sc, fp, d, qi, W.hits, qo, W.pool, W.ctl,
+                                            (int)caps.cap_q, (int)caps.cap_pool);
         }
         for (int d = levels - 1; d >= 0; d--)
-            wf_fold<<<blocks, 128, 0, stream>>>(d, pool, samples, ctl);
-        wf_accum<<<blocks, 128, 0, stream>>>(fp, c0, c1, ppad, tx, samples, sums, ctl);
-        qr_note_launches(stream, 2 + 3 * levels);
-        e = cudaGetLastError();
+            wf_fold<<<blocks, 128, 0, s>>>(d, W.pool, W.samples, W.ctl);
+        /* the chunk's samples join the sums after the chunk before it's */
+        if (np == 2 && c >= 1) e = cudaStreamWaitEvent(s, second->ev[1 + (1 - p)], 0);
+        if (e != cudaSuccess) break;
+        wf_accum<<<blocks, 128, 0, s>>>(fp, c0, c1, ppad, tx, W.samples, sums, W.ctl);
+        if (np == 2) e = cudaEventRecord(second->ev[1 + p], s);
+        qr_note_launches(s, 2 + 3 * levels);
+        if (e == cudaSuccess) e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && np == 2)
+    {
+        /* the second stream's last chunk, then its overflow word */
+        e = cudaStreamWaitEvent(stream, second->ev[2], 0);
+        if (e == cudaSuccess)
+        {
+            wf_merge<<<1, 1, 0, stream>>>(P[0].ctl, P[1].ctl);
+            qr_note_launches(stream, 1);
+            e = cudaGetLastError();
+        }
     }
     if (e == cudaSuccess)
     {
+        WCtl *ctl = P[0].ctl;
         wf_final<<<blocks, 128, 0, stream>>>(fp, sums, acc, frame, ctl);
         const dim3 block(32, 4);
         const dim3 grid((fp.x_res + 2 * QR_TILE_W - 1) / (2 * QR_TILE_W),
