@@ -33,8 +33,10 @@
  *
  * Chunks.  A frame's samples are numbered sample-major (path q = s * Ppad +
  * t, t the pixel's place in the tile order over Ppad padded pixels) and cut
- * into chunks of at most cap_paths paths, rendered one after the other; a
- * pixel's samples are summed in ascending s whatever the chunking.  Queues
+ * into chunks of at most cap_paths paths, rendered one after the other or,
+ * with a second scratch block, two at a time on two streams; either way a
+ * chunk's samples join the sums after the previous chunk's, so a pixel's
+ * samples are summed in ascending s whatever the chunking.  Queues
  * and the node pool have fixed capacities: a level whose children would not
  * fit sets the overflow word; every later stage of the frame then does
  * nothing and wf_fallback renders the whole frame with the per-pixel kernel
