@@ -738,6 +738,28 @@ static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
         }
     }
 
+#ifndef QR_ALWAYS_FRAC
+#define QR_ALWAYS_FRAC 0.2
+#endif
+    /* surfaces whose box covers more than a fifth of the bounded extent's
+     * surface area (the walls of a room) are tested by every ray, as the
+     * unbounded ones are, instead of widening the tree's upper nodes: the
+     * 1280x720 64-spp frame of the closed box takes 121.7 against 157.2 ms
+     * (at a twelfth of the area 130.2 ms, and the animated frame, whose
+     * larger surfaces then leave the tree, 28.6 against 20.1 ms) */
+    double ext_area = 0.0;
+    if (QR_ALWAYS_FRAC > 0.0)
+    {
+        Box all;
+        bool any = false;
+        for (int i = 0; i < d->nsrf; i++)
+        {
+            if (!ok[i] || wbox[i].empty() || !wbox[i].finite()) continue;
+            all = any ? merge(all, wbox[i]) : wbox[i];
+            any = true;
+        }
+        if (any) ext_area = area(all);
+    }
     for (int e = 0; e < d->cam_num; e++)
     {
         const qr_elem &el = d->elems[d->cam_off + e];
@@ -749,7 +771,9 @@ static int accel_build(const qr_scene_desc *d, qr_accel_host *out, int level,
         it.xf = (xf[e] >= 0 && d->srf[xf[e]].amap[3] != 0) ? xf[e] : -1;
         it.pad = 0;
         Box b = wbox[i];
-        if (ok[i] && !b.empty() && b.finite())
+        const bool huge = QR_ALWAYS_FRAC > 0.0 && ext_area > 0.0 && ok[i] && !b.empty() &&
+                          b.finite() && area(b) > QR_ALWAYS_FRAC * ext_area;
+        if (ok[i] && !b.empty() && b.finite() && !huge)
         {
             pad(b);
             for (int k = 0; k < 3; k++)
