@@ -166,6 +166,8 @@ def lib():
         L.qrpy_rotation_bound.restype = None
         L.qrpy_extent.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(ctypes.c_double)]
         L.qrpy_accel_check.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(ctypes.c_int)]
+        L.qrpy_accel_counts.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(ctypes.c_int)]
+        L.qrpy_accel_counts.restype = None
         L.qrpy_extent.restype = None
         L.qrpy_anim_box_check.argtypes = [ctypes.POINTER(QrSceneDesc), ctypes.POINTER(QrAnimNode),
                                           i32, ctypes.POINTER(QrSceneDesc)]

@@ -140,6 +140,18 @@ void qrpy_extent(const qr_scene_desc *d, double *out)
     qr_accel_extent(d, out);
 }
 
+/* level 0 of the hierarchy of scene d: out[0] surfaces in the tree,
+ * out[1] surfaces every ray tests (unbounded, or covering more than a fifth
+ * of the bounded extent's area), out[2] nodes */
+void qrpy_accel_counts(const qr_scene_desc *d, int *out)
+{
+    qr_accel_host acc;
+    qr_accel_build(d, &acc, 0);
+    out[0] = (int)acc.items.size();
+    out[1] = (int)acc.always.size();
+    out[2] = (int)acc.nodes.size();
+}
+
 /* the walk's views of the hierarchy of scene d against its binary tree:
  * per built level, the items a walk of the 4-wide records reaches are
  * those of the binary tree, each once; every slot's box is its source

@@ -353,3 +353,20 @@ def test_walk_views_of_the_hierarchy(qr, kind, seed, nq, flags):
     assert levels.value >= 1
     if nq >= 256 and kind == 2:
         assert levels.value == 3          # the outer levels are built and checked
+
+
+@pytest.mark.parametrize("kind,seed,nq,always", [
+    (3, 1, 32, 5),      # the closed box: its five walls are tested by every ray
+    (2, 1, 64, 1),      # the animated hierarchy: only the unbounded ground plane
+    (1, 1, 16, 1),      # the plain scene: only the unbounded ground plane
+])
+def test_room_walls_leave_the_tree(qr, kind, seed, nq, always):
+    """surfaces covering more than a fifth of the bounded extent's area join
+    the unbounded ones (every ray tests them) instead of the tree"""
+    g = qr.GenScene(kind, seed, nq, 0)
+    f = qr.Flat(g, 320, 240, 0)
+    desc, _ = f.update(0, 4)
+    out = (ctypes.c_int * 3)()
+    qr.lib().qrpy_accel_counts(ctypes.byref(desc), out)
+    assert out[1] == always, list(out)
+    assert out[0] > 0 and out[2] > 0
