@@ -70,7 +70,7 @@ struct WNode
 #define QR_WF_MIN_BLOCKS 6
 #endif
 #ifndef QR_WF_TRACE_MIN_BLOCKS
-#define QR_WF_TRACE_MIN_BLOCKS 6
+#define QR_WF_TRACE_MIN_BLOCKS 7
 #endif
 
 /* a ray's nearest hit from the tracing stage, 32 bytes: hit point and
@@ -111,7 +111,9 @@ wf_trace(const qr_dscene S, const qr_frame_params P, int d, const WRay *__restri
         /* over the 4-wide records: the 720p 64-spp frame 169.2 against
          * 175.1 ms over the binary tree's child records (and 170.0 ms with
          * the binary records for the camera rays only); 5, 7 and 8
-         * resident blocks instead of 6: 174.0, 174.1, 182.3 ms */
+         * resident blocks instead of 6: 174.0, 174.1, 182.3 ms.  With the
+         * room's walls out of the tree: 121.6 ms (binary records 125.0),
+         * at 7 resident blocks 120.0 ms */
         walk_t<1>(S, P, r, off, num, w, NULL);
         /* a ray without a hit has no side (the field is not set) */
         const int side = w.best.srf >= 0 ? (w.best.side & 1) : 0;
