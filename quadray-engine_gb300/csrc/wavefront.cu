@@ -436,7 +436,7 @@ static std::atomic<int> g_step_per_sm(0), g_trace_per_sm(0);
 
 int qr_wf_prepare(void)
 {
-    if (g_step_per_sm.load(std::memory_order_relaxed) == 0)
+    if (g_step_per_sm.load(std::memory_order_acquire) == 0)
     {
         int nb = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, wf_step, 128, 0) != cudaSuccess ||
@@ -447,9 +447,9 @@ int qr_wf_prepare(void)
             nt <= 0)
             nt = QR_WF_TRACE_MIN_BLOCKS;
         g_trace_per_sm.store(nt, std::memory_order_relaxed);
-        g_step_per_sm.store(nb, std::memory_order_relaxed);
+        g_step_per_sm.store(nb, std::memory_order_release);
     }
-    return g_step_per_sm.load(std::memory_order_relaxed);
+    return g_step_per_sm.load(std::memory_order_acquire);
 }
 
 /* a batched request's completion word, once the frame before it on the

@@ -33,6 +33,7 @@
  * would overflow sets the overflow word, every later stage does nothing and
  * wh_fallback renders the frame with the per-pixel code instead.
  */
+#include <atomic>
 #include "wf_common.cuh"
 #include "whitted_wf.h"
 
@@ -464,20 +465,24 @@ cudaError_t qr_wh_launch(const qr_dscene &sc, const qr_frame_params &fp, uint32_
     const int tx = (fp.x_res + 7) / 8, ty = (fp.y_res + 3) / 4;
     const long long total = (long long)tx * ty * 32 * ns;
     const int levels = fp.depth + 1;
-    static int step_per_sm = 0, shadow_per_sm = 0;
-    if (step_per_sm == 0)
+    /* resident blocks a SM of the stepping and shadow stages (queried once;
+     * the values are the same whichever thread stores them) */
+    static std::atomic<int> g_step(0), g_shadow(0);
+    if (g_step.load(std::memory_order_acquire) == 0)
     {
         int nb = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, wh_step, 128, 0) != cudaSuccess ||
             nb <= 0)
             nb = QR_WH_MIN_BLOCKS;
-        step_per_sm = nb;
-        nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, wh_shadow, 128, 0) != cudaSuccess ||
-            nb <= 0)
-            nb = 8;
-        shadow_per_sm = nb;
+        int ns2 = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ns2, wh_shadow, 128, 0) != cudaSuccess ||
+            ns2 <= 0)
+            ns2 = 8;
+        g_shadow.store(ns2, std::memory_order_relaxed);
+        g_step.store(nb, std::memory_order_release);
     }
+    const int step_per_sm = g_step.load(std::memory_order_acquire);
+    const int shadow_per_sm = g_shadow.load(std::memory_order_relaxed);
     const int blocks = sms * 8;
     cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(WhCtl), stream);
     for (long long c0 = 0; c0 < total && e == cudaSuccess; c0 += caps.cap_samples)
