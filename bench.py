@@ -66,7 +66,7 @@ WORKLOADS = {
     "batch": dict(kind=0, seed=1000, nq=0, w=0, h=0, fsaa=0, depth=0, anim=False,
                   batch=256),
     "serve": dict(kind=0, seed=2000, nq=0, w=0, h=0, fsaa=0, depth=0, anim=True,
-                  serve=(120, 500, 2000), seconds=10.0),
+                  serve=(120, 500, 2000), seconds=60.0),
 }
 
 RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
