@@ -593,14 +593,24 @@ def run_reference(args, wl):
     line = {"impl": "reference", "metric": "rays_per_s", "value": v, "unit": "rays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": dict(config_of(args.workload, wl),
-                           l2="none: the scalar port on the host cores",
-                           parallelism="single"),
+            "config": line_config(args.workload, wl, "reference", 1),
             "cpu_baseline": {"value": v, "unit": "rays/s", "cores": cb["cores"],
                              "kind": cb["kind"], "sample": cb["sample"]},
             "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def line_config(name, wl, impl, world):
+    """a line's config: the workload's identity (config_of, the same in
+    both arms) and how the arm timed it"""
+    cfg = config_of(name, wl)
+    if impl == "reference":
+        cfg.update({"l2": "none: the scalar port on the host cores", "parallelism": "single"})
+    else:
+        cfg.update({"l2": "256 MiB buffer written between timed steps",
+                    "parallelism": "replicas" if world > 1 else "single"})
+    return cfg
 
 
 def config_of(name, wl):
@@ -818,9 +828,7 @@ def run_frames(args, wl, rank, world, dist, local):
     # config: the workload's identity (the reference arm's line carries the
     # same keys and values) and how it was timed; the measured workload
     # quantities go beside it
-    cfg = config_of(args.workload, wl)
-    cfg.update({"l2": "256 MiB buffer written between timed steps",
-                "parallelism": "replicas" if world > 1 else "single"})
+    cfg = line_config(args.workload, wl, "ours", world)
     line = {
         "metric": "rays_per_s", "value": value, "unit": "rays/s",
         "n_gpus": world, "steps": K, "warmup": W,
